@@ -1,0 +1,329 @@
+"""Generate ``std_atm_cases.json`` from RRTMG_SW's own example runs.
+
+Run once where the RRTMG_SW source tree is present:
+``python tests/golden/make_golden.py <path-to-RRTMG_SW>``.  The output is
+committed; tests read only the JSON.
+
+For each of the eleven example runs that need no profile builder
+(``run_examples_std_atm/script.run_std_atm`` runs with ``iatm = 0``), this
+script reads the input records exactly as the column driver does
+(``src/rrtmg_sw.1col.f90`` ``readprof`` :1035-1881, ``readcld`` :1884-1958,
+``readaer`` :1961-2127: fixed-column Fortran formats, blank fields read as
+zero, implied decimals for fields without a point) and applies the driver's
+input preparation (mixing ratios to column amounts :1743-1768, albedo
+``1 - semiss`` :650-653, ``cos(sza)``, cloud water split by ice fraction
+:1827-1841, aerosol spectral scaling :2013-2048).  The physics of the column
+(McICA sampling, cloud optics, gas optics, two-stream solve) is left to the
+oracle.  The expected outputs are the committed ``output_rrtm_*`` tables,
+one block per band range.
+"""
+import json
+import math
+import os
+import re
+import sys
+
+CASES = [
+    # name, input file, cloud file, aerosol file, output file
+    ("MLS-clr", "input_rrtm_MLS-clr", None, None, "output_rrtm_MLS-clr"),
+    ("MLS-clr-sza65", "input_rrtm_MLS-clr-sza65", None, None, "output_rrtm_MLS-clr-sza65"),
+    ("MLW-clr", "input_rrtm_MLW-clr", None, None, "output_rrtm_MLW-clr"),
+    ("SAW-clr", "input_rrtm_SAW-clr", None, None, "output_rrtm_SAW-clr"),
+    ("TROP-clr", "input_rrtm_TROP-clr", None, None, "output_rrtm_TROP-clr"),
+    ("MLS-clr-aer12", "input_rrtm_MLS-clr-aer12", None, "in_aer_rrtm-aer12", "output_rrtm_MLS-clr-aer12"),
+    ("MLS-cld6-imca0-icld2", "input_rrtm_MLS-cld-imca0-icld2", "in_cld_rrtm-cld6", None,
+     "output_rrtm_MLS-cld6-imca0-icld2"),
+    ("MLS-cld5-imca1-icld2", "input_rrtm_MLS-cld-imca1-icld2", "in_cld_rrtm-cld5", None,
+     "output_rrtm_MLS-cld5-imca1-icld2"),
+    ("MLS-cld7-imca1-icld2", "input_rrtm_MLS-cld-imca1-icld2", "in_cld_rrtm-cld7", None,
+     "output_rrtm_MLS-cld7-imca1-icld2"),
+    ("MLS-cld7-imca1-icld5-idcor0", "input_rrtm_MLS-cld-imca1-icld5-idcor0", "in_cld_rrtm-cld7", None,
+     "output_rrtm_MLS-cld7-imca1-icld5-idcor0"),
+    ("MLS-cld7-imca1-icld5-idcor1", "input_rrtm_MLS-cld-imca1-icld5-idcor1", "in_cld_rrtm-cld7", None,
+     "output_rrtm_MLS-cld7-imca1-icld5-idcor1"),
+]
+
+WAVENUM1 = [2600., 3250., 4000., 4650., 5150., 6150., 7700., 8050., 12850., 16000., 22650., 29000., 38000., 820.]
+WAVENUM2 = [3250., 4000., 4650., 5150., 6150., 7700., 8050., 12850., 16000., 22650., 29000., 38000., 50000., 2600.]
+
+
+def fnum(field, d=0):
+    """Fortran F/E/G input editing of one field (BLANK='NULL')."""
+    s = field.replace(" ", "")
+    if not s:
+        return 0.0
+    m = re.match(r"^([+-]?)(\d*)(\.?)(\d*)(?:[EeDd]?([+-]?\d+))?$", s)
+    if not m:
+        raise ValueError("bad numeric field %r" % field)
+    sign, ip, dot, fp, ex = m.groups()
+    if dot:
+        val = float((ip or "0") + "." + (fp or "0"))
+    else:
+        val = int(ip + fp) * 10.0 ** (-d)
+    if ex:
+        val = val * 10.0 ** int(ex)
+    return -val if sign == "-" else val
+
+
+def inum(field):
+    s = field.replace(" ", "")
+    return int(s) if s else 0
+
+
+class Rec:
+    """Fixed-column record reader: widths in Fortran format order."""
+
+    def __init__(self, line):
+        self.s = line.rstrip("\n")
+        self.pos = 0
+
+    def skip(self, n):
+        self.pos += n
+
+    def take(self, n):
+        f = self.s[self.pos:self.pos + n].ljust(n)
+        self.pos += n
+        return f
+
+    def i(self, n):
+        return inum(self.take(n))
+
+    def f(self, n, d=0):
+        return fnum(self.take(n), d)
+
+
+def earth_sun(idn, pi):
+    gamma = 2.0 * pi * (idn - 1) / 365.0
+    return (1.000110 + .034221 * math.cos(gamma) + .001289 * math.sin(gamma) +
+            .000719 * math.cos(2.0 * gamma) + .000077 * math.sin(2.0 * gamma))
+
+
+def read_input(path):
+    lines = open(path).read().splitlines()
+    k = 0
+    while not lines[k].startswith("$"):
+        k += 1
+    k += 1
+    r = Rec(lines[k]); k += 1
+    # 9011 format (18x,i2,29x,i1,32x,i1,1x,i1,2x,i3,3x,i1,i1,3x,i1,i1)
+    r.skip(18); iaer = r.i(2); r.skip(29); iatm = r.i(1); r.skip(32); iscat = r.i(1)
+    r.skip(1); istrm = r.i(1); r.skip(2); iout = r.i(3); r.skip(3); imca = r.i(1); icld = r.i(1)
+    r.skip(3); idelm = r.i(1); icos = r.i(1)
+    assert iatm == 0 and iscat == 1 and istrm == 0 and icos == 0
+    # 9020 format (12x, i3, 3x, f7.4, 3x, i2, f10.4, f10.5, 14f10.5)
+    r = Rec(lines[k]); k += 1
+    r.skip(12); juldat = r.i(3); r.skip(3); sza = r.f(7, 4); r.skip(3); isolvar = r.i(2)
+    scon = r.f(10, 4); solcycfrac = r.f(10, 5)
+    solvar = [r.f(10, 5) for _ in range(14)]
+    assert isolvar == 0 and scon == 0.0, "only the isolvar=0, scon=0 examples are iatm=0"
+    pi = 2.0 * math.asin(1.0)
+    zenith = math.cos(sza * pi / 180.0)
+    adjflux_jd = 1.0 if juldat == 0 else earth_sun(juldat, pi)
+    # 9012 format (11x,i1,2x,i1,14f5.3)
+    r = Rec(lines[k]); k += 1
+    r.skip(11); iemis = r.i(1); r.skip(2); ireflect = r.i(1)
+    semiss = [r.f(5, 3) for _ in range(14)]
+    if iemis == 0:
+        semiss = [1.0] * 14
+    elif iemis == 1:
+        semiss = [semiss[0]] * 14
+    idcor, decorr_con, lat = 0, 0.0, 0.0
+    if icld in (4, 5):
+        r = Rec(lines[k]); k += 1
+        r.skip(8); idcor = r.i(2)
+        r = Rec(lines[k]); k += 1
+        if idcor == 0:
+            decorr_con = r.f(10, 3)
+        else:
+            lat = r.f(10, 3)
+    if juldat == 0 and idcor == 1:
+        juldat = 94
+    # 9013 format (1x,i1,i3,i5)
+    r = Rec(lines[k]); k += 1
+    r.skip(1); iform = r.i(1); nlay = r.i(3); nmol = r.i(5)
+    if nmol == 0:
+        nmol = 7
+    assert iform == 1 and nmol == 7
+    pavel, tavel, altz, pz, tz, wkl, wbrodl = [], [], [], [], [], [], []
+    for lay in range(nlay):
+        r = Rec(lines[k]); k += 1
+        pavel.append(r.f(15)); tavel.append(r.f(10)); r.f(10); r.take(3); r.i(2)
+        if lay == 0:
+            r.skip(1)
+            altz.append(r.f(7, 2)); pz.append(r.f(8, 3)); tz.append(r.f(7, 2))
+        else:
+            r.skip(23)
+        altz.append(r.f(7, 2)); pz.append(r.f(8, 3)); tz.append(r.f(7, 2))
+        r = Rec(lines[k]); k += 1
+        vals = [r.f(15) for _ in range(8)]
+        wkl.append(vals[:7]); wbrodl.append(vals[7])
+    # mixing ratio or column amounts (:1743-1768)
+    imix = 1
+    for m in range(nmol):
+        if wkl[0][m] > 1.0:
+            imix = 0
+            break
+    coldry = []
+    for lay in range(nlay):
+        summol = 0.0
+        for imol in range(1, nmol):
+            summol = summol + wkl[lay][imol]
+        if imix == 1:
+            cd = wbrodl[lay] / (1.0 - summol)
+            wkl[lay] = [cd * w for w in wkl[lay]]
+        else:
+            cd = wbrodl[lay] + summol
+        coldry.append(cd)
+    dz = [(altz[l + 1] - altz[l]) * 1000.0 for l in range(nlay)]
+    return dict(nlay=nlay, iaer=iaer, icld=icld, imca=imca, idelm=idelm, iout=iout, juldat=juldat,
+                zenith=zenith, isolvar=isolvar, adjflux=[adjflux_jd] * 14,
+                albedo=[1.0 - e for e in semiss], idcor=idcor, decorr_con=decorr_con, lat=lat,
+                pavel=pavel, tavel=tavel, pz=pz, tz=tz, coldry=coldry,
+                wkl=[w for lay in wkl for w in lay], dz=dz)
+
+
+def read_cloud(path, nlay):
+    lines = open(path).read().splitlines()
+    r = Rec(lines[0])
+    r.skip(3); inflag = r.i(2); r.skip(4); iceflag = r.i(1); r.skip(4); liqflag = r.i(1)
+    cldfrac = [0.0] * nlay
+    dat = [[0.0] * nlay for _ in range(4)]
+    assert inflag != 0
+    for line in lines[1:]:
+        if line.startswith("%"):
+            break
+        r = Rec(line)
+        r.take(1); r.skip(1); lay = r.i(3)
+        frac = r.f(10, 5)
+        d = [r.f(10, 5) for _ in range(4)]
+        cldfrac[lay - 1] = frac
+        for j in range(4):
+            dat[j][lay - 1] = d[j]
+    cwp, fice, rei, rel = dat
+    ciwp = [cwp[l] * fice[l] for l in range(nlay)]
+    clwp = [cwp[l] * (1.0 - fice[l]) for l in range(nlay)]
+    return dict(inflag=inflag, iceflag=iceflag, liqflag=liqflag, cldfrac=cldfrac,
+                ciwp=ciwp, clwp=clwp, rei=rei, rel=rel)
+
+
+def read_aerosol(path, nlay, zenith):
+    lines = open(path).read().splitlines()
+    rnu0 = [2903., 3601., 4310., 4892., 5623., 6872., 7872., 10590., 14420., 18970., 25015., 30390., 43507., 1412.]
+    rnu1 = {23: 10530.7, 24: 14293.3, 25: 18678.0, 26: 24475.1}
+    od0 = {23: 0.1084, 24: 0.167, 25: 0.245, 26: 0.3611}
+    od1 = {23: 0.3144, 24: 0.4822, 25: 0.7013, 26: 1.0239}
+    eps = 1.e-10
+    k = 0
+    r = Rec(lines[k]); k += 1
+    r.skip(3); naer = r.i(2)
+    aod = [0.0] * nlay
+    tauaer = [[0.0] * 14 for _ in range(nlay)]
+    ssaaer = [[0.0] * 14 for _ in range(nlay)]
+    asmaer = [[0.0] * 14 for _ in range(nlay)]
+    for _ in range(naer):
+        r = Rec(lines[k]); k += 1
+        r.skip(2); nl = r.i(3); r.skip(4); iaod = r.i(1); r.skip(4); issa = r.i(1); r.skip(4); iasym = r.i(1)
+        aerpar = [r.f(8, 3) for _ in range(3)]
+        specfac = [0.0] * 14
+        if iaod == 0:
+            if aerpar[1] < eps:
+                aerpar[1] = 1.0
+            for ib in range(14):
+                rl = 10000.0 / rnu0[ib]
+                specfac[ib] = (aerpar[1] + aerpar[2] * rl) / ((aerpar[1] + aerpar[2] - 1.0) + rl ** aerpar[0])
+        lays = []
+        for _ in range(nl):
+            r = Rec(lines[k]); k += 1
+            r.skip(2); lay = r.i(3)
+            aod1 = [r.f(7, 4) for _ in range(14)]
+            lays.append(lay)
+            assert aod[lay - 1] < eps
+            if iaod == 0:
+                aod[lay - 1] = aod1[0]
+                for ib in range(14):
+                    tauaer[lay - 1][ib] = aod[lay - 1] * specfac[ib]
+            else:
+                for ib in range(14):
+                    aod[lay - 1] = max(aod[lay - 1], aod1[ib])
+                    tauaer[lay - 1][ib] = aod1[ib]
+        for band in (23, 24, 25, 26):
+            ib = band - 16
+            if iaod == 0:
+                s = 0.0
+                for lay in lays:
+                    s = s + tauaer[lay - 1][ib]
+                od = s / zenith
+                rnu = rnu0[ib] + (rnu1[band] - rnu0[ib]) * (od - od0[band]) / (od1[band] - od0[band])
+                rln = 10000.0 / rnu
+                sfn = (aerpar[1] + aerpar[2] * rln) / ((aerpar[1] + aerpar[2] - 1.0) + rln ** aerpar[0])
+                for lay in lays:
+                    tauaer[lay - 1][ib] = tauaer[lay - 1][ib] * sfn / specfac[ib]
+        r = Rec(lines[k]); k += 1
+        ssa = [r.f(5, 3) for _ in range(14)]
+        for ib in range(14):
+            for lay in lays:
+                ssaaer[lay - 1][ib] = ssa[0] if issa == 0 else ssa[ib]
+        assert iasym < 2
+        r = Rec(lines[k]); k += 1
+        asym = [r.f(5, 3) for _ in range(14)]
+        for ib in range(14):
+            for lay in lays:
+                asmaer[lay - 1][ib] = asym[0] if iasym == 0 else asym[ib]
+    # (nlay, 14) column-major: element (lay, ib) at [lay + nlay*ib]
+    flat = lambda a: [a[l][ib] for ib in range(14) for l in range(nlay)]
+    return dict(tauaer=flat(tauaer), ssaaer=flat(ssaaer), asmaer=flat(asmaer))
+
+
+def read_output(path):
+    blocks = []
+    cur = None
+    for line in open(path):
+        m = re.match(r"\s*Wavenumbers:\s*([\d.]+)\s*-\s*([\d.]+)", line)
+        if m:
+            cur = dict(wn1=float(m.group(1)), wn2=float(m.group(2)), level=[], p=[], uflx=[], difdflx=[],
+                       dirdflx=[], dflx=[], fnet=[], htr=[])
+            blocks.append(cur)
+            continue
+        parts = line.split()
+        if cur is not None and len(parts) == 8 and re.match(r"^\d+$", parts[0]):
+            vals = [float(x) for x in parts[1:]]
+            cur["level"].append(int(parts[0]))
+            for key, v in zip(("p", "uflx", "difdflx", "dirdflx", "dflx", "fnet", "htr"), vals):
+                cur[key].append(v)
+    for b in blocks:
+        # the tables list levels top-down; store them surface-first
+        order = sorted(range(len(b["level"])), key=lambda i: b["level"][i])
+        for key in ("level", "p", "uflx", "difdflx", "dirdflx", "dflx", "fnet", "htr"):
+            b[key] = [b[key][i] for i in order]
+        if b["wn1"] == 820.0 and b["wn2"] == 50000.0:
+            b["istart"], b["iend"] = 16, 29
+        else:
+            ib = [i for i in range(14) if WAVENUM1[i] == b["wn1"] and WAVENUM2[i] == b["wn2"]][0]
+            b["istart"] = b["iend"] = 16 + ib
+    return blocks
+
+
+def main(ref):
+    d = os.path.join(ref, "run_examples_std_atm")
+    out = []
+    for name, inp, cld, aer, outp in CASES:
+        c = read_input(os.path.join(d, inp))
+        nlay = c["nlay"]
+        c["name"] = name
+        if cld:
+            c.update(read_cloud(os.path.join(d, cld), nlay))
+        else:
+            c.update(dict(inflag=0, iceflag=0, liqflag=0, cldfrac=[0.0] * nlay, ciwp=[0.0] * nlay,
+                          clwp=[0.0] * nlay, rei=[0.0] * nlay, rel=[0.0] * nlay))
+        if aer:
+            c.update(read_aerosol(os.path.join(d, aer), nlay, c["zenith"]))
+        c["expected"] = read_output(os.path.join(d, outp))
+        out.append(c)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "std_atm_cases.json")
+    with open(path, "w") as f:
+        json.dump({"source": "RRTMG_SW run_examples_std_atm (iatm=0 runs)", "cases": out}, f)
+    print("wrote", path, len(out), "cases")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
