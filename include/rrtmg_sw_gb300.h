@@ -1,0 +1,166 @@
+/*
+ * rrtmg_sw_gb300.h -- C ABI of the GB300 (sm_103a) RRTMG_SW shortwave solver.
+ *
+ * Drop-in boundary for the GCM interface of RRTMG_SW.  Every entry point
+ * names the reference routine it replaces (paths relative to the RRTMG_SW
+ * source tree).  Arrays use the reference's Fortran (column-major) layout,
+ * so a Fortran caller passes c_loc(x(1,1)) of its contiguous arrays
+ * unchanged:
+ *   (ncol,nlay)        element (i,l)   at [i + ncol*l]
+ *   (ngpt,ncol,nlay)   element (g,i,l) at [g + 112*(i + ncol*l)]
+ *   (ncol,nlay,nbnd)   element (i,l,b) at [i + ncol*(l + nlay*b)]
+ *   (nbnd,ncol,nlay)   element (b,i,l) at [b + 14*(i + ncol*l)]
+ * Layer 1 is the surface layer (rrtmg_sw_rad.f90:1527-1529).  Units as in
+ * the reference: hPa, K, volume mixing ratio, g m-2, microns; outputs W m-2
+ * and K d-1.
+ *
+ * All entry points return 0 on success or one of the RRTMG_SW_E* codes
+ * below; rrtmg_sw_errstr_c gives the message the reference would `stop`
+ * with.  Outputs are fully overwritten.  The caller owns every array.  The
+ * library owns its device tables (rrtmg_sw_ini_c) and a reusable device
+ * workspace, released by rrtmg_sw_finalize_c.  Calls are serialised
+ * internally; one process drives one GPU.
+ */
+#ifndef RRTMG_SW_GB300_H
+#define RRTMG_SW_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Arguments of rrtmg_sw, in the order of rrtmg_sw_rad.f90:99-111
+ * (declarations :220-388).  Optional Fortran arguments (bndsolvar,
+ * indsolvar, solcycfrac) are nullable.  The eight extra output pointers are
+ * the direct/diffuse and UV/near-IR fluxes that spcvmc_sw computes but the
+ * reference driver keeps local (rrtmg_sw_rad.f90:810-820); each is
+ * (ncol,nlay+1) or NULL.  idelm selects delta-scaled (1, the reference's
+ * hard-coded value, rrtmg_sw_rad.f90:605) or unscaled (0) direct fluxes. */
+typedef struct rrtmg_sw_args {
+    int32_t ncol, nlay, icld, iaer;
+    const double *play, *plev, *tlay, *tlev, *tsfc;
+    const double *h2ovmr, *o3vmr, *co2vmr, *ch4vmr, *n2ovmr, *o2vmr;
+    const double *asdir, *asdif, *aldir, *aldif;
+    const double *coszen;
+    double adjes;
+    int32_t dyofyr;
+    double scon;
+    int32_t isolvar;
+    int32_t inflgsw, iceflgsw, liqflgsw;
+    const double *cldfmcl, *taucmcl, *ssacmcl, *asmcmcl, *fsfcmcl;   /* (ngpt,ncol,nlay) */
+    const double *ciwpmcl, *clwpmcl;                                  /* (ngpt,ncol,nlay) */
+    const double *reicmcl, *relqmcl;                                  /* (ncol,nlay) */
+    const double *tauaer, *ssaaer, *asmaer;                           /* (ncol,nlay,nbnd) */
+    const double *ecaer;                                              /* (ncol,nlay,6) */
+    double *swuflx, *swdflx, *swhr, *swuflxc, *swdflxc, *swhrc;
+    const double *bndsolvar;   /* (14) or NULL */
+    const double *indsolvar;   /* (2)  or NULL */
+    const double *solcycfrac;  /* scalar or NULL */
+    double *dirdflux, *difdflux, *uvdflx, *nidflx, *dirdnuv, *difdnuv, *dirdnir, *difdnir;
+    int32_t idelm;
+    int32_t nthreads;          /* unused by the GPU library (kept for layout) */
+} rrtmg_sw_args;
+
+/* Physical cloud inputs for the fused path: the arguments of
+ * mcica_subcol_sw (mcica_subcol_gen_sw.f90:181-185) that rrtmg_sw_mcica_c
+ * consumes on the device instead of the seven (ngpt,ncol,nlay) subcolumn
+ * arrays.  irng must be 0 (KISS, per-column streams) in the fused path. */
+typedef struct rrtmg_sw_clouds {
+    int32_t permuteseed, irng;
+    const double *cldfrac, *ciwp, *clwp, *rei, *rel;   /* (ncol,nlay) */
+    const double *tauc, *ssac, *asmc, *fsfc;           /* (nbnd,ncol,nlay), used when inflgsw = 0 */
+    const double *alpha;                               /* (ncol,nlay), icld = 4 or 5 (get_alpha) */
+} rrtmg_sw_clouds;
+
+/* Arithmetic form of the solve. */
+enum {
+    RRTMG_SW_FORM_FP64 = 0,    /* plain FP64, reference operation order */
+    RRTMG_SW_FORM_FP32 = 1     /* FP32 bulk, FP64 only in the reftra near-conservative
+                                  branch and the vrtqdr 1/(1-R*R) denominators */
+};
+
+enum {
+    RRTMG_SW_OK = 0,
+    RRTMG_SW_ENOTINIT = 1,     /* rrtmg_sw_ini_c not called */
+    RRTMG_SW_ETABLES = 2,      /* coefficient table file missing or corrupt */
+    RRTMG_SW_EARGS = 3,        /* bad sizes or NULL required pointer */
+    RRTMG_SW_ECUDA = 4,        /* CUDA runtime error (see rrtmg_sw_last_cuda_error_c) */
+    RRTMG_SW_EINFLAG1 = 10,    /* cldprmc:166  INFLAG = 1 OPTION NOT AVAILABLE WITH MCICA */
+    RRTMG_SW_EICERAD = 11,     /* cldprmc:183,204  ICE RADIUS OUT OF BOUNDS */
+    RRTMG_SW_EICEDGE = 12,     /* cldprmc:227  ICE GENERALIZED EFFECTIVE SIZE OUT OF BOUNDS */
+    RRTMG_SW_EICEPROP = 13,    /* cldprmc:196-260  ice optical property outside physical limits */
+    RRTMG_SW_ELIQRAD = 14,     /* cldprmc:273  LIQUID EFFECTIVE RADIUS OUT OF BOUNDS */
+    RRTMG_SW_ELIQPROP = 15,    /* cldprmc:290-294  liquid optical property outside physical limits */
+    RRTMG_SW_EICLD = 20,       /* mcica_subcol_gen_sw.f90:262-264  INVALID ICLD */
+    RRTMG_SW_EKISSSEED = 21,   /* mcica_subcol_gen_sw.f90:472-474  KISSVEC SEED GENERATOR REQUIRES
+                                  PMID FROM BOTTOM FOUR LAYERS */
+    RRTMG_SW_ELAYTROP = 30,    /* profile without layers on both sides of the ~100 hPa switch */
+    RRTMG_SW_EIRNG = 31        /* fused path requires irng = 0 */
+};
+
+/* rrtmg_sw_ini (rrtmg_sw_init.f90:47-173): load the 112-g-point tables
+ * (rrtmg_sw_tables.bin next to the library, or $RRTMG_SW_TABLES), build the
+ * transmittance lookup table and heatfac = grav*secdy/(cpdair*1e2)
+ * (rrtmg_sw_init.f90:258) and upload everything to the current GPU.
+ * Idempotent; a later call only changes cpdair. */
+int rrtmg_sw_ini_c(double cpdair);
+
+/* rrtmg_sw (rrtmg_sw_rad.f90:99-841) with host arrays: copies inputs to the
+ * device, solves every column, copies the outputs back.  icld outside 0..5
+ * becomes 2 and iaer outside {0,6,10} becomes 0 (rrtmg_sw_rad.f90:589,597;
+ * icld 4/5 are accepted). */
+int rrtmg_sw_c(const rrtmg_sw_args *a);
+
+/* Same, all array pointers are device pointers; work is queued on `stream`
+ * (a cudaStream_t, NULL = legacy default stream) and the call returns after
+ * the launch; the status of the device-side input checks is read back. */
+int rrtmg_sw_dev_c(const rrtmg_sw_args *a, void *stream);
+
+/* Fused McICA + rrtmg_sw: mcica_subcol_sw (mcica_subcol_gen_sw.f90:181-296)
+ * and rrtmg_sw in one pass; the subcolumn cloud masks are generated per
+ * (column, g-point) inside the solve and never stored.  a->cldfmcl ..
+ * a->clwpmcl are ignored; a->reicmcl/relqmcl are ignored too (c->rei, c->rel
+ * are used, as mcica_subcol_sw copies them).  Host / device variants. */
+int rrtmg_sw_mcica_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c);
+int rrtmg_sw_mcica_dev_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, void *stream);
+
+/* mcica_subcol_sw (mcica_subcol_gen_sw.f90:181-296), host arrays, outputs
+ * (ngpt,ncol,nlay) and (ncol,nlay).  irng = 0: KISS with per-column streams
+ * (seeded from the bottom four layer pressures, mcica:466-485); irng = 1:
+ * Mersenne Twister, one stream in (subcolumn, column, layer) order seeded
+ * with permuteseed.  icld 4/5 follow mcica_subcol_gen_sw.1col.f90:536-604. */
+int mcica_subcol_sw_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t permuteseed, int32_t irng,
+                      const double *play, const double *cldfrac, const double *ciwp,
+                      const double *clwp, const double *rei, const double *rel,
+                      const double *tauc, const double *ssac, const double *asmc,
+                      const double *fsfc, const double *alpha,
+                      double *cldfmcl, double *ciwpmcl, double *clwpmcl, double *reicmcl,
+                      double *relqmcl, double *taucmcl, double *ssacmcl, double *asmcmcl,
+                      double *fsfcmcl);
+
+/* get_alpha (mcica_subcol_gen_sw.f90:66-178), host arrays. */
+int get_alpha_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t idcor, double decorr_con,
+                const double *dz, const double *lat, int32_t juldat, const double *cldfrac,
+                double *alpha);
+
+/* Select the arithmetic form used by subsequent solves (default FP64). */
+int rrtmg_sw_set_form_c(int32_t form);
+int rrtmg_sw_get_form_c(void);
+
+/* Number of kernels the most recent solve launched (for launch accounting). */
+int rrtmg_sw_last_launch_count_c(void);
+
+/* Reference message for an error code; last CUDA error string. */
+const char *rrtmg_sw_errstr_c(int32_t code);
+const char *rrtmg_sw_last_cuda_error_c(void);
+
+/* Release the device tables and workspace (rrtmg_sw_ini_c may be called
+ * again afterwards). */
+int rrtmg_sw_finalize_c(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,694 @@
+// api.cu -- host side of the GB300 RRTMG_SW library: table loading and
+// upload (rrtmg_sw_ini), the per-call solar-source setup of inatm_sw, the
+// device workspace and the C-ABI entry points of include/rrtmg_sw_gb300.h.
+#include <dlfcn.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/rrtmg_sw_gb300.h"
+#include "launch.h"
+
+using namespace rrsw;
+
+namespace {
+
+const int kNG[14] = {6, 12, 8, 8, 10, 10, 2, 10, 8, 6, 6, 8, 6, 12};
+const int kNSPA[14] = {9, 9, 9, 9, 1, 9, 9, 1, 9, 1, 0, 1, 9, 1};  // rrtmg_sw_init.f90:194
+const int kNSPB[14] = {1, 5, 1, 1, 1, 5, 1, 0, 1, 0, 0, 1, 5, 1};  // rrtmg_sw_init.f90:195
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+struct State {
+    std::mutex mu;
+    bool init = false;
+    int device = 0, num_sms = 0;
+    DevTables tabs{};
+    std::vector<double> blob64;
+    double mgavgcyc[134], sbavgcyc[134];
+    double cpdair = 1.004e3;
+    DevBuf d_tab64, d_tab32, scratch, errw;
+    std::map<std::string, DevBuf> stage;  // host-API staging buffers
+    int* h_err = nullptr;                  // pinned
+    int form = RRTMG_SW_FORM_FP64;
+    int last_launches = 0;
+    std::string last_cuda;
+};
+
+State& S() {
+    static State s;
+    return s;
+}
+
+int cuda_fail(cudaError_t e) {
+    S().last_cuda = cudaGetErrorString(e);
+    return RRTMG_SW_ECUDA;
+}
+#define CK(x)                                 \
+    do {                                      \
+        cudaError_t e_ = (x);                 \
+        if (e_ != cudaSuccess) return cuda_fail(e_); \
+    } while (0)
+
+std::string table_path() {
+    if (const char* env = std::getenv("RRTMG_SW_TABLES")) return env;
+    Dl_info info;
+    if (dladdr((void*)&table_path, &info) && info.dli_fname) {
+        std::string so = info.dli_fname;
+        const std::string dir = so.substr(0, so.find_last_of('/'));
+        for (const char* rel : {"/rrtmg_sw_tables.bin", "/../data/rrtmg_sw_tables.bin", "/data/rrtmg_sw_tables.bin"}) {
+            const std::string p = dir + rel;
+            if (FILE* f = std::fopen(p.c_str(), "rb")) {
+                std::fclose(f);
+                return p;
+            }
+        }
+    }
+    return "rrtmg_sw_tables.bin";
+}
+
+bool read_tables(const std::string& path, std::map<std::string, std::vector<double>>& rec) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) return false;
+    char magic[8];
+    uint32_t n = 0;
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "RRSWTB01", 8) == 0 && std::fread(&n, 4, 1, f) == 1;
+    for (uint32_t r = 0; ok && r < n; ++r) {
+        char name[32];
+        uint32_t hdr[5];
+        uint64_t cnt;
+        ok = std::fread(name, 1, 32, f) == 32 && std::fread(hdr, 4, 5, f) == 5 && std::fread(&cnt, 8, 1, f) == 1;
+        if (!ok || cnt > (1u << 24)) { ok = false; break; }
+        std::vector<double> v(cnt);
+        ok = std::fread(v.data(), 8, cnt, f) == cnt;
+        name[31] = 0;
+        rec[name] = std::move(v);
+    }
+    std::fclose(f);
+    return ok;
+}
+
+// GF(2) matrix of the KISS xorshift y ^= y<<13; y ^= y>>17; y ^= y<<5
+uint32_t xs_step(uint32_t y) {
+    y ^= y << 13;
+    y ^= y >> 17;
+    y ^= y << 5;
+    return y;
+}
+
+// Build the table blob: absorption tables transposed to [ind][ig].
+int build_tables(State& st) {
+    std::map<std::string, std::vector<double>> rec;
+    if (!read_tables(table_path(), rec)) return RRTMG_SW_ETABLES;
+    auto has = [&](const std::string& k) { return rec.count(k) && !rec[k].empty(); };
+    std::vector<double>& B = st.blob64;
+    B.clear();
+    auto put = [&](const std::vector<double>& v) {
+        const int off = (int)B.size();
+        B.insert(B.end(), v.begin(), v.end());
+        return off;
+    };
+    auto put_T = [&](const std::vector<double>& v, int ng) {  // (nind, ng) Fortran -> [ind][ig]
+        const int off = (int)B.size();
+        const size_t nind = v.size() / ng;
+        for (size_t ind = 0; ind < nind; ++ind)
+            for (int ig = 0; ig < ng; ++ig) B.push_back(v[ind + nind * ig]);
+        return off;
+    };
+    DevTables& T = st.tabs;
+    std::memset(&T, 0, sizeof(T));
+    int g0 = 0;
+    for (int ib = 0; ib < 14; ++ib) {
+        const std::string p = "b" + std::to_string(ib + 16) + ".";
+        BandOff& b = T.b[ib];
+        b.ng = kNG[ib];
+        b.g0 = g0;
+        b.nspa = kNSPA[ib];
+        b.nspb = kNSPB[ib];
+        for (int g = 0; g < b.ng; ++g) {
+            T.ngb[g0 + g] = (int8_t)ib;
+            T.gib[g0 + g] = (uint8_t)(g + 1);
+        }
+        g0 += b.ng;
+        if (!has(p + "sfluxref")) return RRTMG_SW_ETABLES;
+        b.absa = has(p + "ka") ? put_T(rec[p + "ka"], b.ng) : -1;
+        b.absb = has(p + "kb") ? put_T(rec[p + "kb"], b.ng) : -1;
+        b.selfref = has(p + "selfref") ? put_T(rec[p + "selfref"], b.ng) : -1;
+        b.forref = has(p + "forref") ? put_T(rec[p + "forref"], b.ng) : -1;
+        b.nfr = has(p + "forref") ? (int)(rec[p + "forref"].size() / b.ng) : 0;
+        b.sfluxref = put(rec[p + "sfluxref"]);
+        b.irradnce = put(rec[p + "irradnce"]);
+        b.facbrght = put(rec[p + "facbrght"]);
+        b.snsptdrk = put(rec[p + "snsptdrk"]);
+        b.rayl = has(p + "rayl") ? put(rec[p + "rayl"]) : -1;
+        b.rayla = has(p + "rayla") ? put(rec[p + "rayla"]) : -1;
+        b.raylb = has(p + "raylb") ? put(rec[p + "raylb"]) : -1;
+        b.abso3a = has(p + "abso3a") ? put(rec[p + "abso3a"]) : -1;
+        b.abso3b = has(p + "abso3b") ? put(rec[p + "abso3b"]) : -1;
+        b.absch4 = has(p + "absch4") ? put(rec[p + "absch4"]) : -1;
+        b.absco2 = has(p + "absco2") ? put(rec[p + "absco2"]) : -1;
+        b.absh2o = has(p + "absh2o") ? put(rec[p + "absh2o"]) : -1;
+    }
+    const char* names[] = {"pref", "preflog", "tref", "extliq1", "ssaliq1", "asyliq1", "extice2", "ssaice2",
+                           "asyice2", "extice3", "ssaice3", "asyice3", "fdlice3", "abari", "bbari", "cbari",
+                           "dbari", "ebari", "fbari", "rsrtaua", "rsrpiza", "rsrasya", "wavenum2", "mgavgcyc",
+                           "sbavgcyc"};
+    for (const char* nm : names)
+        if (!has(nm)) return RRTMG_SW_ETABLES;
+    T.pref = put(rec["pref"]);
+    T.preflog = put(rec["preflog"]);
+    T.tref = put(rec["tref"]);
+    T.extliq1 = put(rec["extliq1"]); T.ssaliq1 = put(rec["ssaliq1"]); T.asyliq1 = put(rec["asyliq1"]);
+    T.extice2 = put(rec["extice2"]); T.ssaice2 = put(rec["ssaice2"]); T.asyice2 = put(rec["asyice2"]);
+    T.extice3 = put(rec["extice3"]); T.ssaice3 = put(rec["ssaice3"]); T.asyice3 = put(rec["asyice3"]);
+    T.fdlice3 = put(rec["fdlice3"]);
+    T.abari = put(rec["abari"]); T.bbari = put(rec["bbari"]); T.cbari = put(rec["cbari"]);
+    T.dbari = put(rec["dbari"]); T.ebari = put(rec["ebari"]); T.fbari = put(rec["fbari"]);
+    T.rsrtaua = put(rec["rsrtaua"]); T.rsrpiza = put(rec["rsrpiza"]); T.rsrasya = put(rec["rsrasya"]);
+    T.wavenum2 = put(rec["wavenum2"]);
+    std::memcpy(st.mgavgcyc, rec["mgavgcyc"].data(), sizeof(st.mgavgcyc));
+    std::memcpy(st.sbavgcyc, rec["sbavgcyc"].data(), sizeof(st.sbavgcyc));
+    // exp_tbl (rrtmg_sw_init.f90:115-123)
+    std::vector<double> et(NTBL + 1);
+    const double expeps = 1.e-20, pade = 0.278;
+    T.bpade = 1.0 / pade;
+    et[0] = 1.0;
+    et[NTBL] = expeps;
+    for (int itr = 1; itr <= NTBL - 1; ++itr) {
+        const double tfn = (double)itr / (double)NTBL;
+        const double tau_tbl = T.bpade * tfn / (1.0 - tfn);
+        et[itr] = std::exp(-tau_tbl);
+        if (et[itr] <= expeps) et[itr] = expeps;
+    }
+    T.exp_tbl = put(et);
+    T.total = (int)B.size();
+    T.oneminus = 1.0 - 1.e-06;  // rrtmg_sw_rad.f90:563-565
+    // xorshift jump matrices
+    for (int j = 0; j < 32; ++j) T.xs_jump[0][j] = xs_step(1u << j);
+    for (int k = 1; k < 32; ++k)
+        for (int j = 0; j < 32; ++j) {
+            uint32_t y = T.xs_jump[k - 1][j], r = 0;
+            for (int b = 0; b < 32; ++b)
+                if (y >> b & 1u) r ^= T.xs_jump[k - 1][b];
+            T.xs_jump[k][j] = r;
+        }
+    return RRTMG_SW_OK;
+}
+
+int upload(State& st) {
+    DevTables& T = st.tabs;
+    const double grav = 9.8066, secdy = 8.6400e4;  // rrtmg_sw_init.f90:207-243
+    T.heatfac = grav * secdy / (st.cpdair * 1.e2);   // rrtmg_sw_init.f90:258
+    CK(st.d_tab64.ensure(st.blob64.size() * sizeof(double)));
+    CK(cudaMemcpy(st.d_tab64.p, st.blob64.data(), st.blob64.size() * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<float> b32(st.blob64.begin(), st.blob64.end());
+    CK(st.d_tab32.ensure(b32.size() * sizeof(float)));
+    CK(cudaMemcpy(st.d_tab32.p, b32.data(), b32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(upload_tables_fp64(T));
+    CK(upload_tables_fp32(T));
+    return RRTMG_SW_OK;
+}
+
+// earth_sun (rrtmg_sw_rad.f90:844-868)
+double earth_sun(int idn) {
+    const double pi = 2.0 * std::asin(1.0);
+    const double gamma = 2.0 * pi * (idn - 1) / 365.0;
+    return 1.000110 + .034221 * std::cos(gamma) + .001289 * std::sin(gamma) + .000719 * std::cos(2.0 * gamma) +
+           .000077 * std::sin(2.0 * gamma);
+}
+
+// Per-call solar variability and Earth-Sun scaling of inatm_sw
+// (rrtmg_sw_rad.f90:1245-1512): scalars of the call, not of a column.
+void solar_setup(const State& st, const rrtmg_sw_args* a, SolveParams& P) {
+    const double Iint = 1360.37, Fint = 0.996047, Sint = -0.511590;
+    const double Foffset = 0.14959542, Soffset = 0.00066696;
+    const double favg = 0.1567652, savg = 902.71260;
+    const double cmin = 0.0189, cmax = 0.3750, dmin2max = 0.3561, dmax2min = 0.6439;
+    const double rrsw_scon = 1.36822e+03;
+    const int isolvar = a->isolvar;
+    double solvar[14];
+    for (int i = 0; i < 14; ++i) {
+        solvar[i] = 1.0;
+        P.svar_f_bnd[i] = P.svar_s_bnd[i] = P.svar_i_bnd[i] = 1.0;
+    }
+    P.isolvar = isolvar;
+    P.svar_f = P.svar_s = P.svar_i = 1.0;
+    double scl[2] = {1.0, 1.0}, ndx[2] = {favg, savg}, scf = 0.0;
+    if (isolvar == 1 && a->indsolvar && a->solcycfrac) {
+        scf = *a->solcycfrac;
+        const double* iv = a->indsolvar;
+        if (iv[0] != 1.0 || iv[1] != 1.0) {
+            if (scf >= 0.0 && scf < cmin) {
+                const double w = (scf + 1.0 - cmax) / dmax2min;
+                scl[0] = iv[0] + w * (1.0 - iv[0]);
+                scl[1] = iv[1] + w * (1.0 - iv[1]);
+            }
+            if (scf >= cmin && scf <= cmax) {
+                const double w = (scf - cmin) / dmin2max;
+                scl[0] = 1.0 + w * (iv[0] - 1.0);
+                scl[1] = 1.0 + w * (iv[1] - 1.0);
+            }
+            if (scf > cmax && scf <= 1.0) {
+                const double w = (scf - cmax) / dmax2min;
+                scl[0] = iv[0] + w * (1.0 - iv[0]);
+                scl[1] = iv[1] + w * (1.0 - iv[1]);
+            }
+        }
+    }
+    if (isolvar == 2 && a->indsolvar) { ndx[0] = a->indsolvar[0]; ndx[1] = a->indsolvar[1]; }
+    double adjflx = a->adjes;
+    if (a->dyofyr > 0) adjflx = earth_sun(a->dyofyr);
+    auto cycle = [&](double& f0, double& s0) {  // mean solar cycle lookup (:1329-1359)
+        const int nf = 134;
+        if (scf <= 0.0) { f0 = st.mgavgcyc[0]; s0 = st.sbavgcyc[0]; return; }
+        if (scf >= 1.0) { f0 = st.mgavgcyc[nf - 1]; s0 = st.sbavgcyc[nf - 1]; return; }
+        const double il = 1.0 / (nf - 2), ih = 0.5 * il;
+        int sfid = 1;
+        double lo = 0.0, hi = ih;
+        if (scf > ih && scf < 1.0 - ih) {
+            sfid = (int)std::floor((scf - ih) * (nf - 2)) + 2;
+            lo = (sfid - 2) * il + ih;
+            hi = lo + il;
+        }
+        if (scf >= 1.0 - ih) { sfid = (nf - 2) + 1; lo = 1.0 - ih; hi = 1.0; }
+        const double fr = (scf - lo) / (hi - lo);
+        f0 = st.mgavgcyc[sfid - 1] + fr * (st.mgavgcyc[sfid] - st.mgavgcyc[sfid - 1]);
+        s0 = st.sbavgcyc[sfid - 1] + fr * (st.sbavgcyc[sfid] - st.sbavgcyc[sfid - 1]);
+    };
+    const double scon = a->scon;
+    if (scon == 0.0) {
+        if (isolvar == -1)
+            for (int i = 0; i < 14; ++i) solvar[i] = a->bndsolvar ? a->bndsolvar[i] : 1.0;
+        if (isolvar == 1) {
+            double f0, s0;
+            cycle(f0, s0);
+            P.svar_f = scl[0] * (f0 - Foffset) / (favg - Foffset);
+            P.svar_s = scl[1] * (s0 - Soffset) / (savg - Soffset);
+        }
+        if (isolvar == 2) {
+            P.svar_f = (ndx[0] - Foffset) / (favg - Foffset);
+            P.svar_s = (ndx[1] - Soffset) / (savg - Soffset);
+        }
+        if (isolvar == 3)
+            for (int i = 0; i < 14; ++i) {
+                solvar[i] = a->bndsolvar ? a->bndsolvar[i] : 1.0;
+                P.svar_f_bnd[i] = P.svar_s_bnd[i] = P.svar_i_bnd[i] = solvar[i];
+            }
+    }
+    if (scon > 0.0) {
+        if (isolvar == -1)
+            for (int i = 0; i < 14; ++i) solvar[i] = a->bndsolvar ? a->bndsolvar[i] * scon / rrsw_scon : scon / rrsw_scon;
+        if (isolvar == 0) {
+            const double r = scon / (Fint + Sint + Iint);
+            P.svar_f = P.svar_s = P.svar_i = r;
+        }
+        if (isolvar == 1) {
+            double f0, s0;
+            cycle(f0, s0);
+            P.svar_i = (scon - (scl[0] * Fint + scl[1] * Sint)) / Iint;
+            P.svar_f = scl[0] * (f0 - Foffset) / (favg - Foffset);
+            P.svar_s = scl[1] * (s0 - Soffset) / (savg - Soffset);
+        }
+        if (isolvar == 3) {
+            const double c = Fint + Sint + Iint;
+            for (int i = 0; i < 14; ++i) {
+                solvar[i] = a->bndsolvar ? a->bndsolvar[i] * scon / c : scon / c;
+                P.svar_f_bnd[i] = P.svar_s_bnd[i] = P.svar_i_bnd[i] = solvar[i];
+            }
+        }
+    }
+    for (int i = 0; i < 14; ++i) P.adjflux[i] = isolvar < 0 ? adjflx * solvar[i] : adjflx;
+}
+
+int check_args(const rrtmg_sw_args* a) {
+    if (!a || a->ncol <= 0 || a->nlay < 4 || a->nlay > MAX_NLAY) return RRTMG_SW_EARGS;
+    const double* req[] = {a->play, a->plev, a->tlay, a->h2ovmr, a->o3vmr, a->co2vmr, a->ch4vmr, a->o2vmr,
+                           a->asdir, a->asdif, a->aldir, a->aldif, a->coszen};
+    for (const double* p : req)
+        if (!p) return RRTMG_SW_EARGS;
+    if (!a->swuflx || !a->swdflx || !a->swhr || !a->swuflxc || !a->swdflxc || !a->swhrc) return RRTMG_SW_EARGS;
+    return RRTMG_SW_OK;
+}
+
+// Fill SolveParams from args whose pointers are device pointers.
+int make_params(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, SolveParams& P) {
+    std::memset(&P, 0, sizeof(P));
+    P.ncol = a->ncol;
+    P.nlay = a->nlay;
+    P.icld = (a->icld < 0 || a->icld > 5) ? 2 : a->icld;   // rrtmg_sw_rad.f90:589 (4/5 accepted)
+    P.iaer = (a->iaer != 0 && a->iaer != 6 && a->iaer != 10) ? 0 : a->iaer;  // :597
+    P.idelm = a->idelm == 0 ? 0 : 1;
+    P.inflag = a->inflgsw;
+    P.iceflag = a->iceflgsw;
+    P.liqflag = a->liqflgsw;
+    P.fused = c ? 1 : 0;
+    P.extra = (a->dirdflux || a->difdflux || a->uvdflx || a->nidflx || a->dirdnuv || a->difdnuv || a->dirdnir ||
+               a->difdnir) ? 1 : 0;
+    P.npairs = (a->ncol + COLS_PER_CTA - 1) / COLS_PER_CTA;
+    solar_setup(st, a, P);
+    P.play = a->play; P.plev = a->plev; P.tlay = a->tlay;
+    P.h2ovmr = a->h2ovmr; P.o3vmr = a->o3vmr; P.co2vmr = a->co2vmr; P.ch4vmr = a->ch4vmr; P.o2vmr = a->o2vmr;
+    P.asdir = a->asdir; P.asdif = a->asdif; P.aldir = a->aldir; P.aldif = a->aldif; P.coszen = a->coszen;
+    if (P.icld >= 1 && !c) {
+        P.cldfmcl = a->cldfmcl; P.taucmcl = a->taucmcl; P.ssacmcl = a->ssacmcl; P.asmcmcl = a->asmcmcl;
+        P.fsfcmcl = a->fsfcmcl; P.ciwpmcl = a->ciwpmcl; P.clwpmcl = a->clwpmcl;
+        P.reicmcl = a->reicmcl; P.relqmcl = a->relqmcl;
+        if (!P.cldfmcl || !P.taucmcl || !P.ssacmcl || !P.asmcmcl || !P.fsfcmcl || !P.ciwpmcl || !P.clwpmcl ||
+            !P.reicmcl || !P.relqmcl)
+            return RRTMG_SW_EARGS;
+    }
+    if (c && P.icld >= 1) {
+        if (c->irng != 0) return RRTMG_SW_EIRNG;
+        P.permuteseed = c->permuteseed;
+        P.cldfrac = c->cldfrac; P.ciwp = c->ciwp; P.clwp = c->clwp; P.rei = c->rei; P.rel = c->rel;
+        P.tauc = c->tauc; P.ssac = c->ssac; P.asmc = c->asmc; P.fsfc = c->fsfc; P.alpha = c->alpha;
+        if (!P.cldfrac || !P.ciwp || !P.clwp || !P.rei || !P.rel) return RRTMG_SW_EARGS;
+        if (P.inflag == 0 && (!P.tauc || !P.ssac || !P.asmc || !P.fsfc)) return RRTMG_SW_EARGS;
+        if (P.icld >= 4 && !P.alpha) return RRTMG_SW_EARGS;
+    }
+    if (P.iaer == 10) {
+        P.tauaer = a->tauaer; P.ssaaer = a->ssaaer; P.asmaer = a->asmaer;
+        if (!P.tauaer || !P.ssaaer || !P.asmaer) return RRTMG_SW_EARGS;
+    }
+    if (P.iaer == 6) {
+        P.ecaer = a->ecaer;
+        if (!P.ecaer) return RRTMG_SW_EARGS;
+    }
+    P.swuflx = a->swuflx; P.swdflx = a->swdflx; P.swhr = a->swhr;
+    P.swuflxc = a->swuflxc; P.swdflxc = a->swdflxc; P.swhrc = a->swhrc;
+    double* xo[8] = {a->dirdflux, a->difdflux, a->uvdflx, a->nidflx, a->dirdnuv, a->difdnuv, a->dirdnir, a->difdnir};
+    for (int i = 0; i < 8; ++i) P.xout[i] = xo[i];
+    return RRTMG_SW_OK;
+}
+
+// Queue one solve on `s`; returns after reading back the device error word.
+int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s) {
+    SolveParams P;
+    int rc = make_params(st, a, c, P);
+    if (rc) return rc;
+    CK(st.errw.ensure(sizeof(int)));
+    P.err = (int*)st.errw.p;
+    const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
+    LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms) : plan_fp64(P, st.num_sms);
+    P.slot_elems = slot_elems(P.nlay, P.idelm);
+    const size_t esz = fp32 ? sizeof(float) : sizeof(double);
+    CK(st.scratch.ensure((size_t)li.grid * P.slot_elems * esz));
+    P.scratch = st.scratch.p;
+    CK(cudaMemsetAsync(P.err, 0, sizeof(int), s));
+    if (fp32) CK(launch_solve_fp32(P, (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, li, s));
+    else CK(launch_solve_fp64(P, (const double*)st.d_tab64.p, li, s));
+    st.last_launches = 1;
+    CK(cudaMemcpyAsync(st.h_err, P.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return *st.h_err;
+}
+
+// Host-array path: stage every array in a named device buffer.
+struct Stager {
+    State& st;
+    cudaStream_t s;
+    cudaError_t err = cudaSuccess;
+    template <typename T>
+    T* in(const char* name, const T* h, size_t n) {
+        if (!h || err != cudaSuccess) return nullptr;
+        DevBuf& b = st.stage[name];
+        if ((err = b.ensure(n * sizeof(T))) != cudaSuccess) return nullptr;
+        err = cudaMemcpyAsync(b.p, h, n * sizeof(T), cudaMemcpyHostToDevice, s);
+        return (T*)b.p;
+    }
+    double* out(const char* name, double* h, size_t n) {
+        if (!h || err != cudaSuccess) return nullptr;
+        DevBuf& b = st.stage[name];
+        if ((err = b.ensure(n * sizeof(double))) != cudaSuccess) return nullptr;
+        return (double*)b.p;
+    }
+    void back(double* h, const double* d, size_t n) {
+        if (h && d && err == cudaSuccess) err = cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, s);
+    }
+};
+
+int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    if (!st.init) return RRTMG_SW_ENOTINIT;
+    int rc = check_args(a);
+    if (rc) return rc;
+    const size_t C = a->ncol, L = a->nlay, CL = C * L, CL1 = C * (L + 1), G = (size_t)NGPT * CL;
+    cudaStream_t s = 0;
+    Stager sg{st, s};
+    rrtmg_sw_args d = *a;
+    d.play = sg.in("play", a->play, CL); d.plev = sg.in("plev", a->plev, CL1); d.tlay = sg.in("tlay", a->tlay, CL);
+    d.tlev = nullptr; d.tsfc = nullptr; d.n2ovmr = nullptr;  // dead inputs in the SW solve
+    d.h2ovmr = sg.in("h2o", a->h2ovmr, CL); d.o3vmr = sg.in("o3", a->o3vmr, CL); d.co2vmr = sg.in("co2", a->co2vmr, CL);
+    d.ch4vmr = sg.in("ch4", a->ch4vmr, CL); d.o2vmr = sg.in("o2", a->o2vmr, CL);
+    d.asdir = sg.in("asdir", a->asdir, C); d.asdif = sg.in("asdif", a->asdif, C);
+    d.aldir = sg.in("aldir", a->aldir, C); d.aldif = sg.in("aldif", a->aldif, C);
+    d.coszen = sg.in("coszen", a->coszen, C);
+    const int icld = (a->icld < 0 || a->icld > 5) ? 2 : a->icld;
+    if (icld >= 1 && !c) {
+        d.cldfmcl = sg.in("cldfmcl", a->cldfmcl, G); d.taucmcl = sg.in("taucmcl", a->taucmcl, G);
+        d.ssacmcl = sg.in("ssacmcl", a->ssacmcl, G); d.asmcmcl = sg.in("asmcmcl", a->asmcmcl, G);
+        d.fsfcmcl = sg.in("fsfcmcl", a->fsfcmcl, G); d.ciwpmcl = sg.in("ciwpmcl", a->ciwpmcl, G);
+        d.clwpmcl = sg.in("clwpmcl", a->clwpmcl, G);
+        d.reicmcl = sg.in("reicmcl", a->reicmcl, CL); d.relqmcl = sg.in("relqmcl", a->relqmcl, CL);
+    }
+    rrtmg_sw_clouds dc{};
+    if (c) {
+        dc = *c;
+        dc.cldfrac = sg.in("cldfrac", c->cldfrac, CL); dc.ciwp = sg.in("ciwp", c->ciwp, CL);
+        dc.clwp = sg.in("clwp", c->clwp, CL); dc.rei = sg.in("rei", c->rei, CL); dc.rel = sg.in("rel", c->rel, CL);
+        dc.tauc = sg.in("tauc", c->tauc, 14 * CL); dc.ssac = sg.in("ssac", c->ssac, 14 * CL);
+        dc.asmc = sg.in("asmc", c->asmc, 14 * CL); dc.fsfc = sg.in("fsfc", c->fsfc, 14 * CL);
+        dc.alpha = sg.in("alpha", c->alpha, CL);
+    }
+    const int iaer = a->iaer;
+    if (iaer == 10) {
+        d.tauaer = sg.in("tauaer", a->tauaer, 14 * CL); d.ssaaer = sg.in("ssaaer", a->ssaaer, 14 * CL);
+        d.asmaer = sg.in("asmaer", a->asmaer, 14 * CL);
+    }
+    if (iaer == 6) d.ecaer = sg.in("ecaer", a->ecaer, 6 * CL);
+    d.swuflx = sg.out("swuflx", a->swuflx, CL1); d.swdflx = sg.out("swdflx", a->swdflx, CL1);
+    d.swuflxc = sg.out("swuflxc", a->swuflxc, CL1); d.swdflxc = sg.out("swdflxc", a->swdflxc, CL1);
+    d.swhr = sg.out("swhr", a->swhr, CL); d.swhrc = sg.out("swhrc", a->swhrc, CL);
+    const char* xn[8] = {"x0", "x1", "x2", "x3", "x4", "x5", "x6", "x7"};
+    double* xh[8] = {a->dirdflux, a->difdflux, a->uvdflx, a->nidflx, a->dirdnuv, a->difdnuv, a->dirdnir, a->difdnir};
+    double* xd[8];
+    for (int i = 0; i < 8; ++i) xd[i] = sg.out(xn[i], xh[i], CL1);
+    d.dirdflux = xd[0]; d.difdflux = xd[1]; d.uvdflx = xd[2]; d.nidflx = xd[3];
+    d.dirdnuv = xd[4]; d.difdnuv = xd[5]; d.dirdnir = xd[6]; d.difdnir = xd[7];
+    if (sg.err != cudaSuccess) return cuda_fail(sg.err);
+    rc = solve_dev(st, &d, c ? &dc : nullptr, s);
+    if (rc) return rc;
+    sg.back(a->swuflx, d.swuflx, CL1); sg.back(a->swdflx, d.swdflx, CL1);
+    sg.back(a->swuflxc, d.swuflxc, CL1); sg.back(a->swdflxc, d.swdflxc, CL1);
+    sg.back(a->swhr, d.swhr, CL); sg.back(a->swhrc, d.swhrc, CL);
+    for (int i = 0; i < 8; ++i) sg.back(xh[i], xd[i], CL1);
+    if (sg.err != cudaSuccess) return cuda_fail(sg.err);
+    CK(cudaStreamSynchronize(s));
+    return RRTMG_SW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rrtmg_sw_ini_c(double cpdair) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    st.cpdair = cpdair;
+    if (!st.init) {
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        st.device = dev;
+        CK(cudaDeviceGetAttribute(&st.num_sms, cudaDevAttrMultiProcessorCount, dev));
+        const int rc = build_tables(st);
+        if (rc) return rc;
+        CK(cudaMallocHost((void**)&st.h_err, sizeof(int)));
+    }
+    const int rc = upload(st);
+    if (rc) return rc;
+    st.init = true;
+    return RRTMG_SW_OK;
+}
+
+int rrtmg_sw_c(const rrtmg_sw_args* a) { return solve_host(a, nullptr); }
+
+int rrtmg_sw_mcica_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c) {
+    if (!c) return RRTMG_SW_EARGS;
+    return solve_host(a, c);
+}
+
+int rrtmg_sw_dev_c(const rrtmg_sw_args* a, void* stream) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    if (!st.init) return RRTMG_SW_ENOTINIT;
+    const int rc = check_args(a);
+    if (rc) return rc;
+    return solve_dev(st, a, nullptr, (cudaStream_t)stream);
+}
+
+int rrtmg_sw_mcica_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, void* stream) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (!c) return RRTMG_SW_EARGS;
+    const int rc = check_args(a);
+    if (rc) return rc;
+    return solve_dev(st, a, c, (cudaStream_t)stream);
+}
+
+int mcica_subcol_sw_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t permuteseed, int32_t irng,
+                      const double* play, const double* cldfrac, const double* ciwp, const double* clwp,
+                      const double* rei, const double* rel, const double* tauc, const double* ssac,
+                      const double* asmc, const double* fsfc, const double* alpha, double* cldfmcl,
+                      double* ciwpmcl, double* clwpmcl, double* reicmcl, double* relqmcl, double* taucmcl,
+                      double* ssacmcl, double* asmcmcl, double* fsfcmcl) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (icld == 0) return RRTMG_SW_OK;                 // mcica:261
+    if (icld < 0 || icld > 5) return RRTMG_SW_EICLD;    // mcica:262-264
+    if (ncol <= 0 || nlay < 4 || !play || !cldfrac || !ciwp || !clwp || !rei || !rel) return RRTMG_SW_EARGS;
+    if (icld >= 4 && !alpha) return RRTMG_SW_EARGS;
+    if (irng != 0) irng = 1;                            // mcica:455
+    const size_t C = ncol, L = nlay, CL = C * L, G = (size_t)NGPT * CL;
+    cudaStream_t s = 0;
+    Stager sg{st, s};
+    const double* d_play = sg.in("m_play", play, CL);
+    const double* d_cf = sg.in("m_cf", cldfrac, CL);
+    const double* d_ciwp = sg.in("m_ciwp", ciwp, CL);
+    const double* d_clwp = sg.in("m_clwp", clwp, CL);
+    const double* d_tauc = sg.in("m_tauc", tauc, 14 * CL);
+    const double* d_ssac = sg.in("m_ssac", ssac, 14 * CL);
+    const double* d_asmc = sg.in("m_asmc", asmc, 14 * CL);
+    const double* d_fsfc = sg.in("m_fsfc", fsfc, 14 * CL);
+    const double* d_alpha = sg.in("m_alpha", alpha, CL);
+    double* o[7];
+    double* h[7] = {cldfmcl, ciwpmcl, clwpmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl};
+    const char* on[7] = {"mo0", "mo1", "mo2", "mo3", "mo4", "mo5", "mo6"};
+    for (int i = 0; i < 7; ++i) {
+        if (!h[i]) return RRTMG_SW_EARGS;
+        o[i] = sg.out(on[i], h[i], G);
+    }
+    if (sg.err != cudaSuccess) return cuda_fail(sg.err);
+    if (!d_tauc || !d_ssac || !d_asmc || !d_fsfc) d_tauc = d_ssac = d_asmc = d_fsfc = nullptr;
+    CK(st.errw.ensure(sizeof(int)));
+    CK(cudaMemsetAsync(st.errw.p, 0, sizeof(int), s));
+    if (irng == 0) {
+        CK(launch_mcica_kiss(ncol, nlay, icld, permuteseed, d_play, d_cf, d_ciwp, d_clwp, d_tauc, d_ssac, d_asmc,
+                             d_fsfc, d_alpha, o[0], o[1], o[2], o[3], o[4], o[5], o[6], (int*)st.errw.p, s));
+        st.last_launches = 1;
+    } else {
+        const size_t nr = (icld >= 4 ? 2 : 1) * (icld == 3 ? (size_t)NGPT * C : G);
+        DevBuf& rs = st.stage["m_stream"];
+        CK(rs.ensure(nr * sizeof(double)));
+        CK(launch_mt_stream(permuteseed, nr, (double*)rs.p, s));
+        CK(launch_mcica_stream(ncol, nlay, icld, (const double*)rs.p, d_cf, d_ciwp, d_clwp, d_tauc, d_ssac, d_asmc,
+                               d_fsfc, d_alpha, o[0], o[1], o[2], o[3], o[4], o[5], o[6], s));
+        st.last_launches = 2;
+    }
+    CK(cudaMemcpyAsync(st.h_err, st.errw.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    for (int i = 0; i < 7; ++i) sg.back(h[i], o[i], G);
+    if (sg.err != cudaSuccess) return cuda_fail(sg.err);
+    CK(cudaStreamSynchronize(s));
+    if (*st.h_err) return *st.h_err;
+    // reicmcl/relqmcl are plain copies (mcica:268-269)
+    if (reicmcl) std::memcpy(reicmcl, rei, CL * sizeof(double));
+    if (relqmcl) std::memcpy(relqmcl, rel, CL * sizeof(double));
+    return RRTMG_SW_OK;
+}
+
+int get_alpha_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t idcor, double decorr_con, const double* dz,
+                const double* lat, int32_t juldat, const double* cldfrac, double* alpha) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (ncol <= 0 || nlay < 1 || !dz || !lat || !cldfrac || !alpha) return RRTMG_SW_EARGS;
+    const size_t CL = (size_t)ncol * nlay;
+    cudaStream_t s = 0;
+    Stager sg{st, s};
+    const double* d_dz = sg.in("a_dz", dz, CL);
+    const double* d_lat = sg.in("a_lat", lat, (size_t)ncol);
+    const double* d_cf = sg.in("a_cf", cldfrac, CL);
+    double* d_al = sg.in("a_alpha", alpha, CL);  // alpha(:,:) keeps input values where not set
+    if (sg.err != cudaSuccess) return cuda_fail(sg.err);
+    CK(launch_get_alpha(ncol, nlay, icld, idcor, decorr_con, d_dz, d_lat, juldat, d_cf, d_al, s));
+    st.last_launches = 1;
+    sg.back(alpha, d_al, CL);
+    if (sg.err != cudaSuccess) return cuda_fail(sg.err);
+    CK(cudaStreamSynchronize(s));
+    return RRTMG_SW_OK;
+}
+
+int rrtmg_sw_set_form_c(int32_t form) {
+    if (form != RRTMG_SW_FORM_FP64 && form != RRTMG_SW_FORM_FP32) return RRTMG_SW_EARGS;
+    S().form = form;
+    return RRTMG_SW_OK;
+}
+
+int rrtmg_sw_get_form_c(void) { return S().form; }
+
+int rrtmg_sw_last_launch_count_c(void) { return S().last_launches; }
+
+const char* rrtmg_sw_errstr_c(int32_t code) {
+    switch (code) {
+    case RRTMG_SW_OK: return "OK";
+    case RRTMG_SW_ENOTINIT: return "RRTMG_SW_INI NOT CALLED";
+    case RRTMG_SW_ETABLES: return "COEFFICIENT TABLE FILE MISSING OR CORRUPT";
+    case RRTMG_SW_EARGS: return "INVALID ARGUMENTS";
+    case RRTMG_SW_ECUDA: return "CUDA ERROR";
+    case RRTMG_SW_EINFLAG1: return "INFLAG = 1 OPTION NOT AVAILABLE WITH MCICA";
+    case RRTMG_SW_EICERAD: return "ICE RADIUS OUT OF BOUNDS";
+    case RRTMG_SW_EICEDGE: return "ICE GENERALIZED EFFECTIVE SIZE OUT OF BOUNDS";
+    case RRTMG_SW_EICEPROP: return "ICE OPTICAL PROPERTY OUT OF PHYSICAL LIMITS";
+    case RRTMG_SW_ELIQRAD: return "LIQUID EFFECTIVE RADIUS OUT OF BOUNDS";
+    case RRTMG_SW_ELIQPROP: return "LIQUID OPTICAL PROPERTY OUT OF PHYSICAL LIMITS";
+    case RRTMG_SW_EICLD: return "MCICA_SUBCOL: INVALID ICLD";
+    case RRTMG_SW_EKISSSEED: return "MCICA_SUBCOL: KISSVEC SEED GENERATOR REQUIRES PMID FROM BOTTOM FOUR LAYERS.";
+    case RRTMG_SW_ELAYTROP: return "PROFILE MUST HAVE LAYERS ON BOTH SIDES OF THE 100 HPA SWITCH";
+    case RRTMG_SW_EIRNG: return "FUSED MCICA REQUIRES IRNG = 0";
+    default: return "UNKNOWN ERROR";
+    }
+}
+
+const char* rrtmg_sw_last_cuda_error_c(void) { return S().last_cuda.c_str(); }
+
+int rrtmg_sw_finalize_c(void) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    st.d_tab64.release();
+    st.d_tab32.release();
+    st.scratch.release();
+    st.errw.release();
+    for (auto& kv : st.stage) kv.second.release();
+    st.stage.clear();
+    if (st.h_err) cudaFreeHost(st.h_err);
+    st.h_err = nullptr;
+    st.init = false;
+    return RRTMG_SW_OK;
+}
+
+}  // extern "C"

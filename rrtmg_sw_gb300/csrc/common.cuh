@@ -1,0 +1,61 @@
+// common.cuh -- device-side tables and shared definitions of the GB300
+// RRTMG_SW solver.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rrsw {
+
+constexpr int NBND = 14;
+constexpr int NGPT = 112;
+constexpr int NTBL = 10000;
+constexpr int COLS_PER_CTA = 2;                  // 2 columns x 112 g-points = 7 warps
+constexpr int CTA_THREADS = COLS_PER_CTA * NGPT;  // 224
+constexpr int MAX_NLAY = 1000;
+
+// Offsets (in elements) of one band's reduced tables inside the table blob.
+// Absorption-type tables are stored transposed so that consecutive
+// g-points of a band are contiguous: absa(ind, ig) -> [(ind-1)*ng + ig-1].
+struct BandOff {
+    int ng, g0, nspa, nspb, nfr;
+    int absa, absb, selfref, forref;
+    int sfluxref, irradnce, facbrght, snsptdrk;  // (ng, js): [(js-1)*ng + ig-1]
+    int rayl, rayla, raylb, abso3a, abso3b, absch4, absco2, absh2o;
+};
+
+struct DevTables {
+    BandOff b[NBND];
+    int pref, preflog, tref;
+    // cloud LUTs, Fortran order (index, band): [(ib-16)*n + index-1]
+    int extliq1, ssaliq1, asyliq1, extice2, ssaice2, asyice2;
+    int extice3, ssaice3, asyice3, fdlice3;
+    int abari, bbari, cbari, dbari, ebari, fbari;
+    int rsrtaua, rsrpiza, rsrasya;  // (14, 6)
+    int wavenum2;
+    int exp_tbl;                    // (0:10000)
+    int total;                      // blob size
+    int8_t ngb[NGPT];               // band index 0..13 of each g-point
+    uint8_t gib[NGPT];              // g index within its band, 1-based
+    double heatfac, bpade, oneminus;
+    // GF(2) jump matrices of the KISS xorshift component: column j of
+    // M^(2^k) at xs_jump[k][j]
+    uint32_t xs_jump[32][32];
+};
+
+// every translation unit that launches kernels holds its own copy, filled by
+// its upload function (no relocatable device code needed)
+static __constant__ DevTables cT;
+
+// Error word: first error code wins.
+__device__ inline void set_error(int* err, int code) {
+    if (err) atomicCAS(err, 0, code);
+}
+
+// Error codes (mirror include/rrtmg_sw_gb300.h)
+enum {
+    E_OK = 0, E_INFLAG1 = 10, E_ICERAD = 11, E_ICEDGE = 12, E_ICEPROP = 13,
+    E_LIQRAD = 14, E_LIQPROP = 15, E_ICLD = 20, E_KISSSEED = 21, E_LAYTROP = 30
+};
+
+}  // namespace rrsw

@@ -1,0 +1,47 @@
+// launch.h -- interface between the host C-ABI (api.cu) and the kernel
+// translation units (solve_fp64.cu built without FMA contraction,
+// solve_fp32.cu built with it).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "solve.cuh"
+
+namespace rrsw {
+
+struct LaunchInfo {
+    int grid;            // CTAs (persistent: each loops over column pairs)
+    size_t smem;         // dynamic shared memory per CTA
+};
+
+// FP64 form
+cudaError_t upload_tables_fp64(const DevTables& t);
+LaunchInfo plan_fp64(const SolveParams& P, int num_sms);
+cudaError_t launch_solve_fp64(const SolveParams& P, const double* tab, const LaunchInfo& li, cudaStream_t s);
+// FP32 form
+cudaError_t upload_tables_fp32(const DevTables& t);
+LaunchInfo plan_fp32(const SolveParams& P, int num_sms);
+cudaError_t launch_solve_fp32(const SolveParams& P, const float* tab, const double* tab64, const LaunchInfo& li,
+                              cudaStream_t s);
+// scratch elements (of the form's type) per CTA slot
+size_t slot_elems(int nlay, int idelm);
+
+// get_alpha (mcica_subcol_gen_sw.f90:66-178) on the device
+cudaError_t launch_get_alpha(int ncol, int nlay, int icld, int idcor, double decorr_con, const double* dz,
+                             const double* lat, int juldat, const double* cldfrac, double* alpha, cudaStream_t s);
+// mcica_subcol_sw with KISS streams (irng = 0) on the device
+cudaError_t launch_mcica_kiss(int ncol, int nlay, int icld, int permuteseed, const double* play,
+                              const double* cldfrac, const double* ciwp, const double* clwp, const double* tauc,
+                              const double* ssac, const double* asmc, const double* fsfc, const double* alpha,
+                              double* cldfmcl, double* ciwpmcl, double* clwpmcl, double* taucmcl,
+                              double* ssacmcl, double* asmcmcl, double* fsfcmcl, int* err, cudaStream_t s);
+// Mersenne Twister stream (getRandomReal values) of length n, seeded with seed
+cudaError_t launch_mt_stream(int seed, size_t n, double* out, cudaStream_t s);
+// mcica_subcol_sw from a precomputed random stream (irng = 1, GCM order)
+cudaError_t launch_mcica_stream(int ncol, int nlay, int icld, const double* stream, const double* cldfrac,
+                                const double* ciwp, const double* clwp, const double* tauc, const double* ssac,
+                                const double* asmc, const double* fsfc, const double* alpha, double* cldfmcl,
+                                double* ciwpmcl, double* clwpmcl, double* taucmcl, double* ssacmcl,
+                                double* asmcmcl, double* fsfcmcl, cudaStream_t s);
+
+}  // namespace rrsw

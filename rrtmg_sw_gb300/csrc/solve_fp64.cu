@@ -1,0 +1,238 @@
+// solve_fp64.cu -- plain FP64 form.  Built with --fmad=false so that every
+// multiply and add rounds separately, as the reference's expressions do;
+// together with the reference's operation order this makes the device
+// results agree with the FP64 oracle to rounding of log/exp only.
+#include "kernel.cuh"
+#include "launch.h"
+
+namespace rrsw {
+
+cudaError_t upload_tables_fp64(const DevTables& t) { return cudaMemcpyToSymbol(cT, &t, sizeof(DevTables)); }
+
+size_t slot_elems(int nlay, int idelm) {
+    return (size_t)nlay * (size_t)(idelm == 0 ? NS_MAX : S_DBTCN) * CTA_THREADS;
+}
+
+template <typename R>
+static size_t smem_bytes(int L, int extra) {
+    const int NQ = extra ? NQ_EXTRA : NQ_BASE;
+    size_t off = (size_t)COLS_PER_CTA * L * sizeof(double) + (size_t)COLS_PER_CTA * NFR * L * sizeof(R) +
+                 (size_t)COLS_PER_CTA * L * sizeof(int) + 4 * sizeof(int);
+    off = (off + 15) & ~(size_t)15;
+    return off + (size_t)KLEV * NQ * CTA_THREADS * sizeof(R) + (size_t)COLS_PER_CTA * NQ * (L + 1) * sizeof(R);
+}
+
+LaunchInfo plan_fp64(const SolveParams& P, int num_sms) {
+    LaunchInfo li;
+    li.smem = smem_bytes<double>(P.nlay, P.extra);
+    cudaFuncSetAttribute(k_solve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<double>, CTA_THREADS, li.smem);
+    if (per_sm < 1) per_sm = 1;
+    li.grid = num_sms * per_sm;
+    if (li.grid > P.npairs) li.grid = P.npairs;
+    if (li.grid < 1) li.grid = 1;
+    return li;
+}
+
+cudaError_t launch_solve_fp64(const SolveParams& P, const double* tab, const LaunchInfo& li, cudaStream_t s) {
+    k_solve<double><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ get_alpha
+// mcica_subcol_gen_sw.f90:119-176, one thread per column (the layer loop
+// is sequential in the reference only through alpha(i,1) = 0).
+__global__ void k_get_alpha(int ncol, int nlay, int icld, int idcor, double decorr_con, const double* dz,
+                            const double* lat, int juldat, const double* cldfrac, double* alpha) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ncol) return;
+    const double am1 = 1.4315, am2 = 2.1219, am4 = -25.584, amr = 7.0;
+    if (icld != 4 && icld != 5) return;
+    double decorr_inv = 1.0, decorr_len;
+    if (idcor == 1) {
+        const double am3 = juldat > 181 ? -4.0 * amr / 365.0 * (double)(juldat - 272)
+                                        : 4.0 * amr / 365.0 * (double)(juldat - 91);
+        const double d = lat[i] - am3;
+        decorr_len = (am1 + am2 * exp(-(d * d) / (am4 * am4))) * 1.e3;
+    } else {
+        decorr_len = decorr_con;
+    }
+    if (decorr_len >= 0.0) decorr_inv = 1.0 / decorr_len;
+    const size_t n = (size_t)ncol;
+    alpha[i] = 0.0;
+    for (int k = 2; k <= nlay; ++k) {
+        const size_t kk = (size_t)i + n * (size_t)(k - 1), km = kk - n;
+        double a = exp(-(0.5 * (dz[kk] + dz[km])) * decorr_inv);
+        if (icld == 5 && cldfrac[kk] == 0.0 && cldfrac[km] > 0.0) a = 0.0;
+        alpha[kk] = a;
+    }
+}
+
+cudaError_t launch_get_alpha(int ncol, int nlay, int icld, int idcor, double decorr_con, const double* dz,
+                             const double* lat, int juldat, const double* cldfrac, double* alpha, cudaStream_t s) {
+    k_get_alpha<<<(ncol + 127) / 128, 128, 0, s>>>(ncol, nlay, icld, idcor, decorr_con, dz, lat, juldat, cldfrac,
+                                                  alpha);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------- McICA
+// Fill of the seven subcolumn arrays (mcica_subcol_gen_sw.f90:666-690).
+__device__ inline void mcica_fill(bool cloudy, int g, size_t kl, size_t kg, const double* ciwp, const double* clwp,
+                                  const double* tauc, const double* ssac, const double* asmc, const double* fsfc,
+                                  double* cldfmcl, double* ciwpmcl, double* clwpmcl, double* taucmcl,
+                                  double* ssacmcl, double* asmcmcl, double* fsfcmcl) {
+    if (cloudy) {
+        const size_t kb = (size_t)cT.ngb[g] + 14 * kl;
+        cldfmcl[kg] = 1.0;
+        clwpmcl[kg] = clwp[kl];
+        ciwpmcl[kg] = ciwp[kl];
+        taucmcl[kg] = tauc ? tauc[kb] : 0.0;
+        ssacmcl[kg] = tauc ? ssac[kb] : 1.0;
+        asmcmcl[kg] = tauc ? asmc[kb] : 0.0;
+        fsfcmcl[kg] = tauc ? fsfc[kb] : 0.0;
+    } else {
+        cldfmcl[kg] = 0.0;
+        clwpmcl[kg] = 0.0;
+        ciwpmcl[kg] = 0.0;
+        taucmcl[kg] = 0.0;
+        ssacmcl[kg] = 1.0;
+        asmcmcl[kg] = 0.0;
+        fsfcmcl[kg] = 0.0;
+    }
+}
+
+// one thread per (column, subcolumn), g fastest for coalesced stores
+__global__ void k_mcica_kiss(int ncol, int nlay, int icld, int permuteseed, const double* play,
+                             const double* cldfrac, const double* ciwp, const double* clwp, const double* tauc,
+                             const double* ssac, const double* asmc, const double* fsfc, const double* alpha,
+                             double* cldfmcl, double* ciwpmcl, double* clwpmcl, double* taucmcl, double* ssacmcl,
+                             double* asmcmcl, double* fsfcmcl, int* err) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)ncol * NGPT) return;
+    const int g = (int)(t % NGPT), col = (int)(t / NGPT);
+    const size_t n = (size_t)ncol;
+    McicaKiss mc;
+    mc.init(play, n, col, g, nlay, icld, permuteseed, err);
+    for (int lay = 1; lay <= nlay; ++lay) {
+        const size_t kl = (size_t)col + n * (size_t)(lay - 1);
+        const bool cloudy = mc.step(lay, cldfrac[kl], icld >= 4 ? alpha[kl] : 0.0);
+        mcica_fill(cloudy, g, kl, (size_t)g + NGPT * kl, ciwp, clwp, tauc, ssac, asmc, fsfc, cldfmcl, ciwpmcl,
+                   clwpmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl);
+    }
+}
+
+cudaError_t launch_mcica_kiss(int ncol, int nlay, int icld, int permuteseed, const double* play,
+                              const double* cldfrac, const double* ciwp, const double* clwp, const double* tauc,
+                              const double* ssac, const double* asmc, const double* fsfc, const double* alpha,
+                              double* cldfmcl, double* ciwpmcl, double* clwpmcl, double* taucmcl,
+                              double* ssacmcl, double* asmcmcl, double* fsfcmcl, int* err, cudaStream_t s) {
+    const size_t nt = (size_t)ncol * NGPT;
+    k_mcica_kiss<<<(unsigned)((nt + 127) / 128), 128, 0, s>>>(ncol, nlay, icld, permuteseed, play, cldfrac, ciwp,
+                                                              clwp, tauc, ssac, asmc, fsfc, alpha, cldfmcl, ciwpmcl,
+                                                              clwpmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl, err);
+    return cudaGetLastError();
+}
+
+// Mersenne Twister MT19937 (mcica_random_numbers.f90:77-306), one CTA: the
+// 624-word state is regenerated in three dependency-free phases per block
+// (k = 0..226, 227..453, 454..622) plus the last word, then tempered in
+// parallel; getRandomReal = u32 / (2^32 - 1).
+__global__ void k_mt_stream(int seed, size_t n, double* out) {
+    __shared__ uint32_t st[624];
+    if (threadIdx.x == 0) {
+        st[0] = (uint32_t)seed;
+        for (int i = 1; i < 624; ++i) st[i] = 1812433253u * (st[i - 1] ^ (st[i - 1] >> 30)) + (uint32_t)i;
+    }
+    __syncthreads();
+    auto twist = [](uint32_t u, uint32_t v) {
+        const uint32_t mix = (u & 0x80000000u) | (v & 0x7fffffffu);
+        return (mix >> 1) ^ ((v & 1u) ? 0x9908b0dfu : 0u);
+    };
+    for (size_t base = 0; base < n; base += 624) {
+        // each phase reads the words it needs before any thread writes
+        // (blockDim >= 227, so one word per thread per phase)
+        const int k = threadIdx.x;
+        uint32_t v = 0;
+        if (k < 227) v = st[k + 397] ^ twist(st[k], st[k + 1]);
+        __syncthreads();
+        if (k < 227) st[k] = v;
+        __syncthreads();
+        if (k < 227) v = st[k] ^ twist(st[k + 227], st[k + 228]);
+        __syncthreads();
+        if (k < 227) st[k + 227] = v;
+        __syncthreads();
+        if (k < 169) v = st[k + 227] ^ twist(st[k + 454], st[k + 455]);
+        __syncthreads();
+        if (k < 169) st[k + 454] = v;
+        __syncthreads();
+        if (k == 0) st[623] = st[396] ^ twist(st[623], st[0]);
+        __syncthreads();
+        for (int kk = threadIdx.x; kk < 624 && base + kk < n; kk += blockDim.x) {
+            uint32_t y = st[kk];
+            y ^= (y >> 11);
+            y ^= (y << 7) & 0x9d2c5680u;
+            y ^= (y << 15) & 0xefc60000u;
+            y ^= (y >> 18);
+            out[base + kk] = (double)y / (4294967296.0 - 1.0);
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_mt_stream(int seed, size_t n, double* out, cudaStream_t s) {
+    k_mt_stream<<<1, 256, 0, s>>>(seed, n, out);
+    return cudaGetLastError();
+}
+
+// McICA from a precomputed stream in the reference's (subcolumn, column,
+// layer) order (irng = 1).
+__global__ void k_mcica_stream(int ncol, int nlay, int icld, const double* rs, const double* cldfrac,
+                               const double* ciwp, const double* clwp, const double* tauc, const double* ssac,
+                               const double* asmc, const double* fsfc, const double* alpha, double* cldfmcl,
+                               double* ciwpmcl, double* clwpmcl, double* taucmcl, double* ssacmcl, double* asmcmcl,
+                               double* fsfcmcl) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)ncol * NGPT) return;
+    const int g = (int)(t % NGPT), col = (int)(t / NGPT);
+    const size_t n = (size_t)ncol, L = (size_t)nlay;
+    const size_t sc = (size_t)g * n + (size_t)col;  // (subcolumn, column) position
+    double cdf_prev = 0.0, cf_prev = 0.0;
+    for (int lay = 1; lay <= nlay; ++lay) {
+        const size_t kl = (size_t)col + n * (size_t)(lay - 1);
+        double cf = cldfrac[kl];
+        if (cf < 1.0e-20) cf = 0.0;
+        double cdf;
+        if (icld == 3) {
+            cdf = rs[sc];
+        } else if (icld >= 4) {
+            const size_t p = 2 * (sc * L + (size_t)(lay - 1));
+            cdf = rs[p];
+            if (lay >= 2 && rs[p + 1] < alpha[kl]) cdf = cdf_prev;
+        } else {
+            cdf = rs[sc * L + (size_t)(lay - 1)];
+            if (icld == 2 && lay >= 2) {
+                if (cdf_prev > 1.0 - cf_prev) cdf = cdf_prev;
+                else cdf = cdf * (1.0 - cf_prev);
+            }
+        }
+        cdf_prev = cdf;
+        cf_prev = cf;
+        mcica_fill(cdf >= 1.0 - cf, g, kl, (size_t)g + NGPT * kl, ciwp, clwp, tauc, ssac, asmc, fsfc, cldfmcl,
+                   ciwpmcl, clwpmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl);
+    }
+}
+
+cudaError_t launch_mcica_stream(int ncol, int nlay, int icld, const double* stream, const double* cldfrac,
+                                const double* ciwp, const double* clwp, const double* tauc, const double* ssac,
+                                const double* asmc, const double* fsfc, const double* alpha, double* cldfmcl,
+                                double* ciwpmcl, double* clwpmcl, double* taucmcl, double* ssacmcl,
+                                double* asmcmcl, double* fsfcmcl, cudaStream_t s) {
+    const size_t nt = (size_t)ncol * NGPT;
+    k_mcica_stream<<<(unsigned)((nt + 127) / 128), 128, 0, s>>>(ncol, nlay, icld, stream, cldfrac, ciwp, clwp, tauc,
+                                                                ssac, asmc, fsfc, alpha, cldfmcl, ciwpmcl, clwpmcl,
+                                                                taucmcl, ssacmcl, asmcmcl, fsfcmcl);
+    return cudaGetLastError();
+}
+
+}  // namespace rrsw

@@ -1,0 +1,230 @@
+"""Python mirror of RRTMG_SW's GCM interface on top of the C ABI.
+
+Same routine names, argument names and meanings as the reference:
+
+* ``rrtmg_sw_ini(cpdair)``                     -- rrtmg_sw_init.f90:47
+* ``rrtmg_sw(ncol, nlay, icld, iaer, play, ...)`` -- rrtmg_sw_rad.f90:99-111
+* ``mcica_subcol_sw(iplon, ncol, nlay, ...)``  -- mcica_subcol_gen_sw.f90:181-185
+* ``get_alpha(iplon, ncol, nlayers, ...)``     -- mcica_subcol_gen_sw.f90:66-67
+
+Arrays are NumPy arrays with the reference's Fortran shapes, e.g. ``play``
+is ``(ncol, nlay)``, ``cldfmcl`` is ``(ngptsw, ncol, nlay)``; they are passed
+in column-major order.  Outputs are returned as Fortran-ordered arrays.
+Errors the reference reports with ``stop`` raise :class:`RRTMGError` with the
+same message.  Every call runs on the GPU through ``librrtmg_sw_gb300.so``;
+there is no CPU path.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "librrtmg_sw_gb300.so")
+NGPTSW = 112
+NBNDSW = 14
+
+FORM_FP64 = 0
+FORM_FP32 = 1
+
+_dp = C.POINTER(C.c_double)
+
+
+class RRTMGError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("rrtmg_sw error %d: %s" % (code, msg))
+        self.code = code
+
+
+class RrtmgSwArgs(C.Structure):
+    """``rrtmg_sw_args`` of include/rrtmg_sw_gb300.h."""
+    _fields_ = [
+        ("ncol", C.c_int32), ("nlay", C.c_int32), ("icld", C.c_int32), ("iaer", C.c_int32),
+        ("play", _dp), ("plev", _dp), ("tlay", _dp), ("tlev", _dp), ("tsfc", _dp),
+        ("h2ovmr", _dp), ("o3vmr", _dp), ("co2vmr", _dp), ("ch4vmr", _dp), ("n2ovmr", _dp), ("o2vmr", _dp),
+        ("asdir", _dp), ("asdif", _dp), ("aldir", _dp), ("aldif", _dp),
+        ("coszen", _dp), ("adjes", C.c_double), ("dyofyr", C.c_int32), ("scon", C.c_double),
+        ("isolvar", C.c_int32), ("inflgsw", C.c_int32), ("iceflgsw", C.c_int32), ("liqflgsw", C.c_int32),
+        ("cldfmcl", _dp), ("taucmcl", _dp), ("ssacmcl", _dp), ("asmcmcl", _dp), ("fsfcmcl", _dp),
+        ("ciwpmcl", _dp), ("clwpmcl", _dp), ("reicmcl", _dp), ("relqmcl", _dp),
+        ("tauaer", _dp), ("ssaaer", _dp), ("asmaer", _dp), ("ecaer", _dp),
+        ("swuflx", _dp), ("swdflx", _dp), ("swhr", _dp), ("swuflxc", _dp), ("swdflxc", _dp), ("swhrc", _dp),
+        ("bndsolvar", _dp), ("indsolvar", _dp), ("solcycfrac", _dp),
+        ("dirdflux", _dp), ("difdflux", _dp), ("uvdflx", _dp), ("nidflx", _dp),
+        ("dirdnuv", _dp), ("difdnuv", _dp), ("dirdnir", _dp), ("difdnir", _dp),
+        ("idelm", C.c_int32), ("nthreads", C.c_int32),
+    ]
+
+
+class RrtmgSwClouds(C.Structure):
+    """``rrtmg_sw_clouds`` of include/rrtmg_sw_gb300.h."""
+    _fields_ = [
+        ("permuteseed", C.c_int32), ("irng", C.c_int32),
+        ("cldfrac", _dp), ("ciwp", _dp), ("clwp", _dp), ("rei", _dp), ("rel", _dp),
+        ("tauc", _dp), ("ssac", _dp), ("asmc", _dp), ("fsfc", _dp), ("alpha", _dp),
+    ]
+
+
+EXTRA_OUTPUTS = ("dirdflux", "difdflux", "uvdflx", "nidflx", "dirdnuv", "difdnuv", "dirdnir", "difdnir")
+_lib = None
+
+
+def lib():
+    """Load the CUDA library; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("librrtmg_sw_gb300.so is not built (run rrtmg_sw_gb300.build.build())")
+        L = C.CDLL(LIB_PATH)
+        L.rrtmg_sw_ini_c.argtypes = [C.c_double]
+        L.rrtmg_sw_c.argtypes = [C.POINTER(RrtmgSwArgs)]
+        L.rrtmg_sw_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.c_void_p]
+        L.rrtmg_sw_mcica_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds)]
+        L.rrtmg_sw_mcica_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_void_p]
+        L.mcica_subcol_sw_c.argtypes = [C.c_int32] * 5 + [_dp] * 11 + [_dp] * 9
+        L.get_alpha_c.argtypes = [C.c_int32] * 4 + [C.c_double, _dp, _dp, C.c_int32, _dp, _dp]
+        L.rrtmg_sw_set_form_c.argtypes = [C.c_int32]
+        L.rrtmg_sw_errstr_c.restype = C.c_char_p
+        L.rrtmg_sw_errstr_c.argtypes = [C.c_int32]
+        L.rrtmg_sw_last_cuda_error_c.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        msg = lib().rrtmg_sw_errstr_c(rc).decode()
+        if rc == 4:
+            msg += " (" + lib().rrtmg_sw_last_cuda_error_c().decode() + ")"
+        raise RRTMGError(rc, msg)
+
+
+def _f(a, shape=None):
+    """Fortran-ordered FP64 copy (or view) of an input array."""
+    if a is None:
+        return None
+    x = np.asfortranarray(np.asarray(a, dtype=np.float64))
+    if shape is not None and x.shape != tuple(shape):
+        x = np.asfortranarray(x.reshape(shape, order="F"))
+    return x
+
+
+def _p(x):
+    return None if x is None else x.ctypes.data_as(_dp)
+
+
+def rrtmg_sw_ini(cpdair=1.004e3):
+    """Load the coefficient tables onto the current GPU (rrtmg_sw_ini)."""
+    _check(lib().rrtmg_sw_ini_c(C.c_double(cpdair)))
+
+
+def set_form(form):
+    """Select the arithmetic form: FORM_FP64 (default) or FORM_FP32."""
+    _check(lib().rrtmg_sw_set_form_c(int(form)))
+
+
+def rrtmg_sw(ncol, nlay, icld, iaer, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr,
+             o2vmr, asdir, asdif, aldir, aldif, coszen, adjes, dyofyr, scon, isolvar, inflgsw, iceflgsw,
+             liqflgsw, cldfmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl, ciwpmcl, clwpmcl, reicmcl, relqmcl,
+             tauaer, ssaaer, asmaer, ecaer, bndsolvar=None, indsolvar=None, solcycfrac=None, idelm=1,
+             extra=False, clouds=None):
+    """rrtmg_sw (rrtmg_sw_rad.f90:99-111).
+
+    Returns ``(swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc)`` with shapes
+    (ncol, nlay+1) and (ncol, nlay), or, with ``extra=True``, a dict that
+    also holds the direct/diffuse and UV/near-IR fluxes.  ``clouds`` (a dict
+    of mcica_subcol_sw's physical inputs plus ``permuteseed``) selects the
+    fused path, in which the subcolumn arrays may be None.
+    """
+    cl, cl1 = (ncol, nlay), (ncol, nlay + 1)
+    gcl = (NGPTSW, ncol, nlay)
+    keep = {}
+    a = RrtmgSwArgs()
+    a.ncol, a.nlay, a.icld, a.iaer = ncol, nlay, icld, iaer
+    for name, val, shp in (("play", play, cl), ("plev", plev, cl1), ("tlay", tlay, cl), ("tlev", tlev, cl1),
+                           ("tsfc", tsfc, (ncol,)), ("h2ovmr", h2ovmr, cl), ("o3vmr", o3vmr, cl),
+                           ("co2vmr", co2vmr, cl), ("ch4vmr", ch4vmr, cl), ("n2ovmr", n2ovmr, cl),
+                           ("o2vmr", o2vmr, cl), ("asdir", asdir, (ncol,)), ("asdif", asdif, (ncol,)),
+                           ("aldir", aldir, (ncol,)), ("aldif", aldif, (ncol,)), ("coszen", coszen, (ncol,)),
+                           ("cldfmcl", cldfmcl, gcl), ("taucmcl", taucmcl, gcl), ("ssacmcl", ssacmcl, gcl),
+                           ("asmcmcl", asmcmcl, gcl), ("fsfcmcl", fsfcmcl, gcl), ("ciwpmcl", ciwpmcl, gcl),
+                           ("clwpmcl", clwpmcl, gcl), ("reicmcl", reicmcl, cl), ("relqmcl", relqmcl, cl),
+                           ("tauaer", tauaer, (ncol, nlay, NBNDSW)), ("ssaaer", ssaaer, (ncol, nlay, NBNDSW)),
+                           ("asmaer", asmaer, (ncol, nlay, NBNDSW)), ("ecaer", ecaer, (ncol, nlay, 6))):
+        keep[name] = _f(val, shp)
+        setattr(a, name, _p(keep[name]))
+    a.adjes, a.dyofyr, a.scon, a.isolvar = adjes, dyofyr, scon, isolvar
+    a.inflgsw, a.iceflgsw, a.liqflgsw = inflgsw, iceflgsw, liqflgsw
+    if bndsolvar is not None:
+        keep["bndsolvar"] = _f(bndsolvar)
+        a.bndsolvar = _p(keep["bndsolvar"])
+    if indsolvar is not None:
+        keep["indsolvar"] = _f(indsolvar)
+        a.indsolvar = _p(keep["indsolvar"])
+    if solcycfrac is not None:
+        keep["solcycfrac"] = _f([solcycfrac])
+        a.solcycfrac = _p(keep["solcycfrac"])
+    out = {k: np.zeros(cl1, order="F") for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}
+    out.update({k: np.zeros(cl, order="F") for k in ("swhr", "swhrc")})
+    if extra:
+        out.update({k: np.zeros(cl1, order="F") for k in EXTRA_OUTPUTS})
+    for k, v in out.items():
+        setattr(a, k, _p(v))
+    a.idelm = idelm
+    if clouds is None:
+        _check(lib().rrtmg_sw_c(C.byref(a)))
+    else:
+        c = RrtmgSwClouds()
+        c.permuteseed = clouds.get("permuteseed", NGPTSW)
+        c.irng = clouds.get("irng", 0)
+        for name, shp in (("cldfrac", cl), ("ciwp", cl), ("clwp", cl), ("rei", cl), ("rel", cl),
+                          ("tauc", (NBNDSW, ncol, nlay)), ("ssac", (NBNDSW, ncol, nlay)),
+                          ("asmc", (NBNDSW, ncol, nlay)), ("fsfc", (NBNDSW, ncol, nlay)), ("alpha", cl)):
+            keep["c_" + name] = _f(clouds.get(name), shp)
+            setattr(c, name, _p(keep["c_" + name]))
+        _check(lib().rrtmg_sw_mcica_c(C.byref(a), C.byref(c)))
+    if extra:
+        return out
+    return tuple(out[k] for k in ("swuflx", "swdflx", "swhr", "swuflxc", "swdflxc", "swhrc"))
+
+
+def mcica_subcol_sw(iplon, ncol, nlay, icld, permuteseed, irng, play, cldfrac, ciwp, clwp, rei, rel, tauc,
+                    ssac, asmc, fsfc, alpha=None):
+    """mcica_subcol_sw (mcica_subcol_gen_sw.f90:181-296).
+
+    Returns ``(cldfmcl, ciwpmcl, clwpmcl, reicmcl, relqmcl, taucmcl, ssacmcl,
+    asmcmcl, fsfcmcl)``; ``irng`` 0 = KISS, 1 = Mersenne Twister.
+    """
+    cl, bcl, gcl = (ncol, nlay), (NBNDSW, ncol, nlay), (NGPTSW, ncol, nlay)
+    ins = [_f(play, cl), _f(cldfrac, cl), _f(ciwp, cl), _f(clwp, cl), _f(rei, cl), _f(rel, cl),
+           _f(tauc, bcl), _f(ssac, bcl), _f(asmc, bcl), _f(fsfc, bcl),
+           _f(alpha if alpha is not None else np.zeros(cl), cl)]
+    outs = [np.zeros(gcl, order="F") for _ in range(3)] + [np.zeros(cl, order="F") for _ in range(2)] + \
+           [np.zeros(gcl, order="F") for _ in range(4)]
+    _check(lib().mcica_subcol_sw_c(ncol, nlay, icld, permuteseed, irng, *[_p(x) for x in ins],
+                                   *[_p(x) for x in outs]))
+    return tuple(outs)
+
+
+def get_alpha(iplon, ncol, nlayers, icld, idcor, decorr_con, dz, lat, juldat, cldfrac):
+    """get_alpha (mcica_subcol_gen_sw.f90:66-178); returns alpha (ncol, nlayers)."""
+    cl = (ncol, nlayers)
+    dz, lat, cldfrac = _f(dz, cl), _f(lat, (ncol,)), _f(cldfrac, cl)
+    alpha = np.zeros(cl, order="F")
+    _check(lib().get_alpha_c(ncol, nlayers, icld, idcor, C.c_double(decorr_con), _p(dz), _p(lat), juldat,
+                             _p(cldfrac), _p(alpha)))
+    return alpha
+
+
+def rrtmg_sw_dev(args, stream=0, clouds=None):
+    """Device-pointer entry point: ``args`` / ``clouds`` are filled
+    :class:`RrtmgSwArgs` / :class:`RrtmgSwClouds` whose pointers are device
+    addresses (e.g. from ``torch.Tensor.data_ptr()``)."""
+    if clouds is None:
+        _check(lib().rrtmg_sw_dev_c(C.byref(args), C.c_void_p(stream)))
+    else:
+        _check(lib().rrtmg_sw_mcica_dev_c(C.byref(args), C.byref(clouds), C.c_void_p(stream)))
+
+
+def last_launch_count():
+    return lib().rrtmg_sw_last_launch_count_c()
