@@ -2,7 +2,7 @@
 
 Translation units are compiled in parallel:
   solve_fp64.cu  --fmad=false (plain FP64 form, reference rounding)
-  solve_fp32.cu  FMA contraction allowed (FP32 form)
+  solve_fp32.cu  FMA contraction, approximate FP32 division/sqrt (FP32 form)
   api.cu         host C-ABI
 """
 import os
@@ -16,10 +16,11 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "librrtmg_sw_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+          "-I", os.path.join(HERE, "..", "include")]
 UNITS = {
     "solve_fp64.cu": ["--fmad=false"],
-    "solve_fp32.cu": [],
+    "solve_fp32.cu": ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "api.cu": [],
 }
 

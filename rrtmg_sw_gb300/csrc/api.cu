@@ -12,7 +12,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/rrtmg_sw_gb300.h"
+#include "rrtmg_sw_gb300.h"
 #include "launch.h"
 
 using namespace rrsw;
@@ -185,6 +185,14 @@ int build_tables(State& st) {
     T.extice2 = put(rec["extice2"]); T.ssaice2 = put(rec["ssaice2"]); T.asyice2 = put(rec["asyice2"]);
     T.extice3 = put(rec["extice3"]); T.ssaice3 = put(rec["ssaice3"]); T.asyice3 = put(rec["asyice3"]);
     T.fdlice3 = put(rec["fdlice3"]);
+    auto co_of = [&](const std::vector<double>& ssa) {
+        std::vector<double> co(ssa.size());
+        for (size_t i = 0; i < ssa.size(); ++i) co[i] = 1.0 - ssa[i];
+        return co;
+    };
+    T.coliq1 = put(co_of(rec["ssaliq1"]));
+    T.coice2 = put(co_of(rec["ssaice2"]));
+    T.coice3 = put(co_of(rec["ssaice3"]));
     T.abari = put(rec["abari"]); T.bbari = put(rec["bbari"]); T.cbari = put(rec["cbari"]);
     T.dbari = put(rec["dbari"]); T.ebari = put(rec["ebari"]); T.fbari = put(rec["fbari"]);
     T.rsrtaua = put(rec["rsrtaua"]); T.rsrpiza = put(rec["rsrpiza"]); T.rsrasya = put(rec["rsrasya"]);
@@ -204,8 +212,54 @@ int build_tables(State& st) {
         if (et[itr] <= expeps) et[itr] = expeps;
     }
     T.exp_tbl = put(et);
+    // band/region descriptors of the FP32 gas optics (rrtmg_sw_taumol.f90:275-1785)
+    enum { H2O = 0, CO2 = 1, O3 = 2, CH4 = 3, O2 = 4, O2CONT = 9 };
+    auto reg = [&](int band, int up, int kind, int sa, int sb, float strrat, float fac, int cont, int minor,
+                   int mtab, int rtype, int rtab) {
+        TmRegion& r = T.tm[band - 16][up];
+        const BandOff& b = T.b[band - 16];
+        r.kind = (int8_t)kind; r.sa = (int8_t)sa; r.sb = (int8_t)sb; r.cont = (int8_t)cont;
+        r.minor = (int8_t)minor; r.rtype = (int8_t)rtype;
+        r.nsp = (int8_t)(kind == 1 ? (up ? b.nspb : b.nspa) : 1);
+        r.jo = (int8_t)(up ? 13 : 1);
+        r.strrat = strrat; r.fac = fac; r.mult = up ? 4.0f : 8.0f;
+        r.ktab = up ? b.absb : b.absa;
+        r.mtab = mtab;
+        r.rtab = rtab;
+    };
+    const BandOff* bb = T.b - 16;
+    reg(16, 0, 1, H2O, CH4, 252.131f, 1.f, 1, -1, 0, 0, bb[16].rayl);
+    reg(16, 1, 2, CH4, 0, 0.f, 1.f, 0, -1, 0, 0, bb[16].rayl);
+    reg(17, 0, 1, H2O, CO2, 0.364641f, 1.f, 1, -1, 0, 0, bb[17].rayl);
+    reg(17, 1, 1, H2O, CO2, 0.364641f, 1.f, 2, -1, 0, 0, bb[17].rayl);
+    reg(18, 0, 1, H2O, CH4, 38.9589f, 1.f, 1, -1, 0, 0, bb[18].rayl);
+    reg(18, 1, 2, CH4, 0, 0.f, 1.f, 0, -1, 0, 0, bb[18].rayl);
+    reg(19, 0, 1, H2O, CO2, 5.49281f, 1.f, 1, -1, 0, 0, bb[19].rayl);
+    reg(19, 1, 2, CO2, 0, 0.f, 1.f, 0, -1, 0, 0, bb[19].rayl);
+    reg(20, 0, 2, H2O, 0, 0.f, 1.f, 1, CH4, bb[20].absch4, 0, bb[20].rayl);
+    reg(20, 1, 2, H2O, 0, 0.f, 1.f, 2, CH4, bb[20].absch4, 0, bb[20].rayl);
+    reg(21, 0, 1, H2O, CO2, 0.0045321f, 1.f, 1, -1, 0, 0, bb[21].rayl);
+    reg(21, 1, 1, H2O, CO2, 0.0045321f, 1.f, 2, -1, 0, 0, bb[21].rayl);
+    reg(22, 0, 1, H2O, O2, (float)(1.6 * 0.022708), 1.f, 1, O2CONT, 0, 0, bb[22].rayl);
+    reg(22, 1, 2, O2, 0, 0.f, 1.6f, 0, O2CONT, 0, 0, bb[22].rayl);
+    reg(23, 0, 2, H2O, 0, 0.f, 1.029f, 1, -1, 0, 1, bb[23].rayl);
+    reg(23, 1, 0, 0, 0, 0.f, 1.f, 0, -1, 0, 1, bb[23].rayl);
+    reg(24, 0, 1, H2O, O2, 0.124692f, 1.f, 1, O3, bb[24].abso3a, 2, bb[24].rayla);
+    reg(24, 1, 2, O2, 0, 0.f, 1.f, 0, O3, bb[24].abso3b, 1, bb[24].raylb);
+    reg(25, 0, 2, H2O, 0, 0.f, 1.f, 0, O3, bb[25].abso3a, 1, bb[25].rayl);
+    reg(25, 1, 0, 0, 0, 0.f, 1.f, 0, O3, bb[25].abso3b, 1, bb[25].rayl);
+    reg(26, 0, 0, 0, 0, 0.f, 1.f, 0, -1, 0, 1, bb[26].rayl);
+    reg(26, 1, 0, 0, 0, 0.f, 1.f, 0, -1, 0, 1, bb[26].rayl);
+    reg(27, 0, 2, O3, 0, 0.f, 1.f, 0, -1, 0, 1, bb[27].rayl);
+    reg(27, 1, 2, O3, 0, 0.f, 1.f, 0, -1, 0, 1, bb[27].rayl);
+    reg(28, 0, 1, O3, O2, 6.67029e-07f, 1.f, 0, -1, 0, 0, bb[28].rayl);
+    reg(28, 1, 1, O3, O2, 6.67029e-07f, 1.f, 0, -1, 0, 0, bb[28].rayl);
+    reg(29, 0, 2, H2O, 0, 0.f, 1.f, 1, CO2, bb[29].absco2, 0, bb[29].rayl);
+    reg(29, 1, 2, CO2, 0, 0.f, 1.f, 0, H2O, bb[29].absh2o, 0, bb[29].rayl);
     T.total = (int)B.size();
     T.oneminus = 1.0 - 1.e-06;  // rrtmg_sw_rad.f90:563-565
+    T.bpade_f = (float)T.bpade;
+    T.oneminus_f = (float)T.oneminus;
     // xorshift jump matrices
     for (int j = 0; j < 32; ++j) T.xs_jump[0][j] = xs_step(1u << j);
     for (int k = 1; k < 32; ++k)

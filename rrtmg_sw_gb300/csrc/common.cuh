@@ -24,6 +24,18 @@ struct BandOff {
     int rayl, rayla, raylb, abso3a, abso3b, absch4, absco2, absh2o;
 };
 
+// Gas optics of one band and region (below / above laytrop) in the form
+// used by the FP32 solve: every taumolNN loop is one of
+//   kind 1: speccomb * 8-point k (binary species parameter, taumol.f90:309-338)
+//   kind 2: column(sa) * fac * 4-point k
+// plus an optional water-vapour continuum, one minor-species term and the
+// Rayleigh depth, so all bands run one code path.
+struct TmRegion {
+    int8_t kind, sa, sb, cont, minor, rtype, nsp, jo;
+    float strrat, fac, mult;
+    int ktab, mtab, rtab;
+};
+
 struct DevTables {
     BandOff b[NBND];
     int pref, preflog, tref;
@@ -31,6 +43,7 @@ struct DevTables {
     int extliq1, ssaliq1, asyliq1, extice2, ssaice2, asyice2;
     int extice3, ssaice3, asyice3, fdlice3;
     int abari, bbari, cbari, dbari, ebari, fbari;
+    int coliq1, coice2, coice3;     // 1 - ssa of the cloud LUTs, formed in FP64 (FP32 form)
     int rsrtaua, rsrpiza, rsrasya;  // (14, 6)
     int wavenum2;
     int exp_tbl;                    // (0:10000)
@@ -38,6 +51,8 @@ struct DevTables {
     int8_t ngb[NGPT];               // band index 0..13 of each g-point
     uint8_t gib[NGPT];              // g index within its band, 1-based
     double heatfac, bpade, oneminus;
+    float bpade_f, oneminus_f;
+    TmRegion tm[NBND][2];
     // GF(2) jump matrices of the KISS xorshift component: column j of
     // M^(2^k) at xs_jump[k][j]
     uint32_t xs_jump[32][32];

@@ -135,10 +135,83 @@ __device__ inline void aerosol(const SolveParams& P, int col, int lay, int ib, c
     }
 }
 
+// FP32 form: when the FP32 estimate of 1 - zwo for a cloudy layer lies
+// within 3e-5 (relative) of the switch 1 - zwcrit = 5e-7, the reference's
+// discontinuous conservative/non-conservative choice (reftra:188) is made
+// again from FP64 cloud optics (cldprmc in FP64 from the FP64 inputs) and
+// the co-albedo, so thick clouds take the reference's branch.
+static __device__ __noinline__ int decide_conservative64(const SolveParams& P, int col, int g, int lay, int ib, float ztauc,
+                                                  float zomcc, float zgcc, float zcoc, const double* __restrict__ tab64) {
+    const size_t n = (size_t)P.ncol;
+    const size_t kl = (size_t)col + n * (size_t)(lay - 1);
+    double cldf = 1.0, ciwp, clwp, rei, rel, tauc = 0.0, ssac = 1.0, asmc = 0.0, fsfc = 0.0;
+    if (P.fused) {
+        ciwp = P.ciwp[kl]; clwp = P.clwp[kl]; rei = P.rei[kl]; rel = P.rel[kl];
+        if (P.tauc) {
+            const size_t kb = (size_t)ib + 14 * kl;
+            tauc = P.tauc[kb]; ssac = P.ssac[kb]; asmc = P.asmc[kb]; fsfc = P.fsfc[kb];
+        }
+    } else {
+        const size_t kg = (size_t)g + NGPT * kl;
+        cldf = P.cldfmcl[kg]; tauc = P.taucmcl[kg]; ssac = P.ssacmcl[kg]; asmc = P.asmcmcl[kg];
+        fsfc = P.fsfcmcl[kg]; ciwp = P.ciwpmcl[kg]; clwp = P.clwpmcl[kg];
+        rei = P.reicmcl[kl]; rel = P.relqmcl[kl];
+    }
+    double taor, coc;
+    cldprmc_g<double>(ib, P.inflag, P.iceflag, P.liqflag, cldf, ciwp, clwp, rei, rel, fsfc, tauc, ssac, asmc, taor,
+                      coc, tab64, nullptr);
+    const double tc = (double)ztauc, oc = (double)zomcc, gcl = (double)zgcc;
+    const double ztauo = tc + tauc;
+    const double scat = tc * oc + tauc * ssac;
+    const double zgco = (tauc * ssac * asmc + tc * oc * gcl) / scat;
+    const double zomco = scat / ztauo;
+    const double zcoo = (tc * (double)zcoc + tauc * coc) / ztauo;
+    return one_minus_zwo<double>(zomco, zcoo, zgco) <= 5.0e-7 ? 1 : 0;
+}
+
 template <typename R>
 __device__ inline void warp_sum4(R& v) {
     v += __shfl_xor_sync(0xffffffffu, v, 1);
     v += __shfl_xor_sync(0xffffffffu, v, 2);
+}
+
+// Shared-memory carve-up of one CTA (two columns); the host sizes the
+// launch with the same function.
+struct Smem {
+    size_t pdp, coef, pk, misc, kc, ka, omcf, cld, seed, aer, xs, red, flux, total;
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+__host__ __device__ inline Smem smem_layout(int L, int nq, bool fused, bool aer_stage, size_t rsz) {
+    Smem m;
+    size_t o = 0;
+    m.pdp = o;  o = align16(o + COLS_PER_CTA * L * sizeof(double));
+    m.coef = o; o = align16(o + COLS_PER_CTA * NFR * L * rsz);
+    m.pk = o;   o = align16(o + COLS_PER_CTA * L * sizeof(int));
+    m.misc = o; o = align16(o + 8 * sizeof(int));
+    m.kc = m.ka = m.omcf = m.cld = m.seed = m.xs = m.aer = o;
+    if (fused) {
+        m.kc = o;   o = align16(o + COLS_PER_CTA * L * sizeof(long long));
+        m.ka = o;   o = align16(o + COLS_PER_CTA * L * sizeof(long long));
+        m.omcf = o; o = align16(o + COLS_PER_CTA * L * sizeof(double));
+        m.cld = o;  o = align16(o + COLS_PER_CTA * 4 * L * rsz);
+        m.seed = o; o = align16(o + COLS_PER_CTA * 4 * sizeof(uint32_t));
+        m.xs = o;   o = align16(o + NGPT * 32 * sizeof(uint32_t));
+    }
+    if (aer_stage) {
+        m.aer = o;  o = align16(o + COLS_PER_CTA * 3 * NBND * L * rsz);
+    }
+    m.red = o;  o = align16(o + KLEV * nq * CTA_THREADS * rsz);
+    m.flux = o; o = align16(o + COLS_PER_CTA * nq * (L + 1) * rsz);
+    m.total = o;
+    return m;
+}
+
+template <typename R>
+__host__ __device__ inline bool stage_aerosol(int iaer) {
+    // the FP32 form converts the FP64 aerosol inputs once per (column, layer, band)
+    return sizeof(R) == 4 && iaer != 0;
 }
 
 template <typename R>
@@ -147,14 +220,22 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = P.nlay;
     const int NQ = P.extra ? NQ_EXTRA : NQ_BASE;
-    double* sPdp = (double*)smem_raw;                      // [2][L]
-    R* sCoef = (R*)(sPdp + COLS_PER_CTA * L);              // [2][NFR][L]
-    int* sPk = (int*)(sCoef + COLS_PER_CTA * NFR * L);     // [2][L]
-    int* sMisc = sPk + COLS_PER_CTA * L;                   // [4]
-    size_t off = (size_t)((unsigned char*)(sMisc + 4) - smem_raw);
-    off = (off + 15) & ~(size_t)15;
-    R* sRed = (R*)(smem_raw + off);                        // [KLEV][NQ][224]
-    R* sFlux = sRed + KLEV * NQ * CTA_THREADS;              // [2][NQ][L+1]
+    const bool fused = P.fused && P.icld >= 1;
+    const bool aer_stage = stage_aerosol<R>(P.iaer);
+    const Smem M = smem_layout(L, NQ, fused, aer_stage, sizeof(R));
+    double* sPdp = (double*)(smem_raw + M.pdp);        // [2][L]
+    R* sCoef = (R*)(smem_raw + M.coef);                // [2][NFR][L]
+    int* sPk = (int*)(smem_raw + M.pk);                // [2][L]
+    int* sMisc = (int*)(smem_raw + M.misc);            // laytrop [2]
+    long long* sKc = (long long*)(smem_raw + M.kc);    // [2][L] McICA threshold of 1 - cldf
+    long long* sKa = (long long*)(smem_raw + M.ka);    // [2][L] McICA threshold of alpha
+    double* sOmcf = (double*)(smem_raw + M.omcf);      // [2][L] 1 - cldf (icld 2)
+    R* sCld = (R*)(smem_raw + M.cld);                  // [2][4][L] ciwp, clwp, rei, rel
+    uint32_t* sSeed = (uint32_t*)(smem_raw + M.seed);  // [2][4]
+    uint32_t* sXs = (uint32_t*)(smem_raw + M.xs);      // [112][32] columns of M^n
+    R* sAer = (R*)(smem_raw + M.aer);                  // [2][3][14][L] tau, ssa, asym
+    R* sRed = (R*)(smem_raw + M.red);                  // [KLEV][NQ][224]
+    R* sFlux = (R*)(smem_raw + M.flux);                // [2][NQ][L+1]
 
     const int tid = threadIdx.x;
     const int cc = tid / NGPT, g = tid % NGPT;
@@ -164,12 +245,59 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
     R* scr = (R*)P.scratch + (size_t)blockIdx.x * P.slot_elems;
     const size_t n = (size_t)P.ncol;
 
+    // McICA stream jump of this subcolumn: once per launch
+    KissJump J{1u, 0u, 1u, 1u};
+    if (fused) {
+        const uint64_t off = kiss_offset(P.icld, g, L, P.permuteseed);
+        J = kiss_jump_consts(off);
+        if (cc == 0) xorshift_power(off, sXs + g * 32);
+    }
+
     for (int pair = blockIdx.x; pair < P.npairs; pair += gridDim.x) {
         __syncthreads();
-        // ---------------- prep
+        // ---------------- prep: one (column, layer) per item, FP64
         for (int it = tid; it < COLS_PER_CTA * L; it += CTA_THREADS) {
             const int c2 = it / L, lay = it % L + 1;
-            prep_layer<R>(P, COLS_PER_CTA * pair + c2, lay, sCoef + c2 * NFR * L, sPk + c2 * L, sPdp + c2 * L, L, tab64);
+            const int pcol = COLS_PER_CTA * pair + c2;
+            prep_layer<R>(P, pcol, lay, sCoef + c2 * NFR * L, sPk + c2 * L, sPdp + c2 * L, L, tab64);
+            const bool real = pcol < P.ncol;
+            const size_t kl = (size_t)pcol + n * (size_t)(lay - 1);
+            if (fused) {
+                double cf = real ? P.cldfrac[kl] : 0.0;
+                if (cf < 1.0e-20) cf = 0.0;
+                const double omcf = DS(1.0, cf);
+                sOmcf[c2 * L + lay - 1] = omcf;
+                sKc[c2 * L + lay - 1] = kiss_threshold(omcf);
+                sKa[c2 * L + lay - 1] = (P.icld >= 4 && real) ? kiss_threshold(P.alpha[kl]) : 0ll;
+                R* cd = sCld + c2 * 4 * L;
+                cd[0 * L + lay - 1] = real ? (R)P.ciwp[kl] : R(0);
+                cd[1 * L + lay - 1] = real ? (R)P.clwp[kl] : R(0);
+                cd[2 * L + lay - 1] = real ? (R)P.rei[kl] : R(0);
+                cd[3 * L + lay - 1] = real ? (R)P.rel[kl] : R(0);
+                if (lay == 1) {
+                    uint32_t* sd = sSeed + c2 * 4;
+                    if (real) {
+                        const double p1 = DM(P.play[pcol], 1.e2), p2 = DM(P.play[pcol + n], 1.e2);
+                        if (p1 < p2) set_error(P.err, E_KISSSEED);
+                        sd[0] = kiss_seed(p1);
+                        sd[1] = kiss_seed(p2);
+                        sd[2] = kiss_seed(DM(P.play[pcol + 2 * n], 1.e2));
+                        sd[3] = kiss_seed(DM(P.play[pcol + 3 * n], 1.e2));
+                    } else {
+                        sd[0] = sd[1] = sd[2] = sd[3] = 1u;
+                    }
+                }
+            }
+            if (aer_stage) {
+                for (int b = 0; b < NBND; ++b) {
+                    double ta = 0.0, oa = 1.0, ga = 0.0;
+                    if (real) aerosol(P, pcol, lay, b, tab64, ta, oa, ga);
+                    R* ad = sAer + c2 * 3 * NBND * L;
+                    ad[(0 * NBND + b) * L + lay - 1] = (R)ta;
+                    ad[(1 * NBND + b) * L + lay - 1] = (R)DS(1.0, oa);  // co-albedo, formed in FP64
+                    ad[(2 * NBND + b) * L + lay - 1] = (R)ga;
+                }
+            }
         }
         __syncthreads();
         if (g == 0) {
@@ -187,72 +315,102 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
         }
 
         // ---------------- per (column, g-point) setup
-        double zincflx = 0.0, albp = 0.0, albd = 0.0, cossza = 1.0;
-        McicaKiss mc;
+        R zinc = R(0), albp = R(0), albd = R(0);
+        double cossza = 1.0;
+        McicaMask mc;
         if (active) {
             cossza = P.coszen[col];
             if (cossza < 1.e-10) cossza = 1.e-10;
             const bool nir = ib <= 8 || ib == 13;
-            albp = nir ? P.aldir[col] : P.asdir[col];
-            albd = nir ? P.aldif[col] : P.asdif[col];
-            zincflx = DM(DM(P.adjflux[ib], solar_source<R>(ib, igb, C, P, tab)), cossza);
-            if (P.fused && P.icld >= 1) mc.init(P.play, n, col, g, L, P.icld, P.permuteseed, P.err);
+            albp = (R)(nir ? P.aldir[col] : P.asdir[col]);
+            albd = (R)(nir ? P.aldif[col] : P.asdif[col]);
+            // zincflx = adjflux * ssi * prmu0 (spcvmc:349-356)
+            R src;
+            if constexpr (sizeof(R) == 4) src = solar_source_generic(ib, igb, C, P, tab);
+            else src = solar_source<R>(ib, igb, C, P, tab);
+            zinc = R(P.adjflux[ib]) * src * (R)cossza;
+            if (fused) mc.start(kiss_start(sSeed + cc * 4, J, sXs + g * 32), P.icld);
         }
         const R prmu0 = (R)cossza;
+        const R* cld = sCld + cc * 4 * L;
+        const R* aer = sAer + cc * 3 * NBND * L;
 
         // ---------------- pass 1: bottom -> top
-        R rupc_b = (R)albp, rupdc_b = (R)albd, rup_b = (R)albp, rupd_b = (R)albd;
+        R rupc_b = albp, rupdc_b = albd, rup_b = albp, rupd_b = albd;
         for (int lay = 1; lay <= L; ++lay) {
             const int jk = L + 1 - lay;
             R* sv = scr + (size_t)(jk - 1) * NS * CTA_THREADS + tid;
             if (!active) continue;
             R taug, taur;
-            taumol_g<R>(ib, igb, lay, C, tab, taug, taur);
-            double ta, oa, ga;
-            aerosol(P, col, lay, ib, tab64, ta, oa, ga);
+            if constexpr (sizeof(R) == 4) {
+                int js;
+                float fs;
+                taumol_generic(ib, igb, lay, C, tab, taug, taur, js, fs);
+            } else {
+                taumol_g<R>(ib, igb, lay, C, tab, taug, taur);
+            }
+            R rta, roa, rga, rcoa;
+            if (aer_stage) {
+                rta = aer[(0 * NBND + ib) * L + lay - 1];
+                rcoa = aer[(1 * NBND + ib) * L + lay - 1];
+                roa = R(1) - rcoa;
+                rga = aer[(2 * NBND + ib) * L + lay - 1];
+            } else if (P.iaer == 0) {
+                rta = R(0); roa = R(1); rga = R(0); rcoa = R(0);
+            } else {
+                double ta, oa, ga;
+                aerosol(P, col, lay, ib, tab64, ta, oa, ga);
+                rta = (R)ta; roa = (R)oa; rga = (R)ga; rcoa = (R)DS(1.0, oa);
+            }
             // cloud of this subcolumn (McICA) at this layer
-            double cldf = 0.0, ciwp = 0.0, clwp = 0.0, tauc = 0.0, ssac = 1.0, asmc = 0.0, fsfc = 0.0, rei = 0.0, rel = 0.0;
+            bool cloudy = false;
+            R cldf = R(0), tc = R(0), oc = R(1), gc = R(0), fsfc = R(0), ciwp = R(0), clwp = R(0), rei = R(0),
+              rel = R(0);
             if (P.icld >= 1) {
                 const size_t kl = (size_t)col + n * (size_t)(lay - 1);
-                if (P.fused) {
-                    if (mc.step(lay, P.cldfrac[kl], P.icld >= 4 ? P.alpha[kl] : 0.0)) {
-                        const size_t kb = (size_t)ib + 14 * kl;
-                        cldf = 1.0;
-                        ciwp = P.ciwp[kl];
-                        clwp = P.clwp[kl];
+                if (fused) {
+                    cloudy = mc.step(lay, sKc[cc * L + lay - 1], sKa[cc * L + lay - 1], sOmcf[cc * L + lay - 1]);
+                    if (cloudy) {
+                        cldf = R(1);
+                        ciwp = cld[0 * L + lay - 1];
+                        clwp = cld[1 * L + lay - 1];
                         if (P.tauc) {
-                            tauc = P.tauc[kb];
-                            ssac = P.ssac[kb];
-                            asmc = P.asmc[kb];
-                            fsfc = P.fsfc[kb];
+                            const size_t kb = (size_t)ib + 14 * kl;
+                            tc = (R)P.tauc[kb];
+                            oc = (R)P.ssac[kb];
+                            gc = (R)P.asmc[kb];
+                            fsfc = (R)P.fsfc[kb];
                         }
                     }
-                    rei = P.rei[kl];
-                    rel = P.rel[kl];
+                    rei = cld[2 * L + lay - 1];
+                    rel = cld[3 * L + lay - 1];
                 } else {
                     const size_t kg = (size_t)g + NGPT * kl;
-                    cldf = P.cldfmcl[kg];
-                    tauc = P.taucmcl[kg];
-                    ssac = P.ssacmcl[kg];
-                    asmc = P.asmcmcl[kg];
-                    fsfc = P.fsfcmcl[kg];
-                    ciwp = P.ciwpmcl[kg];
-                    clwp = P.clwpmcl[kg];
-                    rei = P.reicmcl[kl];
-                    rel = P.relqmcl[kl];
+                    const double cf = P.cldfmcl[kg];
+                    cloudy = cf != 0.0;
+                    cldf = (R)cf;
+                    tc = (R)P.taucmcl[kg];
+                    oc = (R)P.ssacmcl[kg];
+                    gc = (R)P.asmcmcl[kg];
+                    fsfc = (R)P.fsfcmcl[kg];
+                    ciwp = (R)P.ciwpmcl[kg];
+                    clwp = (R)P.clwpmcl[kg];
+                    rei = (R)P.reicmcl[kl];
+                    rel = (R)P.relqmcl[kl];
                 }
             }
-            R tc = (R)tauc, oc = (R)ssac, gc = (R)asmc, taor = (R)tauc;
-            if (P.icld >= 1)
-                cldprmc_g<R>(ib, P.inflag, P.iceflag, P.liqflag, (R)cldf, (R)ciwp, (R)clwp, (R)rei, (R)rel, (R)fsfc,
-                             tc, oc, gc, taor, tab, P.err);
+            R taor = tc, coc = R(1) - oc;
+            if (P.icld >= 1 && cloudy)
+                cldprmc_g<R>(ib, P.inflag, P.iceflag, P.liqflag, cldf, ciwp, clwp, rei, rel, fsfc, tc, oc, gc, taor,
+                             coc, tab, P.err);
             // clear-sky optics including aerosols (spcvmc:442-445)
-            const R rta = (R)ta, roa = (R)oa, rga = (R)ga;
             R ztauc = taur + taug + rta;
             R zomcc = taur * R(1) + rta * roa;
             R zgcc = rga * roa * rta / zomcc;
+            R zcoc = R(0);
+            if constexpr (sizeof(R) == 4) zcoc = (taug + rta * rcoa) / ztauc;  // co-albedo
             zomcc = zomcc / ztauc;
-            const R zclear = R(1) - (R)cldf, zcloud = (R)cldf;
+            const R zclear = R(1) - cldf, zcloud = cldf;
             if (P.idelm == 0) {
                 const R zdbtmc = tbl_exp<R>(ztauc / prmu0, tab);
                 const R tauorig = ztauc + taor;
@@ -266,19 +424,30 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
             ztauc = (R(1) - zwf) * ztauc;
             zomcc = (zomcc - zwf) / (R(1) - zwf);
             zgcc = (zgcc - zf) / (R(1) - zf);
-            const RT<R> rc = reftra_g<R>(ztauc, zomcc, zgcc, prmu0, tab);
+            if constexpr (sizeof(R) == 4) zcoc = zcoc / (R(1) - zwf);
+            const RT<R> rc = reftra_g<R>(ztauc, zomcc, zcoc, zgcc, prmu0, tab, tab64);
             const R zdbtc = tbl_exp<R>(ztauc / prmu0, tab);
             RT<R> rt = rc;
             R zdbt = zdbtc;
-            if (cldf != 0.0) {
-                // total sky: clear + delta-scaled cloud (spcvmc:500-505), reftra
-                // only where cldf > repclc (:427), mixed by cloud fraction (:546-549)
+            if (cloudy) {
+                // total sky: clear + delta-scaled cloud (spcvmc:500-505); reftra
+                // only where cldf > repclc (:427); mixed by cloud fraction (:546-549)
                 const R ztauo = ztauc + tc;
                 R zomco = ztauc * zomcc + tc * oc;
                 const R zgco = (tc * oc * gc + ztauc * zomcc * zgcc) / zomco;
+                R zcoo = R(0);
+                if constexpr (sizeof(R) == 4) zcoo = (ztauc * zcoc + tc * coc) / ztauo;
                 zomco = zomco / ztauo;
                 RT<R> ro;
-                if (cldf > 1.e-12) ro = reftra_g<R>(ztauo, zomco, zgco, prmu0, tab);
+                if (cldf > R(1.e-12)) {
+                    int force = -1;
+                    if constexpr (sizeof(R) == 4) {
+                        const float r = one_minus_zwo(zomco, zcoo, zgco);
+                        if (fabsf(r - 5.0e-7f) <= 1.5e-11f)
+                            force = decide_conservative64(P, col, g, lay, ib, ztauc, zomcc, zgcc, zcoc, tab64);
+                    }
+                    ro = reftra_g<R>(ztauo, zomco, zcoo, zgco, prmu0, tab, tab64, force);
+                }
                 else { ro.ref = R(0); ro.tra = R(1); ro.refd = R(0); ro.trad = R(1); }
                 rt.ref = zclear * rc.ref + zcloud * ro.ref;
                 rt.refd = zclear * rc.refd + zcloud * ro.refd;
@@ -322,7 +491,6 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
         R tdbtc = R(1), tdnc = R(1), rdndc = R(0);
         R tdbt = R(1), tdn = R(1), rdnd = R(0);
         R tdbtcn = R(1), tdbtn = R(1);
-        const R zinc = (R)zincflx;
         for (int jk = 1; jk <= L + 1; ++jk) {
             R q[NQ_EXTRA];
 #pragma unroll
@@ -341,7 +509,7 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
                 rup = sv[S_RUP * CTA_THREADS]; rupd = sv[S_RUPD * CTA_THREADS];
                 if (P.idelm == 0) { dbtcn = sv[S_DBTCN * CTA_THREADS]; dbtn = sv[S_DBTN * CTA_THREADS]; }
             } else {
-                rupc = (R)albp; rupdc = (R)albd; rup = (R)albp; rupd = (R)albd;
+                rupc = albp; rupdc = albd; rup = albp; rupd = albd;
             }
             if (active) {
                 // level fluxes (vrtqdr:163-169)

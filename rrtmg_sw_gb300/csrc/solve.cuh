@@ -66,13 +66,20 @@ struct Coef {
 // as the reference's expressions do.  The FP32 form may contract.
 template <typename R> __device__ inline R rcp(R x) { return R(1) / x; }
 
+template <typename R> __device__ inline R c_bpade();
+template <> __device__ inline double c_bpade<double>() { return cT.bpade; }
+template <> __device__ inline float c_bpade<float>() { return cT.bpade_f; }
+template <typename R> __device__ inline R c_oneminus();
+template <> __device__ inline double c_oneminus<double>() { return cT.oneminus; }
+template <> __device__ inline float c_oneminus<float>() { return cT.oneminus_f; }
+
 // exp(-x) through the lookup table, or the quadratic below od_lo
 // (rrtmg_sw_reftra.f90:203-209; table built at rrtmg_sw_init.f90:115-123)
 template <typename R>
 __device__ inline R tbl_exp(R ze1, const R* __restrict__ tab) {
     const R od_lo = R(0.06);
     if (ze1 <= od_lo) return R(1) - ze1 + R(0.5) * ze1 * ze1;
-    const R tblind = ze1 / (R(cT.bpade) + ze1);
+    const R tblind = ze1 / (c_bpade<R>() + ze1);
     const int itind = (int)(R(10000) * tblind + R(0.5));
     return __ldg(tab + cT.exp_tbl + itind);
 }
@@ -90,7 +97,7 @@ __device__ inline Spec<R> spec(R cola, R colb_scaled, R mult, const Coef<R>& c, 
     Spec<R> s;
     s.speccomb = cola + colb_scaled;
     R specparm = cola / s.speccomb;
-    if (specparm >= R(cT.oneminus)) specparm = R(cT.oneminus);
+    if (specparm >= c_oneminus<R>()) specparm = c_oneminus<R>();
     const R specmult = mult * (specparm);
     const int ij = (int)specmult;
     s.js = 1 + ij;
@@ -303,6 +310,60 @@ __device__ inline void taumol_g(int ib, int ig, int lay, const Coef<R>& c, const
     }
 }
 
+// One g-point of taumol16..29 through the band/region descriptors (FP32
+// form): same terms as taumol_g, one instruction stream for all bands.
+__device__ inline void taumol_generic(int ib, int ig, int lay, const Coef<float>& c, const float* __restrict__ tab,
+                                      float& taug, float& taur, int& js_out, float& fs_out) {
+    const BandOff& B = cT.b[ib];
+    const TmRegion& d = cT.tm[ib][lay <= c.laytrop ? 0 : 1];
+    const int ng = B.ng;
+    const int jp = c.jp(lay) - d.jo, jt = c.jt(lay), jt1 = c.jt1(lay);
+    const float colh2o = c.f(F_H2O, lay);
+    float tg = 0.0f, fs = 0.0f;
+    int js = 1;
+    if (d.kind == 1) {
+        const float ca = c.f(F_H2O + d.sa, lay);
+        const float speccomb = ca + d.strrat * c.f(F_H2O + d.sb, lay);
+        const float specparm = fminf(ca / speccomb, cT.oneminus_f);
+        const float specmult = d.mult * specparm;
+        const int ij = (int)specmult;
+        js = 1 + ij;
+        fs = specmult - (float)ij;
+        const float f00 = c.f(F_FAC00, lay), f01 = c.f(F_FAC01, lay), f10 = c.f(F_FAC10, lay), f11 = c.f(F_FAC11, lay);
+        const int nsp = d.nsp;
+        const int i0 = ((jp * 5 + (jt - 1)) * nsp + js - 1) * ng + ig - 1;
+        const int i1 = (((jp + 1) * 5 + (jt1 - 1)) * nsp + js - 1) * ng + ig - 1;
+        const float* k = tab + d.ktab;
+        const float gs = 1.0f - fs;
+        const float k0 = gs * f00 * __ldg(k + i0) + fs * f00 * __ldg(k + i0 + ng) +
+                         gs * f10 * __ldg(k + i0 + nsp * ng) + fs * f10 * __ldg(k + i0 + (nsp + 1) * ng);
+        const float k1 = gs * f01 * __ldg(k + i1) + fs * f01 * __ldg(k + i1 + ng) +
+                         gs * f11 * __ldg(k + i1 + nsp * ng) + fs * f11 * __ldg(k + i1 + (nsp + 1) * ng);
+        tg = speccomb * (k0 + k1);
+    } else if (d.kind == 2) {
+        const int i0 = (jp * 5 + (jt - 1)) * ng + ig - 1;
+        const int i1 = ((jp + 1) * 5 + (jt1 - 1)) * ng + ig - 1;
+        const float* k = tab + d.ktab;
+        const float kk = c.f(F_FAC00, lay) * __ldg(k + i0) + c.f(F_FAC10, lay) * __ldg(k + i0 + ng) +
+                         c.f(F_FAC01, lay) * __ldg(k + i1) + c.f(F_FAC11, lay) * __ldg(k + i1 + ng);
+        tg = c.f(F_H2O + d.sa, lay) * d.fac * kk;
+    }
+    if (d.cont == 1) tg += colh2o * (selfterm(c, lay, B, tab, ig) + forterm(c, lay, B, tab, ig));
+    else if (d.cont == 2) tg += colh2o * forterm(c, lay, B, tab, ig);
+    if (d.minor == 9) tg += 4.35e-4f * c.f(F_O2, lay) / 700.0f;
+    else if (d.minor >= 0) tg += c.f(F_H2O + d.minor, lay) * __ldg(tab + d.mtab + ig - 1);
+    const float colmol = c.f(F_MOL, lay);
+    if (d.rtype == 0) taur = colmol * __ldg(tab + d.rtab);
+    else if (d.rtype == 1) taur = colmol * __ldg(tab + d.rtab + ig - 1);
+    else {
+        const float ra = __ldg(tab + d.rtab + (js - 1) * ng + ig - 1), rb = __ldg(tab + d.rtab + js * ng + ig - 1);
+        taur = colmol * (ra + fs * (rb - ra));
+    }
+    taug = tg;
+    js_out = js;
+    fs_out = fs;
+}
+
 // Layer at which each band takes its solar source (the laysolfr logic of
 // taumol16..29): bands whose source sits below laytrop scan the lower loop,
 // the others the upper loop; a later match overrides an earlier one.
@@ -336,12 +397,12 @@ __device__ inline int solar_layer(int ib, const Coef<R>& c) {
 // Solar source of g-point ig at its reference layer: sfluxzen (isolvar<0)
 // or ssi (isolvar>=0), e.g. taumol.f90:364-378 and 495-517.
 template <typename R>
-__device__ inline double solar_source(int ib, int ig, const Coef<R>& c, const SolveParams& P, const R* __restrict__ tab) {
+__device__ inline R solar_source(int ib, int ig, const Coef<R>& c, const SolveParams& P, const R* __restrict__ tab) {
     const BandOff& B = cT.b[ib];
     const int band = ib + 16;
     const int lay = solar_layer(ib, c);
     bool interp = false;
-    double fs = 0.0;
+    R fs = R(0);
     int js = 1;
     if (lay >= 1) {
         const R colh2o = c.f(F_H2O, lay), colco2 = c.f(F_CO2, lay), colo3 = c.f(F_O3, lay);
@@ -357,20 +418,51 @@ __device__ inline double solar_source(int ib, int ig, const Coef<R>& c, const So
         case 28: s = spec(colo3, R(6.67029e-07) * colo2, R(4), c, lay); interp = true; break;
         default: break;
         }
-        if (interp) { js = s.js; fs = (double)s.fs; }
+        if (interp) { js = s.js; fs = s.fs; }
     }
-    auto src = [&](int off) -> double {
-        if (!interp) return (double)V(tab, off, ig - 1);
-        const double a = (double)V(tab, off, (js - 1) * B.ng + ig - 1), b = (double)V(tab, off, js * B.ng + ig - 1);
+    auto src = [&](int off) -> R {
+        if (!interp) return V(tab, off, ig - 1);
+        const R a = V(tab, off, (js - 1) * B.ng + ig - 1), b = V(tab, off, js * B.ng + ig - 1);
         return a + fs * (b - a);
     };
     if (P.isolvar < 0) {
-        const double sf = src(B.sfluxref);
-        return band == 27 ? (50.15 / 48.37) * sf : sf;
+        const R sf = src(B.sfluxref);
+        return band == 27 ? R(50.15 / 48.37) * sf : sf;
     }
-    const double fb = src(B.facbrght), sd = src(B.snsptdrk), ir = src(B.irradnce);
-    if (P.isolvar == 3) return P.svar_f_bnd[ib] * fb + P.svar_s_bnd[ib] * sd + P.svar_i_bnd[ib] * ir;
-    return P.svar_f * fb + P.svar_s * sd + P.svar_i * ir;
+    const R fb = src(B.facbrght), sd = src(B.snsptdrk), ir = src(B.irradnce);
+    if (P.isolvar == 3) return R(P.svar_f_bnd[ib]) * fb + R(P.svar_s_bnd[ib]) * sd + R(P.svar_i_bnd[ib]) * ir;
+    return R(P.svar_f) * fb + R(P.svar_s) * sd + R(P.svar_i) * ir;
+}
+
+// Solar source for the FP32 form through the descriptors: the species
+// interpolation of the source tables applies where the source region is a
+// kind-1 (speccomb) loop, as in taumol17,18,19,21,22,24,28.
+__device__ inline float solar_source_generic(int ib, int ig, const Coef<float>& c, const SolveParams& P,
+                                             const float* __restrict__ tab) {
+    const BandOff& B = cT.b[ib];
+    const int band = ib + 16;
+    const int lay = solar_layer(ib, c);
+    const int up = (band == 16 || band == 17 || band == 27 || band == 28 || band == 29) ? 1 : 0;
+    bool interp = false;
+    int js = 1;
+    float fs = 0.0f;
+    if (lay >= 1 && cT.tm[ib][up].kind == 1) {
+        float tg, tr;
+        taumol_generic(ib, ig, lay, c, tab, tg, tr, js, fs);
+        interp = true;
+    }
+    auto src = [&](int off) -> float {
+        if (!interp) return __ldg(tab + off + ig - 1);
+        const float a = __ldg(tab + off + (js - 1) * B.ng + ig - 1), b = __ldg(tab + off + js * B.ng + ig - 1);
+        return a + fs * (b - a);
+    };
+    if (P.isolvar < 0) {
+        const float sf = src(B.sfluxref);
+        return band == 27 ? float(50.15 / 48.37) * sf : sf;
+    }
+    const float fb = src(B.facbrght), sd = src(B.snsptdrk), ir = src(B.irradnce);
+    if (P.isolvar == 3) return float(P.svar_f_bnd[ib]) * fb + float(P.svar_s_bnd[ib]) * sd + float(P.svar_i_bnd[ib]) * ir;
+    return float(P.svar_f) * fb + float(P.svar_s) * sd + float(P.svar_i) * ir;
 }
 
 // --------------------------------------------------------------- cldprmc
@@ -380,20 +472,22 @@ __device__ inline double solar_source(int ib, int ig, const Coef<R>& c, const So
 template <typename R>
 __device__ inline void cldprmc_g(int ib, int inflag, int iceflag, int liqflag, R cldf, R ciwp,
                                  R clwp, R rei, R rel, R fsfc, R& tauc,
-                                 R& ssac, R& asmc, R& taor, const R* __restrict__ tab,
+                                 R& ssac, R& asmc, R& taor, R& co, const R* __restrict__ tab,
                                  int* err) {
     typedef R double_;
-    const R eps = R(1.e-06), cldmin = R(1.e-20);
+    const R eps = R((1.e-06)), cldmin = R((1.e-20));
     taor = tauc;
+    co = R(1) - ssac;  // co-albedo (used by the FP32 form only)
     const double_ cwp = ciwp + clwp;
     if (!(cldf >= cldmin && (cwp >= cldmin || tauc >= cldmin))) return;
     if (inflag == 0) {
         const double_ taucldorig_a = tauc;
         const double_ ffp = fsfc;
-        const double_ ffp1 = 1.0 - ffp;
-        const double_ ffpssa = 1.0 - ffp * ssac;
+        const double_ ffp1 = R(1.0) - ffp;
+        const double_ ffpssa = R(1.0) - ffp * ssac;
         const double_ ssacloud_a = ffp1 * ssac / ffpssa;
         const double_ taucloud_a = ffpssa * taucldorig_a;
+        co = (R(1) - ssac) / ffpssa;
         taor = taucldorig_a;
         ssac = ssacloud_a;
         tauc = taucloud_a;
@@ -402,82 +496,94 @@ __device__ inline void cldprmc_g(int ib, int inflag, int iceflag, int liqflag, R
     }
     if (inflag != 2) { set_error(err, E_INFLAG1); return; }
     double_ extcoice = 0, ssacoice = 0, gice = 0, forwice = 0, extcoliq = 0, ssacoliq = 0, gliq = 0, forwliq = 0;
+    double_ coice = 1, coliq = 1;  // 1 - ssacoice, 1 - ssacoliq from the co-albedo tables
     const int jb = ib + 1;  // band column of the Fortran (index, 16:29) LUTs, 1-based
     auto lut = [&](int off, int n, int index) { return __ldg(tab + off + (jb - 1) * n + index - 1); };
-    if (ciwp == 0.0) {
+    if (ciwp == R(0.0)) {
     } else if (iceflag == 1) {
-        if (rei < 13.0 || rei > 130.0) { set_error(err, E_ICERAD); return; }
+        if (rei < R(13.0) || rei > R(130.0)) { set_error(err, E_ICERAD); return; }
         const double_ w2 = __ldg(tab + cT.wavenum2 + ib);
         int icx = 0;
-        if (w2 > 1.43e04) icx = 1;
-        else if (w2 > 7.7e03) icx = 2;
-        else if (w2 > 5.3e03) icx = 3;
-        else if (w2 > 4.0e03) icx = 4;
-        else if (w2 >= 2.5e03) icx = 5;
+        if (w2 > R(1.43e04)) icx = 1;
+        else if (w2 > R(7.7e03)) icx = 2;
+        else if (w2 > R(5.3e03)) icx = 3;
+        else if (w2 > R(4.0e03)) icx = 4;
+        else if (w2 >= R(2.5e03)) icx = 5;
         extcoice = (__ldg(tab + cT.abari + icx - 1) + __ldg(tab + cT.bbari + icx - 1) / rei);
-        ssacoice = 1.0 - __ldg(tab + cT.cbari + icx - 1) - __ldg(tab + cT.dbari + icx - 1) * rei;
+        ssacoice = R(1.0) - __ldg(tab + cT.cbari + icx - 1) - __ldg(tab + cT.dbari + icx - 1) * rei;
+        coice = __ldg(tab + cT.cbari + icx - 1) + __ldg(tab + cT.dbari + icx - 1) * rei;
         gice = __ldg(tab + cT.ebari + icx - 1) + __ldg(tab + cT.fbari + icx - 1) * rei;
-        if (gice >= 1.0) gice = 1.0 - eps;
+        if (gice >= R(1.0)) gice = R(1.0) - eps;
         forwice = gice * gice;
-        if (extcoice < 0.0 || ssacoice > 1.0 || ssacoice < 0.0 || gice > 1.0 || gice < 0.0) { set_error(err, E_ICEPROP); return; }
+        if (extcoice < R(0.0) || ssacoice > R(1.0) || ssacoice < R(0.0) || gice > R(1.0) || gice < R(0.0)) { set_error(err, E_ICEPROP); return; }
     } else if (iceflag == 2) {
-        if (rei < 5.0 || rei > 131.0) { set_error(err, E_ICERAD); return; }
-        const double_ factor = (rei - 2.0) / 3.0;
+        if (rei < R(5.0) || rei > R(131.0)) { set_error(err, E_ICERAD); return; }
+        const double_ factor = (rei - R(2.0)) / R(3.0);
         int index = (int)factor;
         if (index == 43) index = 42;
         const double_ fint = factor - (double_)index;
         extcoice = lut(cT.extice2, 43, index) + fint * (lut(cT.extice2, 43, index + 1) - lut(cT.extice2, 43, index));
         ssacoice = lut(cT.ssaice2, 43, index) + fint * (lut(cT.ssaice2, 43, index + 1) - lut(cT.ssaice2, 43, index));
+        coice = lut(cT.coice2, 43, index) + fint * (lut(cT.coice2, 43, index + 1) - lut(cT.coice2, 43, index));
         gice = lut(cT.asyice2, 43, index) + fint * (lut(cT.asyice2, 43, index + 1) - lut(cT.asyice2, 43, index));
         forwice = gice * gice;
-        if (extcoice < 0.0 || ssacoice > 1.0 || ssacoice < 0.0 || gice > 1.0 || gice < 0.0) { set_error(err, E_ICEPROP); return; }
+        if (extcoice < R(0.0) || ssacoice > R(1.0) || ssacoice < R(0.0) || gice > R(1.0) || gice < R(0.0)) { set_error(err, E_ICEPROP); return; }
     } else if (iceflag == 3) {
-        if (rei < 5.0 || rei > 140.0) { set_error(err, E_ICEDGE); return; }
-        const double_ factor = (rei - 2.0) / 3.0;
+        if (rei < R(5.0) || rei > R(140.0)) { set_error(err, E_ICEDGE); return; }
+        const double_ factor = (rei - R(2.0)) / R(3.0);
         int index = (int)factor;
         if (index == 46) index = 45;
         const double_ fint = factor - (double_)index;
         extcoice = lut(cT.extice3, 46, index) + fint * (lut(cT.extice3, 46, index + 1) - lut(cT.extice3, 46, index));
         ssacoice = lut(cT.ssaice3, 46, index) + fint * (lut(cT.ssaice3, 46, index + 1) - lut(cT.ssaice3, 46, index));
+        coice = lut(cT.coice3, 46, index) + fint * (lut(cT.coice3, 46, index + 1) - lut(cT.coice3, 46, index));
         gice = lut(cT.asyice3, 46, index) + fint * (lut(cT.asyice3, 46, index + 1) - lut(cT.asyice3, 46, index));
         const double_ fdelta = lut(cT.fdlice3, 46, index) + fint * (lut(cT.fdlice3, 46, index + 1) - lut(cT.fdlice3, 46, index));
-        if (fdelta < 0.0 || fdelta > 1.0) { set_error(err, E_ICEPROP); return; }
-        forwice = fdelta + 0.5 / ssacoice;
+        if (fdelta < R(0.0) || fdelta > R(1.0)) { set_error(err, E_ICEPROP); return; }
+        forwice = fdelta + R(0.5) / ssacoice;
         if (forwice > gice) forwice = gice;
-        if (extcoice < 0.0 || ssacoice > 1.0 || ssacoice < 0.0 || gice > 1.0 || gice < 0.0) { set_error(err, E_ICEPROP); return; }
+        if (extcoice < R(0.0) || ssacoice > R(1.0) || ssacoice < R(0.0) || gice > R(1.0) || gice < R(0.0)) { set_error(err, E_ICEPROP); return; }
     }
-    if (clwp == 0.0) {
+    if (clwp == R(0.0)) {
     } else if (liqflag == 1) {
-        if (rel < 2.5 || rel > 60.0) { set_error(err, E_LIQRAD); return; }
-        int index = (int)(rel - 1.5);
+        if (rel < R(2.5) || rel > R(60.0)) { set_error(err, E_LIQRAD); return; }
+        int index = (int)(rel - R(1.5));
         if (index == 0) index = 1;
         if (index == 58) index = 57;
-        const double_ fint = rel - 1.5 - (double_)index;
+        const double_ fint = rel - R(1.5) - (double_)index;
         extcoliq = lut(cT.extliq1, 58, index) + fint * (lut(cT.extliq1, 58, index + 1) - lut(cT.extliq1, 58, index));
         ssacoliq = lut(cT.ssaliq1, 58, index) + fint * (lut(cT.ssaliq1, 58, index + 1) - lut(cT.ssaliq1, 58, index));
-        if (fint < 0.0 && ssacoliq > 1.0) ssacoliq = lut(cT.ssaliq1, 58, index);
+        coliq = lut(cT.coliq1, 58, index) + fint * (lut(cT.coliq1, 58, index + 1) - lut(cT.coliq1, 58, index));
+        if (fint < R(0.0) && ssacoliq > R(1.0)) {
+            ssacoliq = lut(cT.ssaliq1, 58, index);
+            coliq = lut(cT.coliq1, 58, index);
+        }
         gliq = lut(cT.asyliq1, 58, index) + fint * (lut(cT.asyliq1, 58, index + 1) - lut(cT.asyliq1, 58, index));
         forwliq = gliq * gliq;
-        if (extcoliq < 0.0 || ssacoliq > 1.0 || ssacoliq < 0.0 || gliq > 1.0 || gliq < 0.0) { set_error(err, E_LIQPROP); return; }
+        if (extcoliq < R(0.0) || ssacoliq > R(1.0) || ssacoliq < R(0.0) || gliq > R(1.0) || gliq < R(0.0)) { set_error(err, E_LIQPROP); return; }
     }
     const double_ tauliqorig = clwp * extcoliq;
     const double_ tauiceorig = ciwp * extcoice;
     taor = tauliqorig + tauiceorig;
-    const double_ ssaliq = ssacoliq * (1.0 - forwliq) / (1.0 - forwliq * ssacoliq);
-    const double_ tauliq = (1.0 - forwliq * ssacoliq) * tauliqorig;
-    const double_ ssaice = ssacoice * (1.0 - forwice) / (1.0 - forwice * ssacoice);
-    const double_ tauice = (1.0 - forwice * ssacoice) * tauiceorig;
+    const double_ ssaliq = ssacoliq * (R(1.0) - forwliq) / (R(1.0) - forwliq * ssacoliq);
+    const double_ tauliq = (R(1.0) - forwliq * ssacoliq) * tauliqorig;
+    const double_ ssaice = ssacoice * (R(1.0) - forwice) / (R(1.0) - forwice * ssacoice);
+    const double_ tauice = (R(1.0) - forwice * ssacoice) * tauiceorig;
     const double_ scatliq = ssaliq * tauliq;
     double_ scatice = ssaice * tauice;
     tauc = tauliq + tauice;
-    if (tauc == 0.0) tauc = cldmin;
-    if (scatice == 0.0) scatice = cldmin;
+    const bool zero = tauc == R(0.0);
+    if (tauc == R(0.0)) tauc = cldmin;
+    if (scatice == R(0.0)) scatice = cldmin;
     ssac = (scatliq + scatice) / tauc;
+    // absorption depth tau*(1 - ssa) of each phase is invariant under the
+    // delta scaling: tauliqorig*(1 - ssacoliq) + tauiceorig*(1 - ssacoice)
+    co = zero ? R(0) : (tauliqorig * coliq + tauiceorig * coice) / tauc;
     if (iceflag == 3) {
-        asmc = (1.0 / (scatliq + scatice)) *
-               (scatliq * (gliq - forwliq) / (1.0 - forwliq) + scatice * ((gice - forwice) / (1.0 - forwice)));
+        asmc = (R(1.0) / (scatliq + scatice)) *
+               (scatliq * (gliq - forwliq) / (R(1.0) - forwliq) + scatice * ((gice - forwice) / (R(1.0) - forwice)));
     } else {
-        asmc = (scatliq * (gliq - forwliq) / (1.0 - forwliq) + scatice * (gice - forwice) / (1.0 - forwice)) /
+        asmc = (scatliq * (gliq - forwliq) / (R(1.0) - forwliq) + scatice * (gice - forwice) / (R(1.0) - forwice)) /
                (scatliq + scatice);
     }
 }
@@ -487,12 +593,19 @@ __device__ inline void cldprmc_g(int ib, int inflag, int iceflag, int liqflag, R
 template <typename R>
 struct RT { R ref, refd, tra, trad; };
 
+// zco = 1 - zw carried separately by the FP32 form (unused by FP64);
+// tab64 is the FP64 table blob (the FP32 form's FP64 island needs it)
+// force: -1 = decide the conservative branch here, 0/1 = branch decided by
+// the caller (FP32 form, see decide_conservative64)
 template <typename R>
-__device__ inline RT<R> reftra_g(R zto1, R zw, R zg, R prmuz, const R* __restrict__ tab);
+__device__ inline RT<R> reftra_g(R zto1, R zw, R zco, R zg, R prmuz, const R* __restrict__ tab,
+                                 const double* __restrict__ tab64, int force = -1);
 
 // FP64 form: the reference's expressions verbatim
-template <>
-__device__ inline RT<double> reftra_g<double>(double zto1, double zw, double zg, double prmuz, const double* __restrict__ tab) {
+namespace {
+// out of line: one copy serves the clear-sky and the cloudy call
+__device__ __noinline__ RT<double> reftra_fp64(double zto1, double zw, double zg, double prmuz,
+                                               const double* __restrict__ tab) {
     typedef double R;
     RT<R> o;
     const R zwcrit = 0.9999995, eps = 1.e-08;
@@ -558,16 +671,41 @@ __device__ inline RT<double> reftra_g<double>(double zto1, double zw, double zg,
     }
     return o;
 }
+}  // namespace
+
+template <>
+__device__ inline RT<double> reftra_g<double>(double zto1, double zw, double zco, double zg, double prmuz,
+                                             const double* __restrict__ tab, const double* __restrict__ tab64,
+                                             int force) {
+    (void)zco;
+    (void)tab64;
+    (void)force;
+    return reftra_fp64(zto1, zw, zg, prmuz, tab);
+}
+
+// 1 - zwo of reftra:183-186 from the co-albedo (zwo = zw / (1 - zco q^2),
+// q = zg / (1 - zg)); returns 1 when the reference leaves zwo = 0.
+template <typename R>
+__device__ inline R one_minus_zwo(R zw, R zco, R zg) {
+    if (zg == R(1)) return zw > R(0) ? zco : R(1);
+    const R q = zg / (R(1) - zg);
+    const R q2 = q * q;
+    const R denom = R(1) - zco * q2;
+    if (!(zw > R(0) && denom != R(0))) return R(1);
+    return zco * (R(1) - q2) / denom;
+}
 
 // ------------------------------------------------------------------ KISS
-// KISS generator (mcica_subcol_gen_sw.f90:721-753) with O(log n) jumps:
-// the congruential part is an affine map mod 2^32, the shift register is
-// linear over GF(2) (precomputed M^(2^k) in cT.xs_jump), and each 16-bit
-// multiply-with-carry part x' = a*(x & 0xffff) + (x >> 16) is the
-// multiplicative congruential map x' = a*x mod (a*2^16 - 1).
+// KISS generator (mcica_subcol_gen_sw.f90:721-753).  Subcolumn g of a
+// column consumes the column's stream from position n = permuteseed +
+// g*nlay (x2 for icld 4/5, +g for icld 3), so each thread jumps there in
+// O(1) per column: the congruential part is an affine map mod 2^32, the
+// shift register is linear over GF(2) (M^n precomputed once per launch),
+// and each 16-bit multiply-with-carry part x' = a*(x & 0xffff) + (x >> 16)
+// is the multiplicative map x' = a*x mod (a*2^16 - 1).
 struct Kiss {
     uint32_t s1, s2, s3, s4;
-    __device__ double next() {
+    __device__ int32_t next_int() {
         s1 = 69069u * s1 + 1327217885u;
         uint32_t y = s2;
         y ^= y << 13;
@@ -576,10 +714,26 @@ struct Kiss {
         s2 = y;
         s3 = 18000u * (s3 & 65535u) + (s3 >> 16);
         s4 = 30903u * (s4 & 65535u) + (s4 >> 16);
-        const int32_t kiss = (int32_t)(s1 + s2 + (s3 << 16) + s4);
-        return __dadd_rn(__dmul_rn((double)kiss, 2.328306e-10), 0.5);
+        return (int32_t)(s1 + s2 + (s3 << 16) + s4);
     }
 };
+
+// ran_arr = kiss*2.328306e-10 + 0.5 (mcica:750), two FP64 roundings
+__device__ inline double kiss_real(int32_t k) { return __dadd_rn(__dmul_rn((double)k, 2.328306e-10), 0.5); }
+
+// Smallest k with kiss_real(k) >= x (kiss_real is increasing in k), in
+// [INT_MIN, INT_MAX + 1].  Comparing the raw integer draw with this
+// threshold is the reference's FP64 comparison, bit for bit.
+__device__ inline long long kiss_threshold(double x) {
+    const long long lo = -2147483648ll, hi = 2147483647ll;
+    if (kiss_real((int32_t)lo) >= x) return lo;
+    if (kiss_real((int32_t)hi) < x) return hi + 1;
+    long long k = (long long)floor((x - 0.5) / 2.328306e-10);
+    k = k < lo ? lo : (k > hi ? hi : k);
+    while (k > lo && kiss_real((int32_t)(k - 1)) >= x) --k;
+    while (kiss_real((int32_t)k) < x) ++k;
+    return k;
+}
 
 __device__ inline uint64_t mulmod(uint64_t a, uint64_t b, uint64_t m) { return (a * b) % m; }
 __device__ inline uint64_t powmod(uint64_t a, uint64_t n, uint64_t m) {
@@ -593,33 +747,50 @@ __device__ inline uint64_t powmod(uint64_t a, uint64_t n, uint64_t m) {
     return r;
 }
 
-__device__ inline void kiss_jump(Kiss& k, uint64_t n) {
-    if (n == 0) return;
-    // congruential: x -> 69069 x + 1327217885 (mod 2^32)
+constexpr uint64_t KISS_M3 = 18000ull * 65536ull - 1ull;
+constexpr uint64_t KISS_M4 = 30903ull * 65536ull - 1ull;
+
+// Per-subcolumn jump constants (depend on n only): computed once per launch.
+struct KissJump {
+    uint32_t A, C;      // s1 -> A*s1 + C
+    uint32_t a3n, a4n;  // s3 -> a3n*s3 mod m3, s4 -> a4n*s4 mod m4
+};
+
+__device__ inline KissJump kiss_jump_consts(uint64_t n) {
+    KissJump J;
     uint32_t A = 1, C = 0, a = 69069u, c = 1327217885u;
-    uint64_t m = n;
-    while (m) {
+    for (uint64_t m = n; m; m >>= 1) {
         if (m & 1) { A = a * A; C = a * C + c; }
         c = a * c + c;
         a = a * a;
-        m >>= 1;
     }
-    k.s1 = A * k.s1 + C;
-    // xorshift: y -> M^n y over GF(2)
-    uint32_t y = k.s2;
-    m = n;
-    for (int b = 0; m; ++b, m >>= 1) {
-        if (!(m & 1)) continue;
-        uint32_t r = 0;
-        for (int j = 0; j < 32; ++j)
-            if (y >> j & 1u) r ^= cT.xs_jump[b][j];
-        y = r;
+    J.A = A;
+    J.C = C;
+    J.a3n = (uint32_t)powmod(18000ull, n, KISS_M3);
+    J.a4n = (uint32_t)powmod(30903ull, n, KISS_M4);
+    return J;
+}
+
+// columns of M^n for the xorshift component, from the M^(2^k) table
+__device__ inline void xorshift_power(uint64_t n, uint32_t* col) {
+    for (int j = 0; j < 32; ++j) col[j] = 1u << j;
+    for (int b = 0; n; ++b, n >>= 1) {
+        if (!(n & 1)) continue;
+        for (int j = 0; j < 32; ++j) {
+            uint32_t y = col[j], r = 0;
+            for (int i = 0; i < 32; ++i)
+                if (y >> i & 1u) r ^= cT.xs_jump[b][i];
+            col[j] = r;
+        }
     }
-    k.s2 = y;
-    // multiply-with-carry parts
-    const uint64_t m3 = 18000ull * 65536ull - 1ull, m4 = 30903ull * 65536ull - 1ull;
-    k.s3 = (uint32_t)mulmod(powmod(18000ull, n, m3), k.s3, m3);
-    k.s4 = (uint32_t)mulmod(powmod(30903ull, n, m4), k.s4, m4);
+}
+
+__device__ inline uint32_t gf2_apply(const uint32_t* col, uint32_t y) {
+    uint32_t r = 0;
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+        if (y >> i & 1u) r ^= col[i];
+    return r;
 }
 
 // seed = int((pmid - int(pmid)) * 1e9), pmid in Pa (mcica:475-478)
@@ -628,52 +799,65 @@ __device__ inline uint32_t kiss_seed(double pmid) {
     return (uint32_t)(int32_t)(long long)__dmul_rn(frac, 1000000000.0);
 }
 
-// Subcolumn cloud mask of one (column, subcolumn) walked bottom -> top
-// (generate_stochastic_clouds_sw, KISS branch, mcica_subcol_gen_sw.f90:
-// 466-659; icld 4/5 in the single-column generator's order,
-// mcica_subcol_gen_sw.1col.f90:536-604).  Subcolumn g of a column uses the
-// column's stream from position permuteseed + g*nlay (x2 for icld 4/5).
-struct McicaKiss {
+// position of subcolumn g's first draw in its column's stream
+__device__ inline uint64_t kiss_offset(int icld, int g, int nlay, int permuteseed) {
+    uint64_t n = (uint64_t)permuteseed;
+    if (icld == 3) n += (uint64_t)g;
+    else if (icld >= 4) n += 2ull * (uint64_t)g * (uint64_t)nlay;
+    else n += (uint64_t)g * (uint64_t)nlay;
+    return n;
+}
+
+__device__ inline Kiss kiss_start(const uint32_t* seed, const KissJump& J, const uint32_t* xcol) {
     Kiss k;
-    double cdf_prev, cf_prev, cdf0;
+    k.s1 = J.A * seed[0] + J.C;
+    k.s2 = gf2_apply(xcol, seed[1]);
+    k.s3 = (uint32_t)mulmod(J.a3n, seed[2], KISS_M3);
+    k.s4 = (uint32_t)mulmod(J.a4n, seed[3], KISS_M4);
+    return k;
+}
+
+// Subcolumn cloud mask walked bottom -> top (generate_stochastic_clouds_sw,
+// KISS branch, mcica_subcol_gen_sw.f90:492-659; icld 4/5 in the
+// single-column generator's order, mcica_subcol_gen_sw.1col.f90:536-604).
+// icld 1/3/4/5 compare raw integer draws with per-layer thresholds
+// (kc: 1 - cldf, ka: alpha); icld 2 rescales the CDF and stays in FP64.
+struct McicaMask {
+    Kiss k;
     int icld;
-    __device__ void init(const double* play, size_t ncol, int col, int g, int nlay, int icld_, int permuteseed,
-                         int* err) {
+    int32_t prev, d0;
+    double cdf_prev, omcf_prev;
+    __device__ void start(const Kiss& k0, int icld_) {
+        k = k0;
         icld = icld_;
-        cdf_prev = cf_prev = cdf0 = 0.0;
-        const double p1 = __dmul_rn(play[col], 1.e2), p2 = __dmul_rn(play[col + ncol], 1.e2);
-        if (p1 < p2) set_error(err, E_KISSSEED);
-        k.s1 = kiss_seed(p1);
-        k.s2 = kiss_seed(p2);
-        k.s3 = kiss_seed(__dmul_rn(play[col + 2 * ncol], 1.e2));
-        k.s4 = kiss_seed(__dmul_rn(play[col + 3 * ncol], 1.e2));
-        uint64_t jump = (uint64_t)permuteseed;
-        if (icld == 3) jump += (uint64_t)g;
-        else if (icld >= 4) jump += 2ull * (uint64_t)g * (uint64_t)nlay;
-        else jump += (uint64_t)g * (uint64_t)nlay;
-        kiss_jump(k, jump);
-        if (icld == 3) cdf0 = k.next();
+        prev = 0;
+        cdf_prev = 0.0;
+        omcf_prev = 1.0;
+        d0 = icld == 3 ? k.next_int() : 0;
     }
-    // cf: layer cloud fraction; alpha: get_alpha value of this layer
-    __device__ bool step(int lay, double cf, double alpha) {
-        if (cf < 1.0e-20) cf = 0.0;
-        double cdf;
-        if (icld == 3) {
-            cdf = cdf0;
-        } else if (icld >= 4) {
-            cdf = k.next();
-            const double cdf2 = k.next();
-            if (lay >= 2 && cdf2 < alpha) cdf = cdf_prev;
-        } else {
-            cdf = k.next();
-            if (icld == 2 && lay >= 2) {
-                if (cdf_prev > __dsub_rn(1.0, cf_prev)) cdf = cdf_prev;
-                else cdf = __dmul_rn(cdf, __dsub_rn(1.0, cf_prev));
+    __device__ bool step(int lay, long long kc, long long ka, double omcf) {
+        if (icld == 2) {
+            double cdf = kiss_real(k.next_int());
+            if (lay >= 2) {
+                if (cdf_prev > omcf_prev) cdf = cdf_prev;
+                else cdf = __dmul_rn(cdf, omcf_prev);
             }
+            cdf_prev = cdf;
+            omcf_prev = omcf;
+            return cdf >= omcf;
         }
-        cdf_prev = cdf;
-        cf_prev = cf;
-        return cdf >= __dsub_rn(1.0, cf);
+        int32_t d;
+        if (icld == 3) {
+            d = d0;
+        } else if (icld >= 4) {
+            d = k.next_int();
+            const int32_t d2 = k.next_int();
+            if (lay >= 2 && (long long)d2 < ka) d = prev;
+        } else {
+            d = k.next_int();
+        }
+        prev = d;
+        return (long long)d >= kc;
     }
 };
 

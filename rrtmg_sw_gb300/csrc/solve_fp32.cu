@@ -4,88 +4,124 @@
 
 namespace rrsw {
 
-// reftra_sw (rrtmg_sw_reftra.f90:151-326) with FP32 bulk arithmetic.  The
-// near-conservative branch (zwo >= zwcrit, :188-228) is evaluated in FP64.
+// exp(-x) from the table together with 1 - exp(-x) free of cancellation
+// below od_lo, where the table is replaced by the quadratic 1 - x + x^2/2
+// (rrtmg_sw_reftra.f90:203-209)
+__device__ inline float tbl_exp_om(float x, const float* __restrict__ tab, float& om) {
+    if (x <= 0.06f) {
+        om = x * (1.0f - 0.5f * x);
+        return 1.0f - om;
+    }
+    const float tblind = x / (cT.bpade_f + x);
+    const int itind = (int)(10000.0f * tblind + 0.5f);
+    const float e = __ldg(tab + cT.exp_tbl + itind);
+    om = 1.0f - e;
+    return e;
+}
+
+// reftra_sw (rrtmg_sw_reftra.f90:151-326), kmodts = 2, in FP32 with the
+// single-scattering co-albedo zco = 1 - zw carried from the optics so that
+// no step cancels as zw -> 1:
+//   gamma1 - gamma2 = 2 zco, so k = sqrt(2 zco (gamma1 + gamma2));
+//   1 - zwo = zco (1 - q^2) / (1 - zco q^2) decides the conservative branch;
+//   zrk - gamma1 = -gamma2^2 / (zrk + gamma1), zbeta = gamma2^2 / (zrk + gamma1)^2
+//   and 1 - zbeta exp(-2 k tau) = 2 zrk / (zrk + gamma1) + zbeta (1 - exp(-2 k tau));
+//   1 - exp(-x) is taken from the quadratic itself below od_lo.
+// Mathematically these are the reference's expressions; they only avoid
+// FP32 cancellation.
+// FP64 island: the non-conservative solution has a removable singularity
+// at resonance, k*mu0 = 1 (zrpp = 1 - (k mu0)^2 -> 0, where the numerators
+// of pref/ptra and zdenr vanish together).  There FP32 keeps no digits, so
+// layers with |zrpp| < RESONANCE_TOL are solved with the reference's FP64
+// expressions.
+constexpr float RESONANCE_TOL = 2.0e-3f;
+
+__device__ __noinline__ RT<float> reftra_island(float zto1, float zw, float zg, float prmuz,
+                                                const double* __restrict__ tab64) {
+    const RT<double> d = reftra_g<double>((double)zto1, (double)zw, 0.0, (double)zg, (double)prmuz, tab64, tab64, -1);
+    RT<float> o;
+    o.ref = (float)d.ref;
+    o.refd = (float)d.refd;
+    o.tra = (float)d.tra;
+    o.trad = (float)d.trad;
+    return o;
+}
+
 template <>
-__device__ inline RT<float> reftra_g<float>(float zto1, float zw, float zg, float prmuz, const float* __restrict__ tab) {
-    typedef float R;
-    RT<R> o;
-    const R eps = 1.e-08f;
-    const R zg3 = 3.0f * zg;
-    const R zgamma1 = (8.0f - zw * (5.0f + zg3)) * 0.25f;
-    const R zgamma2 = 3.0f * (zw * (1.0f - zg)) * 0.25f;
-    const R zgamma3 = (2.0f - zg3 * prmuz) * 0.25f;
-    const R zgamma4 = 1.0f - zgamma3;
-    R zwo = 0.0f, denom = 1.0f;
-    if (zg != 1.0f) {
-        const R q = zg / (1.0f - zg);
-        denom = (1.0f - (1.0f - zw) * (q * q));
+__device__ __noinline__ RT<float> reftra_g<float>(float zto1, float zw, float zco, float zg, float prmuz,
+                                           const float* __restrict__ tab, const double* __restrict__ tab64,
+                                           int force) {
+    RT<float> o;
+    const float eps = 1.e-08f;
+    const float zg3 = 3.0f * zg;
+    const float zgamma1 = (8.0f - zw * (5.0f + zg3)) * 0.25f;
+    const float zgamma2 = 3.0f * (zw * (1.0f - zg)) * 0.25f;
+    const float zgamma3 = (2.0f - zg3 * prmuz) * 0.25f;
+    const float zgamma4 = 1.0f - zgamma3;
+    // zwo >= zwcrit  <=>  1 - zwo <= 5e-7  (reftra:183-188)
+    const bool cons = force >= 0 ? force == 1 : one_minus_zwo(zw, zco, zg) <= 5.0e-7f;
+    if (cons) {
+        // conservative scattering (reftra:191-228); ptra = 1 - pref and
+        // ptrad = 1 - prefd written without the subtraction
+        const float za1 = zgamma1 * prmuz - zgamma3;
+        const float zgt = zgamma1 * zto1;
+        float om;
+        const float ze2 = tbl_exp_om(fminf(zto1 / prmuz, 500.0f), tab, om);
+        const float r1 = 1.0f / (1.0f + zgt);
+        o.ref = (zgt - za1 * om) * r1;
+        o.tra = (1.0f + za1 * om) * r1;
+        o.refd = zgt * r1;
+        o.trad = r1;
+        if (ze2 == 1.0f) { o.ref = 0.0f; o.tra = 1.0f; o.refd = 0.0f; o.trad = 1.0f; }
+        return o;
     }
-    if (zw > 0.0f && denom != 0.0f) zwo = zw / denom;
-    if (zwo >= 0.9999995f) {
-        const double g1 = (double)zgamma1, mu = (double)prmuz;
-        const double za1 = g1 * mu - (double)zgamma3;
-        const double zgt = g1 * (double)zto1;
-        const R ze1 = fminf(zto1 / prmuz, 500.0f);
-        const double ze2 = (double)tbl_exp<R>(ze1, tab);
-        o.ref = (R)((zgt - za1 * (1.0 - ze2)) / (1.0 + zgt));
-        o.tra = 1.0f - o.ref;
-        o.refd = (R)(zgt / (1.0 + zgt));
-        o.trad = 1.0f - o.refd;
-        if (ze2 == 1.0) { o.ref = 0.0f; o.tra = 1.0f; o.refd = 0.0f; o.trad = 1.0f; }
+    const float za1 = zgamma1 * zgamma4 + zgamma2 * zgamma3;
+    const float za2 = zgamma1 * zgamma3 + zgamma2 * zgamma4;
+    const float zrk = sqrtf(2.0f * zco * (zgamma1 + zgamma2));
+    const float zrp = zrk * prmuz;
+    const float zrp1 = 1.0f + zrp, zrm1 = 1.0f - zrp;
+    const float zrk2 = 2.0f * zrk;
+    const float zrpp = zrm1 * zrp1;
+    if (fabsf(zrpp) < RESONANCE_TOL) return reftra_island(zto1, zw, zg, prmuz, tab64);
+    const float zrkg = zrk + zgamma1;
+    const float g2 = zgamma2 * zgamma2;
+    const float r_kg = 1.0f / zrkg;
+    const float zr1 = zrm1 * (za2 + zrk * zgamma3);
+    const float zr2 = zrp1 * (za2 - zrk * zgamma3);
+    const float zr3 = zrk2 * (zgamma3 - za2 * prmuz);
+    const float zr4 = zrpp * zrkg;
+    const float zr5 = -zrpp * g2 * r_kg;
+    const float zt1 = zrp1 * (za1 + zrk * zgamma4);
+    const float zt2 = zrm1 * (za1 - zrk * zgamma4);
+    const float zt3 = zrk2 * (zgamma4 + za1 * prmuz);
+    const float zbeta = g2 * r_kg * r_kg;
+    float om1, om2;
+    const float zem1 = tbl_exp_om(fminf(zrk * zto1, 500.0f), tab, om1);
+    const float zem2 = tbl_exp_om(fminf(zto1 / prmuz, 500.0f), tab, om2);
+    const float zep1 = 1.0f / zem1;
+    const float zep2 = 1.0f / zem2;
+    const float zdenr = zr4 * zep1 + zr5 * zem1;
+    if (zdenr >= -eps && zdenr <= eps) {
+        o.ref = eps;
+        o.tra = zem2;
     } else {
-        const R za1 = zgamma1 * zgamma4 + zgamma2 * zgamma3;
-        const R za2 = zgamma1 * zgamma3 + zgamma2 * zgamma4;
-        const R zrk = sqrtf(zgamma1 * zgamma1 - zgamma2 * zgamma2);
-        const R zrp = zrk * prmuz;
-        const R zrp1 = 1.0f + zrp, zrm1 = 1.0f - zrp;
-        const R zrk2 = 2.0f * zrk;
-        const R zrpp = 1.0f - zrp * zrp;
-        const R zrkg = zrk + zgamma1;
-        const R zr1 = zrm1 * (za2 + zrk * zgamma3);
-        const R zr2 = zrp1 * (za2 - zrk * zgamma3);
-        const R zr3 = zrk2 * (zgamma3 - za2 * prmuz);
-        const R zr4 = zrpp * zrkg;
-        const R zr5 = zrpp * (zrk - zgamma1);
-        const R zt1 = zrp1 * (za1 + zrk * zgamma4);
-        const R zt2 = zrm1 * (za1 - zrk * zgamma4);
-        const R zt3 = zrk2 * (zgamma4 + za1 * prmuz);
-        const R zbeta = (zgamma1 - zrk) / zrkg;
-        const R ze1 = fminf(zrk * zto1, 500.0f);
-        const R ze2 = fminf(zto1 / prmuz, 500.0f);
-        const R zem1 = tbl_exp<R>(ze1, tab);
-        const R zep1 = 1.0f / zem1;
-        const R zem2 = tbl_exp<R>(ze2, tab);
-        const R zep2 = 1.0f / zem2;
-        const R zdenr = zr4 * zep1 + zr5 * zem1;
-        if (zdenr >= -eps && zdenr <= eps) {
-            o.ref = eps;
-            o.tra = zem2;
-        } else {
-            o.ref = zw * (zr1 * zep1 - zr2 * zem1 - zr3 * zem2) / zdenr;
-            o.tra = zem2 - zem2 * zw * (zt1 * zep1 - zt2 * zem1 - zt3 * zep2) / zdenr;
-        }
-        const R zemm = zem1 * zem1;
-        const R zdend = 1.0f / ((1.0f - zbeta * zemm) * zrkg);
-        o.refd = zgamma2 * (1.0f - zemm) * zdend;
-        o.trad = zrk2 * zem1 * zdend;
+        const float rd = 1.0f / zdenr;
+        o.ref = zw * (zr1 * zep1 - zr2 * zem1 - zr3 * zem2) * rd;
+        o.tra = zem2 - zem2 * zw * (zt1 * zep1 - zt2 * zem1 - zt3 * zep2) * rd;
     }
+    const float omm = om1 * (1.0f + zem1);  // 1 - zem1^2
+    const float zdend = 1.0f / ((zrk2 * r_kg + zbeta * omm) * zrkg);
+    o.refd = zgamma2 * omm * zdend;
+    o.trad = zrk2 * zem1 * zdend;
     return o;
 }
 
 cudaError_t upload_tables_fp32(const DevTables& t) { return cudaMemcpyToSymbol(cT, &t, sizeof(DevTables)); }
 
-static size_t smem_bytes32(int L, int extra) {
-    const int NQ = extra ? NQ_EXTRA : NQ_BASE;
-    size_t off = (size_t)COLS_PER_CTA * L * sizeof(double) + (size_t)COLS_PER_CTA * NFR * L * sizeof(float) +
-                 (size_t)COLS_PER_CTA * L * sizeof(int) + 4 * sizeof(int);
-    off = (off + 15) & ~(size_t)15;
-    return off + (size_t)KLEV * NQ * CTA_THREADS * sizeof(float) + (size_t)COLS_PER_CTA * NQ * (L + 1) * sizeof(float);
-}
-
 LaunchInfo plan_fp32(const SolveParams& P, int num_sms) {
     LaunchInfo li;
-    li.smem = smem_bytes32(P.nlay, P.extra);
+    li.smem = smem_layout(P.nlay, P.extra ? NQ_EXTRA : NQ_BASE, P.fused && P.icld >= 1,
+                          stage_aerosol<float>(P.iaer), sizeof(float)).total;
     cudaFuncSetAttribute(k_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<float>, CTA_THREADS, li.smem);

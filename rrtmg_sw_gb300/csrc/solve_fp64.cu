@@ -13,18 +13,10 @@ size_t slot_elems(int nlay, int idelm) {
     return (size_t)nlay * (size_t)(idelm == 0 ? NS_MAX : S_DBTCN) * CTA_THREADS;
 }
 
-template <typename R>
-static size_t smem_bytes(int L, int extra) {
-    const int NQ = extra ? NQ_EXTRA : NQ_BASE;
-    size_t off = (size_t)COLS_PER_CTA * L * sizeof(double) + (size_t)COLS_PER_CTA * NFR * L * sizeof(R) +
-                 (size_t)COLS_PER_CTA * L * sizeof(int) + 4 * sizeof(int);
-    off = (off + 15) & ~(size_t)15;
-    return off + (size_t)KLEV * NQ * CTA_THREADS * sizeof(R) + (size_t)COLS_PER_CTA * NQ * (L + 1) * sizeof(R);
-}
-
 LaunchInfo plan_fp64(const SolveParams& P, int num_sms) {
     LaunchInfo li;
-    li.smem = smem_bytes<double>(P.nlay, P.extra);
+    li.smem = smem_layout(P.nlay, P.extra ? NQ_EXTRA : NQ_BASE, P.fused && P.icld >= 1,
+                          stage_aerosol<double>(P.iaer), sizeof(double)).total;
     cudaFuncSetAttribute(k_solve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<double>, CTA_THREADS, li.smem);
@@ -112,11 +104,24 @@ __global__ void k_mcica_kiss(int ncol, int nlay, int icld, int permuteseed, cons
     if (t >= (size_t)ncol * NGPT) return;
     const int g = (int)(t % NGPT), col = (int)(t / NGPT);
     const size_t n = (size_t)ncol;
-    McicaKiss mc;
-    mc.init(play, n, col, g, nlay, icld, permuteseed, err);
+    const uint64_t off = kiss_offset(icld, g, nlay, permuteseed);
+    uint32_t xcol[32];
+    xorshift_power(off, xcol);
+    uint32_t seed[4];
+    const double p1 = __dmul_rn(play[col], 1.e2), p2 = __dmul_rn(play[col + n], 1.e2);
+    if (p1 < p2) set_error(err, E_KISSSEED);
+    seed[0] = kiss_seed(p1);
+    seed[1] = kiss_seed(p2);
+    seed[2] = kiss_seed(__dmul_rn(play[col + 2 * n], 1.e2));
+    seed[3] = kiss_seed(__dmul_rn(play[col + 3 * n], 1.e2));
+    McicaMask mc;
+    mc.start(kiss_start(seed, kiss_jump_consts(off), xcol), icld);
     for (int lay = 1; lay <= nlay; ++lay) {
         const size_t kl = (size_t)col + n * (size_t)(lay - 1);
-        const bool cloudy = mc.step(lay, cldfrac[kl], icld >= 4 ? alpha[kl] : 0.0);
+        double cf = cldfrac[kl];
+        if (cf < 1.0e-20) cf = 0.0;
+        const double omcf = __dsub_rn(1.0, cf);
+        const bool cloudy = mc.step(lay, kiss_threshold(omcf), icld >= 4 ? kiss_threshold(alpha[kl]) : 0ll, omcf);
         mcica_fill(cloudy, g, kl, (size_t)g + NGPT * kl, ciwp, clwp, tauc, ssac, asmc, fsfc, cldfmcl, ciwpmcl,
                    clwpmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl);
     }

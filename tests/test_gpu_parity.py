@@ -186,13 +186,36 @@ def test_night_columns_clamped():
     assert_parity(g, o)
 
 
-def test_fp32_form_error_bounds():
-    c = make_columns(256, 60, 20261207, clouds=True, lat=True)
+@pytest.mark.parametrize("fused", [False, True])
+def test_fp32_form_error_bounds(fused):
+    # FP32 form vs the FP64 oracle: |dF| <= 0.05 W m-2, |dHR| <= 0.01 K/day
+    c = make_columns(512, 60, 20261207, clouds=True, lat=True)
     ncol, nlay = c["play"].shape
     alpha = pyoracle.get_alpha(ncol, nlay, 5, 1, 0.0, c["dz"].ravel(order="F"), c["lat"], 94,
                                c["cldfrac"].ravel(order="F")).reshape((ncol, nlay), order="F")
     m = mcica_oracle(c, 5, 112, 0, alpha)
     kw = gcm_inputs(c, icld=5, iaer=0, mcica=m)
+    o = oracle_call(kw)
+    clouds = None
+    if fused:
+        clouds = dict(permuteseed=112, irng=0, cldfrac=c["cldfrac"], ciwp=c["ciwp"], clwp=c["clwp"], rei=c["rei"],
+                      rel=c["rel"], alpha=alpha)
+        kw = gcm_inputs(c, icld=5, iaer=0)
+    gpu.set_form(gpu.FORM_FP32)
+    try:
+        g = gpu_call(kw, clouds=clouds)
+    finally:
+        gpu.set_form(gpu.FORM_FP64)
+    for k in FLUX:
+        assert np.max(np.abs(g[k] - o[k])) <= 0.05, (k, float(np.max(np.abs(g[k] - o[k]))))
+    for k in HR:
+        assert np.max(np.abs(g[k] - o[k])) <= 0.01, (k, float(np.max(np.abs(g[k] - o[k]))))
+
+
+def test_fp32_form_aerosol_error_bounds():
+    c = make_columns(256, 60, 20261208, clouds=True, aerosol=True)
+    m = mcica_oracle(c, 2, 112)
+    kw = gcm_inputs(c, icld=2, iaer=10, mcica=m)
     o = oracle_call(kw)
     gpu.set_form(gpu.FORM_FP32)
     try:
