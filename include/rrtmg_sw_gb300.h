@@ -86,6 +86,7 @@ enum {
     RRTMG_SW_ETABLES = 2,      /* coefficient table file missing or corrupt */
     RRTMG_SW_EARGS = 3,        /* bad sizes or NULL required pointer */
     RRTMG_SW_ECUDA = 4,        /* CUDA runtime error (see rrtmg_sw_last_cuda_error_c) */
+    RRTMG_SW_ESCRATCH = 5,     /* rrtmg_sw_static_dev_c: request larger than its fixed scratch */
     RRTMG_SW_EINFLAG1 = 10,    /* cldprmc:166  INFLAG = 1 OPTION NOT AVAILABLE WITH MCICA */
     RRTMG_SW_EICERAD = 11,     /* cldprmc:183,204  ICE RADIUS OUT OF BOUNDS */
     RRTMG_SW_EICEDGE = 12,     /* cldprmc:227  ICE GENERALIZED EFFECTIVE SIZE OUT OF BOUNDS */
@@ -124,6 +125,35 @@ int rrtmg_sw_dev_c(const rrtmg_sw_args *a, void *stream);
  * are used, as mcica_subcol_sw copies them).  Host / device variants. */
 int rrtmg_sw_mcica_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c);
 int rrtmg_sw_mcica_dev_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, void *stream);
+
+/* Allocation-free device solve.  No counterpart in the reference: it exists
+ * for callers that must not allocate device memory while they run -- a
+ * model whose memory pool owns the whole GPU, or a time step that forbids
+ * allocation after start-up.  It computes what rrtmg_sw_dev_c (c == NULL)
+ * or rrtmg_sw_mcica_dev_c (c != NULL) computes, on device pointers, in the
+ * current form, but its per-CTA scratch is a fixed 256 MiB area compiled
+ * into the library instead of the growable workspace the other entry points
+ * allocate with cudaMalloc; the call itself allocates nothing, on the device
+ * or the host.
+ *   - The first call on each device looks up the area's address once
+ *     (cudaGetSymbolAddress with that device current) and loads the module
+ *     that holds it; make that first call before any stream capture.
+ *   - Limit: the area must hold one scratch slot per SM.  A slot is
+ *     nlay * (16 with idelm = 0, else 14) * 224 values of the form's type,
+ *     so 256 MiB takes nlay <= 140 (FP32) or <= 70 (FP64) with idelm = 1 on a
+ *     152-SM GPU.  Larger requests return RRTMG_SW_ESCRATCH, nothing runs.
+ *     Fewer resident CTAs than rrtmg_sw_dev_c may run when the slots that
+ *     fit are fewer than its grid; results are identical, only slower.
+ *   - Nothing needs to start at zero: every scratch value is written before
+ *     it is read; the device error word is cleared by the call itself.
+ *   - One area per device and process, shared by every call: two solves
+ *     that use it at the same time race and corrupt each other.  The
+ *     library serialises its own calls and each call waits for its kernel
+ *     before returning, so calls made one after another are safe; do not
+ *     arrange for two of its kernels to be in flight at once.
+ *   - Tables must have been loaded on the current device by rrtmg_sw_ini_c
+ *     (RRTMG_SW_ENOTINIT otherwise). */
+int rrtmg_sw_static_dev_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, void *stream);
 
 /* mcica_subcol_sw (mcica_subcol_gen_sw.f90:181-296), host arrays, outputs
  * (ngpt,ncol,nlay) and (ncol,nlay).  irng = 0: KISS with per-column streams

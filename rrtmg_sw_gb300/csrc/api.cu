@@ -565,6 +565,73 @@ int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c) {
     return RRTMG_SW_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Fixed scratch for rrtmg_sw_static_dev_c.  For callers that may not allocate
+// device memory once they run (a model whose pool owns the GPU, a time step
+// that forbids allocation): the per-CTA pass-1 -> pass-2 scratch lives in
+// this module-scope area instead of the cudaMalloc'd workspace.  Its contents
+// never need clearing (every slot value is written before it is read); the
+// error word is cleared on the stream by each call.  One area per device, so
+// two solves on it at once would race; calls are serialised by State::mu and
+// each call waits for its kernel.
+constexpr size_t kStaticScratchBytes = size_t(256) << 20;
+constexpr int kMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+static __device__ __align__(256) int g_static_err;
+
+struct StaticArea {
+    void* scratch = nullptr;
+    int* err = nullptr;
+};
+StaticArea g_static_area[kMaxDevices];  // filled on the first call per device, under State::mu
+
+// Address of the area on the current device (looked up once per device; the
+// lookup also loads this module on that device).
+cudaError_t static_area(int dev, StaticArea& out) {
+    StaticArea& a = g_static_area[dev];
+    if (!a.scratch) {
+        void* p = nullptr;
+        void* e = nullptr;
+        cudaError_t r = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (r != cudaSuccess) return r;
+        r = cudaGetSymbolAddress(&e, g_static_err);
+        if (r != cudaSuccess) return r;
+        a.scratch = p;
+        a.err = (int*)e;
+    }
+    out = a;
+    return cudaSuccess;
+}
+
+int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s) {
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev != st.device) return RRTMG_SW_ENOTINIT;  // tables live on the device rrtmg_sw_ini_c used
+    if (dev < 0 || dev >= kMaxDevices) return RRTMG_SW_EARGS;
+    SolveParams P;
+    int rc = make_params(st, a, c, P);
+    if (rc) return rc;
+    const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
+    LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms) : plan_fp64(P, st.num_sms);
+    P.slot_elems = slot_elems(P.nlay, P.idelm);
+    const size_t slot_bytes = P.slot_elems * (fp32 ? sizeof(float) : sizeof(double));
+    const size_t slots = kStaticScratchBytes / slot_bytes;
+    if (slots < (size_t)st.num_sms) return RRTMG_SW_ESCRATCH;
+    if ((size_t)li.grid > slots) li.grid = (int)slots;
+    StaticArea area;
+    CK(static_area(dev, area));
+    P.scratch = area.scratch;
+    P.err = area.err;
+    CK(cudaMemsetAsync(P.err, 0, sizeof(int), s));
+    if (fp32) CK(launch_solve_fp32(P, (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, li, s));
+    else CK(launch_solve_fp64(P, (const double*)st.d_tab64.p, li, s));
+    st.last_launches = 1;
+    int h_err = 0;  // pageable: the copy completes before the call returns
+    CK(cudaMemcpyAsync(&h_err, P.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return h_err;
+}
+
 }  // namespace
 
 extern "C" {
@@ -612,6 +679,15 @@ int rrtmg_sw_mcica_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, void*
     const int rc = check_args(a);
     if (rc) return rc;
     return solve_dev(st, a, c, (cudaStream_t)stream);
+}
+
+int rrtmg_sw_static_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, void* stream) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    if (!st.init) return RRTMG_SW_ENOTINIT;
+    const int rc = check_args(a);
+    if (rc) return rc;
+    return solve_static(st, a, c, (cudaStream_t)stream);
 }
 
 int mcica_subcol_sw_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t permuteseed, int32_t irng,
@@ -714,6 +790,7 @@ const char* rrtmg_sw_errstr_c(int32_t code) {
     case RRTMG_SW_ETABLES: return "COEFFICIENT TABLE FILE MISSING OR CORRUPT";
     case RRTMG_SW_EARGS: return "INVALID ARGUMENTS";
     case RRTMG_SW_ECUDA: return "CUDA ERROR";
+    case RRTMG_SW_ESCRATCH: return "REQUEST EXCEEDS THE 256 MIB STATIC SCRATCH (ONE SLOT PER SM)";
     case RRTMG_SW_EINFLAG1: return "INFLAG = 1 OPTION NOT AVAILABLE WITH MCICA";
     case RRTMG_SW_EICERAD: return "ICE RADIUS OUT OF BOUNDS";
     case RRTMG_SW_EICEDGE: return "ICE GENERALIZED EFFECTIVE SIZE OUT OF BOUNDS";

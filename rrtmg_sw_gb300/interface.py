@@ -81,6 +81,7 @@ def lib():
         L.rrtmg_sw_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.c_void_p]
         L.rrtmg_sw_mcica_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds)]
         L.rrtmg_sw_mcica_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_void_p]
+        L.rrtmg_sw_static_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_void_p]
         L.mcica_subcol_sw_c.argtypes = [C.c_int32] * 5 + [_dp] * 11 + [_dp] * 9
         L.get_alpha_c.argtypes = [C.c_int32] * 4 + [C.c_double, _dp, _dp, C.c_int32, _dp, _dp]
         L.rrtmg_sw_set_form_c.argtypes = [C.c_int32]
@@ -224,6 +225,17 @@ def rrtmg_sw_dev(args, stream=0, clouds=None):
         _check(lib().rrtmg_sw_dev_c(C.byref(args), C.c_void_p(stream)))
     else:
         _check(lib().rrtmg_sw_mcica_dev_c(C.byref(args), C.byref(clouds), C.c_void_p(stream)))
+
+
+def rrtmg_sw_static_dev(args, stream=0, clouds=None):
+    """Allocation-free variant of :func:`rrtmg_sw_dev` for callers that may
+    not allocate device memory while they run: the solve's scratch is a
+    fixed 256 MiB area inside the library (one slot per SM must fit, else
+    RRTMGError with code 5).  The first call per device looks the area up
+    and should come before any stream capture; two of its solves must never
+    be in flight at once."""
+    cp = C.byref(clouds) if clouds is not None else None
+    _check(lib().rrtmg_sw_static_dev_c(C.byref(args), cp, C.c_void_p(stream)))
 
 
 def last_launch_count():
