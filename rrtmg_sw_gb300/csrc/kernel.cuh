@@ -6,8 +6,15 @@
 namespace rrsw {
 
 constexpr int KLEV = 4;         // levels buffered per reduction round
-constexpr int NQ_BASE = 6;      // fu, fd, cu, cd, fddir, cddir
-constexpr int NQ_EXTRA = 14;    // + uvfd, uvcd, uvfddir, uvcddir, nifd, nicd, nifddir, nicddir
+constexpr int NQ_MAX = 16;
+// g-point sums per level: fu, fd, cu, cd, fddir, cddir; the FP32 form adds
+// the absorption of the layer below the level (total, clear) for its
+// heating rates; with the extra outputs, + uvfd, uvcd, uvfddir, uvcddir,
+// nifd, nicd, nifddir, nicddir.
+template <typename R>
+__host__ __device__ constexpr int num_abs() { return sizeof(R) == 4 ? 2 : 0; }
+template <typename R>
+__host__ __device__ inline int num_q(bool extra) { return 6 + num_abs<R>() + (extra ? 8 : 0); }
 
 // scratch fields per level (pass 1 -> pass 2)
 enum { S_REFC, S_REFDC, S_TRAC, S_TRADC, S_DBTC, S_RUPC, S_RUPDC,
@@ -169,6 +176,23 @@ static __device__ __noinline__ int decide_conservative64(const SolveParams& P, i
     return one_minus_zwo<double>(zomco, zcoo, zgco) <= 5.0e-7 ? 1 : 0;
 }
 
+// Whether the FP32 estimate of 1 - zwo (reftra:183-188) is too close to the
+// 5e-7 switch to trust its branch.  The window is an error bound from the
+// FP32 optics: 2e-6 relative on the co-albedo and on the asymmetry.  Near
+// zg = 0.5, where the reference's q = zg / (1 - zg) reaches 1, 1 - zwo
+// falls steeply with zg and the window widens accordingly.
+__device__ inline bool near_conservative_edge(float zw, float zco, float zg) {
+    if (zg == 1.0f || !(zw > 0.0f)) return false;
+    const float r = one_minus_zwo(zw, zco, zg);
+    const float q = zg / (1.0f - zg);
+    const float den = 1.0f - zco * q * q;
+    if (den == 0.0f) return true;
+    const float d_dg = 2.0f * zco * q * (1.0f - zco) / (den * den * (1.0f - zg) * (1.0f - zg));
+    const float d_dco = fabsf(1.0f - q * q) / (den * den);
+    const float tol = d_dg * (2.0e-6f * fabsf(zg) + 1.0e-9f) + d_dco * 2.0e-6f * zco + 1.0e-13f;
+    return fabsf(r - 5.0e-7f) <= tol;
+}
+
 template <typename R>
 __device__ inline void warp_sum4(R& v) {
     v += __shfl_xor_sync(0xffffffffu, v, 1);
@@ -219,7 +243,8 @@ __global__ void __launch_bounds__(CTA_THREADS, 2)
 k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict__ tab64) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = P.nlay;
-    const int NQ = P.extra ? NQ_EXTRA : NQ_BASE;
+    const int NQ = num_q<R>(P.extra != 0);
+    constexpr int QX = 6 + num_abs<R>();  // first extra-output sum
     const bool fused = P.fused && P.icld >= 1;
     const bool aer_stage = stage_aerosol<R>(P.iaer);
     const Smem M = smem_layout(L, NQ, fused, aer_stage, sizeof(R));
@@ -442,17 +467,20 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
                 if (cldf > R(1.e-12)) {
                     int force = -1;
                     if constexpr (sizeof(R) == 4) {
-                        const float r = one_minus_zwo(zomco, zcoo, zgco);
-                        if (fabsf(r - 5.0e-7f) <= 1.5e-11f)
+                        if (near_conservative_edge(zomco, zcoo, zgco))
                             force = decide_conservative64(P, col, g, lay, ib, ztauc, zomcc, zgcc, zcoc, tab64);
                     }
                     ro = reftra_g<R>(ztauo, zomco, zcoo, zgco, prmu0, tab, tab64, force);
                 }
-                else { ro.ref = R(0); ro.tra = R(1); ro.refd = R(0); ro.trad = R(1); }
+                else { ro.ref = R(0); ro.tra = R(1); ro.refd = R(0); ro.trad = R(1); ro.adir = R(0); ro.adif = R(0); }
                 rt.ref = zclear * rc.ref + zcloud * ro.ref;
                 rt.refd = zclear * rc.refd + zcloud * ro.refd;
                 rt.tra = zclear * rc.tra + zcloud * ro.tra;
                 rt.trad = zclear * rc.trad + zcloud * ro.trad;
+                if constexpr (sizeof(R) == 4) {
+                    rt.adir = zclear * rc.adir + zcloud * ro.adir;
+                    rt.adif = zclear * rc.adif + zcloud * ro.adif;
+                }
                 const R zdbtmo = tbl_exp<R>(ztauo / prmu0, tab);
                 zdbt = zclear * zdbtc + zcloud * zdbtmo;
             }
@@ -471,17 +499,20 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
                 rup_b = rup;
                 rupd_b = rupd;
             }
+            // the FP32 form keeps the absorptances in the transmittance slots
+            // and rebuilds ptra = 1 - pref - adir, ptrad = 1 - prefd - adif
+            constexpr bool keep_abs = sizeof(R) == 4;
             sv[S_REFC * CTA_THREADS] = rc.ref;
             sv[S_REFDC * CTA_THREADS] = rc.refd;
-            sv[S_TRAC * CTA_THREADS] = rc.tra;
-            sv[S_TRADC * CTA_THREADS] = rc.trad;
+            sv[S_TRAC * CTA_THREADS] = keep_abs ? rc.adir : rc.tra;
+            sv[S_TRADC * CTA_THREADS] = keep_abs ? rc.adif : rc.trad;
             sv[S_DBTC * CTA_THREADS] = zdbtc;
             sv[S_RUPC * CTA_THREADS] = rupc_b;
             sv[S_RUPDC * CTA_THREADS] = rupdc_b;
             sv[S_REF * CTA_THREADS] = rt.ref;
             sv[S_REFD * CTA_THREADS] = rt.refd;
-            sv[S_TRA * CTA_THREADS] = rt.tra;
-            sv[S_TRAD * CTA_THREADS] = rt.trad;
+            sv[S_TRA * CTA_THREADS] = keep_abs ? rt.adir : rt.tra;
+            sv[S_TRAD * CTA_THREADS] = keep_abs ? rt.adif : rt.trad;
             sv[S_DBT * CTA_THREADS] = zdbt;
             sv[S_RUP * CTA_THREADS] = rup_b;
             sv[S_RUPD * CTA_THREADS] = rupd_b;
@@ -491,12 +522,16 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
         R tdbtc = R(1), tdnc = R(1), rdndc = R(0);
         R tdbt = R(1), tdn = R(1), rdnd = R(0);
         R tdbtcn = R(1), tdbtn = R(1);
+        // FP32 form: absorption of the layer above the current level, less
+        // the part that its lower face's upward flux still has to add
+        R absc = R(0), abst = R(0), adifc_up = R(0), adift_up = R(0);
         for (int jk = 1; jk <= L + 1; ++jk) {
-            R q[NQ_EXTRA];
+            R q[NQ_MAX];
 #pragma unroll
-            for (int i = 0; i < NQ_EXTRA; ++i) q[i] = R(0);
+            for (int i = 0; i < NQ_MAX; ++i) q[i] = R(0);
             R refc = R(0), refdc = R(0), trac = R(0), tradc = R(0), dbtc = R(0), rupc, rupdc;
             R ref = R(0), refd = R(0), tra = R(0), trad = R(0), dbt = R(0), rup, rupd, dbtcn = R(0), dbtn = R(0);
+            R adirc = R(0), adifc = R(0), adirt = R(0), adift = R(0);
             if (jk <= L) {
                 const R* sv = scr + (size_t)(jk - 1) * NS * CTA_THREADS + tid;
                 refc = sv[S_REFC * CTA_THREADS]; refdc = sv[S_REFDC * CTA_THREADS];
@@ -506,6 +541,13 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
                 ref = sv[S_REF * CTA_THREADS]; refd = sv[S_REFD * CTA_THREADS];
                 tra = sv[S_TRA * CTA_THREADS]; trad = sv[S_TRAD * CTA_THREADS];
                 dbt = sv[S_DBT * CTA_THREADS];
+                if constexpr (sizeof(R) == 4) {
+                    adirc = trac; adifc = tradc; adirt = tra; adift = trad;
+                    trac = R(1) - refc - adirc;
+                    tradc = R(1) - refdc - adifc;
+                    tra = R(1) - ref - adirt;
+                    trad = R(1) - refd - adift;
+                }
                 rup = sv[S_RUP * CTA_THREADS]; rupd = sv[S_RUPD * CTA_THREADS];
                 if (P.idelm == 0) { dbtcn = sv[S_DBTCN * CTA_THREADS]; dbtn = sv[S_DBTN * CTA_THREADS]; }
             } else {
@@ -515,10 +557,23 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
                 // level fluxes (vrtqdr:163-169)
                 const R zrc = R(1) / (R(1) - rdndc * rupdc);
                 const R cu = (tdbtc * rupc + (tdnc - tdbtc) * rupdc) * zrc;
-                const R cd = tdbtc + (tdnc - tdbtc + tdbtc * rupc * rdndc) * zrc;
+                const R cdif = (tdnc - tdbtc + tdbtc * rupc * rdndc) * zrc;
+                const R cd = tdbtc + cdif;
                 const R zrt = R(1) / (R(1) - rdnd * rupd);
                 const R fu = (tdbt * rup + (tdn - tdbt) * rupd) * zrt;
-                const R fd = tdbt + (tdn - tdbt + tdbt * rup * rdnd) * zrt;
+                const R fdif = (tdn - tdbt + tdbt * rup * rdnd) * zrt;
+                const R fd = tdbt + fdif;
+                if constexpr (sizeof(R) == 4) {
+                    // layer jk-1 absorbs what enters it: the direct and diffuse
+                    // beams at its top (kept from the previous level) and the
+                    // upward flux at its bottom face, this level
+                    q[6] = zinc * (abst + fu * adift_up);
+                    q[7] = zinc * (absc + cu * adifc_up);
+                    abst = tdbt * adirt + fdif * adift;
+                    absc = tdbtc * adirc + cdif * adifc;
+                    adift_up = adift;
+                    adifc_up = adifc;
+                }
                 const R dirf = P.idelm == 0 ? tdbtn : tdbt;
                 const R dirc = P.idelm == 0 ? tdbtcn : tdbtc;
                 q[0] = zinc * fu;
@@ -528,8 +583,8 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
                 q[4] = zinc * dirf;
                 q[5] = zinc * dirc;
                 if (P.extra) {
-                    if (uv) { q[6] = q[1]; q[7] = q[3]; q[8] = q[4]; q[9] = q[5]; }
-                    else { q[10] = q[1]; q[11] = q[3]; q[12] = q[4]; q[13] = q[5]; }
+                    if (uv) { q[QX] = q[1]; q[QX + 1] = q[3]; q[QX + 2] = q[4]; q[QX + 3] = q[5]; }
+                    else { q[QX + 4] = q[1]; q[QX + 5] = q[3]; q[QX + 6] = q[4]; q[QX + 7] = q[5]; }
                 }
                 if (jk <= L) {
                     // downward recurrences (vrtqdr:144-159) and direct beam (spcvmc:575-585)
@@ -549,7 +604,7 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
             }
             const int slot = (jk - 1) % KLEV;
 #pragma unroll
-            for (int i = 0; i < NQ_EXTRA; ++i)
+            for (int i = 0; i < NQ_MAX; ++i)
                 if (i < NQ) sRed[(slot * NQ + i) * CTA_THREADS + tid] = q[i];
             if (slot == KLEV - 1 || jk == L + 1) {
                 __syncthreads();
@@ -594,19 +649,25 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
                 const double* pdp = sPdp + c2 * L;
                 double hr = 0.0, hrc = 0.0;
                 if (l < L - 1) {
-                    const double fu1 = (double)F[0 * (L + 1) + l + 1], fd1 = (double)F[1 * (L + 1) + l + 1];
-                    const double cu1 = (double)F[2 * (L + 1) + l + 1], cd1 = (double)F[3 * (L + 1) + l + 1];
                     const double zdpgcp = cT.heatfac / pdp[l];
-                    hrc = DM(DS(DS(cd1, cu1), DS(cd, cu)), zdpgcp);
-                    hr = DM(DS(DS(fd1, fu1), DS(fd, fu)), zdpgcp);
+                    if constexpr (sizeof(R) == 4) {
+                        // summed layer absorption (= net-flux divergence)
+                        hr = (double)F[6 * (L + 1) + l] * zdpgcp;
+                        hrc = (double)F[7 * (L + 1) + l] * zdpgcp;
+                    } else {
+                        const double fu1 = (double)F[0 * (L + 1) + l + 1], fd1 = (double)F[1 * (L + 1) + l + 1];
+                        const double cu1 = (double)F[2 * (L + 1) + l + 1], cd1 = (double)F[3 * (L + 1) + l + 1];
+                        hrc = DM(DS(DS(cd1, cu1), DS(cd, cu)), zdpgcp);
+                        hr = DM(DS(DS(fd1, fu1), DS(fd, fu)), zdpgcp);
+                    }
                 }
                 P.swhr[o] = hr;
                 P.swhrc[o] = hrc;
             }
             if (P.extra) {
                 const double fddir = (double)F[4 * (L + 1) + l];
-                const double uvfd = (double)F[6 * (L + 1) + l], uvfddir = (double)F[8 * (L + 1) + l];
-                const double nifd = (double)F[10 * (L + 1) + l], nifddir = (double)F[12 * (L + 1) + l];
+                const double uvfd = (double)F[(QX + 0) * (L + 1) + l], uvfddir = (double)F[(QX + 2) * (L + 1) + l];
+                const double nifd = (double)F[(QX + 4) * (L + 1) + l], nifddir = (double)F[(QX + 6) * (L + 1) + l];
                 const double vals[8] = {fddir, DS(fd, fddir), uvfd, nifd, uvfddir, DS(uvfd, uvfddir), nifddir,
                                         DS(nifd, nifddir)};
                 for (int x = 0; x < 8; ++x)

@@ -591,7 +591,12 @@ __device__ inline void cldprmc_g(int ib, int inflag, int iceflag, int liqflag, R
 // --------------------------------------------------------------- reftra
 // One layer of reftra_sw (rrtmg_sw_reftra.f90:151-326), kmodts = 2.
 template <typename R>
-struct RT { R ref, refd, tra, trad; };
+struct RT {
+    R ref, refd, tra, trad;
+    // FP32 form only: absorptances 1 - ref - tra (direct incidence) and
+    // 1 - refd - trad (diffuse incidence), formed without cancellation
+    R adir, adif;
+};
 
 // zco = 1 - zw carried separately by the FP32 form (unused by FP64);
 // tab64 is the FP64 table blob (the FP32 form's FP64 island needs it)
@@ -608,6 +613,7 @@ __device__ __noinline__ RT<double> reftra_fp64(double zto1, double zw, double zg
                                                const double* __restrict__ tab) {
     typedef double R;
     RT<R> o;
+    o.adir = o.adif = 0.0;
     const R zwcrit = 0.9999995, eps = 1.e-08;
     const R zg3 = 3.0 * zg;
     const R zgamma1 = (8.0 - zw * (5.0 + zg3)) * 0.25;

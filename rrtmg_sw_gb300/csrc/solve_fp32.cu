@@ -21,14 +21,23 @@ __device__ inline float tbl_exp_om(float x, const float* __restrict__ tab, float
 
 // reftra_sw (rrtmg_sw_reftra.f90:151-326), kmodts = 2, in FP32 with the
 // single-scattering co-albedo zco = 1 - zw carried from the optics so that
-// no step cancels as zw -> 1:
+// no step cancels as zw -> 1 or as the layer gets thin:
 //   gamma1 - gamma2 = 2 zco, so k = sqrt(2 zco (gamma1 + gamma2));
 //   1 - zwo = zco (1 - q^2) / (1 - zco q^2) decides the conservative branch;
-//   zrk - gamma1 = -gamma2^2 / (zrk + gamma1), zbeta = gamma2^2 / (zrk + gamma1)^2
-//   and 1 - zbeta exp(-2 k tau) = 2 zrk / (zrk + gamma1) + zbeta (1 - exp(-2 k tau));
+//   zrk - gamma1 = -gamma2^2 / (zrk + gamma1), zbeta = gamma2^2 / (zrk + gamma1)^2;
+//   with om = 1 - exp(-x) and p = exp(x) - 1 = om / exp(-x):
+//     zdenr = zrpp (2 zrk + (zrk + gamma1) p1 + gamma2^2 / (zrk + gamma1) om1),
+//     zr1 zep1 - zr2 zem1 - zr3 zem2 = zr1 p1 + zr2 om1 + zr3 om2,
+//     zt1 zep1 - zt2 zem1 - zt3 zep2 = zt1 p1 + zt2 om1 - zt3 p2
+//   (zr1 - zr2 - zr3 = zt1 - zt2 - zt3 = 0), and
+//     1 - zbeta zem1^2 = 2 zrk / (zrk + gamma1) + zbeta om1 (1 + zem1);
 //   1 - exp(-x) is taken from the quadratic itself below od_lo.
-// Mathematically these are the reference's expressions; they only avoid
-// FP32 cancellation.
+// The absorptances follow from the same pieces:
+//   1 - pref - ptra   = om2 - zw (Nr - zem2 Nt) / zdenr,
+//   1 - prefd - ptrad = om1 (zrk om1 + 2 zco (1 + zem1)) zdend,
+// so a heating rate can be summed from layer absorption instead of being
+// differenced from level fluxes.  Mathematically these are the reference's
+// expressions; they only avoid FP32 cancellation.
 // FP64 island: the non-conservative solution has a removable singularity
 // at resonance, k*mu0 = 1 (zrpp = 1 - (k mu0)^2 -> 0, where the numerators
 // of pref/ptra and zdenr vanish together).  There FP32 keeps no digits, so
@@ -44,6 +53,8 @@ __device__ __noinline__ RT<float> reftra_island(float zto1, float zw, float zg, 
     o.refd = (float)d.refd;
     o.tra = (float)d.tra;
     o.trad = (float)d.trad;
+    o.adir = (float)(1.0 - d.ref - d.tra);
+    o.adif = (float)(1.0 - d.refd - d.trad);
     return o;
 }
 
@@ -60,9 +71,11 @@ __device__ __noinline__ RT<float> reftra_g<float>(float zto1, float zw, float zc
     const float zgamma4 = 1.0f - zgamma3;
     // zwo >= zwcrit  <=>  1 - zwo <= 5e-7  (reftra:183-188)
     const bool cons = force >= 0 ? force == 1 : one_minus_zwo(zw, zco, zg) <= 5.0e-7f;
+    o.adir = 0.0f;
+    o.adif = 0.0f;
     if (cons) {
         // conservative scattering (reftra:191-228); ptra = 1 - pref and
-        // ptrad = 1 - prefd written without the subtraction
+        // ptrad = 1 - prefd written without the subtraction; no absorption
         const float za1 = zgamma1 * prmuz - zgamma3;
         const float zgt = zgamma1 * zto1;
         float om;
@@ -84,35 +97,38 @@ __device__ __noinline__ RT<float> reftra_g<float>(float zto1, float zw, float zc
     const float zrpp = zrm1 * zrp1;
     if (fabsf(zrpp) < RESONANCE_TOL) return reftra_island(zto1, zw, zg, prmuz, tab64);
     const float zrkg = zrk + zgamma1;
-    const float g2 = zgamma2 * zgamma2;
     const float r_kg = 1.0f / zrkg;
+    const float g2k = zgamma2 * zgamma2 * r_kg;  // gamma1 - zrk
     const float zr1 = zrm1 * (za2 + zrk * zgamma3);
     const float zr2 = zrp1 * (za2 - zrk * zgamma3);
     const float zr3 = zrk2 * (zgamma3 - za2 * prmuz);
-    const float zr4 = zrpp * zrkg;
-    const float zr5 = -zrpp * g2 * r_kg;
     const float zt1 = zrp1 * (za1 + zrk * zgamma4);
     const float zt2 = zrm1 * (za1 - zrk * zgamma4);
     const float zt3 = zrk2 * (zgamma4 + za1 * prmuz);
-    const float zbeta = g2 * r_kg * r_kg;
+    const float zbeta = g2k * r_kg;
     float om1, om2;
     const float zem1 = tbl_exp_om(fminf(zrk * zto1, 500.0f), tab, om1);
     const float zem2 = tbl_exp_om(fminf(zto1 / prmuz, 500.0f), tab, om2);
-    const float zep1 = 1.0f / zem1;
-    const float zep2 = 1.0f / zem2;
-    const float zdenr = zr4 * zep1 + zr5 * zem1;
+    const float p1 = om1 / zem1;  // zep1 - 1
+    const float p2 = om2 / zem2;  // zep2 - 1
+    const float zdenr = zrpp * (zrk2 + zrkg * p1 + g2k * om1);
     if (zdenr >= -eps && zdenr <= eps) {
         o.ref = eps;
         o.tra = zem2;
+        o.adir = om2 - eps;
     } else {
         const float rd = 1.0f / zdenr;
-        o.ref = zw * (zr1 * zep1 - zr2 * zem1 - zr3 * zem2) * rd;
-        o.tra = zem2 - zem2 * zw * (zt1 * zep1 - zt2 * zem1 - zt3 * zep2) * rd;
+        const float nr = zr1 * p1 + zr2 * om1 + zr3 * om2;
+        const float nt = zt1 * p1 + zt2 * om1 - zt3 * p2;
+        o.ref = zw * nr * rd;
+        o.tra = zem2 - zem2 * zw * nt * rd;
+        o.adir = om2 - zw * rd * (nr - zem2 * nt);
     }
     const float omm = om1 * (1.0f + zem1);  // 1 - zem1^2
     const float zdend = 1.0f / ((zrk2 * r_kg + zbeta * omm) * zrkg);
     o.refd = zgamma2 * omm * zdend;
     o.trad = zrk2 * zem1 * zdend;
+    o.adif = om1 * (zrk * om1 + 2.0f * zco * (1.0f + zem1)) * zdend;
     return o;
 }
 
@@ -120,7 +136,7 @@ cudaError_t upload_tables_fp32(const DevTables& t) { return cudaMemcpyToSymbol(c
 
 LaunchInfo plan_fp32(const SolveParams& P, int num_sms) {
     LaunchInfo li;
-    li.smem = smem_layout(P.nlay, P.extra ? NQ_EXTRA : NQ_BASE, P.fused && P.icld >= 1,
+    li.smem = smem_layout(P.nlay, num_q<float>(P.extra != 0), P.fused && P.icld >= 1,
                           stage_aerosol<float>(P.iaer), sizeof(float)).total;
     cudaFuncSetAttribute(k_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
     int per_sm = 0;
