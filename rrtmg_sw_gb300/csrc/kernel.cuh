@@ -29,10 +29,12 @@ __device__ inline double DS(double a, double b) { return __dsub_rn(a, b); }
 // explicit roundings so both arithmetic forms see identical indices.
 template <typename R>
 __device__ inline void prep_layer(const SolveParams& P, int col, int lay, R* cf, int* pk, double* pdp,
-                                  int L, const double* __restrict__ tab64) {
+                                  int L, const double* __restrict__ tab64, double* cf64 = nullptr) {
     const int i = lay - 1;
     if (col >= P.ncol) {
         for (int f = 0; f < NFR; ++f) cf[f * L + i] = R(0);
+        if (cf64)
+            for (int f = 0; f < NFR; ++f) cf64[f * L + i] = 0.0;
         pk[i] = 1 | (1 << 8) | (1 << 12) | (1 << 16) | (1 << 24);
         pdp[i] = 1.0;
         return;
@@ -93,6 +95,24 @@ __device__ inline void prep_layer(const SolveParams& P, int col, int lay, R* cf,
     if (colch4 == 0.0) colch4 = DM(1.e-32, coldry);
     if (colo2 == 0.0) colo2 = DM(1.e-32, coldry);
     const double compfp = DS(1.0, fp);
+    if (cf64) {
+        // FP32 form: the FP64 coefficients too, for cells redone in FP64
+        cf64[F_FAC10 * L + i] = DM(compfp, ft);
+        cf64[F_FAC00 * L + i] = DM(compfp, DS(1.0, ft));
+        cf64[F_FAC11 * L + i] = DM(fp, ft1);
+        cf64[F_FAC01 * L + i] = DM(fp, DS(1.0, ft1));
+        cf64[F_H2O * L + i] = colh2o;
+        cf64[F_CO2 * L + i] = colco2;
+        cf64[F_O3 * L + i] = colo3;
+        cf64[F_CH4 * L + i] = colch4;
+        cf64[F_O2 * L + i] = colo2;
+        cf64[F_MOL * L + i] = colmol;
+        cf64[F_SELFFAC * L + i] = selffac;
+        cf64[F_SELFFRAC * L + i] = selffrac;
+        cf64[F_FORFAC * L + i] = forfac;
+        cf64[F_FORFRAC * L + i] = forfrac;
+        cf64[F_PDP * L + i] = pdp[i];
+    }
     cf[F_FAC10 * L + i] = (R)DM(compfp, ft);
     cf[F_FAC00 * L + i] = (R)DM(compfp, DS(1.0, ft));
     cf[F_FAC11 * L + i] = (R)DM(fp, ft1);
@@ -142,40 +162,6 @@ __device__ inline void aerosol(const SolveParams& P, int col, int lay, int ib, c
     }
 }
 
-// FP32 form: when the FP32 estimate of 1 - zwo for a cloudy layer lies
-// within 3e-5 (relative) of the switch 1 - zwcrit = 5e-7, the reference's
-// discontinuous conservative/non-conservative choice (reftra:188) is made
-// again from FP64 cloud optics (cldprmc in FP64 from the FP64 inputs) and
-// the co-albedo, so thick clouds take the reference's branch.
-static __device__ __noinline__ int decide_conservative64(const SolveParams& P, int col, int g, int lay, int ib, float ztauc,
-                                                  float zomcc, float zgcc, float zcoc, const double* __restrict__ tab64) {
-    const size_t n = (size_t)P.ncol;
-    const size_t kl = (size_t)col + n * (size_t)(lay - 1);
-    double cldf = 1.0, ciwp, clwp, rei, rel, tauc = 0.0, ssac = 1.0, asmc = 0.0, fsfc = 0.0;
-    if (P.fused) {
-        ciwp = P.ciwp[kl]; clwp = P.clwp[kl]; rei = P.rei[kl]; rel = P.rel[kl];
-        if (P.tauc) {
-            const size_t kb = (size_t)ib + 14 * kl;
-            tauc = P.tauc[kb]; ssac = P.ssac[kb]; asmc = P.asmc[kb]; fsfc = P.fsfc[kb];
-        }
-    } else {
-        const size_t kg = (size_t)g + NGPT * kl;
-        cldf = P.cldfmcl[kg]; tauc = P.taucmcl[kg]; ssac = P.ssacmcl[kg]; asmc = P.asmcmcl[kg];
-        fsfc = P.fsfcmcl[kg]; ciwp = P.ciwpmcl[kg]; clwp = P.clwpmcl[kg];
-        rei = P.reicmcl[kl]; rel = P.relqmcl[kl];
-    }
-    double taor, coc;
-    cldprmc_g<double>(ib, P.inflag, P.iceflag, P.liqflag, cldf, ciwp, clwp, rei, rel, fsfc, tauc, ssac, asmc, taor,
-                      coc, tab64, nullptr);
-    const double tc = (double)ztauc, oc = (double)zomcc, gcl = (double)zgcc;
-    const double ztauo = tc + tauc;
-    const double scat = tc * oc + tauc * ssac;
-    const double zgco = (tauc * ssac * asmc + tc * oc * gcl) / scat;
-    const double zomco = scat / ztauo;
-    const double zcoo = (tc * (double)zcoc + tauc * coc) / ztauo;
-    return one_minus_zwo<double>(zomco, zcoo, zgco) <= 5.0e-7 ? 1 : 0;
-}
-
 // Whether the FP32 estimate of 1 - zwo (reftra:183-188) is too close to the
 // 5e-7 switch to trust its branch.  The window is an error bound from the
 // FP32 optics: 2e-6 relative on the co-albedo and on the asymmetry.  Near
@@ -193,6 +179,272 @@ __device__ inline bool near_conservative_edge(float zw, float zco, float zg) {
     return fabsf(r - 5.0e-7f) <= tol;
 }
 
+// Optical inputs of one (g-point, layer) cell: gas and Rayleigh depths,
+// aerosol (depth, single-scattering albedo, asymmetry, co-albedo) and the
+// subcolumn's cloud after cldprmc (delta-scaled depth, albedo, asymmetry,
+// co-albedo; unscaled depth taor).
+template <typename R>
+struct CellIn {
+    R taug, taur;
+    R rta, roa, rga, rcoa;
+    bool cloudy;
+    R cldf, tc, oc, gc, coc, taor;
+};
+
+// What pass 2 needs of a cell: clear and total layer reflectance and
+// transmittance, the delta-scaled direct-beam transmittances and, for
+// idelm = 0, the unscaled ones.  risky (FP32 form): a discrete choice of
+// the cell -- a lookup-table entry, the conservative switch, the resonance
+// k mu0 = 1 -- is too close to call in FP32.
+template <typename R>
+struct CellOpt {
+    RT<R> rc, rt;
+    R zdbtc, zdbt, dbtcn, dbtn;
+    bool risky;
+};
+
+// Aerosol of band ib at (column, layer) when not staged (spcvmc:442-445 inputs).
+template <typename R>
+__device__ inline void aerosol_in(const SolveParams& P, int col, int lay, int ib, const double* __restrict__ tab64,
+                                  CellIn<R>& ci) {
+    if (P.iaer == 0) {
+        ci.rta = R(0); ci.roa = R(1); ci.rga = R(0); ci.rcoa = R(0);
+        return;
+    }
+    double ta, oa, ga;
+    aerosol(P, col, lay, ib, tab64, ta, oa, ga);
+    ci.rta = (R)ta; ci.roa = (R)oa; ci.rga = (R)ga; ci.rcoa = (R)DS(1.0, oa);
+}
+
+// Cloud of subcolumn g at (column, layer), then cldprmc_sw.  Fused McICA:
+// `cloudy` is the mask, the physical inputs come from `cld` (the CTA's
+// staged copy) or, with cld == nullptr, from the FP64 arrays; unfused: the
+// subcolumn arrays (cldfmcl ...) decide and supply the cloud.
+template <typename R>
+__device__ inline void cloud_in(const SolveParams& P, int col, int g, int lay, int ib, bool fused, bool cloudy,
+                                const R* cld, CellIn<R>& ci, const R* __restrict__ tab) {
+    const size_t n = (size_t)P.ncol;
+    const int L = P.nlay;
+    R cldf = R(0), tc = R(0), oc = R(1), gc = R(0), fsfc = R(0), ciwp = R(0), clwp = R(0), rei = R(0), rel = R(0);
+    if (P.icld >= 1) {
+        const size_t kl = (size_t)col + n * (size_t)(lay - 1);
+        if (fused) {
+            if (cloudy) {
+                cldf = R(1);
+                ciwp = cld ? cld[0 * L + lay - 1] : (R)P.ciwp[kl];
+                clwp = cld ? cld[1 * L + lay - 1] : (R)P.clwp[kl];
+                if (P.tauc) {
+                    const size_t kb = (size_t)ib + 14 * kl;
+                    tc = (R)P.tauc[kb];
+                    oc = (R)P.ssac[kb];
+                    gc = (R)P.asmc[kb];
+                    fsfc = (R)P.fsfc[kb];
+                }
+            }
+            rei = cld ? cld[2 * L + lay - 1] : (R)P.rei[kl];
+            rel = cld ? cld[3 * L + lay - 1] : (R)P.rel[kl];
+        } else {
+            const size_t kg = (size_t)g + NGPT * kl;
+            const double cf = P.cldfmcl[kg];
+            cloudy = cf != 0.0;
+            cldf = (R)cf;
+            tc = (R)P.taucmcl[kg];
+            oc = (R)P.ssacmcl[kg];
+            gc = (R)P.asmcmcl[kg];
+            fsfc = (R)P.fsfcmcl[kg];
+            ciwp = (R)P.ciwpmcl[kg];
+            clwp = (R)P.clwpmcl[kg];
+            rei = (R)P.reicmcl[kl];
+            rel = (R)P.relqmcl[kl];
+        }
+    }
+    R taor = tc, coc = R(1) - oc;
+    if (P.icld >= 1 && cloudy)
+        cldprmc_g<R>(ib, P.inflag, P.iceflag, P.liqflag, cldf, ciwp, clwp, rei, rel, fsfc, tc, oc, gc, taor, coc, tab,
+                     P.err);
+    ci.cloudy = P.icld >= 1 && cloudy;
+    ci.cldf = cldf; ci.tc = tc; ci.oc = oc; ci.gc = gc; ci.coc = coc; ci.taor = taor;
+}
+
+// FP32 form: whether the direct-beam lookup exp(-x) sits so close to the
+// edge between two table entries (rrtmg_sw_spcvmc.f90:558-585) that the
+// FP64 form may take the other one, and the step would move this layer's
+// heating rate by more than BEAM_HR_TOL K/day (hrs = incident flux * heatfac / dp).
+// The window assumes BEAM_EPS relative uncertainty in the FP32 optical depth.
+constexpr float BEAM_EPS = 5.0e-7f;
+constexpr float BEAM_HR_TOL = 2.0e-3f;
+__device__ inline bool beam_risky(float x, float hrs) {
+    if (x <= 0.06f) return false;  // quadratic branch: no table step
+    const float b = cT.bpade_f;
+    const float bx = b + x;
+    const float t = 10000.0f * x / bx + 0.5f;
+    const float fr = t - floorf(t);
+    const float d = fminf(fr, 1.0f - fr);
+    const float win = 10000.0f * b * x / (bx * bx) * BEAM_EPS;
+    if (d >= win) return false;
+    const float step = __expf(-x) * bx * bx / (b * 10000.0f);  // change of exp(-x) per table entry
+    return hrs * step > BEAM_HR_TOL;
+}
+
+// Layer optics of one cell (rrtmg_sw_spcvmc.f90:442-585): clear optics
+// with aerosol, delta-M scaling, reftra for clear and (if cloudy) total sky,
+// cloud-fraction mixing and the direct beams.  Shared by both forms; the
+// FP32 form also carries the co-albedo and flags risky cells.
+template <typename R>
+__device__ inline CellOpt<R> cell_optics(const CellIn<R>& ci, int idelm, R prmu0, const R* __restrict__ tab,
+                                         const double* __restrict__ tab64, float hrs) {
+    CellOpt<R> o;
+    o.risky = false;
+    o.dbtcn = o.dbtn = R(0);
+    R ztauc = ci.taur + ci.taug + ci.rta;
+    R zomcc = ci.taur * R(1) + ci.rta * ci.roa;
+    R zgcc = ci.rga * ci.roa * ci.rta / zomcc;
+    R zcoc = R(0);
+    if constexpr (sizeof(R) == 4) zcoc = (ci.taug + ci.rta * ci.rcoa) / ztauc;  // co-albedo
+    zomcc = zomcc / ztauc;
+    const R zclear = R(1) - ci.cldf, zcloud = ci.cldf;
+    if (idelm == 0) {
+        const R zdbtmc = tbl_exp<R>(ztauc / prmu0, tab);
+        const R tauorig = ztauc + ci.taor;
+        const R zdbtmo = tbl_exp<R>(tauorig / prmu0, tab);
+        o.dbtcn = zdbtmc;
+        o.dbtn = zclear * zdbtmc + zcloud * zdbtmo;
+    }
+    // delta scaling, clear (spcvmc:492-496)
+    const R zf = zgcc * zgcc;
+    const R zwf = zomcc * zf;
+    ztauc = (R(1) - zwf) * ztauc;
+    zomcc = (zomcc - zwf) / (R(1) - zwf);
+    zgcc = (zgcc - zf) / (R(1) - zf);
+    if constexpr (sizeof(R) == 4) zcoc = zcoc / (R(1) - zwf);
+    o.rc = reftra_g<R>(ztauc, zomcc, zcoc, zgcc, prmu0, tab, tab64);
+    const R xc = ztauc / prmu0;
+    o.zdbtc = tbl_exp<R>(xc, tab);
+    if constexpr (sizeof(R) == 4) o.risky = o.rc.risky || beam_risky(xc, hrs);
+    o.rt = o.rc;
+    o.zdbt = o.zdbtc;
+    if (ci.cloudy) {
+        // total sky: clear + delta-scaled cloud (spcvmc:500-505); reftra
+        // only where cldf > repclc (:427); mixed by cloud fraction (:546-549)
+        const R ztauo = ztauc + ci.tc;
+        R zomco = ztauc * zomcc + ci.tc * ci.oc;
+        const R zgco = (ci.tc * ci.oc * ci.gc + ztauc * zomcc * zgcc) / zomco;
+        R zcoo = R(0);
+        if constexpr (sizeof(R) == 4) zcoo = (ztauc * zcoc + ci.tc * ci.coc) / ztauo;
+        zomco = zomco / ztauo;
+        RT<R> ro;
+        if (ci.cldf > R(1.e-12)) {
+            ro = reftra_g<R>(ztauo, zomco, zcoo, zgco, prmu0, tab, tab64);
+        } else {
+            ro.ref = R(0); ro.tra = R(1); ro.refd = R(0); ro.trad = R(1);
+            ro.adir = R(0); ro.adif = R(0); ro.risky = false;
+        }
+        o.rt.ref = zclear * o.rc.ref + zcloud * ro.ref;
+        o.rt.refd = zclear * o.rc.refd + zcloud * ro.refd;
+        o.rt.tra = zclear * o.rc.tra + zcloud * ro.tra;
+        o.rt.trad = zclear * o.rc.trad + zcloud * ro.trad;
+        const R xo = ztauo / prmu0;
+        const R zdbtmo = tbl_exp<R>(xo, tab);
+        o.zdbt = zclear * o.zdbtc + zcloud * zdbtmo;
+        if constexpr (sizeof(R) == 4) {
+            o.rt.adir = zclear * o.rc.adir + zcloud * ro.adir;
+            o.rt.adif = zclear * o.rc.adif + zcloud * ro.adif;
+            o.risky = o.risky || ro.risky || beam_risky(xo, hrs);
+        }
+    }
+    return o;
+}
+
+// FP32 form: one cell exactly as the FP64 form computes it -- gas optics
+// from the FP64 layer coefficients, aerosol and cloud from the FP64 inputs
+// -- returned in FP32 with its absorptances.  Used for the rare risky cells.
+static __device__ __noinline__ CellOpt<float> cell_optics_fp64(const SolveParams& P, const Coef<double>& C64, int col,
+                                                               int g, int lay, int ib, int igb, bool fused,
+                                                               bool cloudy, double cossza,
+                                                               const double* __restrict__ tab64) {
+    CellIn<double> ci;
+    taumol_g<double>(ib, igb, lay, C64, tab64, ci.taug, ci.taur);
+    aerosol_in(P, col, lay, ib, tab64, ci);
+    cloud_in<double>(P, col, g, lay, ib, fused, cloudy, nullptr, ci, tab64);
+    const CellOpt<double> d = cell_optics<double>(ci, P.idelm, cossza, tab64, tab64, 0.0f);
+    CellOpt<float> o;
+    auto cvt = [](const RT<double>& r) {
+        RT<float> f;
+        f.ref = (float)r.ref; f.refd = (float)r.refd; f.tra = (float)r.tra; f.trad = (float)r.trad;
+        f.adir = (float)(1.0 - r.ref - r.tra);
+        f.adif = (float)(1.0 - r.refd - r.trad);
+        f.risky = false;
+        return f;
+    };
+    o.rc = cvt(d.rc);
+    o.rt = cvt(d.rt);
+    o.zdbtc = (float)d.zdbtc;
+    o.zdbt = (float)d.zdbt;
+    o.dbtcn = (float)d.dbtcn;
+    o.dbtn = (float)d.dbtn;
+    o.risky = false;
+    return o;
+}
+
+// FP32 form: redo the marked cells of one (column, g-point) in FP64 and
+// the upward adding recurrence (vrtqdr:122-140) from the lowest of them to
+// the top.  sv0 is the thread's scratch column (stride CTA_THREADS per
+// field, NS fields per level); the transmittance slots hold absorptances.
+static __device__ __noinline__ void redo_cells_fp64(const SolveParams& P, const Coef<double>& C64, float* sv0, int NS,
+                                                    int col, int g, int ib, int igb, bool fused, double cossza,
+                                                    const double* __restrict__ tab64, float albp, float albd,
+                                                    int from) {
+    const int L = P.nlay;
+    auto at = [&](int lay, int fld) -> float& { return sv0[((size_t)(L - lay) * NS + fld) * CTA_THREADS]; };
+    float rupc_b = albp, rupdc_b = albd, rup_b = albp, rupd_b = albd;
+    if (from > 1) {
+        rupc_b = at(from - 1, S_RUPC);
+        rupdc_b = at(from - 1, S_RUPDC);
+        rup_b = at(from - 1, S_RUP);
+        rupd_b = at(from - 1, S_RUPD);
+    }
+    for (int lay = from; lay <= L; ++lay) {
+        const float mark = at(lay, S_DBTC);
+        if (mark < 0.0f) {
+            const CellOpt<float> co = cell_optics_fp64(P, C64, col, g, lay, ib, igb, fused, mark < -1.5f, cossza, tab64);
+            at(lay, S_REFC) = co.rc.ref;
+            at(lay, S_REFDC) = co.rc.refd;
+            at(lay, S_TRAC) = co.rc.adir;
+            at(lay, S_TRADC) = co.rc.adif;
+            at(lay, S_DBTC) = co.zdbtc;
+            at(lay, S_REF) = co.rt.ref;
+            at(lay, S_REFD) = co.rt.refd;
+            at(lay, S_TRA) = co.rt.adir;
+            at(lay, S_TRAD) = co.rt.adif;
+            at(lay, S_DBT) = co.zdbt;
+            if (P.idelm == 0) {
+                at(lay, S_DBTCN) = co.dbtcn;
+                at(lay, S_DBTN) = co.dbtn;
+            }
+        }
+        {
+            const float ref = at(lay, S_REFC), refd = at(lay, S_REFDC), dbt = at(lay, S_DBTC);
+            const float tra = 1.0f - ref - at(lay, S_TRAC), trad = 1.0f - refd - at(lay, S_TRADC);
+            const float zr = 1.0f / (1.0f - rupdc_b * refd);
+            const float rupc = ref + (trad * ((tra - dbt) * rupdc_b + dbt * rupc_b)) * zr;
+            rupdc_b = refd + trad * trad * rupdc_b * zr;
+            rupc_b = rupc;
+            at(lay, S_RUPC) = rupc_b;
+            at(lay, S_RUPDC) = rupdc_b;
+        }
+        {
+            const float ref = at(lay, S_REF), refd = at(lay, S_REFD), dbt = at(lay, S_DBT);
+            const float tra = 1.0f - ref - at(lay, S_TRA), trad = 1.0f - refd - at(lay, S_TRAD);
+            const float zr = 1.0f / (1.0f - rupd_b * refd);
+            const float rup = ref + (trad * ((tra - dbt) * rupd_b + dbt * rup_b)) * zr;
+            rupd_b = refd + trad * trad * rupd_b * zr;
+            rup_b = rup;
+            at(lay, S_RUP) = rup_b;
+            at(lay, S_RUPD) = rupd_b;
+        }
+    }
+}
+
 template <typename R>
 __device__ inline void warp_sum4(R& v) {
     v += __shfl_xor_sync(0xffffffffu, v, 1);
@@ -202,7 +454,7 @@ __device__ inline void warp_sum4(R& v) {
 // Shared-memory carve-up of one CTA (two columns); the host sizes the
 // launch with the same function.
 struct Smem {
-    size_t pdp, coef, pk, misc, kc, ka, omcf, cld, seed, aer, xs, red, flux, total;
+    size_t pdp, coef, coef64, hrf, pk, misc, kc, ka, omcf, cld, seed, aer, xs, red, flux, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -212,6 +464,12 @@ __host__ __device__ inline Smem smem_layout(int L, int nq, bool fused, bool aer_
     size_t o = 0;
     m.pdp = o;  o = align16(o + COLS_PER_CTA * L * sizeof(double));
     m.coef = o; o = align16(o + COLS_PER_CTA * NFR * L * rsz);
+    m.coef64 = m.hrf = o;
+    if (rsz == sizeof(float)) {
+        // FP32 form: FP64 layer coefficients and heatfac / dp per layer
+        m.coef64 = o; o = align16(o + COLS_PER_CTA * NFR * L * sizeof(double));
+        m.hrf = o;    o = align16(o + COLS_PER_CTA * L * sizeof(float));
+    }
     m.pk = o;   o = align16(o + COLS_PER_CTA * L * sizeof(int));
     m.misc = o; o = align16(o + 8 * sizeof(int));
     m.kc = m.ka = m.omcf = m.cld = m.seed = m.xs = m.aer = o;
@@ -250,6 +508,8 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
     const Smem M = smem_layout(L, NQ, fused, aer_stage, sizeof(R));
     double* sPdp = (double*)(smem_raw + M.pdp);        // [2][L]
     R* sCoef = (R*)(smem_raw + M.coef);                // [2][NFR][L]
+    double* sCoef64 = (double*)(smem_raw + M.coef64);  // [2][NFR][L] FP32 form: FP64 coefficients
+    float* sHrf = (float*)(smem_raw + M.hrf);          // [2][L] FP32 form: heatfac / dp
     int* sPk = (int*)(smem_raw + M.pk);                // [2][L]
     int* sMisc = (int*)(smem_raw + M.misc);            // laytrop [2]
     long long* sKc = (long long*)(smem_raw + M.kc);    // [2][L] McICA threshold of 1 - cldf
@@ -284,7 +544,10 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
         for (int it = tid; it < COLS_PER_CTA * L; it += CTA_THREADS) {
             const int c2 = it / L, lay = it % L + 1;
             const int pcol = COLS_PER_CTA * pair + c2;
-            prep_layer<R>(P, pcol, lay, sCoef + c2 * NFR * L, sPk + c2 * L, sPdp + c2 * L, L, tab64);
+            constexpr bool f32 = sizeof(R) == 4;
+            prep_layer<R>(P, pcol, lay, sCoef + c2 * NFR * L, sPk + c2 * L, sPdp + c2 * L, L, tab64,
+                          f32 ? sCoef64 + c2 * NFR * L : nullptr);
+            if (f32) sHrf[c2 * L + lay - 1] = (float)(cT.heatfac / sPdp[c2 * L + lay - 1]);
             const bool real = pcol < P.ncol;
             const size_t kl = (size_t)pcol + n * (size_t)(lay - 1);
             if (fused) {
@@ -333,6 +596,7 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
         __syncthreads();
         const int col = COLS_PER_CTA * pair + cc;
         const Coef<R> C{sCoef + cc * NFR * L, sPk + cc * L, L, sMisc[cc]};
+        const Coef<double> C64{sCoef64 + cc * NFR * L, sPk + cc * L, L, sMisc[cc]};
         bool active = col < P.ncol;
         if (active && (C.laytrop < 1 || C.laytrop >= L)) {
             set_error(P.err, E_LAYTROP);
@@ -362,6 +626,7 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
 
         // ---------------- pass 1: bottom -> top
         R rupc_b = albp, rupdc_b = albd, rup_b = albp, rupd_b = albd;
+        int redo_from = L + 1;  // FP32 form: lowest layer to redo in FP64
         for (int lay = 1; lay <= L; ++lay) {
             const int jk = L + 1 - lay;
             R* sv = scr + (size_t)(jk - 1) * NS * CTA_THREADS + tid;
@@ -374,115 +639,41 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
             } else {
                 taumol_g<R>(ib, igb, lay, C, tab, taug, taur);
             }
-            R rta, roa, rga, rcoa;
+            CellIn<R> ci;
+            ci.taug = taug;
+            ci.taur = taur;
             if (aer_stage) {
-                rta = aer[(0 * NBND + ib) * L + lay - 1];
-                rcoa = aer[(1 * NBND + ib) * L + lay - 1];
-                roa = R(1) - rcoa;
-                rga = aer[(2 * NBND + ib) * L + lay - 1];
-            } else if (P.iaer == 0) {
-                rta = R(0); roa = R(1); rga = R(0); rcoa = R(0);
+                ci.rta = aer[(0 * NBND + ib) * L + lay - 1];
+                ci.rcoa = aer[(1 * NBND + ib) * L + lay - 1];
+                ci.roa = R(1) - ci.rcoa;
+                ci.rga = aer[(2 * NBND + ib) * L + lay - 1];
             } else {
-                double ta, oa, ga;
-                aerosol(P, col, lay, ib, tab64, ta, oa, ga);
-                rta = (R)ta; roa = (R)oa; rga = (R)ga; rcoa = (R)DS(1.0, oa);
+                aerosol_in(P, col, lay, ib, tab64, ci);
             }
             // cloud of this subcolumn (McICA) at this layer
             bool cloudy = false;
-            R cldf = R(0), tc = R(0), oc = R(1), gc = R(0), fsfc = R(0), ciwp = R(0), clwp = R(0), rei = R(0),
-              rel = R(0);
-            if (P.icld >= 1) {
-                const size_t kl = (size_t)col + n * (size_t)(lay - 1);
-                if (fused) {
-                    cloudy = mc.step(lay, sKc[cc * L + lay - 1], sKa[cc * L + lay - 1], sOmcf[cc * L + lay - 1]);
-                    if (cloudy) {
-                        cldf = R(1);
-                        ciwp = cld[0 * L + lay - 1];
-                        clwp = cld[1 * L + lay - 1];
-                        if (P.tauc) {
-                            const size_t kb = (size_t)ib + 14 * kl;
-                            tc = (R)P.tauc[kb];
-                            oc = (R)P.ssac[kb];
-                            gc = (R)P.asmc[kb];
-                            fsfc = (R)P.fsfc[kb];
-                        }
-                    }
-                    rei = cld[2 * L + lay - 1];
-                    rel = cld[3 * L + lay - 1];
-                } else {
-                    const size_t kg = (size_t)g + NGPT * kl;
-                    const double cf = P.cldfmcl[kg];
-                    cloudy = cf != 0.0;
-                    cldf = (R)cf;
-                    tc = (R)P.taucmcl[kg];
-                    oc = (R)P.ssacmcl[kg];
-                    gc = (R)P.asmcmcl[kg];
-                    fsfc = (R)P.fsfcmcl[kg];
-                    ciwp = (R)P.ciwpmcl[kg];
-                    clwp = (R)P.clwpmcl[kg];
-                    rei = (R)P.reicmcl[kl];
-                    rel = (R)P.relqmcl[kl];
+            if (P.icld >= 1 && fused)
+                cloudy = mc.step(lay, sKc[cc * L + lay - 1], sKa[cc * L + lay - 1], sOmcf[cc * L + lay - 1]);
+            cloud_in<R>(P, col, g, lay, ib, fused, cloudy, cld, ci, tab);
+            const R hrs = zinc * sHrf[cc * L + lay - 1];
+            const CellOpt<R> co = cell_optics<R>(ci, P.idelm, prmu0, tab, tab64, hrs);
+            // FP32 form: a table entry, the conservative switch or the
+            // resonance of this cell is too close to call in FP32; it is
+            // marked in the scratch (S_DBTC < 0, -2 if cloudy) and redone
+            // after this pass as the FP64 form does
+            int redo = 0;
+            if constexpr (sizeof(R) == 4) {
+                if (co.risky) {
+                    redo = ci.cloudy ? 2 : 1;
+                    if (lay < redo_from) redo_from = lay;
                 }
             }
-            R taor = tc, coc = R(1) - oc;
-            if (P.icld >= 1 && cloudy)
-                cldprmc_g<R>(ib, P.inflag, P.iceflag, P.liqflag, cldf, ciwp, clwp, rei, rel, fsfc, tc, oc, gc, taor,
-                             coc, tab, P.err);
-            // clear-sky optics including aerosols (spcvmc:442-445)
-            R ztauc = taur + taug + rta;
-            R zomcc = taur * R(1) + rta * roa;
-            R zgcc = rga * roa * rta / zomcc;
-            R zcoc = R(0);
-            if constexpr (sizeof(R) == 4) zcoc = (taug + rta * rcoa) / ztauc;  // co-albedo
-            zomcc = zomcc / ztauc;
-            const R zclear = R(1) - cldf, zcloud = cldf;
+            const RT<R>& rc = co.rc;
+            const RT<R>& rt = co.rt;
+            const R zdbtc = co.zdbtc, zdbt = co.zdbt;
             if (P.idelm == 0) {
-                const R zdbtmc = tbl_exp<R>(ztauc / prmu0, tab);
-                const R tauorig = ztauc + taor;
-                const R zdbtmo = tbl_exp<R>(tauorig / prmu0, tab);
-                sv[S_DBTCN * CTA_THREADS] = zdbtmc;
-                sv[S_DBTN * CTA_THREADS] = zclear * zdbtmc + zcloud * zdbtmo;
-            }
-            // delta scaling, clear (spcvmc:492-496)
-            const R zf = zgcc * zgcc;
-            const R zwf = zomcc * zf;
-            ztauc = (R(1) - zwf) * ztauc;
-            zomcc = (zomcc - zwf) / (R(1) - zwf);
-            zgcc = (zgcc - zf) / (R(1) - zf);
-            if constexpr (sizeof(R) == 4) zcoc = zcoc / (R(1) - zwf);
-            const RT<R> rc = reftra_g<R>(ztauc, zomcc, zcoc, zgcc, prmu0, tab, tab64);
-            const R zdbtc = tbl_exp<R>(ztauc / prmu0, tab);
-            RT<R> rt = rc;
-            R zdbt = zdbtc;
-            if (cloudy) {
-                // total sky: clear + delta-scaled cloud (spcvmc:500-505); reftra
-                // only where cldf > repclc (:427); mixed by cloud fraction (:546-549)
-                const R ztauo = ztauc + tc;
-                R zomco = ztauc * zomcc + tc * oc;
-                const R zgco = (tc * oc * gc + ztauc * zomcc * zgcc) / zomco;
-                R zcoo = R(0);
-                if constexpr (sizeof(R) == 4) zcoo = (ztauc * zcoc + tc * coc) / ztauo;
-                zomco = zomco / ztauo;
-                RT<R> ro;
-                if (cldf > R(1.e-12)) {
-                    int force = -1;
-                    if constexpr (sizeof(R) == 4) {
-                        if (near_conservative_edge(zomco, zcoo, zgco))
-                            force = decide_conservative64(P, col, g, lay, ib, ztauc, zomcc, zgcc, zcoc, tab64);
-                    }
-                    ro = reftra_g<R>(ztauo, zomco, zcoo, zgco, prmu0, tab, tab64, force);
-                }
-                else { ro.ref = R(0); ro.tra = R(1); ro.refd = R(0); ro.trad = R(1); ro.adir = R(0); ro.adif = R(0); }
-                rt.ref = zclear * rc.ref + zcloud * ro.ref;
-                rt.refd = zclear * rc.refd + zcloud * ro.refd;
-                rt.tra = zclear * rc.tra + zcloud * ro.tra;
-                rt.trad = zclear * rc.trad + zcloud * ro.trad;
-                if constexpr (sizeof(R) == 4) {
-                    rt.adir = zclear * rc.adir + zcloud * ro.adir;
-                    rt.adif = zclear * rc.adif + zcloud * ro.adif;
-                }
-                const R zdbtmo = tbl_exp<R>(ztauo / prmu0, tab);
-                zdbt = zclear * zdbtc + zcloud * zdbtmo;
+                sv[S_DBTCN * CTA_THREADS] = co.dbtcn;
+                sv[S_DBTN * CTA_THREADS] = co.dbtn;
             }
             // upward adding recurrence (vrtqdr:122-140)
             {
@@ -506,7 +697,7 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
             sv[S_REFDC * CTA_THREADS] = rc.refd;
             sv[S_TRAC * CTA_THREADS] = keep_abs ? rc.adir : rc.tra;
             sv[S_TRADC * CTA_THREADS] = keep_abs ? rc.adif : rc.trad;
-            sv[S_DBTC * CTA_THREADS] = zdbtc;
+            sv[S_DBTC * CTA_THREADS] = redo ? -(R)redo : zdbtc;
             sv[S_RUPC * CTA_THREADS] = rupc_b;
             sv[S_RUPDC * CTA_THREADS] = rupdc_b;
             sv[S_REF * CTA_THREADS] = rt.ref;
@@ -516,6 +707,11 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
             sv[S_DBT * CTA_THREADS] = zdbt;
             sv[S_RUP * CTA_THREADS] = rup_b;
             sv[S_RUPD * CTA_THREADS] = rupd_b;
+        }
+
+        if constexpr (sizeof(R) == 4) {
+            if (active && redo_from <= L)
+                redo_cells_fp64(P, C64, scr + tid, NS, col, g, ib, igb, fused, cossza, tab64, albp, albd, redo_from);
         }
 
         // ---------------- pass 2: top -> bottom, level fluxes and g sums

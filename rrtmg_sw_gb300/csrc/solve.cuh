@@ -596,6 +596,9 @@ struct RT {
     // FP32 form only: absorptances 1 - ref - tra (direct incidence) and
     // 1 - refd - trad (diffuse incidence), formed without cancellation
     R adir, adif;
+    // FP32 form only: a discrete choice (table entry near resonance, the
+    // conservative switch) is too close to call in FP32
+    bool risky;
 };
 
 // zco = 1 - zw carried separately by the FP32 form (unused by FP64);
@@ -614,6 +617,7 @@ __device__ __noinline__ RT<double> reftra_fp64(double zto1, double zw, double zg
     typedef double R;
     RT<R> o;
     o.adir = o.adif = 0.0;
+    o.risky = false;
     const R zwcrit = 0.9999995, eps = 1.e-08;
     const R zg3 = 3.0 * zg;
     const R zgamma1 = (8.0 - zw * (5.0 + zg3)) * 0.25;

@@ -38,24 +38,27 @@ __device__ inline float tbl_exp_om(float x, const float* __restrict__ tab, float
 // so a heating rate can be summed from layer absorption instead of being
 // differenced from level fluxes.  Mathematically these are the reference's
 // expressions; they only avoid FP32 cancellation.
-// FP64 island: the non-conservative solution has a removable singularity
-// at resonance, k*mu0 = 1 (zrpp = 1 - (k mu0)^2 -> 0, where the numerators
-// of pref/ptra and zdenr vanish together).  There FP32 keeps no digits, so
-// layers with |zrpp| < RESONANCE_TOL are solved with the reference's FP64
-// expressions.
+// Near resonance, k mu0 = 1 (zrpp = 1 - (k mu0)^2 -> 0), the solution has a
+// removable singularity: the numerators of pref/ptra and zdenr vanish
+// together, so the result hinges on zem1 and zem2 coming from consistent
+// table entries.  The scattered part carries a factor zw, so the rounding
+// error of an FP32 cell grows like zw / |zrpp|.  Cells with
+// |zrpp| < RESONANCE_TOL zw, or with |zrpp| < RESONANCE_WIDE and a table
+// lookup too close to an entry edge to be sure of, are flagged risky; the
+// caller then recomputes the cell as the FP64 form does.  So are cells
+// whose conservative switch is too close.
 constexpr float RESONANCE_TOL = 2.0e-3f;
+constexpr float RESONANCE_WIDE = 5.0e-2f;
 
-__device__ __noinline__ RT<float> reftra_island(float zto1, float zw, float zg, float prmuz,
-                                                const double* __restrict__ tab64) {
-    const RT<double> d = reftra_g<double>((double)zto1, (double)zw, 0.0, (double)zg, (double)prmuz, tab64, tab64, -1);
-    RT<float> o;
-    o.ref = (float)d.ref;
-    o.refd = (float)d.refd;
-    o.tra = (float)d.tra;
-    o.trad = (float)d.trad;
-    o.adir = (float)(1.0 - d.ref - d.tra);
-    o.adif = (float)(1.0 - d.refd - d.trad);
-    return o;
+// Whether exp(-x) from the table could come from the neighbouring entry
+// under a 5e-7 relative uncertainty of x.
+__device__ inline bool entry_edge(float x) {
+    if (x <= 0.06f) return false;
+    const float b = cT.bpade_f;
+    const float bx = b + x;
+    const float t = 10000.0f * x / bx + 0.5f;
+    const float fr = t - floorf(t);
+    return fminf(fr, 1.0f - fr) < 10000.0f * b * x / (bx * bx) * 5.0e-7f;
 }
 
 template <>
@@ -70,9 +73,12 @@ __device__ __noinline__ RT<float> reftra_g<float>(float zto1, float zw, float zc
     const float zgamma3 = (2.0f - zg3 * prmuz) * 0.25f;
     const float zgamma4 = 1.0f - zgamma3;
     // zwo >= zwcrit  <=>  1 - zwo <= 5e-7  (reftra:183-188)
-    const bool cons = force >= 0 ? force == 1 : one_minus_zwo(zw, zco, zg) <= 5.0e-7f;
+    (void)force;
+    (void)tab64;
+    const bool cons = one_minus_zwo(zw, zco, zg) <= 5.0e-7f;
     o.adir = 0.0f;
     o.adif = 0.0f;
+    o.risky = near_conservative_edge(zw, zco, zg);
     if (cons) {
         // conservative scattering (reftra:191-228); ptra = 1 - pref and
         // ptrad = 1 - prefd written without the subtraction; no absorption
@@ -95,7 +101,7 @@ __device__ __noinline__ RT<float> reftra_g<float>(float zto1, float zw, float zc
     const float zrp1 = 1.0f + zrp, zrm1 = 1.0f - zrp;
     const float zrk2 = 2.0f * zrk;
     const float zrpp = zrm1 * zrp1;
-    if (fabsf(zrpp) < RESONANCE_TOL) return reftra_island(zto1, zw, zg, prmuz, tab64);
+    if (fabsf(zrpp) < RESONANCE_TOL * zw) o.risky = true;
     const float zrkg = zrk + zgamma1;
     const float r_kg = 1.0f / zrkg;
     const float g2k = zgamma2 * zgamma2 * r_kg;  // gamma1 - zrk
@@ -109,6 +115,8 @@ __device__ __noinline__ RT<float> reftra_g<float>(float zto1, float zw, float zc
     float om1, om2;
     const float zem1 = tbl_exp_om(fminf(zrk * zto1, 500.0f), tab, om1);
     const float zem2 = tbl_exp_om(fminf(zto1 / prmuz, 500.0f), tab, om2);
+    if (fabsf(zrpp) < RESONANCE_WIDE && !o.risky)
+        o.risky = entry_edge(fminf(zrk * zto1, 500.0f)) || entry_edge(fminf(zto1 / prmuz, 500.0f));
     const float p1 = om1 / zem1;  // zep1 - 1
     const float p2 = om2 / zem2;  // zep2 - 1
     const float zdenr = zrpp * (zrk2 + zrkg * p1 + g2k * om1);
