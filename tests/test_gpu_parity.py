@@ -140,7 +140,7 @@ def test_mcica_subcolumns_mt_bitexact(icld):
 
 
 def test_mcica_clouds_aerosol_fp64_parity():
-    # configuration 1 shape at small ncol: icld=2, inflgsw=2/iceflgsw=3/liqflgsw=1, iaer=10
+    # McICA clouds with aerosol at small ncol: icld=2, inflgsw=2/iceflgsw=3/liqflgsw=1, iaer=10
     c = make_columns(128, 60, 20261204, clouds=True, aerosol=True)
     m = mcica_oracle(c, 2, 112)
     kw = gcm_inputs(c, icld=2, iaer=10, mcica=m)
