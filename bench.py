@@ -64,6 +64,12 @@ def algorithmic_flops_per_column(nlay, cloudy_cells_per_col):
     return 112 * (257 * nlay + 48 * (nlay + 1)) + 171 * cloudy_cells_per_col
 
 
+# DRAM bytes per column of k_solve<float> measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum) at 32768 columns x 60 layers, profiles/k_solve_fp32_32768x60_full.md;
+# the traffic is per column pair, so a launch's traffic scales with its columns.
+PROFILED_DRAM_BYTES_PER_COLUMN = 24.78e9 / 32768
+
+
 def algorithmic_bytes_per_column(nlay):
     # FP64 interface, fused McICA: 7 gas/state layer arrays + plev + 4 albedos + coszen,
     # physical clouds 5L + alpha L, outputs 4 (L+1) + 2 L
@@ -332,7 +338,9 @@ def main():
                                            "speedup_fp32_over_fp64": ms64 / ms32,
                                            "max_abs_diff_fp32_vs_fp64": err},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
-                     "frac": (achieved / peak32) if peak32 else None, "traffic": None,
+                     "frac": (achieved / peak32) if peak32 else None,
+                     "traffic": PROFILED_DRAM_BYTES_PER_COLUMN * ncol if NLAY == 60 else None,
+                     "traffic_unit": "bytes per launch (ncu capture at 32768 columns, scaled by columns)",
                      "peak_source": "cuBLAS FP32 (non-TF32) 8192^3 GEMM measured in this run",
                      "flops_per_column": fl, "cloudy_cells_per_column": cloudy},
         "roofline_hbm": {"bound": "hbm", "achieved": bytes_col * ncol / (ms32 / 1e3) / 1e9, "peak": hbm,
