@@ -76,8 +76,10 @@ typedef struct rrtmg_sw_clouds {
 /* Arithmetic form of the solve. */
 enum {
     RRTMG_SW_FORM_FP64 = 0,    /* plain FP64, reference operation order */
-    RRTMG_SW_FORM_FP32 = 1     /* FP32 bulk, FP64 only in the reftra near-conservative
-                                  branch and the vrtqdr 1/(1-R*R) denominators */
+    RRTMG_SW_FORM_FP32 = 1     /* FP32 bulk (co-albedo carried, cancellation-free two-stream,
+                                  heating from layer absorption); FP64 in setcoef, the
+                                  outputs and cells whose table entry, conservative switch
+                                  or resonance is ambiguous in FP32 */
 };
 
 enum {
@@ -139,9 +141,10 @@ int rrtmg_sw_mcica_dev_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, void 
  *     (cudaGetSymbolAddress with that device current) and loads the module
  *     that holds it; make that first call before any stream capture.
  *   - Limit: the area must hold one scratch slot per SM.  A slot is
- *     nlay * (16 with idelm = 0, else 14) * 224 values of the form's type,
- *     so 256 MiB takes nlay <= 140 (FP32) or <= 70 (FP64) with idelm = 1 on a
- *     152-SM GPU.  Larger requests return RRTMG_SW_ESCRATCH, nothing runs.
+ *     nlay * (16 with idelm = 0, else 14) * 224 values of the form's type
+ *     (the FP32 form adds 60 * nlay floats), so 256 MiB takes nlay <= 138
+ *     (FP32) or <= 70 (FP64) with idelm = 1 on a 152-SM GPU.  Larger
+ *     requests return RRTMG_SW_ESCRATCH, nothing runs.
  *     Fewer resident CTAs than rrtmg_sw_dev_c may run when the slots that
  *     fit are fewer than its grid; results are identical, only slower.
  *   - Nothing needs to start at zero: every scratch value is written before

@@ -467,7 +467,7 @@ int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaS
     P.err = (int*)st.errw.p;
     const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
     LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms) : plan_fp64(P, st.num_sms);
-    P.slot_elems = slot_elems(P.nlay, P.idelm);
+    P.slot_elems = slot_elems(P.nlay, P.idelm, fp32);
     const size_t esz = fp32 ? sizeof(float) : sizeof(double);
     CK(st.scratch.ensure((size_t)li.grid * P.slot_elems * esz));
     P.scratch = st.scratch.p;
@@ -613,7 +613,7 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
     if (rc) return rc;
     const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
     LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms) : plan_fp64(P, st.num_sms);
-    P.slot_elems = slot_elems(P.nlay, P.idelm);
+    P.slot_elems = slot_elems(P.nlay, P.idelm, fp32);
     const size_t slot_bytes = P.slot_elems * (fp32 ? sizeof(float) : sizeof(double));
     const size_t slots = kStaticScratchBytes / slot_bytes;
     if (slots < (size_t)st.num_sms) return RRTMG_SW_ESCRATCH;

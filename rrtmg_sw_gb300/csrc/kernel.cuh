@@ -454,7 +454,7 @@ __device__ inline void warp_sum4(R& v) {
 // Shared-memory carve-up of one CTA (two columns); the host sizes the
 // launch with the same function.
 struct Smem {
-    size_t pdp, coef, coef64, hrf, pk, misc, kc, ka, omcf, cld, seed, aer, xs, red, flux, total;
+    size_t pdp, coef, hrf, pk, misc, kc, ka, omcf, cld, seed, aer, xs, red, flux, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -464,11 +464,10 @@ __host__ __device__ inline Smem smem_layout(int L, int nq, bool fused, bool aer_
     size_t o = 0;
     m.pdp = o;  o = align16(o + COLS_PER_CTA * L * sizeof(double));
     m.coef = o; o = align16(o + COLS_PER_CTA * NFR * L * rsz);
-    m.coef64 = m.hrf = o;
+    m.hrf = o;
     if (rsz == sizeof(float)) {
-        // FP32 form: FP64 layer coefficients and heatfac / dp per layer
-        m.coef64 = o; o = align16(o + COLS_PER_CTA * NFR * L * sizeof(double));
-        m.hrf = o;    o = align16(o + COLS_PER_CTA * L * sizeof(float));
+        // FP32 form: heatfac / dp per layer
+        m.hrf = o; o = align16(o + COLS_PER_CTA * L * sizeof(float));
     }
     m.pk = o;   o = align16(o + COLS_PER_CTA * L * sizeof(int));
     m.misc = o; o = align16(o + 8 * sizeof(int));
@@ -508,7 +507,6 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
     const Smem M = smem_layout(L, NQ, fused, aer_stage, sizeof(R));
     double* sPdp = (double*)(smem_raw + M.pdp);        // [2][L]
     R* sCoef = (R*)(smem_raw + M.coef);                // [2][NFR][L]
-    double* sCoef64 = (double*)(smem_raw + M.coef64);  // [2][NFR][L] FP32 form: FP64 coefficients
     float* sHrf = (float*)(smem_raw + M.hrf);          // [2][L] FP32 form: heatfac / dp
     int* sPk = (int*)(smem_raw + M.pk);                // [2][L]
     int* sMisc = (int*)(smem_raw + M.misc);            // laytrop [2]
@@ -528,6 +526,8 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
     const bool uv = ib >= 9 && ib <= 12;  // bands 25-28 (spcvmc:629)
     const int NS = P.idelm == 0 ? NS_MAX : S_DBTCN;
     R* scr = (R*)P.scratch + (size_t)blockIdx.x * P.slot_elems;
+    // FP32 form: the FP64 layer coefficients [2][NFR][L] follow the level fields of the slot
+    double* sCoef64 = (double*)(scr + (size_t)L * NS * CTA_THREADS);
     const size_t n = (size_t)P.ncol;
 
     // McICA stream jump of this subcolumn: once per launch

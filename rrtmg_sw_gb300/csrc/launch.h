@@ -24,7 +24,7 @@ LaunchInfo plan_fp32(const SolveParams& P, int num_sms);
 cudaError_t launch_solve_fp32(const SolveParams& P, const float* tab, const double* tab64, const LaunchInfo& li,
                               cudaStream_t s);
 // scratch elements (of the form's type) per CTA slot
-size_t slot_elems(int nlay, int idelm);
+size_t slot_elems(int nlay, int idelm, bool fp32);
 
 // get_alpha (mcica_subcol_gen_sw.f90:66-178) on the device
 cudaError_t launch_get_alpha(int ncol, int nlay, int icld, int idcor, double decorr_con, const double* dz,
