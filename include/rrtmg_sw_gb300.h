@@ -99,7 +99,8 @@ enum {
     RRTMG_SW_EKISSSEED = 21,   /* mcica_subcol_gen_sw.f90:472-474  KISSVEC SEED GENERATOR REQUIRES
                                   PMID FROM BOTTOM FOUR LAYERS */
     RRTMG_SW_ELAYTROP = 30,    /* profile without layers on both sides of the ~100 hPa switch */
-    RRTMG_SW_EIRNG = 31        /* fused path requires irng = 0 */
+    RRTMG_SW_EIRNG = 31,       /* fused path requires irng = 0 */
+    RRTMG_SW_EPARTIAL = 32     /* rrtmg_sw_rad.nomcica.f90:619-621  PARTIAL CLOUD NOT ALLOWED */
 };
 
 /* rrtmg_sw_ini (rrtmg_sw_init.f90:47-173): load the 112-g-point tables
@@ -127,6 +128,18 @@ int rrtmg_sw_dev_c(const rrtmg_sw_args *a, void *stream);
  * are used, as mcica_subcol_sw copies them).  Host / device variants. */
 int rrtmg_sw_mcica_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c);
 int rrtmg_sw_mcica_dev_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, void *stream);
+
+/* rrtmg_sw without McICA (rrtmg_sw_rad.nomcica.f90:97-109): clouds are
+ * given per layer and band, their optics come from cldprop_sw
+ * (rrtmg_sw_cldprop.f90:53-374) and the solve is spcvrt_sw
+ * (rrtmg_sw_spcvrt.f90:53-667).  The cloud arguments cldfr, cicewp, cliqwp,
+ * reice, reliq (ncol,nlay) and taucld, ssacld, asmcld, fsfcld (nbnd,ncol,nlay)
+ * are c->cldfrac, c->ciwp, c->clwp, c->rei, c->rel and c->tauc .. c->fsfc;
+ * the McICA fields of `a` and c->permuteseed, irng, alpha are ignored.  A
+ * layer cloud fraction strictly between 1e-6 and 1 - 1e-6 returns
+ * RRTMG_SW_EPARTIAL, as the reference stops.  Host / device variants. */
+int rrtmg_sw_nomcica_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c);
+int rrtmg_sw_nomcica_dev_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, void *stream);
 
 /* Allocation-free device solve.  No counterpart in the reference: it exists
  * for callers that must not allocate device memory while they run -- a

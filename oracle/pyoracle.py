@@ -73,6 +73,7 @@ def lib():
         L = C.CDLL(LIB_PATH)
         L.orc_init.argtypes = [C.c_char_p, C.c_double]
         L.orc_rrtmg_sw.argtypes = [C.POINTER(RrtmgSwArgs)]
+        L.orc_rrtmg_sw_nomcica.argtypes = [C.POINTER(RrtmgSwArgs)] + [_dp] * 9
         L.orc_column_mode.argtypes = [C.POINTER(ColumnCase)]
         L.orc_get_alpha.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_int, _dp, _dp]
         L.orc_mcica_subcol_sw.argtypes = [C.c_int] * 5 + [_dp] * 11 + [_dp] * 9
@@ -151,11 +152,15 @@ AER_INPUTS = ("tauaer", "ssaaer", "asmaer", "ecaer")
 EXTRA_OUTPUTS = ("dirdflux", "difdflux", "uvdflx", "nidflx", "dirdnuv", "difdnuv", "dirdnir", "difdnir")
 
 
+NOMCICA_INPUTS = ("cldfr", "taucld", "ssacld", "asmcld", "fsfcld", "cicewp", "cliqwp", "reice", "reliq")
+
+
 def rrtmg_sw(ncol, nlay, icld, iaer, inp, adjes=1.0, dyofyr=0, scon=1360.85, isolvar=0,
              inflgsw=2, iceflgsw=3, liqflgsw=1, idelm=1, nthreads=0, extra=False,
-             bndsolvar=None, indsolvar=None, solcycfrac=None):
+             bndsolvar=None, indsolvar=None, solcycfrac=None, nomcica=False):
     """GCM entry point.  ``inp`` maps argument names to Fortran-ordered
-    (column-major) FP64 arrays flattened to 1-D."""
+    (column-major) FP64 arrays flattened to 1-D.  With ``nomcica=True`` the
+    non-McICA rrtmg_sw runs on the NOMCICA_INPUTS arrays of ``inp``."""
     keep = []
 
     def arr(x):
@@ -194,7 +199,11 @@ def rrtmg_sw(ncol, nlay, icld, iaer, inp, adjes=1.0, dyofyr=0, scon=1360.85, iso
     if solcycfrac is not None:
         a.solcycfrac = arr([solcycfrac])
     a.idelm, a.nthreads = idelm, nthreads
-    rc = lib().orc_rrtmg_sw(C.byref(a))
+    if nomcica:
+        ptrs = [arr(inp[k]) if inp.get(k) is not None else None for k in NOMCICA_INPUTS]
+        rc = lib().orc_rrtmg_sw_nomcica(C.byref(a), *ptrs)
+    else:
+        rc = lib().orc_rrtmg_sw(C.byref(a))
     if rc != 0:
         raise RuntimeError("orc_rrtmg_sw failed: %d" % rc)
     return out

@@ -724,6 +724,151 @@ int cldprmc(int nlay, int inflag, int iceflag, int liqflag, const double* cldfmc
     return ORC_OK;
 }
 
+// ---------------------------------------------------------------- cldprop
+// cldprop_sw (rrtmg_sw_cldprop.f90:53-374): cloud optics per (layer, band)
+// for the non-McICA path.  Inputs cldfrac/ciwp/clwp/rei/rel (nlay) and
+// tauc/ssac/asmc/fsfc (14, nlay) at [(ib-1) + 14*(lay-1)]; outputs
+// (nlay, 14) at [(lay-1) + nlay*(ib-1)].  The reference's stops return
+// their codes.
+int cldprop(int nlay, int inflag, int iceflag, int liqflag, const double* cldfrac, const double* tauc,
+            const double* ssac, const double* asmc, const double* fsfc, const double* ciwp, const double* clwp,
+            const double* rei, const double* rel, double* taucldorig, double* taucloud, double* ssacloud,
+            double* asmcloud) {
+    const double eps = 1.e-06, cldmin = 1.e-20;
+    auto at = [&](double* v, int lay, int ib) -> double& { return v[(lay - 1) + nlay * (ib - 1)]; };
+    auto bi = [&](const double* v, int ib, int lay) { return v[(ib - 1) + 14 * (lay - 1)]; };
+    std::vector<double> tauctot(nlay, 0.0);
+    for (int lay = 1; lay <= nlay; ++lay)  // :140-147
+        for (int ib = 1; ib <= NBND; ++ib) {
+            at(taucldorig, lay, ib) = bi(tauc, ib, lay);
+            at(taucloud, lay, ib) = 0.0;
+            at(ssacloud, lay, ib) = 1.0;
+            at(asmcloud, lay, ib) = 0.0;
+            tauctot[lay - 1] = tauctot[lay - 1] + bi(tauc, ib, lay);
+        }
+    for (int lay = 1; lay <= nlay; ++lay) {
+        const double cwp = ciwp[lay - 1] + clwp[lay - 1];
+        if (!(cldfrac[lay - 1] >= cldmin && (cwp >= cldmin || tauctot[lay - 1] >= cldmin))) continue;
+        if (inflag == 0) {  // :158-174
+            for (int ib = 1; ib <= NBND; ++ib) {
+                const double taucldorig_a = bi(tauc, ib, lay);
+                const double ffp = bi(fsfc, ib, lay);
+                const double ffp1 = 1.0 - ffp;
+                const double ffpssa = 1.0 - ffp * bi(ssac, ib, lay);
+                const double ssacloud_a = ffp1 * bi(ssac, ib, lay) / ffpssa;
+                const double taucloud_a = ffpssa * taucldorig_a;
+                at(taucldorig, lay, ib) = taucldorig_a;
+                at(ssacloud, lay, ib) = ssacloud_a;
+                at(taucloud, lay, ib) = taucloud_a;
+                at(asmcloud, lay, ib) = (bi(asmc, ib, lay) - ffp) / (ffp1);
+            }
+        } else if (inflag == 2) {  // :177-366
+            const double radice = rei[lay - 1];
+            double extcoice[NBND] = {0}, ssacoice[NBND] = {0}, gice[NBND] = {0}, forwice[NBND] = {0};
+            double extcoliq[NBND] = {0}, ssacoliq[NBND] = {0}, gliq[NBND] = {0}, forwliq[NBND] = {0};
+            if (ciwp[lay - 1] == 0.0) {
+            } else if (iceflag == 1) {
+                if (radice < 13.0 || radice > 130.0) return ORC_ERR_ICE_RADIUS;
+                for (int jb = 1; jb <= NBND; ++jb) {
+                    const double w2 = T.wavenum2[jb - 1];
+                    int icx = 0;
+                    if (w2 > 1.43e04) icx = 1;
+                    else if (w2 > 7.7e03) icx = 2;
+                    else if (w2 > 5.3e03) icx = 3;
+                    else if (w2 > 4.0e03) icx = 4;
+                    else if (w2 >= 2.5e03) icx = 5;
+                    extcoice[jb - 1] = T.abari[icx - 1] + T.bbari[icx - 1] / radice;
+                    ssacoice[jb - 1] = 1.0 - T.cbari[icx - 1] - T.dbari[icx - 1] * radice;
+                    gice[jb - 1] = T.ebari[icx - 1] + T.fbari[icx - 1] * radice;
+                    if (gice[jb - 1] >= 1.0) gice[jb - 1] = 1.0 - eps;
+                    forwice[jb - 1] = gice[jb - 1] * gice[jb - 1];
+                    if (extcoice[jb - 1] < 0.0 || ssacoice[jb - 1] > 1.0 || ssacoice[jb - 1] < 0.0 ||
+                        gice[jb - 1] > 1.0 || gice[jb - 1] < 0.0)
+                        return ORC_ERR_ICE_PROPS;
+                }
+            } else if (iceflag == 2) {
+                if (radice < 5.0 || radice > 131.0) return ORC_ERR_ICE_RADIUS;
+                const double factor = (radice - 2.0) / 3.0;
+                int index = (int)factor;
+                if (index == 43) index = 42;
+                const double fint = factor - (double)index;
+                for (int jb = 1; jb <= NBND; ++jb) {
+                    extcoice[jb - 1] = A(T.extice2, 43, index, jb) + fint * (A(T.extice2, 43, index + 1, jb) - A(T.extice2, 43, index, jb));
+                    ssacoice[jb - 1] = A(T.ssaice2, 43, index, jb) + fint * (A(T.ssaice2, 43, index + 1, jb) - A(T.ssaice2, 43, index, jb));
+                    gice[jb - 1] = A(T.asyice2, 43, index, jb) + fint * (A(T.asyice2, 43, index + 1, jb) - A(T.asyice2, 43, index, jb));
+                    forwice[jb - 1] = gice[jb - 1] * gice[jb - 1];
+                    if (extcoice[jb - 1] < 0.0 || ssacoice[jb - 1] > 1.0 || ssacoice[jb - 1] < 0.0 ||
+                        gice[jb - 1] > 1.0 || gice[jb - 1] < 0.0)
+                        return ORC_ERR_ICE_PROPS;
+                }
+            } else if (iceflag == 3) {
+                if (radice < 5.0 || radice > 140.0) return ORC_ERR_ICE_DGE;
+                const double factor = (radice - 2.0) / 3.0;
+                int index = (int)factor;
+                if (index == 46) index = 45;
+                const double fint = factor - (double)index;
+                for (int jb = 1; jb <= NBND; ++jb) {
+                    extcoice[jb - 1] = A(T.extice3, 46, index, jb) + fint * (A(T.extice3, 46, index + 1, jb) - A(T.extice3, 46, index, jb));
+                    ssacoice[jb - 1] = A(T.ssaice3, 46, index, jb) + fint * (A(T.ssaice3, 46, index + 1, jb) - A(T.ssaice3, 46, index, jb));
+                    gice[jb - 1] = A(T.asyice3, 46, index, jb) + fint * (A(T.asyice3, 46, index + 1, jb) - A(T.asyice3, 46, index, jb));
+                    const double fdelta = A(T.fdlice3, 46, index, jb) + fint * (A(T.fdlice3, 46, index + 1, jb) - A(T.fdlice3, 46, index, jb));
+                    if (fdelta < 0.0 || fdelta > 1.0) return ORC_ERR_ICE_PROPS;
+                    forwice[jb - 1] = fdelta + 0.5 / ssacoice[jb - 1];
+                    if (forwice[jb - 1] > gice[jb - 1]) forwice[jb - 1] = gice[jb - 1];
+                    if (extcoice[jb - 1] < 0.0 || ssacoice[jb - 1] > 1.0 || ssacoice[jb - 1] < 0.0 ||
+                        gice[jb - 1] > 1.0 || gice[jb - 1] < 0.0)
+                        return ORC_ERR_ICE_PROPS;
+                }
+            }
+            if (clwp[lay - 1] == 0.0) {
+            } else if (liqflag == 1) {
+                const double radliq = rel[lay - 1];
+                if (radliq < 2.5 || radliq > 60.0) return ORC_ERR_LIQ_RADIUS;
+                int index = (int)(radliq - 1.5);
+                if (index == 0) index = 1;
+                if (index == 58) index = 57;
+                const double fint = radliq - 1.5 - (double)index;
+                for (int jb = 1; jb <= NBND; ++jb) {
+                    extcoliq[jb - 1] = A(T.extliq1, 58, index, jb) + fint * (A(T.extliq1, 58, index + 1, jb) - A(T.extliq1, 58, index, jb));
+                    ssacoliq[jb - 1] = A(T.ssaliq1, 58, index, jb) + fint * (A(T.ssaliq1, 58, index + 1, jb) - A(T.ssaliq1, 58, index, jb));
+                    if (fint < 0.0 && ssacoliq[jb - 1] > 1.0) ssacoliq[jb - 1] = A(T.ssaliq1, 58, index, jb);
+                    gliq[jb - 1] = A(T.asyliq1, 58, index, jb) + fint * (A(T.asyliq1, 58, index + 1, jb) - A(T.asyliq1, 58, index, jb));
+                    forwliq[jb - 1] = gliq[jb - 1] * gliq[jb - 1];
+                    if (extcoliq[jb - 1] < 0.0 || ssacoliq[jb - 1] > 1.0 || ssacoliq[jb - 1] < 0.0 ||
+                        gliq[jb - 1] > 1.0 || gliq[jb - 1] < 0.0)
+                        return ORC_ERR_LIQ_PROPS;
+                }
+            }
+            for (int ib = 1; ib <= NBND; ++ib) {
+                const int j = ib - 1;
+                const double tauliqorig = clwp[lay - 1] * extcoliq[j];
+                const double tauiceorig = ciwp[lay - 1] * extcoice[j];
+                at(taucldorig, lay, ib) = tauliqorig + tauiceorig;
+                const double ssaliq = ssacoliq[j] * (1.0 - forwliq[j]) / (1.0 - forwliq[j] * ssacoliq[j]);
+                const double tauliq = (1.0 - forwliq[j] * ssacoliq[j]) * tauliqorig;
+                const double ssaice = ssacoice[j] * (1.0 - forwice[j]) / (1.0 - forwice[j] * ssacoice[j]);
+                const double tauice = (1.0 - forwice[j] * ssacoice[j]) * tauiceorig;
+                const double scatliq = ssaliq * tauliq;
+                double scatice = ssaice * tauice;
+                at(taucloud, lay, ib) = tauliq + tauice;
+                if (at(taucloud, lay, ib) == 0.0) at(taucloud, lay, ib) = cldmin;
+                if (scatice == 0.0) scatice = cldmin;
+                at(ssacloud, lay, ib) = (scatliq + scatice) / at(taucloud, lay, ib);
+                if (iceflag == 3) {
+                    at(asmcloud, lay, ib) = (1.0 / (scatliq + scatice)) *
+                                            (scatliq * (gliq[j] - forwliq[j]) / (1.0 - forwliq[j]) +
+                                             scatice * ((gice[j] - forwice[j]) / (1.0 - forwice[j])));
+                } else {
+                    at(asmcloud, lay, ib) = (scatliq * (gliq[j] - forwliq[j]) / (1.0 - forwliq[j]) +
+                                             scatice * (gice[j] - forwice[j]) / (1.0 - forwice[j])) /
+                                            (scatliq + scatice);
+                }
+            }
+        }
+    }
+    return ORC_OK;
+}
+
 // ---------------------------------------------------------------- reftra
 // exp(-x) through the lookup table, or the quadratic below od_lo
 // (rrtmg_sw_reftra.f90:203-209)
@@ -861,6 +1006,27 @@ struct ColumnOptics {
     // (lay, band 1..14) -> [(lay-1) + nlay*(ib-1)]
     std::vector<double> taua, asya, omga;
 };
+
+// spcvrt_sw (rrtmg_sw_spcvrt.f90:53-667) differs from spcvmc_sw only in
+// reading the cloud fraction per layer (pclfr, :429,453-454,547-548) and the
+// cloud optics per (layer, band) (ptauc .. ptaucorig indexed by the band of
+// the g-point, :473,503-515).  The oracle therefore runs spcvmc with the
+// band values spread over their g-points and the layer fraction over all
+// g-points.
+void spread_bands(int nlay, const double* cldfrac, const double* taucloud, const double* taucldorig,
+                  const double* ssacloud, const double* asmcloud, ColumnOptics& O) {
+    for (int l = 1; l <= nlay; ++l)
+        for (int ig = 1; ig <= NGPT; ++ig) {
+            const int ib = T.ngb[ig - 1] - 15;
+            const size_t d = (l - 1) + (size_t)nlay * (ig - 1);
+            const size_t s = (l - 1) + (size_t)nlay * (ib - 1);
+            O.cldfmc[d] = cldfrac[l - 1];
+            O.taucmc[d] = taucloud[s];
+            O.taormc[d] = taucldorig[s];
+            O.asycmc[d] = asmcloud[s];
+            O.omgcmc[d] = ssacloud[s];
+        }
+}
 
 // spcvmc_sw (rrtmg_sw_spcvmc.f90:53-663); icpr = 1 (cloud properties from
 // cldprmc, already delta-scaled)
@@ -1316,7 +1482,13 @@ static void solar_setup(const orc_rrtmg_sw_args* a, Solar& S, double* adjflux) {
     for (int i = 0; i < NBND; ++i) adjflux[i] = isolvar < 0 ? adjflx * solvar[i] : adjflx;
 }
 
-int orc_rrtmg_sw(const orc_rrtmg_sw_args* a) {
+struct NomcicaClouds {
+    const double *cldfr, *taucld, *ssacld, *asmcld, *fsfcld, *cicewp, *cliqwp, *reice, *reliq;
+};
+
+// rrtmg_sw (rrtmg_sw_rad.f90:561-841) and, with nm, its non-McICA twin
+// (rrtmg_sw_rad.nomcica.f90:531-815).
+static int rrtmg_sw_impl(const orc_rrtmg_sw_args* a, const NomcicaClouds* nm) {
     if (!T.ok) return ORC_ERR_NOT_INITIALIZED;
     const int ncol = a->ncol, nlay = a->nlay;
     if (ncol <= 0 || nlay <= 1) return ORC_ERR_ARGS;
@@ -1362,7 +1534,43 @@ int orc_rrtmg_sw(const orc_rrtmg_sw_args* a) {
         O.asycmc.assign(nlg, 0.0); O.omgcmc.assign(nlg, 1.0);
         O.taua.assign((size_t)nlay * NBND, 0.0); O.asya.assign((size_t)nlay * NBND, 0.0);
         O.omga.assign((size_t)nlay * NBND, 1.0);
-        if (icld >= 1) {
+        if (icld >= 1 && nm) {
+            // clouds per layer and band, cldprop_sw, no partial cloud
+            // (rrtmg_sw_rad.nomcica.f90:617-625, inatm :1588-1597)
+            std::vector<double> cf(nlay), ci(nlay), cw(nlay), ri(nlay), rl(nlay), tc(14 * nlay), sc(14 * nlay),
+                ac(14 * nlay), fc(14 * nlay);
+            for (int l = 1; l <= nlay; ++l) {
+                const size_t k = iplon + (size_t)ncol * (l - 1);
+                cf[l - 1] = nm->cldfr[k];
+                ci[l - 1] = nm->cicewp[k];
+                cw[l - 1] = nm->cliqwp[k];
+                ri[l - 1] = nm->reice[k];
+                rl[l - 1] = nm->reliq[k];
+                for (int b = 0; b < 14; ++b) {
+                    const size_t kb = b + 14 * k;
+                    tc[b + 14 * (l - 1)] = nm->taucld ? nm->taucld[kb] : 0.0;
+                    sc[b + 14 * (l - 1)] = nm->ssacld ? nm->ssacld[kb] : 1.0;
+                    ac[b + 14 * (l - 1)] = nm->asmcld ? nm->asmcld[kb] : 0.0;
+                    fc[b + 14 * (l - 1)] = nm->fsfcld ? nm->fsfcld[kb] : 0.0;
+                }
+            }
+            const double zepsec = 1.e-06, oneminus = 1.0 - zepsec;
+            bool partial = false;
+            for (int i = 0; i < nlay; ++i)
+                if (cf[i] > zepsec && cf[i] < oneminus) partial = true;
+            std::vector<double> tco((size_t)nlay * 14), tcl((size_t)nlay * 14), scl((size_t)nlay * 14),
+                acl((size_t)nlay * 14);
+            const int e = partial ? ORC_ERR_PARTIAL
+                                  : cldprop(nlay, a->inflgsw, a->iceflgsw, a->liqflgsw, cf.data(), tc.data(), sc.data(),
+                                            ac.data(), fc.data(), ci.data(), cw.data(), ri.data(), rl.data(), tco.data(),
+                                            tcl.data(), scl.data(), acl.data());
+            if (e != ORC_OK) {
+#pragma omp critical
+                err = e;
+                continue;
+            }
+            spread_bands(nlay, cf.data(), tcl.data(), tco.data(), scl.data(), acl.data(), O);
+        } else if (icld >= 1) {
             // cloud arrays (ig, lay) of the McICA inputs, then cldprmc_sw
             std::vector<double> cldf(nlg), tauc(nlg), ssac(nlg), asmc(nlg), fsfc(nlg), ciwp(nlg), clwp(nlg), taor(nlg);
             std::vector<double> rei(nlay), rel(nlay);
@@ -1475,6 +1683,16 @@ int orc_rrtmg_sw(const orc_rrtmg_sw_args* a) {
         a->swhr[iplon + (size_t)ncol * (nlay - 1)] = 0.0;
     }
     return err;
+}
+
+int orc_rrtmg_sw(const orc_rrtmg_sw_args* a) { return rrtmg_sw_impl(a, nullptr); }
+
+int orc_rrtmg_sw_nomcica(const orc_rrtmg_sw_args* a, const double* cldfr, const double* taucld, const double* ssacld,
+                         const double* asmcld, const double* fsfcld, const double* cicewp, const double* cliqwp,
+                         const double* reice, const double* reliq) {
+    const NomcicaClouds nm{cldfr, taucld, ssacld, asmcld, fsfcld, cicewp, cliqwp, reice, reliq};
+    if (a->icld != 0 && (!cldfr || !cicewp || !cliqwp || !reice || !reliq)) return ORC_ERR_ARGS;
+    return rrtmg_sw_impl(a, &nm);
 }
 
 int orc_get_alpha(int ncol, int nlay, int icld, int idcor, double decorr_con, const double* dz,
@@ -1636,7 +1854,9 @@ int orc_column_mode(const orc_column_case* cc) {
     for (int i = 0; i < NBND; ++i) {
         S.svar_f_bnd[i] = cc->svar_f_bnd[i]; S.svar_s_bnd[i] = cc->svar_s_bnd[i]; S.svar_i_bnd[i] = cc->svar_i_bnd[i];
     }
-    if (cc->imca == 0 && cc->icld >= 1) return ORC_ERR_ARGS;  // cldprop_sw/spcvrt_sw path
+    if (cc->imca == 0 && cc->icld >= 1)  // rrtmg_sw.1col.f90:612-617
+        for (int i = 0; i < nlay; ++i)
+            if (cc->cldfrac[i] != 0.0 && cc->cldfrac[i] != 1.0) return ORC_ERR_PARTIAL;
     const int nmca = cc->imca == 1 ? cc->nmca : 1;
     std::vector<double> usum(nlay + 1, 0.0), dsum(nlay + 1, 0.0), dirsum(nlay + 1, 0.0), difsum(nlay + 1, 0.0),
         fnsum(nlay + 1, 0.0), hsum(nlay + 1, 0.0);
@@ -1679,6 +1899,24 @@ int orc_column_mode(const orc_column_case* cc) {
                     O.cldfmc[d] = cldf[s]; O.taucmc[d] = tauc[s]; O.taormc[d] = taor[s];
                     O.asycmc[d] = asmc[s]; O.omgcmc[d] = ssac[s];
                 }
+        }
+        if (cc->imca == 0 && cc->icld >= 1) {
+            // cldprop_sw, then the cloudy layers' band optics (1col:618-620, 669-679)
+            std::vector<double> tco((size_t)nlay * 14), tcl((size_t)nlay * 14), scl((size_t)nlay * 14),
+                acl((size_t)nlay * 14);
+            std::vector<double> z14(14 * nlay, 0.0), o14(14 * nlay, 1.0);
+            const int e = cldprop(nlay, cc->inflag, cc->iceflag, cc->liqflag, cc->cldfrac, cc->tauc ? cc->tauc : z14.data(),
+                                  cc->ssac ? cc->ssac : o14.data(), cc->asmc ? cc->asmc : z14.data(),
+                                  cc->fsfc ? cc->fsfc : z14.data(), cc->ciwp, cc->clwp, cc->rei, cc->rel, tco.data(),
+                                  tcl.data(), scl.data(), acl.data());
+            if (e) return e;
+            for (int i = 1; i <= nlay; ++i)
+                if (!(cc->cldfrac[i - 1] >= 1.e-06))
+                    for (int ib = 1; ib <= NBND; ++ib) {
+                        const size_t s = (i - 1) + (size_t)nlay * (ib - 1);
+                        tcl[s] = 0.0; tco[s] = 0.0; acl[s] = 0.0; scl[s] = 1.0;
+                    }
+            spread_bands(nlay, cc->cldfrac, tcl.data(), tco.data(), scl.data(), acl.data(), O);
         }
         if (cc->iaer == 10) {
             for (int i = 1; i <= nlay; ++i)

@@ -66,7 +66,8 @@ enum {
     ORC_ERR_LIQ_PROPS = 15,        /* cldprmc:290-294  liquid extinction/ssa/asym limits */
     ORC_ERR_ICLD = 20,             /* mcica:262-264  INVALID ICLD */
     ORC_ERR_KISS_SEED = 21,        /* mcica:472-474  KISSVEC SEED GENERATOR REQUIRES PMID FROM BOTTOM FOUR LAYERS */
-    ORC_ERR_LAYTROP = 30           /* profile with no layer above or below the 100 hPa switch */
+    ORC_ERR_LAYTROP = 30,          /* profile with no layer above or below the 100 hPa switch */
+    ORC_ERR_PARTIAL = 32           /* rad.nomcica:619-621 / 1col:612-617  PARTIAL CLOUD NOT ALLOWED */
 };
 
 /* rrtmg_sw_ini (rrtmg_sw_init.f90:47-173): load the reduced tables written
@@ -75,6 +76,15 @@ int orc_init(const char *table_path, double cpdair);
 
 /* rrtmg_sw (rrtmg_sw_rad.f90:99-841). */
 int orc_rrtmg_sw(const orc_rrtmg_sw_args *a);
+
+/* rrtmg_sw without McICA (rrtmg_sw_rad.nomcica.f90:97-841): cloud fraction
+ * cldfr, ice/liquid paths cicewp/cliqwp and sizes reice/reliq (ncol,nlay),
+ * and taucld/ssacld/asmcld/fsfcld (14,ncol,nlay); the McICA fields of `a`
+ * are ignored.  Cloud optics from cldprop_sw, solve by spcvrt_sw. */
+int orc_rrtmg_sw_nomcica(const orc_rrtmg_sw_args *a, const double *cldfr, const double *taucld,
+                         const double *ssacld, const double *asmcld, const double *fsfcld,
+                         const double *cicewp, const double *cliqwp, const double *reice,
+                         const double *reliq);
 
 /* get_alpha (mcica_subcol_gen_sw.f90:66-178). */
 int orc_get_alpha(int ncol, int nlay, int icld, int idcor, double decorr_con,

@@ -227,35 +227,34 @@ int build_tables(State& st) {
         r.mtab = mtab;
         r.rtab = rtab;
     };
-    const BandOff* bb = T.b - 16;
-    reg(16, 0, 1, H2O, CH4, 252.131f, 1.f, 1, -1, 0, 0, bb[16].rayl);
-    reg(16, 1, 2, CH4, 0, 0.f, 1.f, 0, -1, 0, 0, bb[16].rayl);
-    reg(17, 0, 1, H2O, CO2, 0.364641f, 1.f, 1, -1, 0, 0, bb[17].rayl);
-    reg(17, 1, 1, H2O, CO2, 0.364641f, 1.f, 2, -1, 0, 0, bb[17].rayl);
-    reg(18, 0, 1, H2O, CH4, 38.9589f, 1.f, 1, -1, 0, 0, bb[18].rayl);
-    reg(18, 1, 2, CH4, 0, 0.f, 1.f, 0, -1, 0, 0, bb[18].rayl);
-    reg(19, 0, 1, H2O, CO2, 5.49281f, 1.f, 1, -1, 0, 0, bb[19].rayl);
-    reg(19, 1, 2, CO2, 0, 0.f, 1.f, 0, -1, 0, 0, bb[19].rayl);
-    reg(20, 0, 2, H2O, 0, 0.f, 1.f, 1, CH4, bb[20].absch4, 0, bb[20].rayl);
-    reg(20, 1, 2, H2O, 0, 0.f, 1.f, 2, CH4, bb[20].absch4, 0, bb[20].rayl);
-    reg(21, 0, 1, H2O, CO2, 0.0045321f, 1.f, 1, -1, 0, 0, bb[21].rayl);
-    reg(21, 1, 1, H2O, CO2, 0.0045321f, 1.f, 2, -1, 0, 0, bb[21].rayl);
-    reg(22, 0, 1, H2O, O2, (float)(1.6 * 0.022708), 1.f, 1, O2CONT, 0, 0, bb[22].rayl);
-    reg(22, 1, 2, O2, 0, 0.f, 1.6f, 0, O2CONT, 0, 0, bb[22].rayl);
-    reg(23, 0, 2, H2O, 0, 0.f, 1.029f, 1, -1, 0, 1, bb[23].rayl);
-    reg(23, 1, 0, 0, 0, 0.f, 1.f, 0, -1, 0, 1, bb[23].rayl);
-    reg(24, 0, 1, H2O, O2, 0.124692f, 1.f, 1, O3, bb[24].abso3a, 2, bb[24].rayla);
-    reg(24, 1, 2, O2, 0, 0.f, 1.f, 0, O3, bb[24].abso3b, 1, bb[24].raylb);
-    reg(25, 0, 2, H2O, 0, 0.f, 1.f, 0, O3, bb[25].abso3a, 1, bb[25].rayl);
-    reg(25, 1, 0, 0, 0, 0.f, 1.f, 0, O3, bb[25].abso3b, 1, bb[25].rayl);
-    reg(26, 0, 0, 0, 0, 0.f, 1.f, 0, -1, 0, 1, bb[26].rayl);
-    reg(26, 1, 0, 0, 0, 0.f, 1.f, 0, -1, 0, 1, bb[26].rayl);
-    reg(27, 0, 2, O3, 0, 0.f, 1.f, 0, -1, 0, 1, bb[27].rayl);
-    reg(27, 1, 2, O3, 0, 0.f, 1.f, 0, -1, 0, 1, bb[27].rayl);
-    reg(28, 0, 1, O3, O2, 6.67029e-07f, 1.f, 0, -1, 0, 0, bb[28].rayl);
-    reg(28, 1, 1, O3, O2, 6.67029e-07f, 1.f, 0, -1, 0, 0, bb[28].rayl);
-    reg(29, 0, 2, H2O, 0, 0.f, 1.f, 1, CO2, bb[29].absco2, 0, bb[29].rayl);
-    reg(29, 1, 2, CO2, 0, 0.f, 1.f, 0, H2O, bb[29].absh2o, 0, bb[29].rayl);
+    reg(16, 0, 1, H2O, CH4, 252.131f, 1.f, 1, -1, 0, 0, T.b[16 - 16].rayl);
+    reg(16, 1, 2, CH4, 0, 0.f, 1.f, 0, -1, 0, 0, T.b[16 - 16].rayl);
+    reg(17, 0, 1, H2O, CO2, 0.364641f, 1.f, 1, -1, 0, 0, T.b[17 - 16].rayl);
+    reg(17, 1, 1, H2O, CO2, 0.364641f, 1.f, 2, -1, 0, 0, T.b[17 - 16].rayl);
+    reg(18, 0, 1, H2O, CH4, 38.9589f, 1.f, 1, -1, 0, 0, T.b[18 - 16].rayl);
+    reg(18, 1, 2, CH4, 0, 0.f, 1.f, 0, -1, 0, 0, T.b[18 - 16].rayl);
+    reg(19, 0, 1, H2O, CO2, 5.49281f, 1.f, 1, -1, 0, 0, T.b[19 - 16].rayl);
+    reg(19, 1, 2, CO2, 0, 0.f, 1.f, 0, -1, 0, 0, T.b[19 - 16].rayl);
+    reg(20, 0, 2, H2O, 0, 0.f, 1.f, 1, CH4, T.b[20 - 16].absch4, 0, T.b[20 - 16].rayl);
+    reg(20, 1, 2, H2O, 0, 0.f, 1.f, 2, CH4, T.b[20 - 16].absch4, 0, T.b[20 - 16].rayl);
+    reg(21, 0, 1, H2O, CO2, 0.0045321f, 1.f, 1, -1, 0, 0, T.b[21 - 16].rayl);
+    reg(21, 1, 1, H2O, CO2, 0.0045321f, 1.f, 2, -1, 0, 0, T.b[21 - 16].rayl);
+    reg(22, 0, 1, H2O, O2, (float)(1.6 * 0.022708), 1.f, 1, O2CONT, 0, 0, T.b[22 - 16].rayl);
+    reg(22, 1, 2, O2, 0, 0.f, 1.6f, 0, O2CONT, 0, 0, T.b[22 - 16].rayl);
+    reg(23, 0, 2, H2O, 0, 0.f, 1.029f, 1, -1, 0, 1, T.b[23 - 16].rayl);
+    reg(23, 1, 0, 0, 0, 0.f, 1.f, 0, -1, 0, 1, T.b[23 - 16].rayl);
+    reg(24, 0, 1, H2O, O2, 0.124692f, 1.f, 1, O3, T.b[24 - 16].abso3a, 2, T.b[24 - 16].rayla);
+    reg(24, 1, 2, O2, 0, 0.f, 1.f, 0, O3, T.b[24 - 16].abso3b, 1, T.b[24 - 16].raylb);
+    reg(25, 0, 2, H2O, 0, 0.f, 1.f, 0, O3, T.b[25 - 16].abso3a, 1, T.b[25 - 16].rayl);
+    reg(25, 1, 0, 0, 0, 0.f, 1.f, 0, O3, T.b[25 - 16].abso3b, 1, T.b[25 - 16].rayl);
+    reg(26, 0, 0, 0, 0, 0.f, 1.f, 0, -1, 0, 1, T.b[26 - 16].rayl);
+    reg(26, 1, 0, 0, 0, 0.f, 1.f, 0, -1, 0, 1, T.b[26 - 16].rayl);
+    reg(27, 0, 2, O3, 0, 0.f, 1.f, 0, -1, 0, 1, T.b[27 - 16].rayl);
+    reg(27, 1, 2, O3, 0, 0.f, 1.f, 0, -1, 0, 1, T.b[27 - 16].rayl);
+    reg(28, 0, 1, O3, O2, 6.67029e-07f, 1.f, 0, -1, 0, 0, T.b[28 - 16].rayl);
+    reg(28, 1, 1, O3, O2, 6.67029e-07f, 1.f, 0, -1, 0, 0, T.b[28 - 16].rayl);
+    reg(29, 0, 2, H2O, 0, 0.f, 1.f, 1, CO2, T.b[29 - 16].absco2, 0, T.b[29 - 16].rayl);
+    reg(29, 1, 2, CO2, 0, 0.f, 1.f, 0, H2O, T.b[29 - 16].absh2o, 0, T.b[29 - 16].rayl);
     T.total = (int)B.size();
     T.oneminus = 1.0 - 1.e-06;  // rrtmg_sw_rad.f90:563-565
     T.bpade_f = (float)T.bpade;
@@ -408,7 +407,7 @@ int check_args(const rrtmg_sw_args* a) {
 }
 
 // Fill SolveParams from args whose pointers are device pointers.
-int make_params(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, SolveParams& P) {
+int make_params(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, SolveParams& P, bool nomcica = false) {
     std::memset(&P, 0, sizeof(P));
     P.ncol = a->ncol;
     P.nlay = a->nlay;
@@ -418,7 +417,8 @@ int make_params(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, Sol
     P.inflag = a->inflgsw;
     P.iceflag = a->iceflgsw;
     P.liqflag = a->liqflgsw;
-    P.fused = c ? 1 : 0;
+    P.fused = (c && !nomcica) ? 1 : 0;
+    P.nomcica = nomcica ? 1 : 0;
     P.extra = (a->dirdflux || a->difdflux || a->uvdflx || a->nidflx || a->dirdnuv || a->difdnuv || a->dirdnir ||
                a->difdnir) ? 1 : 0;
     P.npairs = (a->ncol + COLS_PER_CTA - 1) / COLS_PER_CTA;
@@ -434,7 +434,14 @@ int make_params(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, Sol
             !P.reicmcl || !P.relqmcl)
             return RRTMG_SW_EARGS;
     }
-    if (c && P.icld >= 1) {
+    if (nomcica && P.icld >= 1) {
+        // rrtmg_sw_rad.nomcica.f90:98-111 cloud arguments (cldfr, taucld .. reliq)
+        P.cldfrac = c->cldfrac; P.ciwp = c->ciwp; P.clwp = c->clwp; P.rei = c->rei; P.rel = c->rel;
+        P.tauc = c->tauc; P.ssac = c->ssac; P.asmc = c->asmc; P.fsfc = c->fsfc;
+        if (!P.cldfrac || !P.ciwp || !P.clwp || !P.rei || !P.rel) return RRTMG_SW_EARGS;
+        if (P.inflag == 0 && (!P.tauc || !P.ssac || !P.asmc || !P.fsfc)) return RRTMG_SW_EARGS;
+    }
+    if (c && !nomcica && P.icld >= 1) {
         if (c->irng != 0) return RRTMG_SW_EIRNG;
         P.permuteseed = c->permuteseed;
         P.cldfrac = c->cldfrac; P.ciwp = c->ciwp; P.clwp = c->clwp; P.rei = c->rei; P.rel = c->rel;
@@ -459,9 +466,9 @@ int make_params(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, Sol
 }
 
 // Queue one solve on `s`; returns after reading back the device error word.
-int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s) {
+int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s, bool nomcica = false) {
     SolveParams P;
-    int rc = make_params(st, a, c, P);
+    int rc = make_params(st, a, c, P, nomcica);
     if (rc) return rc;
     CK(st.errw.ensure(sizeof(int)));
     P.err = (int*)st.errw.p;
@@ -504,7 +511,7 @@ struct Stager {
     }
 };
 
-int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c) {
+int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, bool nomcica = false) {
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
     if (!st.init) return RRTMG_SW_ENOTINIT;
@@ -554,7 +561,7 @@ int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c) {
     d.dirdflux = xd[0]; d.difdflux = xd[1]; d.uvdflx = xd[2]; d.nidflx = xd[3];
     d.dirdnuv = xd[4]; d.difdnuv = xd[5]; d.dirdnir = xd[6]; d.difdnir = xd[7];
     if (sg.err != cudaSuccess) return cuda_fail(sg.err);
-    rc = solve_dev(st, &d, c ? &dc : nullptr, s);
+    rc = solve_dev(st, &d, c ? &dc : nullptr, s, nomcica);
     if (rc) return rc;
     sg.back(a->swuflx, d.swuflx, CL1); sg.back(a->swdflx, d.swdflx, CL1);
     sg.back(a->swuflxc, d.swuflxc, CL1); sg.back(a->swdflxc, d.swdflxc, CL1);
@@ -669,6 +676,21 @@ int rrtmg_sw_dev_c(const rrtmg_sw_args* a, void* stream) {
     const int rc = check_args(a);
     if (rc) return rc;
     return solve_dev(st, a, nullptr, (cudaStream_t)stream);
+}
+
+int rrtmg_sw_nomcica_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c) {
+    if (!c) return RRTMG_SW_EARGS;
+    return solve_host(a, c, true);
+}
+
+int rrtmg_sw_nomcica_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, void* stream) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (!c) return RRTMG_SW_EARGS;
+    const int rc = check_args(a);
+    if (rc) return rc;
+    return solve_dev(st, a, c, (cudaStream_t)stream, true);
 }
 
 int rrtmg_sw_mcica_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, void* stream) {
@@ -801,6 +823,7 @@ const char* rrtmg_sw_errstr_c(int32_t code) {
     case RRTMG_SW_EKISSSEED: return "MCICA_SUBCOL: KISSVEC SEED GENERATOR REQUIRES PMID FROM BOTTOM FOUR LAYERS.";
     case RRTMG_SW_ELAYTROP: return "PROFILE MUST HAVE LAYERS ON BOTH SIDES OF THE 100 HPA SWITCH";
     case RRTMG_SW_EIRNG: return "FUSED MCICA REQUIRES IRNG = 0";
+    case RRTMG_SW_EPARTIAL: return "PARTIAL CLOUD NOT ALLOWED";
     default: return "UNKNOWN ERROR";
     }
 }

@@ -70,7 +70,7 @@ __device__ inline void set_error(int* err, int code) {
 // Error codes (mirror include/rrtmg_sw_gb300.h)
 enum {
     E_OK = 0, E_INFLAG1 = 10, E_ICERAD = 11, E_ICEDGE = 12, E_ICEPROP = 13,
-    E_LIQRAD = 14, E_LIQPROP = 15, E_ICLD = 20, E_KISSSEED = 21, E_LAYTROP = 30
+    E_LIQRAD = 14, E_LIQPROP = 15, E_ICLD = 20, E_KISSSEED = 21, E_LAYTROP = 30, E_PARTIAL = 32
 };
 
 }  // namespace rrsw

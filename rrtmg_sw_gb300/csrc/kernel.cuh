@@ -226,6 +226,39 @@ __device__ inline void cloud_in(const SolveParams& P, int col, int g, int lay, i
     const size_t n = (size_t)P.ncol;
     const int L = P.nlay;
     R cldf = R(0), tc = R(0), oc = R(1), gc = R(0), fsfc = R(0), ciwp = R(0), clwp = R(0), rei = R(0), rel = R(0);
+    if (P.icld >= 1 && P.nomcica) {
+        // cldprop_sw (rrtmg_sw_cldprop.f90:140-370) for band ib, mixed by the
+        // layer's cloud fraction in spcvrt_sw (rrtmg_sw_spcvrt.f90:429,453-454)
+        const size_t kl = (size_t)col + n * (size_t)(lay - 1);
+        const double cf = P.cldfrac[kl];
+        ciwp = cld ? cld[0 * L + lay - 1] : (R)P.ciwp[kl];
+        clwp = cld ? cld[1 * L + lay - 1] : (R)P.clwp[kl];
+        rei = cld ? cld[2 * L + lay - 1] : (R)P.rei[kl];
+        rel = cld ? cld[3 * L + lay - 1] : (R)P.rel[kl];
+        R tin = R(0), tauctot = R(0);
+        if (P.tauc) {
+            const size_t kb = (size_t)ib + 14 * kl;
+            tin = (R)P.tauc[kb];
+            oc = (R)P.ssac[kb];
+            gc = (R)P.asmc[kb];
+            fsfc = (R)P.fsfc[kb];
+            for (int b = 0; b < NBND; ++b) tauctot += (R)P.tauc[(size_t)b + 14 * kl];
+        }
+        cldf = (R)cf;
+        const bool on = cf >= 1.e-20 && ((double)ciwp + (double)clwp >= 1.e-20 || (double)tauctot >= 1.e-20) &&
+                        (P.inflag == 0 || P.inflag == 2);
+        R taor = tin, coc = R(0);
+        if (on) {
+            tc = tin;
+            cldprmc_g<R>(ib, P.inflag, P.iceflag, P.liqflag, cldf, ciwp, clwp, rei, rel, fsfc, tc, oc, gc, taor, coc,
+                         tab, P.err, tauctot);
+        } else {
+            tc = R(0); oc = R(1); gc = R(0);
+        }
+        ci.cloudy = cf != 0.0;
+        ci.cldf = cldf; ci.tc = tc; ci.oc = oc; ci.gc = gc; ci.coc = coc; ci.taor = taor;
+        return;
+    }
     if (P.icld >= 1) {
         const size_t kl = (size_t)col + n * (size_t)(lay - 1);
         if (fused) {
@@ -489,6 +522,10 @@ __host__ __device__ inline Smem smem_layout(int L, int nq, bool fused, bool aer_
     return m;
 }
 
+// Whether the CTA stages per-layer cloud inputs (fused McICA or the
+// non-McICA path); the host sizes shared memory with the same test.
+__host__ __device__ inline bool stages_clouds(const SolveParams& P) { return (P.fused || P.nomcica) && P.icld >= 1; }
+
 template <typename R>
 __host__ __device__ inline bool stage_aerosol(int iaer) {
     // the FP32 form converts the FP64 aerosol inputs once per (column, layer, band)
@@ -503,8 +540,9 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
     const int NQ = num_q<R>(P.extra != 0);
     constexpr int QX = 6 + num_abs<R>();  // first extra-output sum
     const bool fused = P.fused && P.icld >= 1;
+    const bool nomc = P.nomcica && P.icld >= 1;
     const bool aer_stage = stage_aerosol<R>(P.iaer);
-    const Smem M = smem_layout(L, NQ, fused, aer_stage, sizeof(R));
+    const Smem M = smem_layout(L, NQ, stages_clouds(P), aer_stage, sizeof(R));
     double* sPdp = (double*)(smem_raw + M.pdp);        // [2][L]
     R* sCoef = (R*)(smem_raw + M.coef);                // [2][NFR][L]
     float* sHrf = (float*)(smem_raw + M.hrf);          // [2][L] FP32 form: heatfac / dp
@@ -575,6 +613,16 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
                         sd[0] = sd[1] = sd[2] = sd[3] = 1u;
                     }
                 }
+            }
+            if (nomc) {
+                // spcvrt_sw takes clear or overcast layers only (rrtmg_sw_rad.nomcica.f90:617-621)
+                const double cf = real ? P.cldfrac[kl] : 0.0;
+                if (cf > 1.e-6 && cf < 1.0 - 1.e-6) set_error(P.err, E_PARTIAL);
+                R* cd = sCld + c2 * 4 * L;
+                cd[0 * L + lay - 1] = real ? (R)P.ciwp[kl] : R(0);
+                cd[1 * L + lay - 1] = real ? (R)P.clwp[kl] : R(0);
+                cd[2 * L + lay - 1] = real ? (R)P.rei[kl] : R(0);
+                cd[3 * L + lay - 1] = real ? (R)P.rel[kl] : R(0);
             }
             if (aer_stage) {
                 for (int b = 0; b < NBND; ++b) {

@@ -27,6 +27,7 @@ namespace rrsw {
 struct SolveParams {
     int ncol, nlay, icld, iaer, idelm, isolvar, inflag, iceflag, liqflag;
     int fused;       // 1: McICA masks generated in the kernel (KISS)
+    int nomcica;     // 1: non-McICA path (cldprop_sw + spcvrt_sw): layer cloud fraction, band optics
     int extra;       // 1: also the 8 direct/diffuse/UV/NIR outputs
     int permuteseed;
     int npairs;
@@ -473,13 +474,15 @@ template <typename R>
 __device__ inline void cldprmc_g(int ib, int inflag, int iceflag, int liqflag, R cldf, R ciwp,
                                  R clwp, R rei, R rel, R fsfc, R& tauc,
                                  R& ssac, R& asmc, R& taor, R& co, const R* __restrict__ tab,
-                                 int* err) {
+                                 int* err, R ttest = R(-1)) {
     typedef R double_;
     const R eps = R((1.e-06)), cldmin = R((1.e-20));
     taor = tauc;
     co = R(1) - ssac;  // co-albedo (used by the FP32 form only)
     const double_ cwp = ciwp + clwp;
-    if (!(cldf >= cldmin && (cwp >= cldmin || tauc >= cldmin))) return;
+    // cldprmc tests the subcolumn's own depth; cldprop_sw (rrtmg_sw_cldprop.f90:153-154)
+    // passes the layer's band-summed depth as ttest
+    if (!(cldf >= cldmin && (cwp >= cldmin || (ttest < R(0) ? tauc : ttest) >= cldmin))) return;
     if (inflag == 0) {
         const double_ taucldorig_a = tauc;
         const double_ ffp = fsfc;

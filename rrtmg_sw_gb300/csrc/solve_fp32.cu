@@ -144,7 +144,7 @@ cudaError_t upload_tables_fp32(const DevTables& t) { return cudaMemcpyToSymbol(c
 
 LaunchInfo plan_fp32(const SolveParams& P, int num_sms) {
     LaunchInfo li;
-    li.smem = smem_layout(P.nlay, num_q<float>(P.extra != 0), P.fused && P.icld >= 1,
+    li.smem = smem_layout(P.nlay, num_q<float>(P.extra != 0), stages_clouds(P),
                           stage_aerosol<float>(P.iaer), sizeof(float)).total;
     cudaFuncSetAttribute(k_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
     int per_sm = 0;

@@ -17,7 +17,7 @@ size_t slot_elems(int nlay, int idelm, bool fp32) {
 
 LaunchInfo plan_fp64(const SolveParams& P, int num_sms) {
     LaunchInfo li;
-    li.smem = smem_layout(P.nlay, num_q<double>(P.extra != 0), P.fused && P.icld >= 1,
+    li.smem = smem_layout(P.nlay, num_q<double>(P.extra != 0), stages_clouds(P),
                           stage_aerosol<double>(P.iaer), sizeof(double)).total;
     cudaFuncSetAttribute(k_solve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
     int per_sm = 0;

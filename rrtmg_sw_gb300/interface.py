@@ -81,6 +81,8 @@ def lib():
         L.rrtmg_sw_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.c_void_p]
         L.rrtmg_sw_mcica_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds)]
         L.rrtmg_sw_mcica_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_void_p]
+        L.rrtmg_sw_nomcica_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds)]
+        L.rrtmg_sw_nomcica_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_void_p]
         L.rrtmg_sw_static_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_void_p]
         L.mcica_subcol_sw_c.argtypes = [C.c_int32] * 5 + [_dp] * 11 + [_dp] * 9
         L.get_alpha_c.argtypes = [C.c_int32] * 4 + [C.c_double, _dp, _dp, C.c_int32, _dp, _dp]
@@ -128,14 +130,18 @@ def rrtmg_sw(ncol, nlay, icld, iaer, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr
              o2vmr, asdir, asdif, aldir, aldif, coszen, adjes, dyofyr, scon, isolvar, inflgsw, iceflgsw,
              liqflgsw, cldfmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl, ciwpmcl, clwpmcl, reicmcl, relqmcl,
              tauaer, ssaaer, asmaer, ecaer, bndsolvar=None, indsolvar=None, solcycfrac=None, idelm=1,
-             extra=False, clouds=None):
+             extra=False, clouds=None, nomcica=False):
     """rrtmg_sw (rrtmg_sw_rad.f90:99-111).
 
     Returns ``(swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc)`` with shapes
     (ncol, nlay+1) and (ncol, nlay), or, with ``extra=True``, a dict that
     also holds the direct/diffuse and UV/near-IR fluxes.  ``clouds`` (a dict
     of mcica_subcol_sw's physical inputs plus ``permuteseed``) selects the
-    fused path, in which the subcolumn arrays may be None.
+    fused path, in which the subcolumn arrays may be None.  With
+    ``nomcica=True``, ``clouds`` holds the cloud arguments of the non-McICA
+    rrtmg_sw (rrtmg_sw_rad.nomcica.f90:97-109) -- cldfrac (cldfr), ciwp
+    (cicewp), clwp (cliqwp), rei (reice), rel (reliq), tauc/ssac/asmc/fsfc
+    (taucld .. fsfcld) -- and the solve is cldprop_sw + spcvrt_sw.
     """
     cl, cl1 = (ncol, nlay), (ncol, nlay + 1)
     gcl = (NGPTSW, ncol, nlay)
@@ -183,7 +189,10 @@ def rrtmg_sw(ncol, nlay, icld, iaer, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr
                           ("asmc", (NBNDSW, ncol, nlay)), ("fsfc", (NBNDSW, ncol, nlay)), ("alpha", cl)):
             keep["c_" + name] = _f(clouds.get(name), shp)
             setattr(c, name, _p(keep["c_" + name]))
-        _check(lib().rrtmg_sw_mcica_c(C.byref(a), C.byref(c)))
+        if nomcica:
+            _check(lib().rrtmg_sw_nomcica_c(C.byref(a), C.byref(c)))
+        else:
+            _check(lib().rrtmg_sw_mcica_c(C.byref(a), C.byref(c)))
     if extra:
         return out
     return tuple(out[k] for k in ("swuflx", "swdflx", "swhr", "swuflxc", "swdflxc", "swhrc"))

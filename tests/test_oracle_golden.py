@@ -23,11 +23,7 @@ TOL = {"uflx": 5e-5, "difdflx": 5e-5, "dirdflx": 5e-5, "dflx": 5e-5, "fnet": 5e-
 PARAMS = []
 for c in CASES:
     for b in c["expected"]:
-        marks = []
-        if c["imca"] == 0 and c["icld"] > 0:
-            marks = [pytest.mark.xfail(reason="non-McICA cloud path (cldprop_sw/spcvrt_sw) not restated",
-                                       strict=True)]
-        PARAMS.append(pytest.param(c, b, id="%s-b%d-%d" % (c["name"], b["istart"], b["iend"]), marks=marks))
+        PARAMS.append(pytest.param(c, b, id="%s-b%d-%d" % (c["name"], b["istart"], b["iend"])))
 
 
 @pytest.mark.parametrize("case,block", PARAMS)
