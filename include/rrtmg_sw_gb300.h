@@ -60,6 +60,11 @@ typedef struct rrtmg_sw_args {
     double *dirdflux, *difdflux, *uvdflx, *nidflx, *dirdnuv, *difdnuv, *dirdnir, *difdnir;
     int32_t idelm;
     int32_t nthreads;          /* unused by the GPU library (kept for layout) */
+    /* Per-band fluxes (ncol,nlay+1,nbnd) or NULL: total-sky up, down and
+     * direct down, clear-sky up and down, summed over each band's g-points
+     * (the band loop of rrtmg_sw_spcvmc.f90:619-630 that the column driver
+     * prints with iout = 98, rrtmg_sw.1col.f90:573-578). */
+    double *bndfu, *bndfd, *bndfddir, *bndcu, *bndcd;
 } rrtmg_sw_args;
 
 /* Physical cloud inputs for the fused path: the arguments of

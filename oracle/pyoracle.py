@@ -35,6 +35,7 @@ class RrtmgSwArgs(C.Structure):
         ("dirdflux", _dp), ("difdflux", _dp), ("uvdflx", _dp), ("nidflx", _dp),
         ("dirdnuv", _dp), ("difdnuv", _dp), ("dirdnir", _dp), ("difdnir", _dp),
         ("idelm", C.c_int32), ("nthreads", C.c_int32),
+        ("bndfu", _dp), ("bndfd", _dp), ("bndfddir", _dp), ("bndcu", _dp), ("bndcd", _dp),
     ]
 
 
@@ -157,7 +158,7 @@ NOMCICA_INPUTS = ("cldfr", "taucld", "ssacld", "asmcld", "fsfcld", "cicewp", "cl
 
 def rrtmg_sw(ncol, nlay, icld, iaer, inp, adjes=1.0, dyofyr=0, scon=1360.85, isolvar=0,
              inflgsw=2, iceflgsw=3, liqflgsw=1, idelm=1, nthreads=0, extra=False,
-             bndsolvar=None, indsolvar=None, solcycfrac=None, nomcica=False):
+             bndsolvar=None, indsolvar=None, solcycfrac=None, nomcica=False, bands=False):
     """GCM entry point.  ``inp`` maps argument names to Fortran-ordered
     (column-major) FP64 arrays flattened to 1-D.  With ``nomcica=True`` the
     non-McICA rrtmg_sw runs on the NOMCICA_INPUTS arrays of ``inp``."""
@@ -190,6 +191,8 @@ def rrtmg_sw(ncol, nlay, icld, iaer, inp, adjes=1.0, dyofyr=0, scon=1360.85, iso
     out.update({k: np.zeros(ncol * nlay) for k in ("swhr", "swhrc")})
     if extra:
         out.update({k: np.zeros(ncol * (nlay + 1)) for k in EXTRA_OUTPUTS})
+    if bands:
+        out.update({k: np.zeros(ncol * (nlay + 1) * 14) for k in ("bndfu", "bndfd", "bndfddir", "bndcu", "bndcd")})
     for k, v in out.items():
         setattr(a, k, _p(v))
     if bndsolvar is not None:

@@ -993,10 +993,16 @@ void vrtqdr(int klev, const std::vector<double>& pref, const std::vector<double>
 struct Fluxes {  // level arrays 1..nlay+1, bottom to top
     std::vector<double> bbfd, bbfu, bbcd, bbcu, uvfd, uvcd, nifd, nicd;
     std::vector<double> bbfddir, bbcddir, uvfddir, uvcddir, nifddir, nicddir;
+    // per band (ibm 1..14): total up, down, direct down, clear up, down at
+    // [(ibm-1)*(n+2) + level]
+    std::vector<double> bnd[5];
+    int nlev2 = 0;
     void alloc(int n) {
         for (auto* v : {&bbfd, &bbfu, &bbcd, &bbcu, &uvfd, &uvcd, &nifd, &nicd, &bbfddir, &bbcddir,
                         &uvfddir, &uvcddir, &nifddir, &nicddir})
             v->assign(n + 2, 0.0);
+        nlev2 = n + 2;
+        for (auto& v : bnd) v.assign((size_t)14 * (n + 2), 0.0);
     }
 };
 
@@ -1144,6 +1150,12 @@ void spcvmc(int nlay, int istart, int iend, int idelm, int iout, const double* p
                 const double dirc = idelm == 0 ? ztdbtc_nodel[jk] : ztdbtc[jk];
                 F.bbfddir[ikl] = F.bbfddir[ikl] + zincflx * dirf;
                 F.bbcddir[ikl] = F.bbcddir[ikl] + zincflx * dirc;
+                const size_t bo = (size_t)(ibm - 1) * F.nlev2 + ikl;
+                F.bnd[0][bo] += zincflx * zfu[jk];
+                F.bnd[1][bo] += zincflx * zfd[jk];
+                F.bnd[2][bo] += zincflx * dirf;
+                F.bnd[3][bo] += zincflx * zcu[jk];
+                F.bnd[4][bo] += zincflx * zcd[jk];
                 if (ibm >= 10 && ibm <= 13) {
                     F.uvcd[ikl] = F.uvcd[ikl] + zincflx * zcd[jk];
                     F.uvfd[ikl] = F.uvfd[ikl] + zincflx * zfd[jk];
@@ -1672,6 +1684,11 @@ static int rrtmg_sw_impl(const orc_rrtmg_sw_args* a, const NomcicaClouds* nm) {
             if (a->difdnir) a->difdnir[k] = F.nifd[i] - F.nifddir[i];
             swnflxc[i] = F.bbcd[i] - F.bbcu[i];
             swnflx[i] = F.bbfd[i] - F.bbfu[i];
+            double* bo[5] = {a->bndfu, a->bndfd, a->bndfddir, a->bndcu, a->bndcd};
+            for (int q = 0; q < 5; ++q)
+                if (bo[q])
+                    for (int ib = 0; ib < 14; ++ib)
+                        bo[q][k + (size_t)ncol * (nlay + 1) * ib] = F.bnd[q][(size_t)ib * F.nlev2 + i];
         }
         for (int i = 1; i <= nlay; ++i) {
             const double zdpgcp = T.heatfac / pdp[i - 1];

@@ -50,6 +50,7 @@ typedef struct orc_rrtmg_sw_args {
     double *dirdflux, *difdflux, *uvdflx, *nidflx, *dirdnuv, *difdnuv, *dirdnir, *difdnir;
     int32_t idelm;             /* reference hard-codes 1 (rrtmg_sw_rad.f90:605) */
     int32_t nthreads;          /* OpenMP threads over columns, <=0: default */
+    double *bndfu, *bndfd, *bndfddir, *bndcu, *bndcd;  /* (ncol,nlay+1,14) per-band fluxes or NULL */
 } orc_rrtmg_sw_args;
 
 /* Error codes: 0 = success; values mirror the reference's `stop` sites. */

@@ -462,6 +462,12 @@ int make_params(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, Sol
     P.swuflxc = a->swuflxc; P.swdflxc = a->swdflxc; P.swhrc = a->swhrc;
     double* xo[8] = {a->dirdflux, a->difdflux, a->uvdflx, a->nidflx, a->dirdnuv, a->difdnuv, a->dirdnir, a->difdnir};
     for (int i = 0; i < 8; ++i) P.xout[i] = xo[i];
+    double* bo[5] = {a->bndfu, a->bndfd, a->bndfddir, a->bndcu, a->bndcd};
+    P.bands = 0;
+    for (int i = 0; i < 5; ++i) {
+        P.bout[i] = bo[i];
+        if (bo[i]) P.bands = 1;
+    }
     return RRTMG_SW_OK;
 }
 
@@ -560,6 +566,11 @@ int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, bool nomcica = 
     for (int i = 0; i < 8; ++i) xd[i] = sg.out(xn[i], xh[i], CL1);
     d.dirdflux = xd[0]; d.difdflux = xd[1]; d.uvdflx = xd[2]; d.nidflx = xd[3];
     d.dirdnuv = xd[4]; d.difdnuv = xd[5]; d.dirdnir = xd[6]; d.difdnir = xd[7];
+    const char* bn[5] = {"b0", "b1", "b2", "b3", "b4"};
+    double* bh[5] = {a->bndfu, a->bndfd, a->bndfddir, a->bndcu, a->bndcd};
+    double* bd[5];
+    for (int i = 0; i < 5; ++i) bd[i] = sg.out(bn[i], bh[i], 14 * CL1);
+    d.bndfu = bd[0]; d.bndfd = bd[1]; d.bndfddir = bd[2]; d.bndcu = bd[3]; d.bndcd = bd[4];
     if (sg.err != cudaSuccess) return cuda_fail(sg.err);
     rc = solve_dev(st, &d, c ? &dc : nullptr, s, nomcica);
     if (rc) return rc;
@@ -567,6 +578,7 @@ int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, bool nomcica = 
     sg.back(a->swuflxc, d.swuflxc, CL1); sg.back(a->swdflxc, d.swdflxc, CL1);
     sg.back(a->swhr, d.swhr, CL); sg.back(a->swhrc, d.swhrc, CL);
     for (int i = 0; i < 8; ++i) sg.back(xh[i], xd[i], CL1);
+    for (int i = 0; i < 5; ++i) sg.back(bh[i], bd[i], 14 * CL1);
     if (sg.err != cudaSuccess) return cuda_fail(sg.err);
     CK(cudaStreamSynchronize(s));
     return RRTMG_SW_OK;

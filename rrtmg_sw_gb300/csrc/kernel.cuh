@@ -872,6 +872,22 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
                         sFlux[(c2 * NQ + qi) * (L + 1) + (L + 1 - jl)] = v;
                     }
                 }
+                if (P.bands) {
+                    // per-band sums of fu, fd, fddir, cu, cd (spcvmc:619-630 per band)
+                    const int bitems = COLS_PER_CTA * NBND * 5 * nlev;
+                    for (int t = tid; t < bitems; t += CTA_THREADS) {
+                        const int s = t % nlev, qs = (t / nlev) % 5, b = (t / (nlev * 5)) % NBND;
+                        const int c2 = t / (nlev * 5 * NBND);
+                        const int qi = qs == 0 ? 0 : qs == 1 ? 1 : qs == 2 ? 4 : qs == 3 ? 2 : 3;
+                        const R* src = sRed + (s * NQ + qi) * CTA_THREADS + c2 * NGPT + cT.b[b].g0;
+                        R v = R(0);
+                        for (int j = 0; j < cT.b[b].ng; ++j) v += src[j];
+                        const int ocol = COLS_PER_CTA * pair + c2;
+                        const int l = L + 1 - (jk - slot + s);  // level index, 0 = surface
+                        if (ocol < P.ncol && P.bout[qs])
+                            P.bout[qs][(size_t)ocol + n * ((size_t)l + (size_t)(L + 1) * b)] = (double)v;
+                    }
+                }
                 __syncthreads();
             }
         }

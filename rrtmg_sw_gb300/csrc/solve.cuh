@@ -40,6 +40,8 @@ struct SolveParams {
     const double *cldfrac, *ciwp, *clwp, *rei, *rel, *tauc, *ssac, *asmc, *fsfc, *alpha;
     double *swuflx, *swdflx, *swhr, *swuflxc, *swdflxc, *swhrc;
     double *xout[8];  // dirdflux, difdflux, uvdflx, nidflx, dirdnuv, difdnuv, dirdnir, difdnir
+    int bands;        // 1: per-band fluxes requested
+    double *bout[5];  // bndfu, bndfd, bndfddir, bndcu, bndcd (ncol,nlay+1,nbnd)
     void *scratch;
     size_t slot_elems;
     int *err;

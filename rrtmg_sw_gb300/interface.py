@@ -53,6 +53,7 @@ class RrtmgSwArgs(C.Structure):
         ("dirdflux", _dp), ("difdflux", _dp), ("uvdflx", _dp), ("nidflx", _dp),
         ("dirdnuv", _dp), ("difdnuv", _dp), ("dirdnir", _dp), ("difdnir", _dp),
         ("idelm", C.c_int32), ("nthreads", C.c_int32),
+        ("bndfu", _dp), ("bndfd", _dp), ("bndfddir", _dp), ("bndcu", _dp), ("bndcd", _dp),
     ]
 
 
@@ -66,6 +67,7 @@ class RrtmgSwClouds(C.Structure):
 
 
 EXTRA_OUTPUTS = ("dirdflux", "difdflux", "uvdflx", "nidflx", "dirdnuv", "difdnuv", "dirdnir", "difdnir")
+BAND_OUTPUTS = ("bndfu", "bndfd", "bndfddir", "bndcu", "bndcd")
 _lib = None
 
 
@@ -130,12 +132,13 @@ def rrtmg_sw(ncol, nlay, icld, iaer, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr
              o2vmr, asdir, asdif, aldir, aldif, coszen, adjes, dyofyr, scon, isolvar, inflgsw, iceflgsw,
              liqflgsw, cldfmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl, ciwpmcl, clwpmcl, reicmcl, relqmcl,
              tauaer, ssaaer, asmaer, ecaer, bndsolvar=None, indsolvar=None, solcycfrac=None, idelm=1,
-             extra=False, clouds=None, nomcica=False):
+             extra=False, clouds=None, nomcica=False, bands=False):
     """rrtmg_sw (rrtmg_sw_rad.f90:99-111).
 
     Returns ``(swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc)`` with shapes
     (ncol, nlay+1) and (ncol, nlay), or, with ``extra=True``, a dict that
-    also holds the direct/diffuse and UV/near-IR fluxes.  ``clouds`` (a dict
+    also holds the direct/diffuse and UV/near-IR fluxes; ``bands=True`` adds
+    the per-band fluxes BAND_OUTPUTS, shape (ncol, nlay+1, 14).  ``clouds`` (a dict
     of mcica_subcol_sw's physical inputs plus ``permuteseed``) selects the
     fused path, in which the subcolumn arrays may be None.  With
     ``nomcica=True``, ``clouds`` holds the cloud arguments of the non-McICA
@@ -175,6 +178,8 @@ def rrtmg_sw(ncol, nlay, icld, iaer, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr
     out.update({k: np.zeros(cl, order="F") for k in ("swhr", "swhrc")})
     if extra:
         out.update({k: np.zeros(cl1, order="F") for k in EXTRA_OUTPUTS})
+    if bands:
+        out.update({k: np.zeros((ncol, nlay + 1, NBNDSW), order="F") for k in BAND_OUTPUTS})
     for k, v in out.items():
         setattr(a, k, _p(v))
     a.idelm = idelm
@@ -193,7 +198,7 @@ def rrtmg_sw(ncol, nlay, icld, iaer, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr
             _check(lib().rrtmg_sw_nomcica_c(C.byref(a), C.byref(c)))
         else:
             _check(lib().rrtmg_sw_mcica_c(C.byref(a), C.byref(c)))
-    if extra:
+    if extra or bands:
         return out
     return tuple(out[k] for k in ("swuflx", "swdflx", "swhr", "swuflxc", "swdflxc", "swhrc"))
 
