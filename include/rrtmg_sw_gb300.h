@@ -146,6 +146,30 @@ int rrtmg_sw_mcica_dev_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, void 
 int rrtmg_sw_nomcica_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c);
 int rrtmg_sw_nomcica_dev_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, void *stream);
 
+/* Batches: many independent rrtmg_sw calls (ncol and nlay may differ) in
+ * one persistent launch.  a[0..n) and, for instances with icld >= 1, c[0..n)
+ * (fused McICA, irng = 0; c may be NULL when every instance is clear) hold
+ * device pointers, as for rrtmg_sw_mcica_dev_c; they must stay valid, and
+ * their contents may change, between runs.  The plan lists each instance's
+ * sunlit columns (coszen > 0) on the device before the solve and skips the
+ * others, whose outputs are set to zero (the reference solves them with mu0
+ * clamped to 1e-10, i.e. 1e-10 of a daytime flux).  Planning runs an
+ * autotuner (instance order as given or deepest first, 1 or 2 resident CTAs
+ * per SM when shared memory allows; one timed trial each, on the current
+ * data) and captures the compaction and the solve in a CUDA graph; a run
+ * replays the graph on `stream` and returns the device error status.  The
+ * arithmetic form is the one current at planning.  No counterpart in the
+ * reference (a GCM calls rrtmg_sw per chunk of columns). */
+int rrtmg_sw_batch_plan_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, int32_t n, void *stream,
+                          void **plan);
+int rrtmg_sw_batch_run_c(void *plan, void *stream);
+/* The autotuner's choice (grid size, deepest-first order) and its trial
+ * times in ms, in the order (given order: 1, 2 CTAs per SM; deepest first:
+ * 1, 2); ntrials holds the capacity of trial_ms on entry. */
+int rrtmg_sw_batch_info_c(void *plan, int32_t *grid, int32_t *deepest_first, float *trial_ms,
+                          int32_t *ntrials);
+int rrtmg_sw_batch_free_c(void *plan);
+
 /* Allocation-free device solve.  No counterpart in the reference: it exists
  * for callers that must not allocate device memory while they run -- a
  * model whose memory pool owns the whole GPU, or a time step that forbids

@@ -3,6 +3,7 @@
 // device workspace and the C-ABI entry points of include/rrtmg_sw_gb300.h.
 #include <dlfcn.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -651,6 +652,148 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
     return h_err;
 }
 
+// ---------------------------------------------------------------------------
+// Batch plans: many instances in one persistent launch (k_compact + k_solve_batch),
+// captured once in a CUDA graph and replayed.
+struct BatchPlan {
+    int n = 0, form = 0, grid = 0, desc = 0, device = 0;
+    size_t smem = 0;
+    DevBuf params, maps, offs, counts, scratch, errw;
+    int* h_err = nullptr;  // pinned
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<float> tune_ms;  // per candidate: (order, blocks per SM) in trial order
+};
+
+cudaError_t batch_launch(State& st, BatchPlan& bp, int grid, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(bp.errw.p, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    e = launch_compact((const SolveParams*)bp.params.p, bp.n, (int*)bp.maps.p, (const long long*)bp.offs.p,
+                       (int*)bp.counts.p, s);
+    if (e != cudaSuccess) return e;
+    if (bp.form == RRTMG_SW_FORM_FP32)
+        return launch_batch_fp32((const SolveParams*)bp.params.p, bp.n, (const int*)bp.counts.p,
+                                 (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, grid, bp.smem, s);
+    return launch_batch_fp64((const SolveParams*)bp.params.p, bp.n, (const int*)bp.counts.p,
+                             (const double*)st.d_tab64.p, grid, bp.smem, s);
+}
+
+// Upload the instances' parameters in the given order (sunlit lists and
+// counts follow the order).
+cudaError_t batch_upload(BatchPlan& bp, std::vector<SolveParams> P, const std::vector<int>& order, cudaStream_t s) {
+    std::vector<SolveParams> Q(bp.n);
+    std::vector<long long> off(bp.n);
+    long long o = 0;
+    for (int k = 0; k < bp.n; ++k) {
+        Q[k] = P[order[k]];
+        off[k] = o;
+        Q[k].colmap = (const int*)bp.maps.p + o;
+        Q[k].mapcount = (const int*)bp.counts.p + k;
+        o += Q[k].ncol;
+    }
+    cudaError_t e = cudaMemcpyAsync(bp.params.p, Q.data(), sizeof(SolveParams) * bp.n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(bp.offs.p, off.data(), sizeof(long long) * bp.n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);
+}
+
+void batch_release(BatchPlan* bp) {
+    if (!bp) return;
+    if (bp->exec) cudaGraphExecDestroy(bp->exec);
+    if (bp->graph) cudaGraphDestroy(bp->graph);
+    bp->params.release(); bp->maps.release(); bp->offs.release(); bp->counts.release();
+    bp->scratch.release(); bp->errw.release();
+    if (bp->h_err) cudaFreeHost(bp->h_err);
+    delete bp;
+}
+
+int batch_plan(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, int n, cudaStream_t s, BatchPlan** out) {
+    if (n < 1 || n > MAX_BATCH) return RRTMG_SW_EARGS;
+    BatchPlan* bp = new BatchPlan();
+    bp->n = n;
+    bp->form = st.form;
+    bp->device = st.device;
+    const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
+    std::vector<SolveParams> P(n);
+    size_t slot = 0, smem = 0;
+    long long cols = 0;
+    for (int i = 0; i < n; ++i) {
+        int rc = check_args(a + i);
+        if (!rc) rc = make_params(st, a + i, (c && a[i].icld >= 1) ? c + i : nullptr, P[i]);
+        if (rc) { batch_release(bp); return rc; }
+        const size_t si = slot_elems(P[i].nlay, P[i].idelm, fp32);
+        if (si > slot) slot = si;
+        const size_t mi = fp32 ? solve_smem_fp32(P[i]) : solve_smem_fp64(P[i]);
+        if (mi > smem) smem = mi;
+        cols += P[i].ncol;
+    }
+    bp->smem = smem;
+    const int per_sm = fp32 ? batch_blocks_per_sm_fp32(smem) : batch_blocks_per_sm_fp64(smem);
+    if (per_sm < 1) { batch_release(bp); return RRTMG_SW_EARGS; }
+    const int grid_max = st.num_sms * per_sm;
+    const size_t esz = fp32 ? sizeof(float) : sizeof(double);
+    cudaError_t e = cudaSuccess;
+    if ((e = bp->params.ensure(sizeof(SolveParams) * n)) != cudaSuccess ||
+        (e = bp->maps.ensure(sizeof(int) * (size_t)(cols > 0 ? cols : 1))) != cudaSuccess ||
+        (e = bp->offs.ensure(sizeof(long long) * n)) != cudaSuccess ||
+        (e = bp->counts.ensure(sizeof(int) * n)) != cudaSuccess ||
+        (e = bp->scratch.ensure((size_t)grid_max * slot * esz)) != cudaSuccess ||
+        (e = bp->errw.ensure(sizeof(int))) != cudaSuccess ||
+        (e = cudaMallocHost((void**)&bp->h_err, sizeof(int))) != cudaSuccess) {
+        batch_release(bp);
+        return cuda_fail(e);
+    }
+    for (int i = 0; i < n; ++i) {
+        P[i].scratch = bp->scratch.p;
+        P[i].slot_elems = slot;
+        P[i].err = (int*)bp->errw.p;
+    }
+    // autotuner: instance order (as given / deepest first) x resident CTAs per SM, one timed trial each
+    std::vector<int> given(n), desc(n);
+    for (int i = 0; i < n; ++i) given[i] = desc[i] = i;
+    std::stable_sort(desc.begin(), desc.end(), [&](int x, int y) { return P[x].nlay > P[y].nlay; });
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int best_k = 1, best_desc = 0;
+    for (int od = 0; od < 2 && e == cudaSuccess; ++od) {
+        if ((e = batch_upload(*bp, P, od ? desc : given, s)) != cudaSuccess) break;
+        for (int k = 1; k <= per_sm && e == cudaSuccess; ++k) {
+            const int grid = st.num_sms * k;
+            if ((e = batch_launch(st, *bp, grid, s)) != cudaSuccess) break;  // warm-up
+            cudaEventRecord(e0, s);
+            if ((e = batch_launch(st, *bp, grid, s)) != cudaSuccess) break;
+            cudaEventRecord(e1, s);
+            if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            bp->tune_ms.push_back(ms);
+            if (ms < best) { best = ms; best_k = k; best_desc = od; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e == cudaSuccess) e = batch_upload(*bp, P, best_desc ? desc : given, s);
+    bp->grid = st.num_sms * best_k;
+    bp->desc = best_desc;
+    // capture compaction + solve into a graph on a private stream
+    cudaStream_t cs = nullptr;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        const cudaError_t le = batch_launch(st, *bp, bp->grid, cs);
+        e = cudaStreamEndCapture(cs, &bp->graph);
+        if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&bp->exec, bp->graph, 0);
+    if (cs) cudaStreamDestroy(cs);
+    if (e != cudaSuccess) { batch_release(bp); return cuda_fail(e); }
+    *out = bp;
+    return RRTMG_SW_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -841,6 +984,51 @@ const char* rrtmg_sw_errstr_c(int32_t code) {
 }
 
 const char* rrtmg_sw_last_cuda_error_c(void) { return S().last_cuda.c_str(); }
+
+int rrtmg_sw_batch_plan_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, int32_t n, void* stream, void** plan) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (!a || !plan) return RRTMG_SW_EARGS;
+    BatchPlan* bp = nullptr;
+    const int rc = batch_plan(st, a, c, n, (cudaStream_t)stream, &bp);
+    *plan = bp;
+    return rc;
+}
+
+int rrtmg_sw_batch_run_c(void* plan, void* stream) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    BatchPlan* bp = (BatchPlan*)plan;
+    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (!bp) return RRTMG_SW_EARGS;
+    cudaStream_t s = (cudaStream_t)stream;
+    CK(cudaGraphLaunch(bp->exec, s));
+    st.last_launches = 2;
+    CK(cudaMemcpyAsync(bp->h_err, bp->errw.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return *bp->h_err;
+}
+
+int rrtmg_sw_batch_info_c(void* plan, int32_t* grid, int32_t* deepest_first, float* trial_ms, int32_t* ntrials) {
+    BatchPlan* bp = (BatchPlan*)plan;
+    if (!bp) return RRTMG_SW_EARGS;
+    if (grid) *grid = bp->grid;
+    if (deepest_first) *deepest_first = bp->desc;
+    if (ntrials) {
+        const int cap = *ntrials;
+        *ntrials = (int)bp->tune_ms.size();
+        for (int i = 0; trial_ms && i < cap && i < (int)bp->tune_ms.size(); ++i) trial_ms[i] = bp->tune_ms[i];
+    }
+    return RRTMG_SW_OK;
+}
+
+int rrtmg_sw_batch_free_c(void* plan) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    batch_release((BatchPlan*)plan);
+    return RRTMG_SW_OK;
+}
 
 int rrtmg_sw_finalize_c(void) {
     State& st = S();

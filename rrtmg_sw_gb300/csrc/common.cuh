@@ -67,6 +67,8 @@ __device__ inline void set_error(int* err, int code) {
     if (err) atomicCAS(err, 0, code);
 }
 
+constexpr int MAX_BATCH = 1024;  // instances per batch launch
+
 // Error codes (mirror include/rrtmg_sw_gb300.h)
 enum {
     E_OK = 0, E_INFLAG1 = 10, E_ICERAD = 11, E_ICEDGE = 12, E_ICEPROP = 13,

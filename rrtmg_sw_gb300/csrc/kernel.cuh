@@ -532,409 +532,565 @@ __host__ __device__ inline bool stage_aerosol(int iaer) {
     return sizeof(R) == 4 && iaer != 0;
 }
 
+// Shared-memory views of one CTA for the parameters P (two columns).
 template <typename R>
-__global__ void __launch_bounds__(CTA_THREADS, 2)
-k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict__ tab64) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+struct CtaView {
+    double* sPdp;       // [2][L]
+    R* sCoef;           // [2][NFR][L]
+    float* sHrf;        // [2][L] FP32 form: heatfac / dp
+    int* sPk;           // [2][L]
+    int* sMisc;         // laytrop [2]
+    long long* sKc;     // [2][L] McICA threshold of 1 - cldf
+    long long* sKa;     // [2][L] McICA threshold of alpha
+    double* sOmcf;      // [2][L] 1 - cldf (icld 2)
+    R* sCld;            // [2][4][L] ciwp, clwp, rei, rel
+    uint32_t* sSeed;    // [2][4]
+    uint32_t* sXs;      // [112][32] columns of M^n
+    R* sAer;            // [2][3][14][L] tau, ssa, asym
+    R* sRed;            // [KLEV][NQ][224]
+    R* sFlux;           // [2][NQ][L+1]
+};
+
+template <typename R>
+__device__ inline CtaView<R> cta_view(unsigned char* smem_raw, const SolveParams& P) {
+    const Smem M = smem_layout(P.nlay, num_q<R>(P.extra != 0), stages_clouds(P), stage_aerosol<R>(P.iaer), sizeof(R));
+    CtaView<R> v;
+    v.sPdp = (double*)(smem_raw + M.pdp);
+    v.sCoef = (R*)(smem_raw + M.coef);
+    v.sHrf = (float*)(smem_raw + M.hrf);
+    v.sPk = (int*)(smem_raw + M.pk);
+    v.sMisc = (int*)(smem_raw + M.misc);
+    v.sKc = (long long*)(smem_raw + M.kc);
+    v.sKa = (long long*)(smem_raw + M.ka);
+    v.sOmcf = (double*)(smem_raw + M.omcf);
+    v.sCld = (R*)(smem_raw + M.cld);
+    v.sSeed = (uint32_t*)(smem_raw + M.seed);
+    v.sXs = (uint32_t*)(smem_raw + M.xs);
+    v.sAer = (R*)(smem_raw + M.aer);
+    v.sRed = (R*)(smem_raw + M.red);
+    v.sFlux = (R*)(smem_raw + M.flux);
+    return v;
+}
+
+// McICA stream jump of this thread's subcolumn for parameters P; the
+// xorshift part goes to sXs (one column of M^n per g-point).
+__device__ inline KissJump kiss_setup(const SolveParams& P, uint32_t* sXs) {
+    KissJump J{1u, 0u, 1u, 1u};
+    if (P.fused && P.icld >= 1) {
+        const int g = threadIdx.x % NGPT;
+        const uint64_t off = kiss_offset(P.icld, g, P.nlay, P.permuteseed);
+        J = kiss_jump_consts(off);
+        if (threadIdx.x / NGPT == 0) xorshift_power(off, sXs + g * 32);
+    }
+    return J;
+}
+
+// Column of slot c2 of column pair `pair`: consecutive columns, or through
+// the sunlit-column list of a batch (P.colmap, nmapped entries); ncol marks
+// an empty slot.
+__device__ inline int pair_col(const SolveParams& P, int pair, int c2, int nmapped) {
+    const int k = COLS_PER_CTA * pair + c2;
+    if (!P.colmap) return k;
+    return k < nmapped ? P.colmap[k] : P.ncol;
+}
+
+// One column pair: prep, pass 1, pass 2 and outputs.
+template <typename R>
+__device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const CtaView<R>& V, const KissJump& J,
+                                           R* scr, const R* __restrict__ tab, const double* __restrict__ tab64) {
     const int L = P.nlay;
     const int NQ = num_q<R>(P.extra != 0);
     constexpr int QX = 6 + num_abs<R>();  // first extra-output sum
     const bool fused = P.fused && P.icld >= 1;
     const bool nomc = P.nomcica && P.icld >= 1;
     const bool aer_stage = stage_aerosol<R>(P.iaer);
-    const Smem M = smem_layout(L, NQ, stages_clouds(P), aer_stage, sizeof(R));
-    double* sPdp = (double*)(smem_raw + M.pdp);        // [2][L]
-    R* sCoef = (R*)(smem_raw + M.coef);                // [2][NFR][L]
-    float* sHrf = (float*)(smem_raw + M.hrf);          // [2][L] FP32 form: heatfac / dp
-    int* sPk = (int*)(smem_raw + M.pk);                // [2][L]
-    int* sMisc = (int*)(smem_raw + M.misc);            // laytrop [2]
-    long long* sKc = (long long*)(smem_raw + M.kc);    // [2][L] McICA threshold of 1 - cldf
-    long long* sKa = (long long*)(smem_raw + M.ka);    // [2][L] McICA threshold of alpha
-    double* sOmcf = (double*)(smem_raw + M.omcf);      // [2][L] 1 - cldf (icld 2)
-    R* sCld = (R*)(smem_raw + M.cld);                  // [2][4][L] ciwp, clwp, rei, rel
-    uint32_t* sSeed = (uint32_t*)(smem_raw + M.seed);  // [2][4]
-    uint32_t* sXs = (uint32_t*)(smem_raw + M.xs);      // [112][32] columns of M^n
-    R* sAer = (R*)(smem_raw + M.aer);                  // [2][3][14][L] tau, ssa, asym
-    R* sRed = (R*)(smem_raw + M.red);                  // [KLEV][NQ][224]
-    R* sFlux = (R*)(smem_raw + M.flux);                // [2][NQ][L+1]
-
+    double* sPdp = V.sPdp;
+    R* sCoef = V.sCoef;
+    float* sHrf = V.sHrf;
+    int* sPk = V.sPk;
+    int* sMisc = V.sMisc;
+    long long* sKc = V.sKc;
+    long long* sKa = V.sKa;
+    double* sOmcf = V.sOmcf;
+    R* sCld = V.sCld;
+    uint32_t* sSeed = V.sSeed;
+    uint32_t* sXs = V.sXs;
+    R* sAer = V.sAer;
+    R* sRed = V.sRed;
+    R* sFlux = V.sFlux;
     const int tid = threadIdx.x;
     const int cc = tid / NGPT, g = tid % NGPT;
     const int ib = cT.ngb[g], igb = cT.gib[g];
     const bool uv = ib >= 9 && ib <= 12;  // bands 25-28 (spcvmc:629)
     const int NS = P.idelm == 0 ? NS_MAX : S_DBTCN;
-    R* scr = (R*)P.scratch + (size_t)blockIdx.x * P.slot_elems;
     // FP32 form: the FP64 layer coefficients [2][NFR][L] follow the level fields of the slot
     double* sCoef64 = (double*)(scr + (size_t)L * NS * CTA_THREADS);
     const size_t n = (size_t)P.ncol;
-
-    // McICA stream jump of this subcolumn: once per launch
-    KissJump J{1u, 0u, 1u, 1u};
-    if (fused) {
-        const uint64_t off = kiss_offset(P.icld, g, L, P.permuteseed);
-        J = kiss_jump_consts(off);
-        if (cc == 0) xorshift_power(off, sXs + g * 32);
+    const int nmapped = P.colmap ? *P.mapcount : 0;
+    (void)nomc;
+    __syncthreads();
+    // ---------------- prep: one (column, layer) per item, FP64
+    for (int it = tid; it < COLS_PER_CTA * L; it += CTA_THREADS) {
+        const int c2 = it / L, lay = it % L + 1;
+        const int pcol = pair_col(P, pair, c2, nmapped);
+        constexpr bool f32 = sizeof(R) == 4;
+        prep_layer<R>(P, pcol, lay, sCoef + c2 * NFR * L, sPk + c2 * L, sPdp + c2 * L, L, tab64,
+                      f32 ? sCoef64 + c2 * NFR * L : nullptr);
+        if (f32) sHrf[c2 * L + lay - 1] = (float)(cT.heatfac / sPdp[c2 * L + lay - 1]);
+        const bool real = pcol < P.ncol;
+        const size_t kl = (size_t)pcol + n * (size_t)(lay - 1);
+        if (fused) {
+            double cf = real ? P.cldfrac[kl] : 0.0;
+            if (cf < 1.0e-20) cf = 0.0;
+            const double omcf = DS(1.0, cf);
+            sOmcf[c2 * L + lay - 1] = omcf;
+            sKc[c2 * L + lay - 1] = kiss_threshold(omcf);
+            sKa[c2 * L + lay - 1] = (P.icld >= 4 && real) ? kiss_threshold(P.alpha[kl]) : 0ll;
+            R* cd = sCld + c2 * 4 * L;
+            cd[0 * L + lay - 1] = real ? (R)P.ciwp[kl] : R(0);
+            cd[1 * L + lay - 1] = real ? (R)P.clwp[kl] : R(0);
+            cd[2 * L + lay - 1] = real ? (R)P.rei[kl] : R(0);
+            cd[3 * L + lay - 1] = real ? (R)P.rel[kl] : R(0);
+            if (lay == 1) {
+                uint32_t* sd = sSeed + c2 * 4;
+                if (real) {
+                    const double p1 = DM(P.play[pcol], 1.e2), p2 = DM(P.play[pcol + n], 1.e2);
+                    if (p1 < p2) set_error(P.err, E_KISSSEED);
+                    sd[0] = kiss_seed(p1);
+                    sd[1] = kiss_seed(p2);
+                    sd[2] = kiss_seed(DM(P.play[pcol + 2 * n], 1.e2));
+                    sd[3] = kiss_seed(DM(P.play[pcol + 3 * n], 1.e2));
+                } else {
+                    sd[0] = sd[1] = sd[2] = sd[3] = 1u;
+                }
+            }
+        }
+        if (nomc) {
+            // spcvrt_sw takes clear or overcast layers only (rrtmg_sw_rad.nomcica.f90:617-621)
+            const double cf = real ? P.cldfrac[kl] : 0.0;
+            if (cf > 1.e-6 && cf < 1.0 - 1.e-6) set_error(P.err, E_PARTIAL);
+            R* cd = sCld + c2 * 4 * L;
+            cd[0 * L + lay - 1] = real ? (R)P.ciwp[kl] : R(0);
+            cd[1 * L + lay - 1] = real ? (R)P.clwp[kl] : R(0);
+            cd[2 * L + lay - 1] = real ? (R)P.rei[kl] : R(0);
+            cd[3 * L + lay - 1] = real ? (R)P.rel[kl] : R(0);
+        }
+        if (aer_stage) {
+            for (int b = 0; b < NBND; ++b) {
+                double ta = 0.0, oa = 1.0, ga = 0.0;
+                if (real) aerosol(P, pcol, lay, b, tab64, ta, oa, ga);
+                R* ad = sAer + c2 * 3 * NBND * L;
+                ad[(0 * NBND + b) * L + lay - 1] = (R)ta;
+                ad[(1 * NBND + b) * L + lay - 1] = (R)DS(1.0, oa);  // co-albedo, formed in FP64
+                ad[(2 * NBND + b) * L + lay - 1] = (R)ga;
+            }
+        }
+    }
+    __syncthreads();
+    if (g == 0) {
+        int lt = 0;
+        for (int i = 0; i < L; ++i) lt += (sPk[cc * L + i] >> 30) & 1;
+        sMisc[cc] = lt;
+    }
+    __syncthreads();
+    const int col = pair_col(P, pair, cc, nmapped);
+    const Coef<R> C{sCoef + cc * NFR * L, sPk + cc * L, L, sMisc[cc]};
+    const Coef<double> C64{sCoef64 + cc * NFR * L, sPk + cc * L, L, sMisc[cc]};
+    bool active = col < P.ncol;
+    if (active && (C.laytrop < 1 || C.laytrop >= L)) {
+        set_error(P.err, E_LAYTROP);
+        active = false;
     }
 
-    for (int pair = blockIdx.x; pair < P.npairs; pair += gridDim.x) {
-        __syncthreads();
-        // ---------------- prep: one (column, layer) per item, FP64
-        for (int it = tid; it < COLS_PER_CTA * L; it += CTA_THREADS) {
-            const int c2 = it / L, lay = it % L + 1;
-            const int pcol = COLS_PER_CTA * pair + c2;
-            constexpr bool f32 = sizeof(R) == 4;
-            prep_layer<R>(P, pcol, lay, sCoef + c2 * NFR * L, sPk + c2 * L, sPdp + c2 * L, L, tab64,
-                          f32 ? sCoef64 + c2 * NFR * L : nullptr);
-            if (f32) sHrf[c2 * L + lay - 1] = (float)(cT.heatfac / sPdp[c2 * L + lay - 1]);
-            const bool real = pcol < P.ncol;
-            const size_t kl = (size_t)pcol + n * (size_t)(lay - 1);
-            if (fused) {
-                double cf = real ? P.cldfrac[kl] : 0.0;
-                if (cf < 1.0e-20) cf = 0.0;
-                const double omcf = DS(1.0, cf);
-                sOmcf[c2 * L + lay - 1] = omcf;
-                sKc[c2 * L + lay - 1] = kiss_threshold(omcf);
-                sKa[c2 * L + lay - 1] = (P.icld >= 4 && real) ? kiss_threshold(P.alpha[kl]) : 0ll;
-                R* cd = sCld + c2 * 4 * L;
-                cd[0 * L + lay - 1] = real ? (R)P.ciwp[kl] : R(0);
-                cd[1 * L + lay - 1] = real ? (R)P.clwp[kl] : R(0);
-                cd[2 * L + lay - 1] = real ? (R)P.rei[kl] : R(0);
-                cd[3 * L + lay - 1] = real ? (R)P.rel[kl] : R(0);
-                if (lay == 1) {
-                    uint32_t* sd = sSeed + c2 * 4;
-                    if (real) {
-                        const double p1 = DM(P.play[pcol], 1.e2), p2 = DM(P.play[pcol + n], 1.e2);
-                        if (p1 < p2) set_error(P.err, E_KISSSEED);
-                        sd[0] = kiss_seed(p1);
-                        sd[1] = kiss_seed(p2);
-                        sd[2] = kiss_seed(DM(P.play[pcol + 2 * n], 1.e2));
-                        sd[3] = kiss_seed(DM(P.play[pcol + 3 * n], 1.e2));
-                    } else {
-                        sd[0] = sd[1] = sd[2] = sd[3] = 1u;
-                    }
-                }
-            }
-            if (nomc) {
-                // spcvrt_sw takes clear or overcast layers only (rrtmg_sw_rad.nomcica.f90:617-621)
-                const double cf = real ? P.cldfrac[kl] : 0.0;
-                if (cf > 1.e-6 && cf < 1.0 - 1.e-6) set_error(P.err, E_PARTIAL);
-                R* cd = sCld + c2 * 4 * L;
-                cd[0 * L + lay - 1] = real ? (R)P.ciwp[kl] : R(0);
-                cd[1 * L + lay - 1] = real ? (R)P.clwp[kl] : R(0);
-                cd[2 * L + lay - 1] = real ? (R)P.rei[kl] : R(0);
-                cd[3 * L + lay - 1] = real ? (R)P.rel[kl] : R(0);
-            }
-            if (aer_stage) {
-                for (int b = 0; b < NBND; ++b) {
-                    double ta = 0.0, oa = 1.0, ga = 0.0;
-                    if (real) aerosol(P, pcol, lay, b, tab64, ta, oa, ga);
-                    R* ad = sAer + c2 * 3 * NBND * L;
-                    ad[(0 * NBND + b) * L + lay - 1] = (R)ta;
-                    ad[(1 * NBND + b) * L + lay - 1] = (R)DS(1.0, oa);  // co-albedo, formed in FP64
-                    ad[(2 * NBND + b) * L + lay - 1] = (R)ga;
-                }
-            }
-        }
-        __syncthreads();
-        if (g == 0) {
-            int lt = 0;
-            for (int i = 0; i < L; ++i) lt += (sPk[cc * L + i] >> 30) & 1;
-            sMisc[cc] = lt;
-        }
-        __syncthreads();
-        const int col = COLS_PER_CTA * pair + cc;
-        const Coef<R> C{sCoef + cc * NFR * L, sPk + cc * L, L, sMisc[cc]};
-        const Coef<double> C64{sCoef64 + cc * NFR * L, sPk + cc * L, L, sMisc[cc]};
-        bool active = col < P.ncol;
-        if (active && (C.laytrop < 1 || C.laytrop >= L)) {
-            set_error(P.err, E_LAYTROP);
-            active = false;
-        }
+    // ---------------- per (column, g-point) setup
+    R zinc = R(0), albp = R(0), albd = R(0);
+    double cossza = 1.0;
+    McicaMask mc;
+    if (active) {
+        cossza = P.coszen[col];
+        if (cossza < 1.e-10) cossza = 1.e-10;
+        const bool nir = ib <= 8 || ib == 13;
+        albp = (R)(nir ? P.aldir[col] : P.asdir[col]);
+        albd = (R)(nir ? P.aldif[col] : P.asdif[col]);
+        // zincflx = adjflux * ssi * prmu0 (spcvmc:349-356)
+        R src;
+        if constexpr (sizeof(R) == 4) src = solar_source_generic(ib, igb, C, P, tab);
+        else src = solar_source<R>(ib, igb, C, P, tab);
+        zinc = R(P.adjflux[ib]) * src * (R)cossza;
+        if (fused) mc.start(kiss_start(sSeed + cc * 4, J, sXs + g * 32), P.icld);
+    }
+    const R prmu0 = (R)cossza;
+    const R* cld = sCld + cc * 4 * L;
+    const R* aer = sAer + cc * 3 * NBND * L;
 
-        // ---------------- per (column, g-point) setup
-        R zinc = R(0), albp = R(0), albd = R(0);
-        double cossza = 1.0;
-        McicaMask mc;
-        if (active) {
-            cossza = P.coszen[col];
-            if (cossza < 1.e-10) cossza = 1.e-10;
-            const bool nir = ib <= 8 || ib == 13;
-            albp = (R)(nir ? P.aldir[col] : P.asdir[col]);
-            albd = (R)(nir ? P.aldif[col] : P.asdif[col]);
-            // zincflx = adjflux * ssi * prmu0 (spcvmc:349-356)
-            R src;
-            if constexpr (sizeof(R) == 4) src = solar_source_generic(ib, igb, C, P, tab);
-            else src = solar_source<R>(ib, igb, C, P, tab);
-            zinc = R(P.adjflux[ib]) * src * (R)cossza;
-            if (fused) mc.start(kiss_start(sSeed + cc * 4, J, sXs + g * 32), P.icld);
-        }
-        const R prmu0 = (R)cossza;
-        const R* cld = sCld + cc * 4 * L;
-        const R* aer = sAer + cc * 3 * NBND * L;
-
-        // ---------------- pass 1: bottom -> top
-        R rupc_b = albp, rupdc_b = albd, rup_b = albp, rupd_b = albd;
-        int redo_from = L + 1;  // FP32 form: lowest layer to redo in FP64
-        for (int lay = 1; lay <= L; ++lay) {
-            const int jk = L + 1 - lay;
-            R* sv = scr + (size_t)(jk - 1) * NS * CTA_THREADS + tid;
-            if (!active) continue;
-            R taug, taur;
-            if constexpr (sizeof(R) == 4) {
-                int js;
-                float fs;
-                taumol_generic(ib, igb, lay, C, tab, taug, taur, js, fs);
-            } else {
-                taumol_g<R>(ib, igb, lay, C, tab, taug, taur);
-            }
-            CellIn<R> ci;
-            ci.taug = taug;
-            ci.taur = taur;
-            if (aer_stage) {
-                ci.rta = aer[(0 * NBND + ib) * L + lay - 1];
-                ci.rcoa = aer[(1 * NBND + ib) * L + lay - 1];
-                ci.roa = R(1) - ci.rcoa;
-                ci.rga = aer[(2 * NBND + ib) * L + lay - 1];
-            } else {
-                aerosol_in(P, col, lay, ib, tab64, ci);
-            }
-            // cloud of this subcolumn (McICA) at this layer
-            bool cloudy = false;
-            if (P.icld >= 1 && fused)
-                cloudy = mc.step(lay, sKc[cc * L + lay - 1], sKa[cc * L + lay - 1], sOmcf[cc * L + lay - 1]);
-            cloud_in<R>(P, col, g, lay, ib, fused, cloudy, cld, ci, tab);
-            const R hrs = zinc * sHrf[cc * L + lay - 1];
-            const CellOpt<R> co = cell_optics<R>(ci, P.idelm, prmu0, tab, tab64, hrs);
-            // FP32 form: a table entry, the conservative switch or the
-            // resonance of this cell is too close to call in FP32; it is
-            // marked in the scratch (S_DBTC < 0, -2 if cloudy) and redone
-            // after this pass as the FP64 form does
-            int redo = 0;
-            if constexpr (sizeof(R) == 4) {
-                if (co.risky) {
-                    redo = ci.cloudy ? 2 : 1;
-                    if (lay < redo_from) redo_from = lay;
-                }
-            }
-            const RT<R>& rc = co.rc;
-            const RT<R>& rt = co.rt;
-            const R zdbtc = co.zdbtc, zdbt = co.zdbt;
-            if (P.idelm == 0) {
-                sv[S_DBTCN * CTA_THREADS] = co.dbtcn;
-                sv[S_DBTN * CTA_THREADS] = co.dbtn;
-            }
-            // upward adding recurrence (vrtqdr:122-140)
-            {
-                const R zr = R(1) / (R(1) - rupdc_b * rc.refd);
-                const R rupc = rc.ref + (rc.trad * ((rc.tra - zdbtc) * rupdc_b + zdbtc * rupc_b)) * zr;
-                const R rupdc = rc.refd + rc.trad * rc.trad * rupdc_b * zr;
-                rupc_b = rupc;
-                rupdc_b = rupdc;
-            }
-            {
-                const R zr = R(1) / (R(1) - rupd_b * rt.refd);
-                const R rup = rt.ref + (rt.trad * ((rt.tra - zdbt) * rupd_b + zdbt * rup_b)) * zr;
-                const R rupd = rt.refd + rt.trad * rt.trad * rupd_b * zr;
-                rup_b = rup;
-                rupd_b = rupd;
-            }
-            // the FP32 form keeps the absorptances in the transmittance slots
-            // and rebuilds ptra = 1 - pref - adir, ptrad = 1 - prefd - adif
-            constexpr bool keep_abs = sizeof(R) == 4;
-            sv[S_REFC * CTA_THREADS] = rc.ref;
-            sv[S_REFDC * CTA_THREADS] = rc.refd;
-            sv[S_TRAC * CTA_THREADS] = keep_abs ? rc.adir : rc.tra;
-            sv[S_TRADC * CTA_THREADS] = keep_abs ? rc.adif : rc.trad;
-            sv[S_DBTC * CTA_THREADS] = redo ? -(R)redo : zdbtc;
-            sv[S_RUPC * CTA_THREADS] = rupc_b;
-            sv[S_RUPDC * CTA_THREADS] = rupdc_b;
-            sv[S_REF * CTA_THREADS] = rt.ref;
-            sv[S_REFD * CTA_THREADS] = rt.refd;
-            sv[S_TRA * CTA_THREADS] = keep_abs ? rt.adir : rt.tra;
-            sv[S_TRAD * CTA_THREADS] = keep_abs ? rt.adif : rt.trad;
-            sv[S_DBT * CTA_THREADS] = zdbt;
-            sv[S_RUP * CTA_THREADS] = rup_b;
-            sv[S_RUPD * CTA_THREADS] = rupd_b;
-        }
-
+    // ---------------- pass 1: bottom -> top
+    R rupc_b = albp, rupdc_b = albd, rup_b = albp, rupd_b = albd;
+    int redo_from = L + 1;  // FP32 form: lowest layer to redo in FP64
+    for (int lay = 1; lay <= L; ++lay) {
+        const int jk = L + 1 - lay;
+        R* sv = scr + (size_t)(jk - 1) * NS * CTA_THREADS + tid;
+        if (!active) continue;
+        R taug, taur;
         if constexpr (sizeof(R) == 4) {
-            if (active && redo_from <= L)
-                redo_cells_fp64(P, C64, scr + tid, NS, col, g, ib, igb, fused, cossza, tab64, albp, albd, redo_from);
+            int js;
+            float fs;
+            taumol_generic(ib, igb, lay, C, tab, taug, taur, js, fs);
+        } else {
+            taumol_g<R>(ib, igb, lay, C, tab, taug, taur);
         }
-
-        // ---------------- pass 2: top -> bottom, level fluxes and g sums
-        R tdbtc = R(1), tdnc = R(1), rdndc = R(0);
-        R tdbt = R(1), tdn = R(1), rdnd = R(0);
-        R tdbtcn = R(1), tdbtn = R(1);
-        // FP32 form: absorption of the layer above the current level, less
-        // the part that its lower face's upward flux still has to add
-        R absc = R(0), abst = R(0), adifc_up = R(0), adift_up = R(0);
-        for (int jk = 1; jk <= L + 1; ++jk) {
-            R q[NQ_MAX];
-#pragma unroll
-            for (int i = 0; i < NQ_MAX; ++i) q[i] = R(0);
-            R refc = R(0), refdc = R(0), trac = R(0), tradc = R(0), dbtc = R(0), rupc, rupdc;
-            R ref = R(0), refd = R(0), tra = R(0), trad = R(0), dbt = R(0), rup, rupd, dbtcn = R(0), dbtn = R(0);
-            R adirc = R(0), adifc = R(0), adirt = R(0), adift = R(0);
-            if (jk <= L) {
-                const R* sv = scr + (size_t)(jk - 1) * NS * CTA_THREADS + tid;
-                refc = sv[S_REFC * CTA_THREADS]; refdc = sv[S_REFDC * CTA_THREADS];
-                trac = sv[S_TRAC * CTA_THREADS]; tradc = sv[S_TRADC * CTA_THREADS];
-                dbtc = sv[S_DBTC * CTA_THREADS];
-                rupc = sv[S_RUPC * CTA_THREADS]; rupdc = sv[S_RUPDC * CTA_THREADS];
-                ref = sv[S_REF * CTA_THREADS]; refd = sv[S_REFD * CTA_THREADS];
-                tra = sv[S_TRA * CTA_THREADS]; trad = sv[S_TRAD * CTA_THREADS];
-                dbt = sv[S_DBT * CTA_THREADS];
-                if constexpr (sizeof(R) == 4) {
-                    adirc = trac; adifc = tradc; adirt = tra; adift = trad;
-                    trac = R(1) - refc - adirc;
-                    tradc = R(1) - refdc - adifc;
-                    tra = R(1) - ref - adirt;
-                    trad = R(1) - refd - adift;
-                }
-                rup = sv[S_RUP * CTA_THREADS]; rupd = sv[S_RUPD * CTA_THREADS];
-                if (P.idelm == 0) { dbtcn = sv[S_DBTCN * CTA_THREADS]; dbtn = sv[S_DBTN * CTA_THREADS]; }
-            } else {
-                rupc = albp; rupdc = albd; rup = albp; rupd = albd;
-            }
-            if (active) {
-                // level fluxes (vrtqdr:163-169)
-                const R zrc = R(1) / (R(1) - rdndc * rupdc);
-                const R cu = (tdbtc * rupc + (tdnc - tdbtc) * rupdc) * zrc;
-                const R cdif = (tdnc - tdbtc + tdbtc * rupc * rdndc) * zrc;
-                const R cd = tdbtc + cdif;
-                const R zrt = R(1) / (R(1) - rdnd * rupd);
-                const R fu = (tdbt * rup + (tdn - tdbt) * rupd) * zrt;
-                const R fdif = (tdn - tdbt + tdbt * rup * rdnd) * zrt;
-                const R fd = tdbt + fdif;
-                if constexpr (sizeof(R) == 4) {
-                    // layer jk-1 absorbs what enters it: the direct and diffuse
-                    // beams at its top (kept from the previous level) and the
-                    // upward flux at its bottom face, this level
-                    q[6] = zinc * (abst + fu * adift_up);
-                    q[7] = zinc * (absc + cu * adifc_up);
-                    abst = tdbt * adirt + fdif * adift;
-                    absc = tdbtc * adirc + cdif * adifc;
-                    adift_up = adift;
-                    adifc_up = adifc;
-                }
-                const R dirf = P.idelm == 0 ? tdbtn : tdbt;
-                const R dirc = P.idelm == 0 ? tdbtcn : tdbtc;
-                q[0] = zinc * fu;
-                q[1] = zinc * fd;
-                q[2] = zinc * cu;
-                q[3] = zinc * cd;
-                q[4] = zinc * dirf;
-                q[5] = zinc * dirc;
-                if (P.extra) {
-                    if (uv) { q[QX] = q[1]; q[QX + 1] = q[3]; q[QX + 2] = q[4]; q[QX + 3] = q[5]; }
-                    else { q[QX + 4] = q[1]; q[QX + 5] = q[3]; q[QX + 6] = q[4]; q[QX + 7] = q[5]; }
-                }
-                if (jk <= L) {
-                    // downward recurrences (vrtqdr:144-159) and direct beam (spcvmc:575-585)
-                    const R zr1 = R(1) / (R(1) - refdc * rdndc);
-                    const R tdnc_n = tdbtc * trac + (tradc * ((tdnc - tdbtc) + tdbtc * refc * rdndc)) * zr1;
-                    rdndc = refdc + tradc * tradc * rdndc * zr1;
-                    tdnc = tdnc_n;
-                    const R zr2 = R(1) / (R(1) - refd * rdnd);
-                    const R tdn_n = tdbt * tra + (trad * ((tdn - tdbt) + tdbt * ref * rdnd)) * zr2;
-                    rdnd = refd + trad * trad * rdnd * zr2;
-                    tdn = tdn_n;
-                    tdbtc = dbtc * tdbtc;
-                    tdbt = dbt * tdbt;
-                    tdbtcn = dbtcn * tdbtcn;
-                    tdbtn = dbtn * tdbtn;
-                }
-            }
-            const int slot = (jk - 1) % KLEV;
-#pragma unroll
-            for (int i = 0; i < NQ_MAX; ++i)
-                if (i < NQ) sRed[(slot * NQ + i) * CTA_THREADS + tid] = q[i];
-            if (slot == KLEV - 1 || jk == L + 1) {
-                __syncthreads();
-                const int nlev = slot + 1;
-                const int items = COLS_PER_CTA * NQ * nlev;
-                for (int base = 0; base < items * 4; base += CTA_THREADS) {
-                    const int t = base + tid;
-                    const int item = t >> 2, part = t & 3;
-                    R v = R(0);
-                    int c2 = 0, qi = 0, s = 0;
-                    if (item < items) {
-                        c2 = item / (NQ * nlev);
-                        qi = (item / nlev) % NQ;
-                        s = item % nlev;
-                        const R* src = sRed + (s * NQ + qi) * CTA_THREADS + c2 * NGPT + part * 28;
-                        for (int j = 0; j < 28; ++j) v += src[j];
-                    }
-                    warp_sum4(v);
-                    if (item < items && part == 0) {
-                        const int jl = jk - slot + s;  // level (1 = top)
-                        sFlux[(c2 * NQ + qi) * (L + 1) + (L + 1 - jl)] = v;
-                    }
-                }
-                if (P.bands) {
-                    // per-band sums of fu, fd, fddir, cu, cd (spcvmc:619-630 per band)
-                    const int bitems = COLS_PER_CTA * NBND * 5 * nlev;
-                    for (int t = tid; t < bitems; t += CTA_THREADS) {
-                        const int s = t % nlev, qs = (t / nlev) % 5, b = (t / (nlev * 5)) % NBND;
-                        const int c2 = t / (nlev * 5 * NBND);
-                        const int qi = qs == 0 ? 0 : qs == 1 ? 1 : qs == 2 ? 4 : qs == 3 ? 2 : 3;
-                        const R* src = sRed + (s * NQ + qi) * CTA_THREADS + c2 * NGPT + cT.b[b].g0;
-                        R v = R(0);
-                        for (int j = 0; j < cT.b[b].ng; ++j) v += src[j];
-                        const int ocol = COLS_PER_CTA * pair + c2;
-                        const int l = L + 1 - (jk - slot + s);  // level index, 0 = surface
-                        if (ocol < P.ncol && P.bout[qs])
-                            P.bout[qs][(size_t)ocol + n * ((size_t)l + (size_t)(L + 1) * b)] = (double)v;
-                    }
-                }
-                __syncthreads();
+        CellIn<R> ci;
+        ci.taug = taug;
+        ci.taur = taur;
+        if (aer_stage) {
+            ci.rta = aer[(0 * NBND + ib) * L + lay - 1];
+            ci.rcoa = aer[(1 * NBND + ib) * L + lay - 1];
+            ci.roa = R(1) - ci.rcoa;
+            ci.rga = aer[(2 * NBND + ib) * L + lay - 1];
+        } else {
+            aerosol_in(P, col, lay, ib, tab64, ci);
+        }
+        // cloud of this subcolumn (McICA) at this layer
+        bool cloudy = false;
+        if (P.icld >= 1 && fused)
+            cloudy = mc.step(lay, sKc[cc * L + lay - 1], sKa[cc * L + lay - 1], sOmcf[cc * L + lay - 1]);
+        cloud_in<R>(P, col, g, lay, ib, fused, cloudy, cld, ci, tab);
+        const R hrs = zinc * sHrf[cc * L + lay - 1];
+        const CellOpt<R> co = cell_optics<R>(ci, P.idelm, prmu0, tab, tab64, hrs);
+        // FP32 form: a table entry, the conservative switch or the
+        // resonance of this cell is too close to call in FP32; it is
+        // marked in the scratch (S_DBTC < 0, -2 if cloudy) and redone
+        // after this pass as the FP64 form does
+        int redo = 0;
+        if constexpr (sizeof(R) == 4) {
+            if (co.risky) {
+                redo = ci.cloudy ? 2 : 1;
+                if (lay < redo_from) redo_from = lay;
             }
         }
+        const RT<R>& rc = co.rc;
+        const RT<R>& rt = co.rt;
+        const R zdbtc = co.zdbtc, zdbt = co.zdbt;
+        if (P.idelm == 0) {
+            sv[S_DBTCN * CTA_THREADS] = co.dbtcn;
+            sv[S_DBTN * CTA_THREADS] = co.dbtn;
+        }
+        // upward adding recurrence (vrtqdr:122-140)
+        {
+            const R zr = R(1) / (R(1) - rupdc_b * rc.refd);
+            const R rupc = rc.ref + (rc.trad * ((rc.tra - zdbtc) * rupdc_b + zdbtc * rupc_b)) * zr;
+            const R rupdc = rc.refd + rc.trad * rc.trad * rupdc_b * zr;
+            rupc_b = rupc;
+            rupdc_b = rupdc;
+        }
+        {
+            const R zr = R(1) / (R(1) - rupd_b * rt.refd);
+            const R rup = rt.ref + (rt.trad * ((rt.tra - zdbt) * rupd_b + zdbt * rup_b)) * zr;
+            const R rupd = rt.refd + rt.trad * rt.trad * rupd_b * zr;
+            rup_b = rup;
+            rupd_b = rupd;
+        }
+        // the FP32 form keeps the absorptances in the transmittance slots
+        // and rebuilds ptra = 1 - pref - adir, ptrad = 1 - prefd - adif
+        constexpr bool keep_abs = sizeof(R) == 4;
+        sv[S_REFC * CTA_THREADS] = rc.ref;
+        sv[S_REFDC * CTA_THREADS] = rc.refd;
+        sv[S_TRAC * CTA_THREADS] = keep_abs ? rc.adir : rc.tra;
+        sv[S_TRADC * CTA_THREADS] = keep_abs ? rc.adif : rc.trad;
+        sv[S_DBTC * CTA_THREADS] = redo ? -(R)redo : zdbtc;
+        sv[S_RUPC * CTA_THREADS] = rupc_b;
+        sv[S_RUPDC * CTA_THREADS] = rupdc_b;
+        sv[S_REF * CTA_THREADS] = rt.ref;
+        sv[S_REFD * CTA_THREADS] = rt.refd;
+        sv[S_TRA * CTA_THREADS] = keep_abs ? rt.adir : rt.tra;
+        sv[S_TRAD * CTA_THREADS] = keep_abs ? rt.adif : rt.trad;
+        sv[S_DBT * CTA_THREADS] = zdbt;
+        sv[S_RUP * CTA_THREADS] = rup_b;
+        sv[S_RUPD * CTA_THREADS] = rupd_b;
+    }
 
-        // ---------------- outputs (level 0 = surface)
-        for (int it = tid; it < COLS_PER_CTA * (L + 1); it += CTA_THREADS) {
-            const int c2 = it / (L + 1), l = it % (L + 1);
-            const int ocol = COLS_PER_CTA * pair + c2;
-            if (ocol >= P.ncol) continue;
-            const R* F = sFlux + c2 * NQ * (L + 1);
-            const size_t o = (size_t)ocol + n * (size_t)l;
-            const double fu = (double)F[0 * (L + 1) + l], fd = (double)F[1 * (L + 1) + l];
-            const double cu = (double)F[2 * (L + 1) + l], cd = (double)F[3 * (L + 1) + l];
-            P.swuflx[o] = fu;
-            P.swdflx[o] = fd;
-            P.swuflxc[o] = cu;
-            P.swdflxc[o] = cd;
-            if (l < L) {
-                const double* pdp = sPdp + c2 * L;
-                double hr = 0.0, hrc = 0.0;
-                if (l < L - 1) {
-                    const double zdpgcp = cT.heatfac / pdp[l];
-                    if constexpr (sizeof(R) == 4) {
-                        // summed layer absorption (= net-flux divergence)
-                        hr = (double)F[6 * (L + 1) + l] * zdpgcp;
-                        hrc = (double)F[7 * (L + 1) + l] * zdpgcp;
-                    } else {
-                        const double fu1 = (double)F[0 * (L + 1) + l + 1], fd1 = (double)F[1 * (L + 1) + l + 1];
-                        const double cu1 = (double)F[2 * (L + 1) + l + 1], cd1 = (double)F[3 * (L + 1) + l + 1];
-                        hrc = DM(DS(DS(cd1, cu1), DS(cd, cu)), zdpgcp);
-                        hr = DM(DS(DS(fd1, fu1), DS(fd, fu)), zdpgcp);
-                    }
-                }
-                P.swhr[o] = hr;
-                P.swhrc[o] = hrc;
+    if constexpr (sizeof(R) == 4) {
+        if (active && redo_from <= L)
+            redo_cells_fp64(P, C64, scr + tid, NS, col, g, ib, igb, fused, cossza, tab64, albp, albd, redo_from);
+    }
+
+    // ---------------- pass 2: top -> bottom, level fluxes and g sums
+    R tdbtc = R(1), tdnc = R(1), rdndc = R(0);
+    R tdbt = R(1), tdn = R(1), rdnd = R(0);
+    R tdbtcn = R(1), tdbtn = R(1);
+    // FP32 form: absorption of the layer above the current level, less
+    // the part that its lower face's upward flux still has to add
+    R absc = R(0), abst = R(0), adifc_up = R(0), adift_up = R(0);
+    for (int jk = 1; jk <= L + 1; ++jk) {
+        R q[NQ_MAX];
+#pragma unroll
+        for (int i = 0; i < NQ_MAX; ++i) q[i] = R(0);
+        R refc = R(0), refdc = R(0), trac = R(0), tradc = R(0), dbtc = R(0), rupc, rupdc;
+        R ref = R(0), refd = R(0), tra = R(0), trad = R(0), dbt = R(0), rup, rupd, dbtcn = R(0), dbtn = R(0);
+        R adirc = R(0), adifc = R(0), adirt = R(0), adift = R(0);
+        if (jk <= L) {
+            const R* sv = scr + (size_t)(jk - 1) * NS * CTA_THREADS + tid;
+            refc = sv[S_REFC * CTA_THREADS]; refdc = sv[S_REFDC * CTA_THREADS];
+            trac = sv[S_TRAC * CTA_THREADS]; tradc = sv[S_TRADC * CTA_THREADS];
+            dbtc = sv[S_DBTC * CTA_THREADS];
+            rupc = sv[S_RUPC * CTA_THREADS]; rupdc = sv[S_RUPDC * CTA_THREADS];
+            ref = sv[S_REF * CTA_THREADS]; refd = sv[S_REFD * CTA_THREADS];
+            tra = sv[S_TRA * CTA_THREADS]; trad = sv[S_TRAD * CTA_THREADS];
+            dbt = sv[S_DBT * CTA_THREADS];
+            if constexpr (sizeof(R) == 4) {
+                adirc = trac; adifc = tradc; adirt = tra; adift = trad;
+                trac = R(1) - refc - adirc;
+                tradc = R(1) - refdc - adifc;
+                tra = R(1) - ref - adirt;
+                trad = R(1) - refd - adift;
             }
+            rup = sv[S_RUP * CTA_THREADS]; rupd = sv[S_RUPD * CTA_THREADS];
+            if (P.idelm == 0) { dbtcn = sv[S_DBTCN * CTA_THREADS]; dbtn = sv[S_DBTN * CTA_THREADS]; }
+        } else {
+            rupc = albp; rupdc = albd; rup = albp; rupd = albd;
+        }
+        if (active) {
+            // level fluxes (vrtqdr:163-169)
+            const R zrc = R(1) / (R(1) - rdndc * rupdc);
+            const R cu = (tdbtc * rupc + (tdnc - tdbtc) * rupdc) * zrc;
+            const R cdif = (tdnc - tdbtc + tdbtc * rupc * rdndc) * zrc;
+            const R cd = tdbtc + cdif;
+            const R zrt = R(1) / (R(1) - rdnd * rupd);
+            const R fu = (tdbt * rup + (tdn - tdbt) * rupd) * zrt;
+            const R fdif = (tdn - tdbt + tdbt * rup * rdnd) * zrt;
+            const R fd = tdbt + fdif;
+            if constexpr (sizeof(R) == 4) {
+                // layer jk-1 absorbs what enters it: the direct and diffuse
+                // beams at its top (kept from the previous level) and the
+                // upward flux at its bottom face, this level
+                q[6] = zinc * (abst + fu * adift_up);
+                q[7] = zinc * (absc + cu * adifc_up);
+                abst = tdbt * adirt + fdif * adift;
+                absc = tdbtc * adirc + cdif * adifc;
+                adift_up = adift;
+                adifc_up = adifc;
+            }
+            const R dirf = P.idelm == 0 ? tdbtn : tdbt;
+            const R dirc = P.idelm == 0 ? tdbtcn : tdbtc;
+            q[0] = zinc * fu;
+            q[1] = zinc * fd;
+            q[2] = zinc * cu;
+            q[3] = zinc * cd;
+            q[4] = zinc * dirf;
+            q[5] = zinc * dirc;
             if (P.extra) {
-                const double fddir = (double)F[4 * (L + 1) + l];
-                const double uvfd = (double)F[(QX + 0) * (L + 1) + l], uvfddir = (double)F[(QX + 2) * (L + 1) + l];
-                const double nifd = (double)F[(QX + 4) * (L + 1) + l], nifddir = (double)F[(QX + 6) * (L + 1) + l];
-                const double vals[8] = {fddir, DS(fd, fddir), uvfd, nifd, uvfddir, DS(uvfd, uvfddir), nifddir,
-                                        DS(nifd, nifddir)};
-                for (int x = 0; x < 8; ++x)
-                    if (P.xout[x]) P.xout[x][o] = vals[x];
+                if (uv) { q[QX] = q[1]; q[QX + 1] = q[3]; q[QX + 2] = q[4]; q[QX + 3] = q[5]; }
+                else { q[QX + 4] = q[1]; q[QX + 5] = q[3]; q[QX + 6] = q[4]; q[QX + 7] = q[5]; }
             }
+            if (jk <= L) {
+                // downward recurrences (vrtqdr:144-159) and direct beam (spcvmc:575-585)
+                const R zr1 = R(1) / (R(1) - refdc * rdndc);
+                const R tdnc_n = tdbtc * trac + (tradc * ((tdnc - tdbtc) + tdbtc * refc * rdndc)) * zr1;
+                rdndc = refdc + tradc * tradc * rdndc * zr1;
+                tdnc = tdnc_n;
+                const R zr2 = R(1) / (R(1) - refd * rdnd);
+                const R tdn_n = tdbt * tra + (trad * ((tdn - tdbt) + tdbt * ref * rdnd)) * zr2;
+                rdnd = refd + trad * trad * rdnd * zr2;
+                tdn = tdn_n;
+                tdbtc = dbtc * tdbtc;
+                tdbt = dbt * tdbt;
+                tdbtcn = dbtcn * tdbtcn;
+                tdbtn = dbtn * tdbtn;
+            }
+        }
+        const int slot = (jk - 1) % KLEV;
+#pragma unroll
+        for (int i = 0; i < NQ_MAX; ++i)
+            if (i < NQ) sRed[(slot * NQ + i) * CTA_THREADS + tid] = q[i];
+        if (slot == KLEV - 1 || jk == L + 1) {
+            __syncthreads();
+            const int nlev = slot + 1;
+            const int items = COLS_PER_CTA * NQ * nlev;
+            for (int base = 0; base < items * 4; base += CTA_THREADS) {
+                const int t = base + tid;
+                const int item = t >> 2, part = t & 3;
+                R v = R(0);
+                int c2 = 0, qi = 0, s = 0;
+                if (item < items) {
+                    c2 = item / (NQ * nlev);
+                    qi = (item / nlev) % NQ;
+                    s = item % nlev;
+                    const R* src = sRed + (s * NQ + qi) * CTA_THREADS + c2 * NGPT + part * 28;
+                    for (int j = 0; j < 28; ++j) v += src[j];
+                }
+                warp_sum4(v);
+                if (item < items && part == 0) {
+                    const int jl = jk - slot + s;  // level (1 = top)
+                    sFlux[(c2 * NQ + qi) * (L + 1) + (L + 1 - jl)] = v;
+                }
+            }
+            if (P.bands) {
+                // per-band sums of fu, fd, fddir, cu, cd (spcvmc:619-630 per band)
+                const int bitems = COLS_PER_CTA * NBND * 5 * nlev;
+                for (int t = tid; t < bitems; t += CTA_THREADS) {
+                    const int s = t % nlev, qs = (t / nlev) % 5, b = (t / (nlev * 5)) % NBND;
+                    const int c2 = t / (nlev * 5 * NBND);
+                    const int qi = qs == 0 ? 0 : qs == 1 ? 1 : qs == 2 ? 4 : qs == 3 ? 2 : 3;
+                    const R* src = sRed + (s * NQ + qi) * CTA_THREADS + c2 * NGPT + cT.b[b].g0;
+                    R v = R(0);
+                    for (int j = 0; j < cT.b[b].ng; ++j) v += src[j];
+                    const int ocol = pair_col(P, pair, c2, nmapped);
+                    const int l = L + 1 - (jk - slot + s);  // level index, 0 = surface
+                    if (ocol < P.ncol && P.bout[qs])
+                        P.bout[qs][(size_t)ocol + n * ((size_t)l + (size_t)(L + 1) * b)] = (double)v;
+                }
+            }
+            __syncthreads();
         }
     }
+
+    // ---------------- outputs (level 0 = surface)
+    for (int it = tid; it < COLS_PER_CTA * (L + 1); it += CTA_THREADS) {
+        const int c2 = it / (L + 1), l = it % (L + 1);
+        const int ocol = pair_col(P, pair, c2, nmapped);
+        if (ocol >= P.ncol) continue;
+        const R* F = sFlux + c2 * NQ * (L + 1);
+        const size_t o = (size_t)ocol + n * (size_t)l;
+        const double fu = (double)F[0 * (L + 1) + l], fd = (double)F[1 * (L + 1) + l];
+        const double cu = (double)F[2 * (L + 1) + l], cd = (double)F[3 * (L + 1) + l];
+        P.swuflx[o] = fu;
+        P.swdflx[o] = fd;
+        P.swuflxc[o] = cu;
+        P.swdflxc[o] = cd;
+        if (l < L) {
+            const double* pdp = sPdp + c2 * L;
+            double hr = 0.0, hrc = 0.0;
+            if (l < L - 1) {
+                const double zdpgcp = cT.heatfac / pdp[l];
+                if constexpr (sizeof(R) == 4) {
+                    // summed layer absorption (= net-flux divergence)
+                    hr = (double)F[6 * (L + 1) + l] * zdpgcp;
+                    hrc = (double)F[7 * (L + 1) + l] * zdpgcp;
+                } else {
+                    const double fu1 = (double)F[0 * (L + 1) + l + 1], fd1 = (double)F[1 * (L + 1) + l + 1];
+                    const double cu1 = (double)F[2 * (L + 1) + l + 1], cd1 = (double)F[3 * (L + 1) + l + 1];
+                    hrc = DM(DS(DS(cd1, cu1), DS(cd, cu)), zdpgcp);
+                    hr = DM(DS(DS(fd1, fu1), DS(fd, fu)), zdpgcp);
+                }
+            }
+            P.swhr[o] = hr;
+            P.swhrc[o] = hrc;
+        }
+        if (P.extra) {
+            const double fddir = (double)F[4 * (L + 1) + l];
+            const double uvfd = (double)F[(QX + 0) * (L + 1) + l], uvfddir = (double)F[(QX + 2) * (L + 1) + l];
+            const double nifd = (double)F[(QX + 4) * (L + 1) + l], nifddir = (double)F[(QX + 6) * (L + 1) + l];
+            const double vals[8] = {fddir, DS(fd, fddir), uvfd, nifd, uvfddir, DS(uvfd, uvfddir), nifddir,
+                                    DS(nifd, nifddir)};
+            for (int x = 0; x < 8; ++x)
+                if (P.xout[x]) P.xout[x][o] = vals[x];
+        }
+    }
+
+}
+
+template <typename R>
+__global__ void __launch_bounds__(CTA_THREADS, 2)
+k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict__ tab64) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const CtaView<R> V = cta_view<R>(smem_raw, P);
+    const KissJump J = kiss_setup(P, V.sXs);  // once per launch
+    R* scr = (R*)P.scratch + (size_t)blockIdx.x * P.slot_elems;
+    for (int pair = blockIdx.x; pair < P.npairs; pair += gridDim.x) solve_pair<R>(P, pair, V, J, scr, tab, tab64);
+}
+
+// ------------------------------------------------------------------ batch
+// Many independent instances (ncol and nlay differ) in one persistent
+// launch.  Each instance's sunlit columns were listed by k_compact; the work
+// items are the column pairs of those lists, instance after instance, and a
+// CTA takes every gridDim.x-th item.  The parameters of the instance at hand
+// are copied to shared memory when the CTA moves to a new instance.
+
+template <typename R>
+__global__ void __launch_bounds__(CTA_THREADS, 2)
+k_solve_batch(const SolveParams* __restrict__ Pb, int ninst, const int* __restrict__ counts,
+              const R* __restrict__ tab, const double* __restrict__ tab64) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_pref[MAX_BATCH + 1];
+    __shared__ __align__(16) SolveParams sP;
+    if (threadIdx.x == 0) {
+        s_pref[0] = 0;
+        for (int i = 0; i < ninst; ++i) s_pref[i + 1] = s_pref[i] + (counts[i] + COLS_PER_CTA - 1) / COLS_PER_CTA;
+    }
+    __syncthreads();
+    const int total = s_pref[ninst];
+    int cur = -1;
+    CtaView<R> V{};
+    KissJump J{1u, 0u, 1u, 1u};
+    for (int item = blockIdx.x; item < total; item += gridDim.x) {
+        int lo = 0, hi = ninst;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) / 2;
+            if (s_pref[mid] <= item) lo = mid;
+            else hi = mid;
+        }
+        if (lo != cur) {
+            __syncthreads();  // the previous instance's shared data is no longer read
+            {
+                const int* src = (const int*)(Pb + lo);
+                int* dst = (int*)&sP;
+                for (int w = threadIdx.x; w < (int)(sizeof(SolveParams) / sizeof(int)); w += CTA_THREADS) dst[w] = src[w];
+            }
+            __syncthreads();
+            V = cta_view<R>(smem_raw, sP);
+            J = kiss_setup(sP, V.sXs);
+            cur = lo;
+        }
+        R* scr = (R*)sP.scratch + (size_t)blockIdx.x * sP.slot_elems;
+        solve_pair<R>(sP, item - s_pref[lo], V, J, scr, tab, tab64);
+    }
+}
+
+// Sunlit-column compaction of one instance per CTA: the columns with
+// coszen > 0, in order, go to map[0 .. count); the outputs of the others
+// (night columns, which the reference solves with mu0 clamped to 1e-10 and
+// which come out at 1e-10 of a daytime flux) are set to zero.
+static __global__ void __launch_bounds__(1024)
+k_compact(const SolveParams* __restrict__ Pb, int* __restrict__ map_all, const long long* __restrict__ map_off,
+          int* __restrict__ counts) {
+    __shared__ int s_warp[32];
+    __shared__ int s_base;
+    const SolveParams& P = Pb[blockIdx.x];
+    int* map = map_all + map_off[blockIdx.x];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_base = 0;
+    __syncthreads();
+    const size_t n = (size_t)P.ncol, L = (size_t)P.nlay;
+    for (int c0 = 0; c0 < P.ncol; c0 += 1024) {
+        const int c = c0 + threadIdx.x;
+        const bool inb = c < P.ncol;
+        const bool sun = inb && P.coszen[c] > 0.0;
+        const unsigned m = __ballot_sync(0xffffffffu, sun);
+        if (lane == 0) s_warp[wid] = __popc(m);
+        __syncthreads();
+        int before = 0, tot = 0;
+        for (int w = 0; w < 32; ++w) {
+            if (w < wid) before += s_warp[w];
+            tot += s_warp[w];
+        }
+        const int rank = s_base + before + __popc(m & ((1u << lane) - 1u));
+        if (sun) map[rank] = c;
+        if (inb && !sun) {
+            for (size_t l = 0; l <= L; ++l) {
+                const size_t o = (size_t)c + n * l;
+                P.swuflx[o] = 0.0; P.swdflx[o] = 0.0; P.swuflxc[o] = 0.0; P.swdflxc[o] = 0.0;
+                for (int x = 0; x < 8; ++x)
+                    if (P.xout[x]) P.xout[x][o] = 0.0;
+                for (int q = 0; q < 5; ++q)
+                    if (P.bout[q])
+                        for (int b = 0; b < NBND; ++b) P.bout[q][o + n * (L + 1) * (size_t)b] = 0.0;
+                if (l < L) { P.swhr[o] = 0.0; P.swhrc[o] = 0.0; }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_base += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) counts[blockIdx.x] = s_base;
 }
 
 }  // namespace rrsw

@@ -23,6 +23,18 @@ cudaError_t upload_tables_fp32(const DevTables& t);
 LaunchInfo plan_fp32(const SolveParams& P, int num_sms);
 cudaError_t launch_solve_fp32(const SolveParams& P, const float* tab, const double* tab64, const LaunchInfo& li,
                               cudaStream_t s);
+// batch of instances (device array of SolveParams, sunlit lists built by
+// launch_compact); smem is the largest instance's dynamic shared memory
+cudaError_t launch_compact(const SolveParams* dPb, int n, int* map_all, const long long* map_off, int* counts,
+                           cudaStream_t s);
+size_t solve_smem_fp64(const SolveParams& P);
+size_t solve_smem_fp32(const SolveParams& P);
+int batch_blocks_per_sm_fp64(size_t smem);
+int batch_blocks_per_sm_fp32(size_t smem);
+cudaError_t launch_batch_fp64(const SolveParams* dPb, int n, const int* counts, const double* tab, int grid,
+                              size_t smem, cudaStream_t s);
+cudaError_t launch_batch_fp32(const SolveParams* dPb, int n, const int* counts, const float* tab,
+                              const double* tab64, int grid, size_t smem, cudaStream_t s);
 // scratch elements (of the form's type) per CTA slot
 size_t slot_elems(int nlay, int idelm, bool fp32);
 

@@ -42,6 +42,8 @@ struct SolveParams {
     double *xout[8];  // dirdflux, difdflux, uvdflx, nidflx, dirdnuv, difdnuv, dirdnir, difdnir
     int bands;        // 1: per-band fluxes requested
     double *bout[5];  // bndfu, bndfd, bndfddir, bndcu, bndcd (ncol,nlay+1,nbnd)
+    const int *colmap;   // batch: this instance's sunlit columns (nullptr: all columns in order)
+    const int *mapcount; // batch: number of entries of colmap (device)
     void *scratch;
     size_t slot_elems;
     int *err;

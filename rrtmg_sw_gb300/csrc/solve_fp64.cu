@@ -34,6 +34,30 @@ cudaError_t launch_solve_fp64(const SolveParams& P, const double* tab, const Lau
     return cudaGetLastError();
 }
 
+cudaError_t launch_compact(const SolveParams* dPb, int n, int* map_all, const long long* map_off, int* counts,
+                           cudaStream_t s) {
+    k_compact<<<n, 1024, 0, s>>>(dPb, map_all, map_off, counts);
+    return cudaGetLastError();
+}
+
+size_t solve_smem_fp64(const SolveParams& P) {
+    return smem_layout(P.nlay, num_q<double>(P.extra != 0), stages_clouds(P), stage_aerosol<double>(P.iaer),
+                       sizeof(double)).total;
+}
+
+int batch_blocks_per_sm_fp64(size_t smem) {
+    cudaFuncSetAttribute(k_solve_batch<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_batch<double>, CTA_THREADS, smem);
+    return per_sm;
+}
+
+cudaError_t launch_batch_fp64(const SolveParams* dPb, int n, const int* counts, const double* tab, int grid,
+                              size_t smem, cudaStream_t s) {
+    k_solve_batch<double><<<grid, CTA_THREADS, smem, s>>>(dPb, n, counts, tab, tab);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ get_alpha
 // mcica_subcol_gen_sw.f90:119-176, one thread per column (the layer loop
 // is sequential in the reference only through alpha(i,1) = 0).

@@ -84,6 +84,12 @@ def lib():
         L.rrtmg_sw_mcica_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds)]
         L.rrtmg_sw_mcica_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_void_p]
         L.rrtmg_sw_nomcica_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds)]
+        L.rrtmg_sw_batch_plan_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_int32, C.c_void_p,
+                                            C.POINTER(C.c_void_p)]
+        L.rrtmg_sw_batch_run_c.argtypes = [C.c_void_p, C.c_void_p]
+        L.rrtmg_sw_batch_info_c.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                            C.POINTER(C.c_float), C.POINTER(C.c_int32)]
+        L.rrtmg_sw_batch_free_c.argtypes = [C.c_void_p]
         L.rrtmg_sw_nomcica_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_void_p]
         L.rrtmg_sw_static_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_void_p]
         L.mcica_subcol_sw_c.argtypes = [C.c_int32] * 5 + [_dp] * 11 + [_dp] * 9
@@ -250,6 +256,41 @@ def rrtmg_sw_static_dev(args, stream=0, clouds=None):
     be in flight at once."""
     cp = C.byref(clouds) if clouds is not None else None
     _check(lib().rrtmg_sw_static_dev_c(C.byref(args), cp, C.c_void_p(stream)))
+
+
+class BatchPlan:
+    """A planned batch of device-pointer instances (rrtmg_sw_batch_plan_c):
+    ``args`` and ``clouds`` are lists of :class:`RrtmgSwArgs` /
+    :class:`RrtmgSwClouds` (clouds may be None for an all-clear batch)."""
+
+    def __init__(self, args, clouds=None, stream=0):
+        n = len(args)
+        self._a = (RrtmgSwArgs * n)(*args)
+        self._c = None
+        if clouds is not None:
+            self._c = (RrtmgSwClouds * n)(*[c if c is not None else RrtmgSwClouds() for c in clouds])
+        self.handle = C.c_void_p()
+        _check(lib().rrtmg_sw_batch_plan_c(self._a, self._c, n, C.c_void_p(stream), C.byref(self.handle)))
+
+    def run(self, stream=0):
+        _check(lib().rrtmg_sw_batch_run_c(self.handle, C.c_void_p(stream)))
+
+    def info(self):
+        grid, desc, nt = C.c_int32(), C.c_int32(), C.c_int32(16)
+        ms = (C.c_float * 16)()
+        _check(lib().rrtmg_sw_batch_info_c(self.handle, C.byref(grid), C.byref(desc), ms, C.byref(nt)))
+        return {"grid": grid.value, "deepest_first": bool(desc.value), "trial_ms": list(ms[:min(nt.value, 16)])}
+
+    def close(self):
+        if self.handle:
+            lib().rrtmg_sw_batch_free_c(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def last_launch_count():
