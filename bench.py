@@ -42,6 +42,9 @@ def parse():
     p.add_argument("--ncol", type=int, default=NCOL)
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--workload", default="fp32", choices=["fp32", "batch"],
+                   help="fp32: the FP32-form headline; batch: 48 ragged instances in one launch (FP64 form)")
+    p.add_argument("--instances", type=int, default=48)
     return p.parse_args()
 
 
@@ -167,10 +170,91 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_batch(args):
+    """48 ragged instances (ncol log-uniform in 512..131072, nlay from
+    {40,47,60,72,91,137}, 40 % night columns, McICA clouds icld=2 with
+    inflgsw=2/iceflgsw=3/liqflgsw=1, FP64 form) in one persistent launch
+    replayed from a CUDA graph; per-instance figures from single calls."""
+    import torch
+    from rrtmg_sw_gb300 import build, interface as gi
+    from rrtmg_sw_gb300.synthetic import make_columns
+    build.build()
+    gi.rrtmg_sw_ini(1.004e3)
+    gi.set_form(gi.FORM_FP64)
+    rng = np.random.default_rng(20261203 + 2)
+    dev = torch.device("cuda", 0)
+    ptr = lambda t: C.cast(C.c_void_p(t.data_ptr()), gi._dp)
+    insts = []
+    for i in range(args.instances):
+        ncol = int(round(np.exp(rng.uniform(np.log(512), np.log(131072)))))
+        nlay = int(rng.choice([40, 47, 60, 72, 91, 137]))
+        c = make_columns(ncol, nlay, 20261203 + 2 + 1000 * i, clouds=True, night_frac=0.4)
+        T = lambda x: torch.from_numpy(np.asfortranarray(x).ravel(order="F").copy()).to(dev)
+        t = {k: T(c[k]) for k in ("play", "plev", "tlay", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "o2vmr", "asdir",
+                                  "asdif", "aldir", "aldif", "coszen", "cldfrac", "ciwp", "clwp", "rei", "rel")}
+        for k in ("swuflx", "swdflx", "swuflxc", "swdflxc"):
+            t[k] = torch.empty(ncol * (nlay + 1), dtype=torch.float64, device=dev)
+        for k in ("swhr", "swhrc"):
+            t[k] = torch.empty(ncol * nlay, dtype=torch.float64, device=dev)
+        a = gi.RrtmgSwArgs()
+        a.ncol, a.nlay, a.icld, a.iaer = ncol, nlay, 2, 0
+        for k in ("play", "plev", "tlay", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "o2vmr", "asdir", "asdif", "aldir",
+                  "aldif", "coszen", "swuflx", "swdflx", "swuflxc", "swdflxc", "swhr", "swhrc"):
+            setattr(a, k, ptr(t[k]))
+        a.adjes, a.dyofyr, a.scon, a.isolvar = 1.0, 0, 1360.85, 0
+        a.inflgsw, a.iceflgsw, a.liqflgsw = 2, 3, 1
+        a.idelm = 1
+        cl = gi.RrtmgSwClouds()
+        cl.permuteseed, cl.irng = 112, 0
+        for k in ("cldfrac", "ciwp", "clwp", "rei", "rel"):
+            setattr(cl, k, ptr(t[k]))
+        insts.append(dict(t=t, a=a, c=cl, ncol=ncol, nlay=nlay, sunlit=int((c["coszen"] > 0).sum())))
+    stream = torch.cuda.current_stream(dev)
+    sid = stream.cuda_stream
+    plan = gi.BatchPlan([x["a"] for x in insts], [x["c"] for x in insts], stream=sid)
+    for _ in range(max(1, args.warmup - 1)):
+        plan.run(sid)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(1, args.steps // 5)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        plan.run(sid)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    sunlit = sum(x["sunlit"] for x in insts)
+    per = []
+    for x in insts:  # each instance alone through rrtmg_sw_mcica_dev_c
+        gi.rrtmg_sw_dev(x["a"], sid, x["c"])
+        torch.cuda.synchronize()
+        e0.record(stream)
+        gi.rrtmg_sw_dev(x["a"], sid, x["c"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        m1 = e0.elapsed_time(e1)
+        per.append({"ncol": x["ncol"], "nlay": x["nlay"], "sunlit": x["sunlit"], "single_ms": m1,
+                    "single_columns_per_s": x["sunlit"] / (m1 / 1e3)})
+    info = plan.info()
+    plan.close()
+    line = {"metric": "sunlit columns/s, 48 ragged instances in one persistent launch (FP64 form)",
+            "value": sunlit / (ms / 1e3), "unit": "columns/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "%d instances, ncol log-uniform 512..131072, nlay in {40,47,60,72,91,137}, 40%% "
+                                   "night, McICA icld=2, FP64 form" % len(insts),
+                       "columns": sum(x["ncol"] for x in insts), "sunlit": sunlit},
+            "sum_of_single_calls_ms": sum(p["single_ms"] for p in per),
+            "autotuner": info, "instances": per}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
     import torch
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
