@@ -42,7 +42,7 @@ def parse():
     p.add_argument("--ncol", type=int, default=NCOL)
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--workload", default="fp32", choices=["fp32", "batch"],
+    p.add_argument("--workload", default="fp32", choices=["fp32", "batch", "adjoint"],
                    help="fp32: the FP32-form headline; batch: 48 ragged instances in one launch (FP64 form)")
     p.add_argument("--instances", type=int, default=48)
     return p.parse_args()
@@ -249,12 +249,63 @@ def run_batch(args):
     print(json.dumps(line))
 
 
+def run_adjoint(args):
+    """Adjoint cost: 65536 columns x 60 layers, McICA clouds (icld=2, masks
+    frozen), objective TOA up + surface net + heating-rate sum; forward,
+    tangent-linear and adjoint (stored / recomputed local Jacobians) through
+    the host-array C ABI, each timed end to end."""
+    from rrtmg_sw_gb300 import build, interface as gi
+    from rrtmg_sw_gb300.synthetic import gcm_inputs, make_columns
+    build.build()
+    gi.rrtmg_sw_ini(1.004e3)
+    gi.set_form(gi.FORM_FP64)
+    ncol = args.ncol if args.ncol != NCOL else 65536
+    c = make_columns(ncol, NLAY, 20261203 + 4, clouds=True)
+    kw = gcm_inputs(c, icld=2, iaer=0)
+    for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl", "taucmcl", "ssacmcl", "asmcmcl", "fsfcmcl"):
+        kw[k] = None  # fused McICA: the subcolumn arrays are not passed
+    cl = dict(permuteseed=112, irng=0, cldfrac=c["cldfrac"], ciwp=c["ciwp"], clwp=c["clwp"], rei=c["rei"],
+              rel=c["rel"])
+    w = (1.0, 1.0, 1.0)
+
+    def best(f, k=3):
+        f()
+        ts = []
+        for _ in range(k):
+            t0 = time.perf_counter()
+            f()
+            ts.append(time.perf_counter() - t0)
+        return min(ts) * 1e3
+
+    fwd = best(lambda: gi.rrtmg_sw(**kw, clouds=cl))
+    d = {k: np.ones_like(kw["tlay"]) for k in gi.AD_LAYER}
+    tl = best(lambda: gi.rrtmg_sw_tl(kw, d, cl, w))
+    ad_s = best(lambda: gi.rrtmg_sw_ad(kw, cl, w, store=True))
+    ad_r = best(lambda: gi.rrtmg_sw_ad(kw, cl, w, store=False))
+    sms = 152
+    try:
+        import torch
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        pass
+    slot = lambda fields: ((NLAY + 1) * fields * 224 + 2 * 15 * NLAY * 4) * 8
+    line = {"metric": "adjoint cost relative to the FP64 forward (host-array calls, end to end)",
+            "value": ad_s / fwd, "unit": "x forward", "n_gpus": 1, "higher_is_better": False,
+            "config": {"workload": "%d columns x %d layers, McICA icld=2, objective TOA up + sfc net + HR sum"
+                                   % (ncol, NLAY)},
+            "forward_fp64_ms": fwd, "tangent_linear_ms": tl, "adjoint_store_ms": ad_s, "adjoint_recompute_ms": ad_r,
+            "scratch_bytes_store": slot(45) * sms, "scratch_bytes_recompute": slot(20) * sms}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
     import torch
     rank, world, local = dist_env()
     torch.cuda.set_device(local)

@@ -146,6 +146,32 @@ int rrtmg_sw_mcica_dev_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, void 
 int rrtmg_sw_nomcica_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c);
 int rrtmg_sw_nomcica_dev_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, void *stream);
 
+/* Tangent-linear and adjoint (rrtmg_sw_tl / rrtmg_sw_ad; no counterpart in
+ * the reference).  Objective per column, total sky:
+ *   J = w_toa_up * swuflx(top) + w_sfc_net * (swdflx(sfc) - swuflx(sfc))
+ *     + w_hr_sum * (sum of swhr over layers 1 .. nlay-1)
+ * as a function of tlay, h2ovmr, o3vmr, the in-cloud water paths clwp and
+ * ciwp of the fused McICA clouds (subcolumn masks frozen: they depend on
+ * cldfrac and the seeds only) and the surface albedos.  The model is the
+ * FP64 form with exp(-x) in place of the nearest-entry transmittance table
+ * (whose derivative is zero almost everywhere); J is that model's value.
+ * Host arrays; c is the fused McICA cloud input (irng = 0) or NULL for
+ * clear sky (icld = 0).  rrtmg_sw_ad_c writes J and the gradient arrays
+ * (any may be NULL); rrtmg_sw_tl_c reads the same arrays as a direction and
+ * writes J and dJ = dJ/dx . direction.  store = 1 keeps each cell's local
+ * Jacobian from the forward pass (more memory), 0 recomputes it in the
+ * reverse pass. */
+typedef struct rrtmg_sw_ad_args {
+    double w_toa_up, w_sfc_net, w_hr_sum;
+    int32_t store, pad;
+    double *J;                                    /* (ncol) */
+    double *dJ;                                   /* (ncol), rrtmg_sw_tl_c */
+    double *tlay, *h2ovmr, *o3vmr, *clwp, *ciwp;  /* (ncol,nlay) gradients / direction */
+    double *asdir, *asdif, *aldir, *aldif;        /* (ncol) gradients / direction */
+} rrtmg_sw_ad_args;
+int rrtmg_sw_ad_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, const rrtmg_sw_ad_args *ad);
+int rrtmg_sw_tl_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, const rrtmg_sw_ad_args *ad);
+
 /* Batches: many independent rrtmg_sw calls (ncol and nlay may differ) in
  * one persistent launch.  a[0..n) and, for instances with icld >= 1, c[0..n)
  * (fused McICA, irng = 0; c may be NULL when every instance is clear) hold

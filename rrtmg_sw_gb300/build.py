@@ -21,6 +21,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relax
 UNITS = {
     "solve_fp64.cu": ["--fmad=false"],
     "solve_fp32.cu": ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
+    "solve_ad.cu": [],
     "api.cu": [],
 }
 

@@ -283,6 +283,7 @@ int upload(State& st) {
     CK(cudaMemcpy(st.d_tab32.p, b32.data(), b32.size() * sizeof(float), cudaMemcpyHostToDevice));
     CK(upload_tables_fp64(T));
     CK(upload_tables_fp32(T));
+    CK(upload_tables_ad(T));
     return RRTMG_SW_OK;
 }
 
@@ -653,6 +654,88 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
 }
 
 // ---------------------------------------------------------------------------
+// Tangent-linear / adjoint with host arrays (see solve_ad.cu).
+int solve_ad_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, const rrtmg_sw_ad_args* ad, bool tl) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (!a || !ad || a->ncol <= 0 || a->nlay < 4 || a->nlay > MAX_NLAY) return RRTMG_SW_EARGS;
+    const double* req[] = {a->play, a->plev, a->tlay, a->h2ovmr, a->o3vmr, a->co2vmr, a->ch4vmr, a->o2vmr,
+                           a->asdir, a->asdif, a->aldir, a->aldif, a->coszen};
+    for (const double* p : req)
+        if (!p) return RRTMG_SW_EARGS;
+    const int icld = (a->icld < 0 || a->icld > 5) ? 2 : a->icld;
+    if (icld >= 1 && !c) return RRTMG_SW_EARGS;
+    const size_t C = a->ncol, L = a->nlay, CL = C * L, CL1 = C * (L + 1);
+    cudaStream_t s = 0;
+    Stager sg{st, s};
+    rrtmg_sw_args d = *a;
+    d.play = sg.in("play", a->play, CL); d.plev = sg.in("plev", a->plev, CL1); d.tlay = sg.in("tlay", a->tlay, CL);
+    d.h2ovmr = sg.in("h2o", a->h2ovmr, CL); d.o3vmr = sg.in("o3", a->o3vmr, CL); d.co2vmr = sg.in("co2", a->co2vmr, CL);
+    d.ch4vmr = sg.in("ch4", a->ch4vmr, CL); d.o2vmr = sg.in("o2", a->o2vmr, CL);
+    d.asdir = sg.in("asdir", a->asdir, C); d.asdif = sg.in("asdif", a->asdif, C);
+    d.aldir = sg.in("aldir", a->aldir, C); d.aldif = sg.in("aldif", a->aldif, C);
+    d.coszen = sg.in("coszen", a->coszen, C);
+    d.tlev = nullptr; d.tsfc = nullptr; d.n2ovmr = nullptr;
+    if (a->iaer == 10) {
+        d.tauaer = sg.in("tauaer", a->tauaer, 14 * CL); d.ssaaer = sg.in("ssaaer", a->ssaaer, 14 * CL);
+        d.asmaer = sg.in("asmaer", a->asmaer, 14 * CL);
+    }
+    if (a->iaer == 6) d.ecaer = sg.in("ecaer", a->ecaer, 6 * CL);
+    rrtmg_sw_clouds dc{};
+    if (c && icld >= 1) {
+        dc = *c;
+        dc.cldfrac = sg.in("cldfrac", c->cldfrac, CL); dc.ciwp = sg.in("ciwp", c->ciwp, CL);
+        dc.clwp = sg.in("clwp", c->clwp, CL); dc.rei = sg.in("rei", c->rei, CL); dc.rel = sg.in("rel", c->rel, CL);
+        dc.tauc = sg.in("tauc", c->tauc, 14 * CL); dc.ssac = sg.in("ssac", c->ssac, 14 * CL);
+        dc.asmc = sg.in("asmc", c->asmc, 14 * CL); dc.fsfc = sg.in("fsfc", c->fsfc, 14 * CL);
+        dc.alpha = sg.in("alpha", c->alpha, CL);
+    }
+    // the flux outputs are not written; make_params only records them
+    AdParams A{};
+    A.w_toa = ad->w_toa_up; A.w_net = ad->w_sfc_net; A.w_hr = ad->w_hr_sum;
+    A.store = ad->store ? 1 : 0;
+    A.tl = tl ? 1 : 0;
+    A.J = sg.out("adJ", ad->J, C);
+    A.dJ = tl ? sg.out("addJ", ad->dJ, C) : nullptr;
+    double* gh[5] = {ad->tlay, ad->h2ovmr, ad->o3vmr, ad->clwp, ad->ciwp};
+    double* ah[4] = {ad->asdir, ad->asdif, ad->aldir, ad->aldif};
+    const char* gn[5] = {"adg0", "adg1", "adg2", "adg3", "adg4"};
+    const char* an[4] = {"ada0", "ada1", "ada2", "ada3"};
+    double* gd[5];
+    double* ad4[4];
+    for (int i = 0; i < 5; ++i) {
+        if (tl) { A.dir[i] = sg.in(gn[i], (const double*)gh[i], CL); gd[i] = nullptr; }
+        else { gd[i] = sg.out(gn[i], gh[i], CL); A.g[i] = gd[i]; }
+    }
+    for (int i = 0; i < 4; ++i) {
+        if (tl) { A.dira[i] = sg.in(an[i], (const double*)ah[i], C); ad4[i] = nullptr; }
+        else { ad4[i] = sg.out(an[i], ah[i], C); A.ga[i] = ad4[i]; }
+    }
+    if (sg.err != cudaSuccess) return cuda_fail(sg.err);
+    SolveParams P;
+    int rc = make_params(st, &d, (c && icld >= 1) ? &dc : nullptr, P);
+    if (rc) return rc;
+    CK(st.errw.ensure(sizeof(int)));
+    P.err = (int*)st.errw.p;
+    const int grid = adjoint_grid(P, st.num_sms);
+    P.slot_elems = adjoint_slot_elems(P.nlay, A.store);
+    CK(st.scratch.ensure((size_t)grid * P.slot_elems * sizeof(double)));
+    P.scratch = st.scratch.p;
+    CK(cudaMemsetAsync(P.err, 0, sizeof(int), s));
+    CK(launch_adjoint(P, A, (const double*)st.d_tab64.p, st.num_sms, nullptr, s));
+    st.last_launches = 1;
+    sg.back(ad->J, A.J, C);
+    if (tl) sg.back(ad->dJ, A.dJ, C);
+    for (int i = 0; i < 5 && !tl; ++i) sg.back(gh[i], gd[i], CL);
+    for (int i = 0; i < 4 && !tl; ++i) sg.back(ah[i], ad4[i], C);
+    CK(cudaMemcpyAsync(st.h_err, P.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (sg.err != cudaSuccess) return cuda_fail(sg.err);
+    CK(cudaStreamSynchronize(s));
+    return *st.h_err;
+}
+
+// ---------------------------------------------------------------------------
 // Batch plans: many instances in one persistent launch (k_compact + k_solve_batch),
 // captured once in a CUDA graph and replayed.
 struct BatchPlan {
@@ -984,6 +1067,14 @@ const char* rrtmg_sw_errstr_c(int32_t code) {
 }
 
 const char* rrtmg_sw_last_cuda_error_c(void) { return S().last_cuda.c_str(); }
+
+int rrtmg_sw_ad_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, const rrtmg_sw_ad_args* ad) {
+    return solve_ad_host(a, c, ad, false);
+}
+
+int rrtmg_sw_tl_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, const rrtmg_sw_ad_args* ad) {
+    return solve_ad_host(a, c, ad, true);
+}
 
 int rrtmg_sw_batch_plan_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, int32_t n, void* stream, void** plan) {
     State& st = S();

@@ -35,6 +35,12 @@ cudaError_t launch_batch_fp64(const SolveParams* dPb, int n, const int* counts, 
                               size_t smem, cudaStream_t s);
 cudaError_t launch_batch_fp32(const SolveParams* dPb, int n, const int* counts, const float* tab,
                               const double* tab64, int grid, size_t smem, cudaStream_t s);
+// tangent-linear / adjoint (solve_ad.cu)
+cudaError_t upload_tables_ad(const DevTables& t);
+size_t adjoint_slot_elems(int nlay, int store);
+int adjoint_grid(const SolveParams& P, int num_sms);
+cudaError_t launch_adjoint(const SolveParams& P, const AdParams& A, const double* tab64, int num_sms, int* grid_out,
+                           cudaStream_t s);
 // scratch elements (of the form's type) per CTA slot
 size_t slot_elems(int nlay, int idelm, bool fp32);
 

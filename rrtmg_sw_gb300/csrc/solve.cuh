@@ -49,6 +49,20 @@ struct SolveParams {
     int *err;
 };
 
+// Tangent-linear / adjoint request (solve_ad.cu): objective weights and
+// the device arrays of the objective, its gradients or its direction.
+struct AdParams {
+    double w_toa, w_net, w_hr;   // objective weights
+    int store;                   // 1: local Jacobians kept from pass 1, 0: recomputed in the reverse pass
+    int tl;                      // 1: tangent-linear (dJ along dir), 0: adjoint (gradients)
+    double* J;                   // (ncol)
+    double* dJ;                  // (ncol), tangent-linear
+    double* g[5];                // adjoint: dJ/d tlay, h2ovmr, o3vmr, clwp, ciwp (ncol,nlay)
+    double* ga[4];               // adjoint: dJ/d asdir, asdif, aldir, aldif (ncol)
+    const double* dir[5];        // tangent-linear direction, same layout
+    const double* dira[4];
+};
+
 // shared-memory fields of the per-column coefficients
 enum { F_FAC00, F_FAC01, F_FAC10, F_FAC11, F_H2O, F_CO2, F_O3, F_CH4, F_O2, F_MOL,
        F_SELFFAC, F_SELFFRAC, F_FORFAC, F_FORFRAC, F_PDP, NFR };
@@ -65,6 +79,14 @@ struct Coef {
     __device__ int indself(int lay) const { return (pk[lay - 1] >> 16) & 0xff; }
     __device__ int indfor(int lay) const { return (pk[lay - 1] >> 24) & 0xf; }   // bit 30: layer below 100 hPa
 };
+
+// Element type of the coefficient tables read by arithmetic type R: the
+// table of R itself for float and double; derivative types read the FP64
+// tables.
+template <typename R>
+struct TabOf { typedef R type; };
+template <typename R>
+using TabT = typename TabOf<R>::type;
 
 // ----------------------------------------------------- arithmetic helpers
 // The FP64 form is compiled without FMA contraction, so a*b+c rounds twice
@@ -121,46 +143,46 @@ __device__ inline Spec<R> spec(R cola, R colb_scaled, R mult, const Coef<R>& c, 
 
 // k(ind, ig) of a transposed table: [(ind-1)*ng + ig-1]
 template <typename R>
-__device__ inline R K(const R* __restrict__ tab, int off, int ng, int ind, int ig) {
-    return __ldg(tab + off + (ind - 1) * ng + (ig - 1));
+__device__ inline R K(const TabT<R>* __restrict__ tab, int off, int ng, int ind, int ig) {
+    return R(__ldg(tab + off + (ind - 1) * ng + (ig - 1)));
 }
 
 template <typename R>
-__device__ inline R k8(const Spec<R>& s, const R* __restrict__ tab, int off, int ng, int ind0, int ind1, int ig, int d1) {
-    return (s.f000 * K(tab, off, ng, ind0, ig) + s.f100 * K(tab, off, ng, ind0 + 1, ig) +
-            s.f010 * K(tab, off, ng, ind0 + d1, ig) + s.f110 * K(tab, off, ng, ind0 + d1 + 1, ig) +
-            s.f001 * K(tab, off, ng, ind1, ig) + s.f101 * K(tab, off, ng, ind1 + 1, ig) +
-            s.f011 * K(tab, off, ng, ind1 + d1, ig) + s.f111 * K(tab, off, ng, ind1 + d1 + 1, ig));
+__device__ inline R k8(const Spec<R>& s, const TabT<R>* __restrict__ tab, int off, int ng, int ind0, int ind1, int ig, int d1) {
+    return (s.f000 * K<R>(tab, off, ng, ind0, ig) + s.f100 * K<R>(tab, off, ng, ind0 + 1, ig) +
+            s.f010 * K<R>(tab, off, ng, ind0 + d1, ig) + s.f110 * K<R>(tab, off, ng, ind0 + d1 + 1, ig) +
+            s.f001 * K<R>(tab, off, ng, ind1, ig) + s.f101 * K<R>(tab, off, ng, ind1 + 1, ig) +
+            s.f011 * K<R>(tab, off, ng, ind1 + d1, ig) + s.f111 * K<R>(tab, off, ng, ind1 + d1 + 1, ig));
 }
 
 template <typename R>
-__device__ inline R k4(const Coef<R>& c, int lay, const R* __restrict__ tab, int off, int ng, int ind0, int ind1, int ig) {
-    return c.f(F_FAC00, lay) * K(tab, off, ng, ind0, ig) + c.f(F_FAC10, lay) * K(tab, off, ng, ind0 + 1, ig) +
-           c.f(F_FAC01, lay) * K(tab, off, ng, ind1, ig) + c.f(F_FAC11, lay) * K(tab, off, ng, ind1 + 1, ig);
+__device__ inline R k4(const Coef<R>& c, int lay, const TabT<R>* __restrict__ tab, int off, int ng, int ind0, int ind1, int ig) {
+    return c.f(F_FAC00, lay) * K<R>(tab, off, ng, ind0, ig) + c.f(F_FAC10, lay) * K<R>(tab, off, ng, ind0 + 1, ig) +
+           c.f(F_FAC01, lay) * K<R>(tab, off, ng, ind1, ig) + c.f(F_FAC11, lay) * K<R>(tab, off, ng, ind1 + 1, ig);
 }
 
 template <typename R>
-__device__ inline R selfterm(const Coef<R>& c, int lay, const BandOff& B, const R* __restrict__ tab, int ig) {
+__device__ inline R selfterm(const Coef<R>& c, int lay, const BandOff& B, const TabT<R>* __restrict__ tab, int ig) {
     const int inds = c.indself(lay);
-    const R a = K(tab, B.selfref, B.ng, inds, ig), b = K(tab, B.selfref, B.ng, inds + 1, ig);
+    const R a = K<R>(tab, B.selfref, B.ng, inds, ig), b = K<R>(tab, B.selfref, B.ng, inds + 1, ig);
     return c.f(F_SELFFAC, lay) * (a + c.f(F_SELFFRAC, lay) * (b - a));
 }
 template <typename R>
-__device__ inline R forpart(const Coef<R>& c, int lay, const BandOff& B, const R* __restrict__ tab, int ig) {
+__device__ inline R forpart(const Coef<R>& c, int lay, const BandOff& B, const TabT<R>* __restrict__ tab, int ig) {
     const int indf = c.indfor(lay);
-    const R a = K(tab, B.forref, B.ng, indf, ig), b = K(tab, B.forref, B.ng, indf + 1, ig);
+    const R a = K<R>(tab, B.forref, B.ng, indf, ig), b = K<R>(tab, B.forref, B.ng, indf + 1, ig);
     return (a + c.f(F_FORFRAC, lay) * (b - a));
 }
 template <typename R>
-__device__ inline R forterm(const Coef<R>& c, int lay, const BandOff& B, const R* __restrict__ tab, int ig) {
+__device__ inline R forterm(const Coef<R>& c, int lay, const BandOff& B, const TabT<R>* __restrict__ tab, int ig) {
     return c.f(F_FORFAC, lay) * forpart(c, lay, B, tab, ig);
 }
 template <typename R>
-__device__ inline R selffor(const Coef<R>& c, int lay, const BandOff& B, const R* __restrict__ tab, int ig) {
+__device__ inline R selffor(const Coef<R>& c, int lay, const BandOff& B, const TabT<R>* __restrict__ tab, int ig) {
     return selfterm(c, lay, B, tab, ig) + forterm(c, lay, B, tab, ig);
 }
 template <typename R>
-__device__ inline R V(const R* __restrict__ tab, int off, int i) { return __ldg(tab + off + i); }
+__device__ inline R V(const TabT<R>* __restrict__ tab, int off, int i) { return R(__ldg(tab + off + i)); }
 
 // Lower/upper table base indices (taumol.f90:326-327, 357-358)
 __device__ inline int ind_lo(int jp, int jt, int nsp, int js) { return ((jp - 1) * 5 + (jt - 1)) * nsp + js; }
@@ -172,7 +194,7 @@ __device__ inline int ind_up1(int jp, int jt1, int nsp, int js) { return ((jp - 
 // its band) at layer `lay`: one g-point of taumol16..taumol29
 // (rrtmg_sw_taumol.f90:275-1785), same expressions and association order.
 template <typename R>
-__device__ inline void taumol_g(int ib, int ig, int lay, const Coef<R>& c, const R* __restrict__ tab, R& taug, R& taur) {
+__device__ inline void taumol_g(int ib, int ig, int lay, const Coef<R>& c, const TabT<R>* __restrict__ tab, R& taug, R& taur) {
     const BandOff& B = cT.b[ib];
     const bool low = lay <= c.laytrop;
     const R colh2o = c.f(F_H2O, lay), colco2 = c.f(F_CO2, lay), colo3 = c.f(F_O3, lay);
@@ -187,7 +209,7 @@ __device__ inline void taumol_g(int ib, int ig, int lay, const Coef<R>& c, const
         } else {
             taug = colch4 * k4(c, lay, tab, B.absb, B.ng, ind_up(jp, jt, 1, 1), ind_up1(jp, jt1, 1, 1), ig);
         }
-        taur = colmol * V(tab, B.rayl, 0);
+        taur = colmol * V<R>(tab, B.rayl, 0);
         break;
     case 17:
         if (low) {
@@ -199,7 +221,7 @@ __device__ inline void taumol_g(int ib, int ig, int lay, const Coef<R>& c, const
             taug = s.speccomb * k8(s, tab, B.absb, B.ng, ind_up(jp, jt, 5, s.js), ind_up1(jp, jt1, 5, s.js), ig, 5) +
                    colh2o * c.f(F_FORFAC, lay) * forpart(c, lay, B, tab, ig);
         }
-        taur = colmol * V(tab, B.rayl, 0);
+        taur = colmol * V<R>(tab, B.rayl, 0);
         break;
     case 18:
     case 19: {
@@ -211,20 +233,20 @@ __device__ inline void taumol_g(int ib, int ig, int lay, const Coef<R>& c, const
         } else {
             taug = colb * k4(c, lay, tab, B.absb, B.ng, ind_up(jp, jt, 1, 1), ind_up1(jp, jt1, 1, 1), ig);
         }
-        taur = colmol * V(tab, B.rayl, 0);
+        taur = colmol * V<R>(tab, B.rayl, 0);
         break;
     }
     case 20:
         if (low) {
             taug = colh2o * ((k4(c, lay, tab, B.absa, B.ng, ind_lo(jp, jt, 1, 1), ind_lo1(jp, jt1, 1, 1), ig)) +
                              selfterm(c, lay, B, tab, ig) + forterm(c, lay, B, tab, ig)) +
-                   colch4 * V(tab, B.absch4, ig - 1);
+                   colch4 * V<R>(tab, B.absch4, ig - 1);
         } else {
             taug = colh2o * (k4(c, lay, tab, B.absb, B.ng, ind_up(jp, jt, 1, 1), ind_up1(jp, jt1, 1, 1), ig) +
                              forterm(c, lay, B, tab, ig)) +
-                   colch4 * V(tab, B.absch4, ig - 1);
+                   colch4 * V<R>(tab, B.absch4, ig - 1);
         }
-        taur = colmol * V(tab, B.rayl, 0);
+        taur = colmol * V<R>(tab, B.rayl, 0);
         break;
     case 21:
         if (low) {
@@ -236,7 +258,7 @@ __device__ inline void taumol_g(int ib, int ig, int lay, const Coef<R>& c, const
             taug = s.speccomb * k8(s, tab, B.absb, B.ng, ind_up(jp, jt, 5, s.js), ind_up1(jp, jt1, 5, s.js), ig, 5) +
                    colh2o * c.f(F_FORFAC, lay) * forpart(c, lay, B, tab, ig);
         }
-        taur = colmol * V(tab, B.rayl, 0);
+        taur = colmol * V<R>(tab, B.rayl, 0);
         break;
     case 22: {
         const R o2adj = R(1.6);
@@ -248,7 +270,7 @@ __device__ inline void taumol_g(int ib, int ig, int lay, const Coef<R>& c, const
         } else {
             taug = colo2 * o2adj * k4(c, lay, tab, B.absb, B.ng, ind_up(jp, jt, 1, 1), ind_up1(jp, jt1, 1, 1), ig) + o2cont;
         }
-        taur = colmol * V(tab, B.rayl, 0);
+        taur = colmol * V<R>(tab, B.rayl, 0);
         break;
     }
     case 23:
@@ -258,36 +280,36 @@ __device__ inline void taumol_g(int ib, int ig, int lay, const Coef<R>& c, const
         } else {
             taug = R(0);
         }
-        taur = colmol * V(tab, B.rayl, ig - 1);
+        taur = colmol * V<R>(tab, B.rayl, ig - 1);
         break;
     case 24:
         if (low) {
             const Spec<R> s = spec(colh2o, R(0.124692) * colo2, R(8), c, lay);
-            const R ra = V(tab, B.rayla, (s.js - 1) * B.ng + ig - 1), rb = V(tab, B.rayla, s.js * B.ng + ig - 1);
+            const R ra = V<R>(tab, B.rayla, (s.js - 1) * B.ng + ig - 1), rb = V<R>(tab, B.rayla, s.js * B.ng + ig - 1);
             taur = colmol * (ra + s.fs * (rb - ra));
             taug = s.speccomb * k8(s, tab, B.absa, B.ng, ind_lo(jp, jt, 9, s.js), ind_lo1(jp, jt1, 9, s.js), ig, 9) +
-                   colo3 * V(tab, B.abso3a, ig - 1) + colh2o * selffor(c, lay, B, tab, ig);
+                   colo3 * V<R>(tab, B.abso3a, ig - 1) + colh2o * selffor(c, lay, B, tab, ig);
         } else {
-            taur = colmol * V(tab, B.raylb, ig - 1);
+            taur = colmol * V<R>(tab, B.raylb, ig - 1);
             taug = colo2 * k4(c, lay, tab, B.absb, B.ng, ind_up(jp, jt, 1, 1), ind_up1(jp, jt1, 1, 1), ig) +
-                   colo3 * V(tab, B.abso3b, ig - 1);
+                   colo3 * V<R>(tab, B.abso3b, ig - 1);
         }
         break;
     case 25:
-        taur = colmol * V(tab, B.rayl, ig - 1);
+        taur = colmol * V<R>(tab, B.rayl, ig - 1);
         if (low) {
             taug = colh2o * k4(c, lay, tab, B.absa, B.ng, ind_lo(jp, jt, 1, 1), ind_lo1(jp, jt1, 1, 1), ig) +
-                   colo3 * V(tab, B.abso3a, ig - 1);
+                   colo3 * V<R>(tab, B.abso3a, ig - 1);
         } else {
-            taug = colo3 * V(tab, B.abso3b, ig - 1);
+            taug = colo3 * V<R>(tab, B.abso3b, ig - 1);
         }
         break;
     case 26:
         taug = R(0);
-        taur = colmol * V(tab, B.rayl, ig - 1);
+        taur = colmol * V<R>(tab, B.rayl, ig - 1);
         break;
     case 27:
-        taur = colmol * V(tab, B.rayl, ig - 1);
+        taur = colmol * V<R>(tab, B.rayl, ig - 1);
         if (low) taug = colo3 * k4(c, lay, tab, B.absa, B.ng, ind_lo(jp, jt, 1, 1), ind_lo1(jp, jt1, 1, 1), ig);
         else taug = colo3 * k4(c, lay, tab, B.absb, B.ng, ind_up(jp, jt, 1, 1), ind_up1(jp, jt1, 1, 1), ig);
         break;
@@ -299,18 +321,18 @@ __device__ inline void taumol_g(int ib, int ig, int lay, const Coef<R>& c, const
             const Spec<R> s = spec(colo3, R(6.67029e-07) * colo2, R(4), c, lay);
             taug = s.speccomb * k8(s, tab, B.absb, B.ng, ind_up(jp, jt, 5, s.js), ind_up1(jp, jt1, 5, s.js), ig, 5);
         }
-        taur = colmol * V(tab, B.rayl, 0);
+        taur = colmol * V<R>(tab, B.rayl, 0);
         break;
     default:  // 29
         if (low) {
             taug = colh2o * ((k4(c, lay, tab, B.absa, B.ng, ind_lo(jp, jt, 1, 1), ind_lo1(jp, jt1, 1, 1), ig)) +
                              selfterm(c, lay, B, tab, ig) + forterm(c, lay, B, tab, ig)) +
-                   colco2 * V(tab, B.absco2, ig - 1);
+                   colco2 * V<R>(tab, B.absco2, ig - 1);
         } else {
             taug = colco2 * k4(c, lay, tab, B.absb, B.ng, ind_up(jp, jt, 1, 1), ind_up1(jp, jt1, 1, 1), ig) +
-                   colh2o * V(tab, B.absh2o, ig - 1);
+                   colh2o * V<R>(tab, B.absh2o, ig - 1);
         }
-        taur = colmol * V(tab, B.rayl, 0);
+        taur = colmol * V<R>(tab, B.rayl, 0);
         break;
     }
 }
@@ -402,7 +424,7 @@ __device__ inline int solar_layer(int ib, const Coef<R>& c) {
 // Solar source of g-point ig at its reference layer: sfluxzen (isolvar<0)
 // or ssi (isolvar>=0), e.g. taumol.f90:364-378 and 495-517.
 template <typename R>
-__device__ inline R solar_source(int ib, int ig, const Coef<R>& c, const SolveParams& P, const R* __restrict__ tab) {
+__device__ inline R solar_source(int ib, int ig, const Coef<R>& c, const SolveParams& P, const TabT<R>* __restrict__ tab) {
     const BandOff& B = cT.b[ib];
     const int band = ib + 16;
     const int lay = solar_layer(ib, c);
@@ -426,8 +448,8 @@ __device__ inline R solar_source(int ib, int ig, const Coef<R>& c, const SolvePa
         if (interp) { js = s.js; fs = s.fs; }
     }
     auto src = [&](int off) -> R {
-        if (!interp) return V(tab, off, ig - 1);
-        const R a = V(tab, off, (js - 1) * B.ng + ig - 1), b = V(tab, off, js * B.ng + ig - 1);
+        if (!interp) return V<R>(tab, off, ig - 1);
+        const R a = V<R>(tab, off, (js - 1) * B.ng + ig - 1), b = V<R>(tab, off, js * B.ng + ig - 1);
         return a + fs * (b - a);
     };
     if (P.isolvar < 0) {
@@ -477,7 +499,7 @@ __device__ inline float solar_source_generic(int ib, int ig, const Coef<float>& 
 template <typename R>
 __device__ inline void cldprmc_g(int ib, int inflag, int iceflag, int liqflag, R cldf, R ciwp,
                                  R clwp, R rei, R rel, R fsfc, R& tauc,
-                                 R& ssac, R& asmc, R& taor, R& co, const R* __restrict__ tab,
+                                 R& ssac, R& asmc, R& taor, R& co, const TabT<R>* __restrict__ tab,
                                  int* err, R ttest = R(-1)) {
     typedef R double_;
     const R eps = R((1.e-06)), cldmin = R((1.e-20));
@@ -505,21 +527,21 @@ __device__ inline void cldprmc_g(int ib, int inflag, int iceflag, int liqflag, R
     double_ extcoice = 0, ssacoice = 0, gice = 0, forwice = 0, extcoliq = 0, ssacoliq = 0, gliq = 0, forwliq = 0;
     double_ coice = 1, coliq = 1;  // 1 - ssacoice, 1 - ssacoliq from the co-albedo tables
     const int jb = ib + 1;  // band column of the Fortran (index, 16:29) LUTs, 1-based
-    auto lut = [&](int off, int n, int index) { return __ldg(tab + off + (jb - 1) * n + index - 1); };
+    auto lut = [&](int off, int n, int index) { return R(__ldg(tab + off + (jb - 1) * n + index - 1)); };
     if (ciwp == R(0.0)) {
     } else if (iceflag == 1) {
         if (rei < R(13.0) || rei > R(130.0)) { set_error(err, E_ICERAD); return; }
-        const double_ w2 = __ldg(tab + cT.wavenum2 + ib);
+        const double_ w2 = R(__ldg(tab + cT.wavenum2 + ib));
         int icx = 0;
         if (w2 > R(1.43e04)) icx = 1;
         else if (w2 > R(7.7e03)) icx = 2;
         else if (w2 > R(5.3e03)) icx = 3;
         else if (w2 > R(4.0e03)) icx = 4;
         else if (w2 >= R(2.5e03)) icx = 5;
-        extcoice = (__ldg(tab + cT.abari + icx - 1) + __ldg(tab + cT.bbari + icx - 1) / rei);
-        ssacoice = R(1.0) - __ldg(tab + cT.cbari + icx - 1) - __ldg(tab + cT.dbari + icx - 1) * rei;
-        coice = __ldg(tab + cT.cbari + icx - 1) + __ldg(tab + cT.dbari + icx - 1) * rei;
-        gice = __ldg(tab + cT.ebari + icx - 1) + __ldg(tab + cT.fbari + icx - 1) * rei;
+        extcoice = (R(__ldg(tab + cT.abari + icx - 1)) + R(__ldg(tab + cT.bbari + icx - 1)) / rei);
+        ssacoice = R(1.0) - R(__ldg(tab + cT.cbari + icx - 1)) - R(__ldg(tab + cT.dbari + icx - 1)) * rei;
+        coice = R(__ldg(tab + cT.cbari + icx - 1)) + R(__ldg(tab + cT.dbari + icx - 1)) * rei;
+        gice = R(__ldg(tab + cT.ebari + icx - 1)) + R(__ldg(tab + cT.fbari + icx - 1)) * rei;
         if (gice >= R(1.0)) gice = R(1.0) - eps;
         forwice = gice * gice;
         if (extcoice < R(0.0) || ssacoice > R(1.0) || ssacoice < R(0.0) || gice > R(1.0) || gice < R(0.0)) { set_error(err, E_ICEPROP); return; }

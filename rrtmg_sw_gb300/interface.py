@@ -57,6 +57,16 @@ class RrtmgSwArgs(C.Structure):
     ]
 
 
+class RrtmgSwAdArgs(C.Structure):
+    """``rrtmg_sw_ad_args`` of include/rrtmg_sw_gb300.h."""
+    _fields_ = [
+        ("w_toa_up", C.c_double), ("w_sfc_net", C.c_double), ("w_hr_sum", C.c_double),
+        ("store", C.c_int32), ("pad", C.c_int32), ("J", _dp), ("dJ", _dp),
+        ("tlay", _dp), ("h2ovmr", _dp), ("o3vmr", _dp), ("clwp", _dp), ("ciwp", _dp),
+        ("asdir", _dp), ("asdif", _dp), ("aldir", _dp), ("aldif", _dp),
+    ]
+
+
 class RrtmgSwClouds(C.Structure):
     """``rrtmg_sw_clouds`` of include/rrtmg_sw_gb300.h."""
     _fields_ = [
@@ -84,6 +94,8 @@ def lib():
         L.rrtmg_sw_mcica_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds)]
         L.rrtmg_sw_mcica_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_void_p]
         L.rrtmg_sw_nomcica_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds)]
+        L.rrtmg_sw_ad_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.POINTER(RrtmgSwAdArgs)]
+        L.rrtmg_sw_tl_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.POINTER(RrtmgSwAdArgs)]
         L.rrtmg_sw_batch_plan_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_int32, C.c_void_p,
                                             C.POINTER(C.c_void_p)]
         L.rrtmg_sw_batch_run_c.argtypes = [C.c_void_p, C.c_void_p]
@@ -245,6 +257,72 @@ def rrtmg_sw_dev(args, stream=0, clouds=None):
         _check(lib().rrtmg_sw_dev_c(C.byref(args), C.c_void_p(stream)))
     else:
         _check(lib().rrtmg_sw_mcica_dev_c(C.byref(args), C.byref(clouds), C.c_void_p(stream)))
+
+
+AD_LAYER = ("tlay", "h2ovmr", "o3vmr", "clwp", "ciwp")
+AD_SFC = ("asdir", "asdif", "aldir", "aldif")
+
+
+def _ad_call(kw, clouds, weights, store, direction):
+    ncol, nlay = kw["ncol"], kw["nlay"]
+    cl, cl1 = (ncol, nlay), (ncol, nlay + 1)
+    keep = {}
+    a = RrtmgSwArgs()
+    a.ncol, a.nlay, a.icld, a.iaer = ncol, nlay, kw["icld"], kw["iaer"]
+    for name, shp in (("play", cl), ("plev", cl1), ("tlay", cl), ("h2ovmr", cl), ("o3vmr", cl), ("co2vmr", cl),
+                      ("ch4vmr", cl), ("o2vmr", cl), ("asdir", (ncol,)), ("asdif", (ncol,)), ("aldir", (ncol,)),
+                      ("aldif", (ncol,)), ("coszen", (ncol,)), ("tauaer", (ncol, nlay, NBNDSW)),
+                      ("ssaaer", (ncol, nlay, NBNDSW)), ("asmaer", (ncol, nlay, NBNDSW)), ("ecaer", (ncol, nlay, 6))):
+        keep[name] = _f(kw.get(name), shp)
+        setattr(a, name, _p(keep[name]))
+    a.adjes, a.dyofyr, a.scon, a.isolvar = kw["adjes"], kw["dyofyr"], kw["scon"], kw["isolvar"]
+    a.inflgsw, a.iceflgsw, a.liqflgsw = kw["inflgsw"], kw["iceflgsw"], kw["liqflgsw"]
+    a.idelm = 1
+    c = None
+    if clouds is not None:
+        c = RrtmgSwClouds()
+        c.permuteseed = clouds.get("permuteseed", NGPTSW)
+        c.irng = clouds.get("irng", 0)
+        for name, shp in (("cldfrac", cl), ("ciwp", cl), ("clwp", cl), ("rei", cl), ("rel", cl),
+                          ("tauc", (NBNDSW, ncol, nlay)), ("ssac", (NBNDSW, ncol, nlay)),
+                          ("asmc", (NBNDSW, ncol, nlay)), ("fsfc", (NBNDSW, ncol, nlay)), ("alpha", cl)):
+            keep["c_" + name] = _f(clouds.get(name), shp)
+            setattr(c, name, _p(keep["c_" + name]))
+    d = RrtmgSwAdArgs()
+    d.w_toa_up, d.w_sfc_net, d.w_hr_sum = weights
+    d.store = 1 if store else 0
+    out = {"J": np.zeros(ncol)}
+    if direction is None:
+        out.update({k: np.zeros(cl, order="F") for k in AD_LAYER})
+        out.update({k: np.zeros(ncol) for k in AD_SFC})
+        for k in AD_LAYER + AD_SFC:
+            setattr(d, k, _p(out[k]))
+    else:
+        out["dJ"] = np.zeros(ncol)
+        d.dJ = _p(out["dJ"])
+        for k in AD_LAYER + AD_SFC:
+            if direction.get(k) is not None:
+                keep["dir_" + k] = _f(direction[k], cl if k in AD_LAYER else (ncol,))
+                setattr(d, k, _p(keep["dir_" + k]))
+    d.J = _p(out["J"])
+    cp = C.byref(c) if c is not None else None
+    if direction is None:
+        _check(lib().rrtmg_sw_ad_c(C.byref(a), cp, C.byref(d)))
+    else:
+        _check(lib().rrtmg_sw_tl_c(C.byref(a), cp, C.byref(d)))
+    return out
+
+
+def rrtmg_sw_ad(kw, clouds=None, weights=(1.0, 0.0, 0.0), store=True):
+    """Adjoint: J and its gradients (dict keyed by AD_LAYER + AD_SFC) for the
+    objective J = w_toa_up*swuflx(top) + w_sfc_net*net flux(sfc) + w_hr_sum*sum(swhr);
+    ``kw`` holds the rrtmg_sw arguments (as for :func:`rrtmg_sw`)."""
+    return _ad_call(kw, clouds, weights, store, None)
+
+
+def rrtmg_sw_tl(kw, direction, clouds=None, weights=(1.0, 0.0, 0.0)):
+    """Tangent-linear: J and dJ along ``direction`` (dict keyed like the gradients)."""
+    return _ad_call(kw, clouds, weights, True, direction)
 
 
 def rrtmg_sw_static_dev(args, stream=0, clouds=None):

@@ -27,12 +27,12 @@ def _temperature(z_km):
     return t
 
 
-def make_columns(ncol, nlay, seed, clouds=False, aerosol=False, night_frac=0.0, lat=False):
-    """Return a dict of GCM-interface inputs for ``ncol`` columns."""
+def make_columns(ncol, nlay, seed, clouds=False, aerosol=False, night_frac=0.0, lat=False, ptop=0.01):
+    """Return a dict of GCM-interface inputs for ``ncol`` columns (top level at ``ptop`` hPa)."""
     rng = np.random.default_rng(seed)
     psfc = rng.uniform(980.0, 1030.0, ncol)
     frac = np.linspace(0.0, 1.0, nlay + 1)
-    logp = np.log(psfc)[:, None] + frac[None, :] * (np.log(0.01) - np.log(psfc))[:, None]
+    logp = np.log(psfc)[:, None] + frac[None, :] * (np.log(ptop) - np.log(psfc))[:, None]
     plev = np.exp(logp)
     jit = 1.0 + rng.uniform(-0.02, 0.02, (ncol, nlay + 1))
     jit[:, 0] = 1.0
