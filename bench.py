@@ -68,8 +68,8 @@ def algorithmic_flops_per_column(nlay, cloudy_cells_per_col):
 
 
 # DRAM bytes per column of k_solve<float> measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) at 32768 columns x 60 layers, profiles/k_solve_fp32_32768x60_full.md;
-# the traffic is per column pair, so a launch's traffic scales with its columns.
+# dram__bytes_write.sum) in a full capture at 32768 columns x 60 layers; the traffic is
+# per column pair, so a launch's traffic scales with its columns.
 PROFILED_DRAM_BYTES_PER_COLUMN = 24.78e9 / 32768
 
 
@@ -373,8 +373,9 @@ def main():
             ms = float(t.item())
         return ms
 
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    with Clocks(os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")) as clk:
+    import tempfile
+    clk_path = os.path.join(tempfile.gettempdir(), "rrtmg_sw_bench_clocks_%d.csv" % os.getpid())
+    with Clocks(clk_path) as clk:
         ms32 = timed(gi.FORM_FP32, args.steps, args.warmup)
     clocks = clk.summary()
     res32 = {k: v.cpu().numpy() for k, v in outs.items()}
