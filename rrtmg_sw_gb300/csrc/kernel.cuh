@@ -5,7 +5,10 @@
 
 namespace rrsw {
 
-constexpr int KLEV = 4;         // levels buffered per reduction round
+// levels buffered per reduction round of the g-point sums
+constexpr int KLEV = 4;
+constexpr int KLEV_F32 = 4;
+__host__ __device__ constexpr int klev_of(size_t rsz) { return rsz == 4 ? KLEV_F32 : KLEV; }
 constexpr int NQ_MAX = 16;
 // g-point sums per level: fu, fd, cu, cd, fddir, cddir; the FP32 form adds
 // the absorption of the layer below the level (total, clear) for its
@@ -299,24 +302,29 @@ __device__ inline void cloud_in(const SolveParams& P, int col, int g, int lay, i
     ci.cldf = cldf; ci.tc = tc; ci.oc = oc; ci.gc = gc; ci.coc = coc; ci.taor = taor;
 }
 
-// FP32 form: whether the direct-beam lookup exp(-x) sits so close to the
-// edge between two table entries (rrtmg_sw_spcvmc.f90:558-585) that the
-// FP64 form may take the other one, and the step would move this layer's
-// heating rate by more than BEAM_HR_TOL K/day (hrs = incident flux * heatfac / dp).
-// The window assumes BEAM_EPS relative uncertainty in the FP32 optical depth.
+// FP32 form: a direct-beam lookup exp(-x) (rrtmg_sw_spcvmc.f90:558-585) is
+// risky when it sits so close to the edge between two table entries that
+// the FP64 form may take the other one, and the step would move this
+// layer's heating rate by more than BEAM_HR_TOL K/day (hrs = incident flux
+// * heatfac / dp).  The window assumes BEAM_EPS relative uncertainty in the
+// FP32 optical depth.
 constexpr float BEAM_EPS = 5.0e-7f;
 constexpr float BEAM_HR_TOL = 2.0e-3f;
-__device__ inline bool beam_risky(float x, float hrs) {
-    if (x <= 0.06f) return false;  // quadratic branch: no table step
-    const float b = cT.bpade_f;
-    const float bx = b + x;
-    const float t = 10000.0f * x / bx + 0.5f;
-    const float fr = t - floorf(t);
-    const float d = fminf(fr, 1.0f - fr);
-    const float win = 10000.0f * b * x / (bx * bx) * BEAM_EPS;
-    if (d >= win) return false;
-    const float step = __expf(-x) * bx * bx / (b * 10000.0f);  // change of exp(-x) per table entry
-    return hrs * step > BEAM_HR_TOL;
+// The direct-beam lookup of tbl_exp (x > od_lo: u = x / (bpade + x), entry
+// int(1e4 u + 0.5)) together with beam_risky's test, sharing its division:
+// the window 1e4 b x / (b + x)^2 * BEAM_EPS is 1e4 u (1 - u) * BEAM_EPS.
+__device__ inline float tbl_exp_beam(float x, const float* __restrict__ tab, float hrs, bool& risky) {
+    if (x <= 0.06f) return 1.0f - x + 0.5f * x * x;
+    const float u = x / (cT.bpade_f + x);
+    const float t = 10000.0f * u + 0.5f;
+    const int itind = (int)t;
+    const float e = __ldg(tab + cT.exp_tbl + itind);
+    const float fr = t - (float)itind;
+    if (fminf(fr, 1.0f - fr) < 10000.0f * u * (1.0f - u) * BEAM_EPS) {
+        const float bx = cT.bpade_f + x;
+        if (hrs * e * bx * bx / (cT.bpade_f * 10000.0f) > BEAM_HR_TOL) risky = true;
+    }
+    return e;
 }
 
 // Layer optics of one cell (rrtmg_sw_spcvmc.f90:442-585): clear optics
@@ -352,8 +360,13 @@ __device__ inline CellOpt<R> cell_optics(const CellIn<R>& ci, int idelm, R prmu0
     if constexpr (sizeof(R) == 4) zcoc = zcoc / (R(1) - zwf);
     o.rc = reftra_g<R>(ztauc, zomcc, zcoc, zgcc, prmu0, tab, tab64);
     const R xc = ztauc / prmu0;
-    o.zdbtc = tbl_exp<R>(xc, tab);
-    if constexpr (sizeof(R) == 4) o.risky = o.rc.risky || beam_risky(xc, hrs);
+    if constexpr (sizeof(R) == 4) {
+        bool br = false;
+        o.zdbtc = tbl_exp_beam(xc, tab, hrs, br);
+        o.risky = o.rc.risky || br;
+    } else {
+        o.zdbtc = tbl_exp<R>(xc, tab);
+    }
     o.rt = o.rc;
     o.zdbt = o.zdbtc;
     if (ci.cloudy) {
@@ -377,12 +390,15 @@ __device__ inline CellOpt<R> cell_optics(const CellIn<R>& ci, int idelm, R prmu0
         o.rt.tra = zclear * o.rc.tra + zcloud * ro.tra;
         o.rt.trad = zclear * o.rc.trad + zcloud * ro.trad;
         const R xo = ztauo / prmu0;
-        const R zdbtmo = tbl_exp<R>(xo, tab);
+        R zdbtmo;
+        bool bro = false;
+        if constexpr (sizeof(R) == 4) zdbtmo = tbl_exp_beam(xo, tab, hrs, bro);
+        else zdbtmo = tbl_exp<R>(xo, tab);
         o.zdbt = zclear * o.zdbtc + zcloud * zdbtmo;
         if constexpr (sizeof(R) == 4) {
             o.rt.adir = zclear * o.rc.adir + zcloud * ro.adir;
             o.rt.adif = zclear * o.rc.adif + zcloud * ro.adif;
-            o.risky = o.risky || ro.risky || beam_risky(xo, hrs);
+            o.risky = o.risky || ro.risky || bro;
         }
     }
     return o;
@@ -516,7 +532,7 @@ __host__ __device__ inline Smem smem_layout(int L, int nq, bool fused, bool aer_
     if (aer_stage) {
         m.aer = o;  o = align16(o + COLS_PER_CTA * 3 * NBND * L * rsz);
     }
-    m.red = o;  o = align16(o + KLEV * nq * CTA_THREADS * rsz);
+    m.red = o;  o = align16(o + klev_of(rsz) * nq * CTA_THREADS * rsz);
     m.flux = o; o = align16(o + COLS_PER_CTA * nq * (L + 1) * rsz);
     m.total = o;
     return m;
@@ -897,11 +913,12 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
                 tdbtn = dbtn * tdbtn;
             }
         }
-        const int slot = (jk - 1) % KLEV;
+        constexpr int KL = klev_of(sizeof(R));
+        const int slot = (jk - 1) % KL;
 #pragma unroll
         for (int i = 0; i < NQ_MAX; ++i)
             if (i < NQ) sRed[(slot * NQ + i) * CTA_THREADS + tid] = q[i];
-        if (slot == KLEV - 1 || jk == L + 1) {
+        if (slot == KL - 1 || jk == L + 1) {
             __syncthreads();
             const int nlev = slot + 1;
             const int items = COLS_PER_CTA * NQ * nlev;
@@ -988,8 +1005,10 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
 
 }
 
+// FP32 form: 3 resident CTAs per SM (80 registers, ~61 KB shared memory each
+// at 60 layers) hide more latency than 2 CTAs with 128 registers.
 template <typename R>
-__global__ void __launch_bounds__(CTA_THREADS, 2)
+__global__ void __launch_bounds__(CTA_THREADS, sizeof(R) == 4 ? 3 : 2)
 k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict__ tab64) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const CtaView<R> V = cta_view<R>(smem_raw, P);
