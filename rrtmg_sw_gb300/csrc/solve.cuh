@@ -632,8 +632,8 @@ struct RT {
 
 // zco = 1 - zw carried separately by the FP32 form (unused by FP64);
 // tab64 is the FP64 table blob (the FP32 form's FP64 island needs it)
-// force: -1 = decide the conservative branch here, 0/1 = branch decided by
-// the caller (FP32 form, see decide_conservative64)
+// force (FP32 form): 1 = also test every table lookup for an ambiguous entry
+// (cloudy total sky), -1 = only near resonance
 template <typename R>
 __device__ inline RT<R> reftra_g(R zto1, R zw, R zco, R zg, R prmuz, const R* __restrict__ tab,
                                  const double* __restrict__ tab64, int force = -1);

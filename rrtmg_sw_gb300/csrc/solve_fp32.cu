@@ -49,16 +49,17 @@ __device__ inline float tbl_exp_om(float x, const float* __restrict__ tab, float
 // whose conservative switch is too close.
 constexpr float RESONANCE_TOL = 2.0e-3f;
 constexpr float RESONANCE_WIDE = 5.0e-2f;
+constexpr float CLOUD_EDGE_EPS = 2.0e-7f;  // window of the cloudy total-sky lookups
 
 // Whether exp(-x) from the table could come from the neighbouring entry
-// under a 5e-7 relative uncertainty of x.
-__device__ inline bool entry_edge(float x) {
+// under a relative uncertainty eps of x.
+__device__ inline bool entry_edge(float x, float eps) {
     if (x <= 0.06f) return false;
     const float b = cT.bpade_f;
     const float bx = b + x;
     const float t = 10000.0f * x / bx + 0.5f;
     const float fr = t - floorf(t);
-    return fminf(fr, 1.0f - fr) < 10000.0f * b * x / (bx * bx) * 5.0e-7f;
+    return fminf(fr, 1.0f - fr) < 10000.0f * b * x / (bx * bx) * eps;
 }
 
 template <>
@@ -73,7 +74,6 @@ __device__ __noinline__ RT<float> reftra_g<float>(float zto1, float zw, float zc
     const float zgamma3 = (2.0f - zg3 * prmuz) * 0.25f;
     const float zgamma4 = 1.0f - zgamma3;
     // zwo >= zwcrit  <=>  1 - zwo <= 5e-7  (reftra:183-188)
-    (void)force;
     (void)tab64;
     const bool cons = one_minus_zwo(zw, zco, zg) <= 5.0e-7f;
     o.adir = 0.0f;
@@ -115,8 +115,12 @@ __device__ __noinline__ RT<float> reftra_g<float>(float zto1, float zw, float zc
     float om1, om2;
     const float zem1 = tbl_exp_om(fminf(zrk * zto1, 500.0f), tab, om1);
     const float zem2 = tbl_exp_om(fminf(zto1 / prmuz, 500.0f), tab, om2);
-    if (fabsf(zrpp) < RESONANCE_WIDE && !o.risky)
-        o.risky = entry_edge(fminf(zrk * zto1, 500.0f)) || entry_edge(fminf(zto1 / prmuz, 500.0f));
+    // force = 1 (cloudy total sky): a neighbouring table entry moves pref/ptra
+    // of a thick layer enough to show in the fluxes, so every lookup is tested
+    if ((force == 1 || fabsf(zrpp) < RESONANCE_WIDE) && !o.risky) {
+        const float eps = fabsf(zrpp) < RESONANCE_WIDE ? 5.0e-7f : CLOUD_EDGE_EPS;
+        o.risky = entry_edge(fminf(zrk * zto1, 500.0f), eps) || entry_edge(fminf(zto1 / prmuz, 500.0f), eps);
+    }
     const float p1 = om1 / zem1;  // zep1 - 1
     const float p2 = om2 / zem2;  // zep2 - 1
     const float zdenr = zrpp * (zrk2 + zrkg * p1 + g2k * om1);
