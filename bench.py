@@ -45,6 +45,8 @@ def parse():
     p.add_argument("--workload", default="fp32", choices=["fp32", "batch", "adjoint"],
                    help="fp32: the FP32-form headline; batch: 48 ragged instances in one launch (FP64 form)")
     p.add_argument("--instances", type=int, default=48)
+    p.add_argument("--irng", type=int, default=0, choices=[0, 1],
+                   help="McICA generator of the fused solve: 0 KISS, 1 MT19937 (one stream per call, GCM order)")
     return p.parse_args()
 
 
@@ -70,7 +72,7 @@ def algorithmic_flops_per_column(nlay, cloudy_cells_per_col):
 # DRAM bytes per column of k_solve<float> measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum) in a full capture at 32768 columns x 60 layers; the traffic is
 # per column pair, so a launch's traffic scales with its columns.
-PROFILED_DRAM_BYTES_PER_COLUMN = 24.78e9 / 32768
+PROFILED_DRAM_BYTES_PER_COLUMN = 27.91e9 / 32768
 
 
 def algorithmic_bytes_per_column(nlay):
@@ -343,7 +345,7 @@ def main():
         setattr(a, k, ptr(v))
     a.idelm = 1
     cl = gi.RrtmgSwClouds()
-    cl.permuteseed, cl.irng = 112, 0
+    cl.permuteseed, cl.irng = 112, args.irng
     for k in ("cldfrac", "ciwp", "clwp", "rei", "rel", "alpha"):
         setattr(cl, k, ptr(d[k]))
     stream = torch.cuda.current_stream(dev)
@@ -387,6 +389,23 @@ def main():
         err = {k: float(np.max(np.abs(res32[k] - res64[k]))) for k in res32}
     gi.set_form(gi.FORM_FP32)
 
+    # irng = 1: the MT19937 generator alone on the call's stream (icld 5: two draws per cell)
+    mt_stream = None
+    if args.irng == 1:
+        nmt = 2 * 112 * ncol * NLAY
+        buf = torch.empty(nmt, dtype=torch.int32, device=dev)
+        gi.mt_stream_dev(112, nmt, buf.data_ptr(), 0, sid)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            gi.mt_stream_dev(112, nmt, buf.data_ptr(), 0, sid)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        mt_ms = e0.elapsed_time(e1) / 3
+        mt_stream = {"words": nmt, "ms": mt_ms, "gwords_per_s": nmt / (mt_ms / 1e3) / 1e9,
+                     "write_gbs": 4 * nmt / (mt_ms / 1e3) / 1e9}
+        del buf
+
     # end to end through the host-array C ABI (pinned host buffers)
     e2e = None
     if not args.no_e2e:
@@ -407,7 +426,7 @@ def main():
             setattr(ah, k, ptr(v))
         ah.idelm = 1
         ch = gi.RrtmgSwClouds()
-        ch.permuteseed, ch.irng = 112, 0
+        ch.permuteseed, ch.irng = 112, args.irng
         for k in ("cldfrac", "ciwp", "clwp", "rei", "rel", "alpha"):
             setattr(ch, k, ptr(h[k]))
         used = ("play", "plev", "tlay", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "o2vmr", "asdir", "asdif", "aldir",
@@ -467,7 +486,9 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "fused McICA + shortwave solve, %d columns x %d layers per GPU, icld=5 idcor=1, "
-                               "inflgsw=2 iceflgsw=3 liqflgsw=1, iaer=0, all sunlit" % (ncol, NLAY),
+                               "inflgsw=2 iceflgsw=3 liqflgsw=1, iaer=0, all sunlit%s" %
+                               (ncol, NLAY, ", irng=1 (MT19937 stream in GCM order, generated by jump-ahead "
+                                            "segments inside each step)" if args.irng else ""),
                    "ncol": ncol, "nlay": NLAY, "form": "fp32", "l2": "inputs %.2f GB > L2, no flush" %
                    (sum(v.numel() * 8 for v in d.values()) / 1e9)},
         "fp64": None if ms64 is None else {"value": sunlit * world / (ms64 / 1e3), "ms_per_step": ms64,
@@ -483,9 +504,11 @@ def main():
                          "unit": "GB/s", "frac": bytes_col * ncol / (ms32 / 1e3) / 1e9 / hbm,
                          "bytes_per_column": bytes_col, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
         "e2e": e2e,
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * (3 if args.irng else 1),
         "clocks": clocks,
     }
+    if mt_stream is not None:
+        line["mt_stream"] = mt_stream
     if rank == 0:
         cores = os.cpu_count() or 1
         try:
@@ -498,7 +521,7 @@ def main():
                                     cs["cldfrac"].ravel(order="F"))
             z14 = np.zeros(14 * sample * NLAY)
             t0 = time.perf_counter()
-            mm = pyoracle.mcica_subcol_sw(sample, NLAY, 5, 112, 0, *(cs[k].ravel(order="F") for k in
+            mm = pyoracle.mcica_subcol_sw(sample, NLAY, 5, 112, args.irng, *(cs[k].ravel(order="F") for k in
                                                                      ("play", "cldfrac", "ciwp", "clwp", "rei",
                                                                       "rel")), z14, z14 + 1.0, z14, z14, al)
             names = ("cldfmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl", "taucmcl", "ssacmcl", "asmcmcl",

@@ -70,7 +70,11 @@ typedef struct rrtmg_sw_args {
 /* Physical cloud inputs for the fused path: the arguments of
  * mcica_subcol_sw (mcica_subcol_gen_sw.f90:181-185) that rrtmg_sw_mcica_c
  * consumes on the device instead of the seven (ngpt,ncol,nlay) subcolumn
- * arrays.  irng must be 0 (KISS, per-column streams) in the fused path. */
+ * arrays.  irng = 0: KISS, per-column streams; irng = 1: MT19937, one
+ * stream for the call in (subcolumn, column, layer) order seeded with
+ * permuteseed, generated on the device before the solve (rrtmg_sw_mcica_c /
+ * _dev_c only; the static, batch and TL/AD entry points return
+ * RRTMG_SW_EIRNG). */
 typedef struct rrtmg_sw_clouds {
     int32_t permuteseed, irng;
     const double *cldfrac, *ciwp, *clwp, *rei, *rel;   /* (ncol,nlay) */
@@ -104,7 +108,7 @@ enum {
     RRTMG_SW_EKISSSEED = 21,   /* mcica_subcol_gen_sw.f90:472-474  KISSVEC SEED GENERATOR REQUIRES
                                   PMID FROM BOTTOM FOUR LAYERS */
     RRTMG_SW_ELAYTROP = 30,    /* profile without layers on both sides of the ~100 hPa switch */
-    RRTMG_SW_EIRNG = 31,       /* fused path requires irng = 0 */
+    RRTMG_SW_EIRNG = 31,       /* irng = 1 (MT19937) on the static, batch or TL/AD entry points */
     RRTMG_SW_EPARTIAL = 32     /* rrtmg_sw_rad.nomcica.f90:619-621  PARTIAL CLOUD NOT ALLOWED */
 };
 
@@ -239,6 +243,23 @@ int mcica_subcol_sw_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t permutes
                       double *cldfmcl, double *ciwpmcl, double *clwpmcl, double *reicmcl,
                       double *relqmcl, double *taucmcl, double *ssacmcl, double *asmcmcl,
                       double *fsfcmcl);
+
+/* MT19937 streams of the McICA generator (mcica_random_numbers.f90:77-306)
+ * with jump-ahead; no reference counterpart (the reference draws its stream
+ * sequentially).  The fused entry points (rrtmg_sw_mcica_c / _dev_c with
+ * clouds->irng = 1) and mcica_subcol_sw_c use the device generator
+ * internally; these two expose it, e.g. to split one GCM-order stream over
+ * several processes.
+ *   rrtmg_sw_mt_window_c: the 624 raw (untempered) state words behind
+ *     outputs offset .. offset+623 of the stream seeded with seed, computed on
+ *     the host (no GPU needed; offset < 2^48).  Tempering window[0] gives
+ *     output number offset.
+ *   rrtmg_sw_mt_stream_dev_c: outputs 0 .. n-1 (tempered u32, getRandomReal
+ *     = u32 / (2^32 - 1)) into device memory `out`, generated as segments of
+ *     2^log_seg words (log_seg <= 0: chosen from n), each started by a
+ *     jump-ahead; same words for every log_seg. */
+int rrtmg_sw_mt_window_c(int32_t seed, uint64_t offset, uint32_t *window);
+int rrtmg_sw_mt_stream_dev_c(int32_t seed, uint64_t n, uint32_t *out, int32_t log_seg, void *stream);
 
 /* get_alpha (mcica_subcol_gen_sw.f90:66-178), host arrays. */
 int get_alpha_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t idcor, double decorr_con,

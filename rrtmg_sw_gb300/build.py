@@ -3,6 +3,8 @@
 Translation units are compiled in parallel:
   solve_fp64.cu  --fmad=false (plain FP64 form, reference rounding)
   solve_fp32.cu  FMA contraction, approximate FP32 division/sqrt (FP32 form)
+  solve_ad.cu    tangent-linear / adjoint of the FP64 form
+  mt19937.cu     MT19937 streams with jump-ahead (McICA irng = 1)
   api.cu         host C-ABI
 """
 import os
@@ -22,6 +24,7 @@ UNITS = {
     "solve_fp64.cu": ["--fmad=false"],
     "solve_fp32.cu": ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "solve_ad.cu": [],
+    "mt19937.cu": [],
     "api.cu": [],
 }
 

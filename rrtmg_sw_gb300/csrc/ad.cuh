@@ -490,7 +490,7 @@ k_adjoint(const SolveParams P, const AdParams A, const double* __restrict__ tab6
         double cossza = 1.0, albp = 0.0, albd = 0.0, talbp = 0.0, talbd = 0.0;
         Dual<3> zinc(0.0);
         int lsol = -1;
-        McicaMask mc;
+        McicaMask<false> mc;
         if (active) {
             cossza = P.coszen[col];
             if (cossza < 1.e-10) cossza = 1.e-10;

@@ -310,7 +310,7 @@ void solar_setup(const State& st, const rrtmg_sw_args* a, SolveParams& P) {
         P.svar_f_bnd[i] = P.svar_s_bnd[i] = P.svar_i_bnd[i] = 1.0;
     }
     P.isolvar = isolvar;
-    P.svar_f = P.svar_s = P.svar_i = 1.0;
+    double svar_f = 1.0, svar_s = 1.0, svar_i = 1.0;  // per-call factors of isolvar 0-2
     double scl[2] = {1.0, 1.0}, ndx[2] = {favg, savg}, scf = 0.0;
     if (isolvar == 1 && a->indsolvar && a->solcycfrac) {
         scf = *a->solcycfrac;
@@ -360,12 +360,12 @@ void solar_setup(const State& st, const rrtmg_sw_args* a, SolveParams& P) {
         if (isolvar == 1) {
             double f0, s0;
             cycle(f0, s0);
-            P.svar_f = scl[0] * (f0 - Foffset) / (favg - Foffset);
-            P.svar_s = scl[1] * (s0 - Soffset) / (savg - Soffset);
+            svar_f = scl[0] * (f0 - Foffset) / (favg - Foffset);
+            svar_s = scl[1] * (s0 - Soffset) / (savg - Soffset);
         }
         if (isolvar == 2) {
-            P.svar_f = (ndx[0] - Foffset) / (favg - Foffset);
-            P.svar_s = (ndx[1] - Soffset) / (savg - Soffset);
+            svar_f = (ndx[0] - Foffset) / (favg - Foffset);
+            svar_s = (ndx[1] - Soffset) / (savg - Soffset);
         }
         if (isolvar == 3)
             for (int i = 0; i < 14; ++i) {
@@ -378,14 +378,14 @@ void solar_setup(const State& st, const rrtmg_sw_args* a, SolveParams& P) {
             for (int i = 0; i < 14; ++i) solvar[i] = a->bndsolvar ? a->bndsolvar[i] * scon / rrsw_scon : scon / rrsw_scon;
         if (isolvar == 0) {
             const double r = scon / (Fint + Sint + Iint);
-            P.svar_f = P.svar_s = P.svar_i = r;
+            svar_f = svar_s = svar_i = r;
         }
         if (isolvar == 1) {
             double f0, s0;
             cycle(f0, s0);
-            P.svar_i = (scon - (scl[0] * Fint + scl[1] * Sint)) / Iint;
-            P.svar_f = scl[0] * (f0 - Foffset) / (favg - Foffset);
-            P.svar_s = scl[1] * (s0 - Soffset) / (savg - Soffset);
+            svar_i = (scon - (scl[0] * Fint + scl[1] * Sint)) / Iint;
+            svar_f = scl[0] * (f0 - Foffset) / (favg - Foffset);
+            svar_s = scl[1] * (s0 - Soffset) / (savg - Soffset);
         }
         if (isolvar == 3) {
             const double c = Fint + Sint + Iint;
@@ -395,6 +395,13 @@ void solar_setup(const State& st, const rrtmg_sw_args* a, SolveParams& P) {
             }
         }
     }
+    // the kernel reads per-band factors: isolvar 0-2 use the same three everywhere
+    if (isolvar != 3)
+        for (int i = 0; i < 14; ++i) {
+            P.svar_f_bnd[i] = svar_f;
+            P.svar_s_bnd[i] = svar_s;
+            P.svar_i_bnd[i] = svar_i;
+        }
     for (int i = 0; i < 14; ++i) P.adjflux[i] = isolvar < 0 ? adjflx * solvar[i] : adjflx;
 }
 
@@ -444,7 +451,7 @@ int make_params(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, Sol
         if (P.inflag == 0 && (!P.tauc || !P.ssac || !P.asmc || !P.fsfc)) return RRTMG_SW_EARGS;
     }
     if (c && !nomcica && P.icld >= 1) {
-        if (c->irng != 0) return RRTMG_SW_EIRNG;
+        P.irng = c->irng != 0 ? 1 : 0;  // mcica:455
         P.permuteseed = c->permuteseed;
         P.cldfrac = c->cldfrac; P.ciwp = c->ciwp; P.clwp = c->clwp; P.rei = c->rei; P.rel = c->rel;
         P.tauc = c->tauc; P.ssac = c->ssac; P.asmc = c->asmc; P.fsfc = c->fsfc; P.alpha = c->alpha;
@@ -473,6 +480,15 @@ int make_params(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, Sol
     return RRTMG_SW_OK;
 }
 
+// Draws of a call's MT stream (mcica_subcol_gen_sw.f90 MT branch): one per
+// (subcolumn, column, layer), two for icld 4/5, one per (subcolumn, column)
+// for icld 3.
+uint64_t mt_stream_length(int icld, int ncol, int nlay) {
+    const uint64_t sc = (uint64_t)NGPT * (uint64_t)ncol;
+    if (icld == 3) return sc;
+    return (icld >= 4 ? 2ull : 1ull) * sc * (uint64_t)nlay;
+}
+
 // Queue one solve on `s`; returns after reading back the device error word.
 int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s, bool nomcica = false) {
     SolveParams P;
@@ -480,6 +496,16 @@ int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaS
     if (rc) return rc;
     CK(st.errw.ensure(sizeof(int)));
     P.err = (int*)st.errw.p;
+    int launches = 1;
+    if (P.fused && P.icld >= 1 && P.irng) {
+        // the call's MT stream, generated in parallel segments, read by the solve
+        const uint64_t nr = mt_stream_length(P.icld, P.ncol, P.nlay);
+        DevBuf& rs = st.stage["mt_stream"];
+        CK(rs.ensure((nr + 2) * sizeof(uint32_t)));  // + the mask's read-ahead past the last run
+        CK(launch_mt_jump((uint32_t)P.permuteseed, nr, (uint32_t*)rs.p, st.num_sms, 0, s));
+        P.mt = (const uint32_t*)rs.p;
+        launches += 2;
+    }
     const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
     LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms) : plan_fp64(P, st.num_sms);
     P.slot_elems = slot_elems(P.nlay, P.idelm, fp32);
@@ -489,7 +515,7 @@ int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaS
     CK(cudaMemsetAsync(P.err, 0, sizeof(int), s));
     if (fp32) CK(launch_solve_fp32(P, (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, li, s));
     else CK(launch_solve_fp64(P, (const double*)st.d_tab64.p, li, s));
-    st.last_launches = 1;
+    st.last_launches = launches;
     CK(cudaMemcpyAsync(st.h_err, P.err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     return *st.h_err;
@@ -632,6 +658,7 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
     SolveParams P;
     int rc = make_params(st, a, c, P);
     if (rc) return rc;
+    if (P.irng) return RRTMG_SW_EIRNG;  // the MT stream needs a device buffer
     const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
     LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms) : plan_fp64(P, st.num_sms);
     P.slot_elems = slot_elems(P.nlay, P.idelm, fp32);
@@ -716,6 +743,7 @@ int solve_ad_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, const rrtmg_
     SolveParams P;
     int rc = make_params(st, &d, (c && icld >= 1) ? &dc : nullptr, P);
     if (rc) return rc;
+    if (P.irng) return RRTMG_SW_EIRNG;
     CK(st.errw.ensure(sizeof(int)));
     P.err = (int*)st.errw.p;
     const int grid = adjoint_grid(P, st.num_sms);
@@ -804,6 +832,7 @@ int batch_plan(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, int 
     for (int i = 0; i < n; ++i) {
         int rc = check_args(a + i);
         if (!rc) rc = make_params(st, a + i, (c && a[i].icld >= 1) ? c + i : nullptr, P[i]);
+        if (!rc && P[i].irng) rc = RRTMG_SW_EIRNG;
         if (rc) { batch_release(bp); return rc; }
         const size_t si = slot_elems(P[i].nlay, P[i].idelm, fp32);
         if (si > slot) slot = si;
@@ -992,13 +1021,13 @@ int mcica_subcol_sw_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t permutes
                              d_fsfc, d_alpha, o[0], o[1], o[2], o[3], o[4], o[5], o[6], (int*)st.errw.p, s));
         st.last_launches = 1;
     } else {
-        const size_t nr = (icld >= 4 ? 2 : 1) * (icld == 3 ? (size_t)NGPT * C : G);
-        DevBuf& rs = st.stage["m_stream"];
-        CK(rs.ensure(nr * sizeof(double)));
-        CK(launch_mt_stream(permuteseed, nr, (double*)rs.p, s));
-        CK(launch_mcica_stream(ncol, nlay, icld, (const double*)rs.p, d_cf, d_ciwp, d_clwp, d_tauc, d_ssac, d_asmc,
+        const uint64_t nr = mt_stream_length(icld, ncol, nlay);
+        DevBuf& rs = st.stage["mt_stream"];
+        CK(rs.ensure((nr + 2) * sizeof(uint32_t)));  // + the mask's read-ahead past the last run
+        CK(launch_mt_jump((uint32_t)permuteseed, nr, (uint32_t*)rs.p, st.num_sms, 0, s));
+        CK(launch_mcica_stream(ncol, nlay, icld, (const uint32_t*)rs.p, d_cf, d_ciwp, d_clwp, d_tauc, d_ssac, d_asmc,
                                d_fsfc, d_alpha, o[0], o[1], o[2], o[3], o[4], o[5], o[6], s));
-        st.last_launches = 2;
+        st.last_launches = 3;
     }
     CK(cudaMemcpyAsync(st.h_err, st.errw.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     for (int i = 0; i < 7; ++i) sg.back(h[i], o[i], G);
@@ -1008,6 +1037,22 @@ int mcica_subcol_sw_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t permutes
     // reicmcl/relqmcl are plain copies (mcica:268-269)
     if (reicmcl) std::memcpy(reicmcl, rei, CL * sizeof(double));
     if (relqmcl) std::memcpy(relqmcl, rel, CL * sizeof(double));
+    return RRTMG_SW_OK;
+}
+
+int rrtmg_sw_mt_window_c(int32_t seed, uint64_t offset, uint32_t* window) {
+    if (!window) return RRTMG_SW_EARGS;
+    return mt_window_host((uint32_t)seed, offset, window) == 0 ? RRTMG_SW_OK : RRTMG_SW_EARGS;
+}
+
+int rrtmg_sw_mt_stream_dev_c(int32_t seed, uint64_t n, uint32_t* out, int32_t log_seg, void* stream) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (!out || log_seg > 40) return RRTMG_SW_EARGS;
+    CK(launch_mt_jump((uint32_t)seed, n, out, st.num_sms, log_seg, (cudaStream_t)stream));
+    st.last_launches = n ? 2 : 0;
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
     return RRTMG_SW_OK;
 }
 
@@ -1060,7 +1105,7 @@ const char* rrtmg_sw_errstr_c(int32_t code) {
     case RRTMG_SW_EICLD: return "MCICA_SUBCOL: INVALID ICLD";
     case RRTMG_SW_EKISSSEED: return "MCICA_SUBCOL: KISSVEC SEED GENERATOR REQUIRES PMID FROM BOTTOM FOUR LAYERS.";
     case RRTMG_SW_ELAYTROP: return "PROFILE MUST HAVE LAYERS ON BOTH SIDES OF THE 100 HPA SWITCH";
-    case RRTMG_SW_EIRNG: return "FUSED MCICA REQUIRES IRNG = 0";
+    case RRTMG_SW_EIRNG: return "IRNG = 1 (MT19937) NOT AVAILABLE ON THIS ENTRY POINT";
     case RRTMG_SW_EPARTIAL: return "PARTIAL CLOUD NOT ALLOWED";
     default: return "UNKNOWN ERROR";
     }

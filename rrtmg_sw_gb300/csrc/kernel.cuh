@@ -611,7 +611,7 @@ __device__ inline int pair_col(const SolveParams& P, int pair, int c2, int nmapp
 }
 
 // One column pair: prep, pass 1, pass 2 and outputs.
-template <typename R>
+template <typename R, bool MT = false>
 __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const CtaView<R>& V, const KissJump& J,
                                            R* scr, const R* __restrict__ tab, const double* __restrict__ tab64) {
     const int L = P.nlay;
@@ -660,8 +660,13 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
             if (cf < 1.0e-20) cf = 0.0;
             const double omcf = DS(1.0, cf);
             sOmcf[c2 * L + lay - 1] = omcf;
-            sKc[c2 * L + lay - 1] = kiss_threshold(omcf);
-            sKa[c2 * L + lay - 1] = (P.icld >= 4 && real) ? kiss_threshold(P.alpha[kl]) : 0ll;
+            if constexpr (MT) {
+                sKc[c2 * L + lay - 1] = mt_threshold(omcf);
+                sKa[c2 * L + lay - 1] = (P.icld >= 4 && real) ? mt_threshold(P.alpha[kl]) : 0ll;
+            } else {
+                sKc[c2 * L + lay - 1] = kiss_threshold(omcf);
+                sKa[c2 * L + lay - 1] = (P.icld >= 4 && real) ? kiss_threshold(P.alpha[kl]) : 0ll;
+            }
             R* cd = sCld + c2 * 4 * L;
             cd[0 * L + lay - 1] = real ? (R)P.ciwp[kl] : R(0);
             cd[1 * L + lay - 1] = real ? (R)P.clwp[kl] : R(0);
@@ -669,7 +674,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
             cd[3 * L + lay - 1] = real ? (R)P.rel[kl] : R(0);
             if (lay == 1) {
                 uint32_t* sd = sSeed + c2 * 4;
-                if (real) {
+                if (real && !MT) {
                     const double p1 = DM(P.play[pcol], 1.e2), p2 = DM(P.play[pcol + n], 1.e2);
                     if (p1 < p2) set_error(P.err, E_KISSSEED);
                     sd[0] = kiss_seed(p1);
@@ -721,7 +726,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
     // ---------------- per (column, g-point) setup
     R zinc = R(0), albp = R(0), albd = R(0);
     double cossza = 1.0;
-    McicaMask mc;
+    McicaMask<MT> mc;
     if (active) {
         cossza = P.coszen[col];
         if (cossza < 1.e-10) cossza = 1.e-10;
@@ -733,7 +738,9 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         if constexpr (sizeof(R) == 4) src = solar_source_generic(ib, igb, C, P, tab);
         else src = solar_source<R>(ib, igb, C, P, tab);
         zinc = R(P.adjflux[ib]) * src * (R)cossza;
-        if (fused) mc.start(kiss_start(sSeed + cc * 4, J, sXs + g * 32), P.icld);
+        if (fused)
+            mc.start(kiss_start(sSeed + cc * 4, J, sXs + g * 32), P.icld,
+                     MT ? P.mt + mt_offset(P.icld, g, col, P.ncol, L) : nullptr);
     }
     const R prmu0 = (R)cossza;
     const R* cld = sCld + cc * 4 * L;
@@ -1006,15 +1013,17 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
 }
 
 // FP32 form: 3 resident CTAs per SM (80 registers, ~61 KB shared memory each
-// at 60 layers) hide more latency than 2 CTAs with 128 registers.
-template <typename R>
+// at 60 layers) hide more latency than 2 CTAs with 128 registers.  MT: fused
+// McICA from the call's MT19937 stream (P.mt) instead of KISS.
+template <typename R, bool MT>
 __global__ void __launch_bounds__(CTA_THREADS, sizeof(R) == 4 ? 3 : 2)
 k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict__ tab64) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const CtaView<R> V = cta_view<R>(smem_raw, P);
     const KissJump J = kiss_setup(P, V.sXs);  // once per launch
     R* scr = (R*)P.scratch + (size_t)blockIdx.x * P.slot_elems;
-    for (int pair = blockIdx.x; pair < P.npairs; pair += gridDim.x) solve_pair<R>(P, pair, V, J, scr, tab, tab64);
+    for (int pair = blockIdx.x; pair < P.npairs; pair += gridDim.x)
+        solve_pair<R, MT>(P, pair, V, J, scr, tab, tab64);
 }
 
 // ------------------------------------------------------------------ batch

@@ -53,10 +53,15 @@ cudaError_t launch_mcica_kiss(int ncol, int nlay, int icld, int permuteseed, con
                               const double* ssac, const double* asmc, const double* fsfc, const double* alpha,
                               double* cldfmcl, double* ciwpmcl, double* clwpmcl, double* taucmcl,
                               double* ssacmcl, double* asmcmcl, double* fsfcmcl, int* err, cudaStream_t s);
-// Mersenne Twister stream (getRandomReal values) of length n, seeded with seed
-cudaError_t launch_mt_stream(int seed, size_t n, double* out, cudaStream_t s);
-// mcica_subcol_sw from a precomputed random stream (irng = 1, GCM order)
-cudaError_t launch_mcica_stream(int ncol, int nlay, int icld, const double* stream, const double* cldfrac,
+// MT19937 stream of the reference generator seeded with seed: n tempered
+// words, segments of 2^log_seg words generated in parallel after a
+// jump-ahead (log_seg <= 0: chosen from n and num_sms) (mt19937.cu)
+cudaError_t launch_mt_jump(uint32_t seed, uint64_t n, uint32_t* out, int num_sms, int log_seg, cudaStream_t s);
+// raw (untempered) words behind outputs offset .. offset+623, on the host;
+// 0 or -1 (offset >= 2^48 or jump tables unavailable)
+int mt_window_host(uint32_t seed, uint64_t offset, uint32_t* window);
+// mcica_subcol_sw from the call's MT stream (irng = 1, GCM order)
+cudaError_t launch_mcica_stream(int ncol, int nlay, int icld, const uint32_t* stream, const double* cldfrac,
                                 const double* ciwp, const double* clwp, const double* tauc, const double* ssac,
                                 const double* asmc, const double* fsfc, const double* alpha, double* cldfmcl,
                                 double* ciwpmcl, double* clwpmcl, double* taucmcl, double* ssacmcl,

@@ -26,13 +26,12 @@ namespace rrsw {
 // --------------------------------------------------------------- params
 struct SolveParams {
     int ncol, nlay, icld, iaer, idelm, isolvar, inflag, iceflag, liqflag;
-    int fused;       // 1: McICA masks generated in the kernel (KISS)
+    int fused;       // 1: McICA masks generated in the kernel
     int nomcica;     // 1: non-McICA path (cldprop_sw + spcvrt_sw): layer cloud fraction, band optics
     int extra;       // 1: also the 8 direct/diffuse/UV/NIR outputs
     int permuteseed;
     int npairs;
-    double svar_f, svar_s, svar_i;
-    double svar_f_bnd[NBND], svar_s_bnd[NBND], svar_i_bnd[NBND], adjflux[NBND];
+    double svar_f_bnd[NBND], svar_s_bnd[NBND], svar_i_bnd[NBND], adjflux[NBND];  // solar variability factors
     const double *play, *plev, *tlay, *h2ovmr, *o3vmr, *co2vmr, *ch4vmr, *o2vmr;
     const double *asdir, *asdif, *aldir, *aldif, *coszen;
     const double *cldfmcl, *taucmcl, *ssacmcl, *asmcmcl, *fsfcmcl, *ciwpmcl, *clwpmcl, *reicmcl, *relqmcl;
@@ -41,12 +40,14 @@ struct SolveParams {
     double *swuflx, *swdflx, *swhr, *swuflxc, *swdflxc, *swhrc;
     double *xout[8];  // dirdflux, difdflux, uvdflx, nidflx, dirdnuv, difdnuv, dirdnir, difdnir
     int bands;        // 1: per-band fluxes requested
+    int irng;         // fused McICA generator: 0 KISS, 1 MT19937 (stream in mt)
     double *bout[5];  // bndfu, bndfd, bndfddir, bndcu, bndcd (ncol,nlay+1,nbnd)
     const int *colmap;   // batch: this instance's sunlit columns (nullptr: all columns in order)
     const int *mapcount; // batch: number of entries of colmap (device)
     void *scratch;
     size_t slot_elems;
     int *err;
+    const uint32_t* mt;  // irng 1: tempered MT words of the call's stream (subcolumn, column, layer order)
 };
 
 // Tangent-linear / adjoint request (solve_ad.cu): objective weights and
@@ -457,8 +458,7 @@ __device__ inline R solar_source(int ib, int ig, const Coef<R>& c, const SolvePa
         return band == 27 ? R(50.15 / 48.37) * sf : sf;
     }
     const R fb = src(B.facbrght), sd = src(B.snsptdrk), ir = src(B.irradnce);
-    if (P.isolvar == 3) return R(P.svar_f_bnd[ib]) * fb + R(P.svar_s_bnd[ib]) * sd + R(P.svar_i_bnd[ib]) * ir;
-    return R(P.svar_f) * fb + R(P.svar_s) * sd + R(P.svar_i) * ir;
+    return R(P.svar_f_bnd[ib]) * fb + R(P.svar_s_bnd[ib]) * sd + R(P.svar_i_bnd[ib]) * ir;
 }
 
 // Solar source for the FP32 form through the descriptors: the species
@@ -488,8 +488,7 @@ __device__ inline float solar_source_generic(int ib, int ig, const Coef<float>& 
         return band == 27 ? float(50.15 / 48.37) * sf : sf;
     }
     const float fb = src(B.facbrght), sd = src(B.snsptdrk), ir = src(B.irradnce);
-    if (P.isolvar == 3) return float(P.svar_f_bnd[ib]) * fb + float(P.svar_s_bnd[ib]) * sd + float(P.svar_i_bnd[ib]) * ir;
-    return float(P.svar_f) * fb + float(P.svar_s) * sd + float(P.svar_i) * ir;
+    return float(P.svar_f_bnd[ib]) * fb + float(P.svar_s_bnd[ib]) * sd + float(P.svar_i_bnd[ib]) * ir;
 }
 
 // --------------------------------------------------------------- cldprmc
@@ -856,47 +855,135 @@ __device__ inline Kiss kiss_start(const uint32_t* seed, const KissJump& J, const
     return k;
 }
 
+// getRandomReal (mcica_random_numbers.f90:276-295): u32 / (2^32 - 1) in FP64
+__device__ inline double mt_real(uint32_t y) { return __ddiv_rn((double)y, 4294967295.0); }
+
+// MT draws are carried as signed words, u32 ^ 2^31 (same order as the u32
+// value), so both generators fit the same 32-bit mask state.
+__device__ inline int32_t mt_signed(uint32_t u) { return (int32_t)(u ^ 0x80000000u); }
+
+// Smallest signed MT draw d with mt_real(d ^ 2^31) >= x, in [-2^31, 2^31]:
+// comparing the draw with it is the reference's FP64 comparison (mt_real is
+// increasing).
+__device__ inline long long mt_threshold(double x) {
+    const long long hi = 4294967295ll;
+    long long k;
+    if (mt_real(0u) >= x) {
+        k = 0;
+    } else if (mt_real(0xffffffffu) < x) {
+        k = hi + 1;
+    } else {
+        k = (long long)floor(x * 4294967295.0);
+        k = k < 0 ? 0 : (k > hi ? hi : k);
+        while (k > 0 && mt_real((uint32_t)(k - 1)) >= x) --k;
+        while (mt_real((uint32_t)k) < x) ++k;
+    }
+    return k - 2147483648ll;
+}
+
+// position of (subcolumn g, column col)'s first draw in the MT stream of a
+// call: one stream in (subcolumn, column, layer) order (mcica_subcol_gen_sw.f90
+// MT branch), two draws per layer for icld 4/5, one per column for icld 3
+__device__ inline size_t mt_offset(int icld, int g, int col, int ncol, int nlay) {
+    const size_t sc = (size_t)g * (size_t)ncol + (size_t)col;
+    if (icld == 3) return sc;
+    if (icld >= 4) return 2 * sc * (size_t)nlay;
+    return sc * (size_t)nlay;
+}
+
 // Subcolumn cloud mask walked bottom -> top (generate_stochastic_clouds_sw,
-// KISS branch, mcica_subcol_gen_sw.f90:492-659; icld 4/5 in the
-// single-column generator's order, mcica_subcol_gen_sw.1col.f90:536-604).
-// icld 1/3/4/5 compare raw integer draws with per-layer thresholds
-// (kc: 1 - cldf, ka: alpha); icld 2 rescales the CDF and stays in FP64.
+// mcica_subcol_gen_sw.f90:492-659; icld 4/5 in the single-column
+// generator's order, mcica_subcol_gen_sw.1col.f90:536-604).  Draws come from
+// the KISS state (MT = false, irng 0) or from this subcolumn's run of a
+// precomputed MT stream (MT = true, irng 1), whose address the KISS words
+// hold (s1, s2) with the next layer's draws (s3, s4), loaded one layer
+// ahead.  icld 1/3/4/5 compare the draws with per-layer thresholds (kc:
+// 1 - cldf, ka: alpha, from kiss_threshold or mt_threshold); icld 2
+// rescales the CDF in FP64.
+template <bool MT>
 struct McicaMask {
     Kiss k;
     int icld;
     int32_t prev, d0;
     double cdf_prev, omcf_prev;
-    __device__ void start(const Kiss& k0, int icld_) {
-        k = k0;
+    __device__ const uint32_t* run() const {
+        return (const uint32_t*)(((uint64_t)k.s2 << 32) | (uint64_t)k.s1);
+    }
+    // MT draws of layer lay (two for icld 4/5: the run starts at an even
+    // word, so the pair is 8-byte aligned).  The stream buffer carries two
+    // words of padding, so the read one layer past the last run stays inside.
+    __device__ void fetch(int lay) {
+        const uint32_t* r = run();
+        if (icld >= 4) {
+            const uint2 v = __ldg((const uint2*)r + (lay - 1));
+            k.s3 = v.x;
+            k.s4 = v.y;
+        } else {
+            k.s3 = __ldg(r + (lay - 1));
+        }
+    }
+    __device__ void start(const Kiss& k0, int icld_, const uint32_t* mt = nullptr) {
         icld = icld_;
         prev = 0;
         cdf_prev = 0.0;
         omcf_prev = 1.0;
-        d0 = icld == 3 ? k.next_int() : 0;
+        if constexpr (MT) {
+            k.s1 = (uint32_t)(uint64_t)mt;
+            k.s2 = (uint32_t)((uint64_t)mt >> 32);
+            d0 = 0;
+            if (icld == 3) d0 = mt_signed(__ldg(mt));
+            else fetch(1);
+        } else {
+            k = k0;
+            d0 = icld == 3 ? k.next_int() : 0;
+        }
     }
     __device__ bool step(int lay, long long kc, long long ka, double omcf) {
-        if (icld == 2) {
-            double cdf = kiss_real(k.next_int());
-            if (lay >= 2) {
-                if (cdf_prev > omcf_prev) cdf = cdf_prev;
-                else cdf = __dmul_rn(cdf, omcf_prev);
+        if constexpr (MT) {
+            int32_t d = 0, d2 = 0;
+            if (icld != 3) {
+                d = mt_signed(k.s3);
+                d2 = mt_signed(k.s4);
+                fetch(lay + 1);
             }
-            cdf_prev = cdf;
-            omcf_prev = omcf;
-            return cdf >= omcf;
-        }
-        int32_t d;
-        if (icld == 3) {
-            d = d0;
-        } else if (icld >= 4) {
-            d = k.next_int();
-            const int32_t d2 = k.next_int();
-            if (lay >= 2 && (long long)d2 < ka) d = prev;
+            if (icld == 2) {
+                double cdf = mt_real((uint32_t)d ^ 0x80000000u);
+                if (lay >= 2) {
+                    if (cdf_prev > omcf_prev) cdf = cdf_prev;
+                    else cdf = __dmul_rn(cdf, omcf_prev);
+                }
+                cdf_prev = cdf;
+                omcf_prev = omcf;
+                return cdf >= omcf;
+            }
+            if (icld == 3) d = d0;
+            else if (icld >= 4 && lay >= 2 && (long long)d2 < ka) d = prev;
+            prev = d;
+            return (long long)d >= kc;
         } else {
-            d = k.next_int();
+            if (icld == 2) {
+                double cdf = kiss_real(k.next_int());
+                if (lay >= 2) {
+                    if (cdf_prev > omcf_prev) cdf = cdf_prev;
+                    else cdf = __dmul_rn(cdf, omcf_prev);
+                }
+                cdf_prev = cdf;
+                omcf_prev = omcf;
+                return cdf >= omcf;
+            }
+            int32_t d;
+            if (icld == 3) {
+                d = d0;
+            } else if (icld >= 4) {
+                d = k.next_int();
+                const int32_t d2 = k.next_int();
+                if (lay >= 2 && (long long)d2 < ka) d = prev;
+            } else {
+                d = k.next_int();
+            }
+            prev = d;
+            return (long long)d >= kc;
         }
-        prev = d;
-        return (long long)d >= kc;
     }
 };
 

@@ -150,9 +150,10 @@ LaunchInfo plan_fp32(const SolveParams& P, int num_sms) {
     LaunchInfo li;
     li.smem = smem_layout(P.nlay, num_q<float>(P.extra != 0), stages_clouds(P),
                           stage_aerosol<float>(P.iaer), sizeof(float)).total;
-    cudaFuncSetAttribute(k_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
+    const auto kern = P.mt ? k_solve<float, true> : k_solve<float, false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<float>, CTA_THREADS, li.smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CTA_THREADS, li.smem);
     if (per_sm < 1) per_sm = 1;
     li.grid = num_sms * per_sm;
     if (li.grid > P.npairs) li.grid = P.npairs;
@@ -162,7 +163,8 @@ LaunchInfo plan_fp32(const SolveParams& P, int num_sms) {
 
 cudaError_t launch_solve_fp32(const SolveParams& P, const float* tab, const double* tab64, const LaunchInfo& li,
                               cudaStream_t s) {
-    k_solve<float><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab64);
+    if (P.mt) k_solve<float, true><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab64);
+    else k_solve<float, false><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab64);
     return cudaGetLastError();
 }
 

@@ -19,9 +19,10 @@ LaunchInfo plan_fp64(const SolveParams& P, int num_sms) {
     LaunchInfo li;
     li.smem = smem_layout(P.nlay, num_q<double>(P.extra != 0), stages_clouds(P),
                           stage_aerosol<double>(P.iaer), sizeof(double)).total;
-    cudaFuncSetAttribute(k_solve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
+    const auto kern = P.mt ? k_solve<double, true> : k_solve<double, false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<double>, CTA_THREADS, li.smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CTA_THREADS, li.smem);
     if (per_sm < 1) per_sm = 1;
     li.grid = num_sms * per_sm;
     if (li.grid > P.npairs) li.grid = P.npairs;
@@ -30,7 +31,8 @@ LaunchInfo plan_fp64(const SolveParams& P, int num_sms) {
 }
 
 cudaError_t launch_solve_fp64(const SolveParams& P, const double* tab, const LaunchInfo& li, cudaStream_t s) {
-    k_solve<double><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab);
+    if (P.mt) k_solve<double, true><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab);
+    else k_solve<double, false><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab);
     return cudaGetLastError();
 }
 
@@ -140,7 +142,7 @@ __global__ void k_mcica_kiss(int ncol, int nlay, int icld, int permuteseed, cons
     seed[1] = kiss_seed(p2);
     seed[2] = kiss_seed(__dmul_rn(play[col + 2 * n], 1.e2));
     seed[3] = kiss_seed(__dmul_rn(play[col + 3 * n], 1.e2));
-    McicaMask mc;
+    McicaMask<false> mc;
     mc.start(kiss_start(seed, kiss_jump_consts(off), xcol), icld);
     for (int lay = 1; lay <= nlay; ++lay) {
         const size_t kl = (size_t)col + n * (size_t)(lay - 1);
@@ -165,60 +167,10 @@ cudaError_t launch_mcica_kiss(int ncol, int nlay, int icld, int permuteseed, con
     return cudaGetLastError();
 }
 
-// Mersenne Twister MT19937 (mcica_random_numbers.f90:77-306), one CTA: the
-// 624-word state is regenerated in three dependency-free phases per block
-// (k = 0..226, 227..453, 454..622) plus the last word, then tempered in
-// parallel; getRandomReal = u32 / (2^32 - 1).
-__global__ void k_mt_stream(int seed, size_t n, double* out) {
-    __shared__ uint32_t st[624];
-    if (threadIdx.x == 0) {
-        st[0] = (uint32_t)seed;
-        for (int i = 1; i < 624; ++i) st[i] = 1812433253u * (st[i - 1] ^ (st[i - 1] >> 30)) + (uint32_t)i;
-    }
-    __syncthreads();
-    auto twist = [](uint32_t u, uint32_t v) {
-        const uint32_t mix = (u & 0x80000000u) | (v & 0x7fffffffu);
-        return (mix >> 1) ^ ((v & 1u) ? 0x9908b0dfu : 0u);
-    };
-    for (size_t base = 0; base < n; base += 624) {
-        // each phase reads the words it needs before any thread writes
-        // (blockDim >= 227, so one word per thread per phase)
-        const int k = threadIdx.x;
-        uint32_t v = 0;
-        if (k < 227) v = st[k + 397] ^ twist(st[k], st[k + 1]);
-        __syncthreads();
-        if (k < 227) st[k] = v;
-        __syncthreads();
-        if (k < 227) v = st[k] ^ twist(st[k + 227], st[k + 228]);
-        __syncthreads();
-        if (k < 227) st[k + 227] = v;
-        __syncthreads();
-        if (k < 169) v = st[k + 227] ^ twist(st[k + 454], st[k + 455]);
-        __syncthreads();
-        if (k < 169) st[k + 454] = v;
-        __syncthreads();
-        if (k == 0) st[623] = st[396] ^ twist(st[623], st[0]);
-        __syncthreads();
-        for (int kk = threadIdx.x; kk < 624 && base + kk < n; kk += blockDim.x) {
-            uint32_t y = st[kk];
-            y ^= (y >> 11);
-            y ^= (y << 7) & 0x9d2c5680u;
-            y ^= (y << 15) & 0xefc60000u;
-            y ^= (y >> 18);
-            out[base + kk] = (double)y / (4294967296.0 - 1.0);
-        }
-        __syncthreads();
-    }
-}
-
-cudaError_t launch_mt_stream(int seed, size_t n, double* out, cudaStream_t s) {
-    k_mt_stream<<<1, 256, 0, s>>>(seed, n, out);
-    return cudaGetLastError();
-}
-
-// McICA from a precomputed stream in the reference's (subcolumn, column,
-// layer) order (irng = 1).
-__global__ void k_mcica_stream(int ncol, int nlay, int icld, const double* rs, const double* cldfrac,
+// McICA from the call's MT19937 stream (irng = 1; tempered words in the
+// reference's (subcolumn, column, layer) order, from launch_mt_jump), with
+// the same mask walk as the fused solve.
+__global__ void k_mcica_stream(int ncol, int nlay, int icld, const uint32_t* rs, const double* cldfrac,
                                const double* ciwp, const double* clwp, const double* tauc, const double* ssac,
                                const double* asmc, const double* fsfc, const double* alpha, double* cldfmcl,
                                double* ciwpmcl, double* clwpmcl, double* taucmcl, double* ssacmcl, double* asmcmcl,
@@ -226,35 +178,21 @@ __global__ void k_mcica_stream(int ncol, int nlay, int icld, const double* rs, c
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (size_t)ncol * NGPT) return;
     const int g = (int)(t % NGPT), col = (int)(t / NGPT);
-    const size_t n = (size_t)ncol, L = (size_t)nlay;
-    const size_t sc = (size_t)g * n + (size_t)col;  // (subcolumn, column) position
-    double cdf_prev = 0.0, cf_prev = 0.0;
+    const size_t n = (size_t)ncol;
+    McicaMask<true> mc;
+    mc.start(Kiss{1u, 1u, 1u, 1u}, icld, rs + mt_offset(icld, g, col, ncol, nlay));
     for (int lay = 1; lay <= nlay; ++lay) {
         const size_t kl = (size_t)col + n * (size_t)(lay - 1);
         double cf = cldfrac[kl];
         if (cf < 1.0e-20) cf = 0.0;
-        double cdf;
-        if (icld == 3) {
-            cdf = rs[sc];
-        } else if (icld >= 4) {
-            const size_t p = 2 * (sc * L + (size_t)(lay - 1));
-            cdf = rs[p];
-            if (lay >= 2 && rs[p + 1] < alpha[kl]) cdf = cdf_prev;
-        } else {
-            cdf = rs[sc * L + (size_t)(lay - 1)];
-            if (icld == 2 && lay >= 2) {
-                if (cdf_prev > 1.0 - cf_prev) cdf = cdf_prev;
-                else cdf = cdf * (1.0 - cf_prev);
-            }
-        }
-        cdf_prev = cdf;
-        cf_prev = cf;
-        mcica_fill(cdf >= 1.0 - cf, g, kl, (size_t)g + NGPT * kl, ciwp, clwp, tauc, ssac, asmc, fsfc, cldfmcl,
+        const double omcf = __dsub_rn(1.0, cf);
+        const bool cloudy = mc.step(lay, mt_threshold(omcf), icld >= 4 ? mt_threshold(alpha[kl]) : 0ll, omcf);
+        mcica_fill(cloudy, g, kl, (size_t)g + NGPT * kl, ciwp, clwp, tauc, ssac, asmc, fsfc, cldfmcl,
                    ciwpmcl, clwpmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl);
     }
 }
 
-cudaError_t launch_mcica_stream(int ncol, int nlay, int icld, const double* stream, const double* cldfrac,
+cudaError_t launch_mcica_stream(int ncol, int nlay, int icld, const uint32_t* stream, const double* cldfrac,
                                 const double* ciwp, const double* clwp, const double* tauc, const double* ssac,
                                 const double* asmc, const double* fsfc, const double* alpha, double* cldfmcl,
                                 double* ciwpmcl, double* clwpmcl, double* taucmcl, double* ssacmcl,

@@ -107,6 +107,8 @@ def lib():
         L.mcica_subcol_sw_c.argtypes = [C.c_int32] * 5 + [_dp] * 11 + [_dp] * 9
         L.get_alpha_c.argtypes = [C.c_int32] * 4 + [C.c_double, _dp, _dp, C.c_int32, _dp, _dp]
         L.rrtmg_sw_set_form_c.argtypes = [C.c_int32]
+        L.rrtmg_sw_mt_window_c.argtypes = [C.c_int32, C.c_uint64, C.POINTER(C.c_uint32)]
+        L.rrtmg_sw_mt_stream_dev_c.argtypes = [C.c_int32, C.c_uint64, C.c_void_p, C.c_int32, C.c_void_p]
         L.rrtmg_sw_errstr_c.restype = C.c_char_p
         L.rrtmg_sw_errstr_c.argtypes = [C.c_int32]
         L.rrtmg_sw_last_cuda_error_c.restype = C.c_char_p
@@ -237,6 +239,31 @@ def mcica_subcol_sw(iplon, ncol, nlay, icld, permuteseed, irng, play, cldfrac, c
     _check(lib().mcica_subcol_sw_c(ncol, nlay, icld, permuteseed, irng, *[_p(x) for x in ins],
                                    *[_p(x) for x in outs]))
     return tuple(outs)
+
+
+def mt_window(seed, offset):
+    """The 624 raw MT19937 state words behind outputs ``offset`` ..
+    ``offset + 623`` of the McICA generator seeded with ``seed``, computed on
+    the host by jump-ahead (no GPU needed)."""
+    w = np.zeros(624, dtype=np.uint32)
+    _check(lib().rrtmg_sw_mt_window_c(seed, offset, w.ctypes.data_as(C.POINTER(C.c_uint32))))
+    return w
+
+
+def mt_temper(y):
+    """MT19937 output tempering of raw state words (uint32 array)."""
+    y = np.asarray(y, dtype=np.uint32).copy()
+    y ^= y >> np.uint32(11)
+    y ^= (y << np.uint32(7)) & np.uint32(0x9d2c5680)
+    y ^= (y << np.uint32(15)) & np.uint32(0xefc60000)
+    y ^= y >> np.uint32(18)
+    return y
+
+
+def mt_stream_dev(seed, n, out_ptr, log_seg=0, stream=0):
+    """Outputs 0 .. n-1 of the MT19937 stream (tempered uint32) into the
+    device buffer at ``out_ptr``, in segments of 2**log_seg words."""
+    _check(lib().rrtmg_sw_mt_stream_dev_c(seed, n, C.c_void_p(out_ptr), log_seg, C.c_void_p(stream)))
 
 
 def get_alpha(iplon, ncol, nlayers, icld, idcor, decorr_con, dz, lat, juldat, cldfrac):
