@@ -36,6 +36,15 @@ struct TmRegion {
     int ktab, mtab, rtab;
 };
 
+// One band/region descriptor with the band's continuum offsets, as the FP32
+// solve keeps it in shared memory: a warp's g-points span several bands, and
+// indexing the constant bank by band serialises; three 16-byte shared loads
+// per layer replace those constant loads.
+struct alignas(16) TmSmem {
+    TmRegion r;
+    int selfref, forref, ng, pad;
+};
+
 struct DevTables {
     BandOff b[NBND];
     int pref, preflog, tref;

@@ -503,7 +503,7 @@ __device__ inline void warp_sum4(R& v) {
 // Shared-memory carve-up of one CTA (two columns); the host sizes the
 // launch with the same function.
 struct Smem {
-    size_t pdp, coef, hrf, pk, misc, kc, ka, omcf, cld, seed, aer, xs, red, flux, total;
+    size_t tm, pdp, coef, hrf, pk, misc, kc, ka, omcf, cld, seed, aer, xs, red, flux, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -511,6 +511,10 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t
 __host__ __device__ inline Smem smem_layout(int L, int nq, bool fused, bool aer_stage, size_t rsz) {
     Smem m;
     size_t o = 0;
+    m.tm = o;
+    // FP32 form: taumol descriptors first, at a fixed offset (the batch
+    // kernel fills them once and re-lays the rest out per instance)
+    if (rsz == sizeof(float)) o = align16(o + NBND * 2 * sizeof(TmSmem));
     m.pdp = o;  o = align16(o + COLS_PER_CTA * L * sizeof(double));
     m.coef = o; o = align16(o + COLS_PER_CTA * NFR * L * rsz);
     m.hrf = o;
@@ -551,6 +555,7 @@ __host__ __device__ inline bool stage_aerosol(int iaer) {
 // Shared-memory views of one CTA for the parameters P (two columns).
 template <typename R>
 struct CtaView {
+    const TmSmem* sTm;  // [14][2] FP32 form: taumol descriptors
     double* sPdp;       // [2][L]
     R* sCoef;           // [2][NFR][L]
     float* sHrf;        // [2][L] FP32 form: heatfac / dp
@@ -571,6 +576,7 @@ template <typename R>
 __device__ inline CtaView<R> cta_view(unsigned char* smem_raw, const SolveParams& P) {
     const Smem M = smem_layout(P.nlay, num_q<R>(P.extra != 0), stages_clouds(P), stage_aerosol<R>(P.iaer), sizeof(R));
     CtaView<R> v;
+    v.sTm = (const TmSmem*)(smem_raw + M.tm);
     v.sPdp = (double*)(smem_raw + M.pdp);
     v.sCoef = (R*)(smem_raw + M.coef);
     v.sHrf = (float*)(smem_raw + M.hrf);
@@ -586,6 +592,24 @@ __device__ inline CtaView<R> cta_view(unsigned char* smem_raw, const SolveParams
     v.sRed = (R*)(smem_raw + M.red);
     v.sFlux = (R*)(smem_raw + M.flux);
     return v;
+}
+
+// FP32 form: the taumol descriptors of every band and region into shared
+// memory (offset 0 of the dynamic area); read after the next barrier.
+template <typename R>
+__device__ inline void fill_tm(unsigned char* smem_raw) {
+    if constexpr (sizeof(R) == 4) {
+        TmSmem* d = (TmSmem*)smem_raw;
+        for (int i = threadIdx.x; i < NBND * 2; i += blockDim.x) {
+            TmSmem t;
+            t.r = cT.tm[i / 2][i % 2];
+            t.selfref = cT.b[i / 2].selfref;
+            t.forref = cT.b[i / 2].forref;
+            t.ng = cT.b[i / 2].ng;
+            t.pad = 0;
+            d[i] = t;
+        }
+    }
 }
 
 // McICA stream jump of this thread's subcolumn for parameters P; the
@@ -735,7 +759,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         albd = (R)(nir ? P.aldif[col] : P.asdif[col]);
         // zincflx = adjflux * ssi * prmu0 (spcvmc:349-356)
         R src;
-        if constexpr (sizeof(R) == 4) src = solar_source_generic(ib, igb, C, P, tab);
+        if constexpr (sizeof(R) == 4) src = solar_source_generic(ib, igb, C, P, tab, V.sTm);
         else src = solar_source<R>(ib, igb, C, P, tab);
         zinc = R(P.adjflux[ib]) * src * (R)cossza;
         if (fused)
@@ -757,7 +781,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         if constexpr (sizeof(R) == 4) {
             int js;
             float fs;
-            taumol_generic(ib, igb, lay, C, tab, taug, taur, js, fs);
+            taumol_generic(ib, igb, lay, C, tab, V.sTm, taug, taur, js, fs);
         } else {
             taumol_g<R>(ib, igb, lay, C, tab, taug, taur);
         }
@@ -1019,6 +1043,7 @@ template <typename R, bool MT>
 __global__ void __launch_bounds__(CTA_THREADS, sizeof(R) == 4 ? 3 : 2)
 k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict__ tab64) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    fill_tm<R>(smem_raw);
     const CtaView<R> V = cta_view<R>(smem_raw, P);
     const KissJump J = kiss_setup(P, V.sXs);  // once per launch
     R* scr = (R*)P.scratch + (size_t)blockIdx.x * P.slot_elems;
@@ -1040,6 +1065,7 @@ k_solve_batch(const SolveParams* __restrict__ Pb, int ninst, const int* __restri
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_pref[MAX_BATCH + 1];
     __shared__ __align__(16) SolveParams sP;
+    fill_tm<R>(smem_raw);
     if (threadIdx.x == 0) {
         s_pref[0] = 0;
         for (int i = 0; i < ninst; ++i) s_pref[i + 1] = s_pref[i] + (counts[i] + COLS_PER_CTA - 1) / COLS_PER_CTA;

@@ -339,12 +339,14 @@ __device__ inline void taumol_g(int ib, int ig, int lay, const Coef<R>& c, const
 }
 
 // One g-point of taumol16..29 through the band/region descriptors (FP32
-// form): same terms as taumol_g, one instruction stream for all bands.
+// form): same terms as taumol_g, one instruction stream for all bands.  The
+// descriptors come from shared memory (sTm[band][region]).
 __device__ inline void taumol_generic(int ib, int ig, int lay, const Coef<float>& c, const float* __restrict__ tab,
-                                      float& taug, float& taur, int& js_out, float& fs_out) {
-    const BandOff& B = cT.b[ib];
-    const TmRegion& d = cT.tm[ib][lay <= c.laytrop ? 0 : 1];
-    const int ng = B.ng;
+                                      const TmSmem* __restrict__ sTm, float& taug, float& taur, int& js_out,
+                                      float& fs_out) {
+    const TmSmem t = sTm[ib * 2 + (lay <= c.laytrop ? 0 : 1)];
+    const TmRegion& d = t.r;
+    const int ng = t.ng;
     const int jp = c.jp(lay) - d.jo, jt = c.jt(lay), jt1 = c.jt1(lay);
     const float colh2o = c.f(F_H2O, lay);
     float tg = 0.0f, fs = 0.0f;
@@ -376,8 +378,18 @@ __device__ inline void taumol_generic(int ib, int ig, int lay, const Coef<float>
                          c.f(F_FAC01, lay) * __ldg(k + i1) + c.f(F_FAC11, lay) * __ldg(k + i1 + ng);
         tg = c.f(F_H2O + d.sa, lay) * d.fac * kk;
     }
-    if (d.cont == 1) tg += colh2o * (selfterm(c, lay, B, tab, ig) + forterm(c, lay, B, tab, ig));
-    else if (d.cont == 2) tg += colh2o * forterm(c, lay, B, tab, ig);
+    if (d.cont >= 1) {
+        const int indf = c.indfor(lay);
+        const float fa = __ldg(tab + t.forref + (indf - 1) * ng + ig - 1), fb = __ldg(tab + t.forref + indf * ng + ig - 1);
+        float cont = c.f(F_FORFAC, lay) * (fa + c.f(F_FORFRAC, lay) * (fb - fa));
+        if (d.cont == 1) {
+            const int inds = c.indself(lay);
+            const float sa = __ldg(tab + t.selfref + (inds - 1) * ng + ig - 1);
+            const float sb = __ldg(tab + t.selfref + inds * ng + ig - 1);
+            cont = c.f(F_SELFFAC, lay) * (sa + c.f(F_SELFFRAC, lay) * (sb - sa)) + cont;
+        }
+        tg += colh2o * cont;
+    }
     if (d.minor == 9) tg += 4.35e-4f * c.f(F_O2, lay) / 700.0f;
     else if (d.minor >= 0) tg += c.f(F_H2O + d.minor, lay) * __ldg(tab + d.mtab + ig - 1);
     const float colmol = c.f(F_MOL, lay);
@@ -465,7 +477,7 @@ __device__ inline R solar_source(int ib, int ig, const Coef<R>& c, const SolvePa
 // interpolation of the source tables applies where the source region is a
 // kind-1 (speccomb) loop, as in taumol17,18,19,21,22,24,28.
 __device__ inline float solar_source_generic(int ib, int ig, const Coef<float>& c, const SolveParams& P,
-                                             const float* __restrict__ tab) {
+                                             const float* __restrict__ tab, const TmSmem* __restrict__ sTm) {
     const BandOff& B = cT.b[ib];
     const int band = ib + 16;
     const int lay = solar_layer(ib, c);
@@ -475,7 +487,7 @@ __device__ inline float solar_source_generic(int ib, int ig, const Coef<float>& 
     float fs = 0.0f;
     if (lay >= 1 && cT.tm[ib][up].kind == 1) {
         float tg, tr;
-        taumol_generic(ib, ig, lay, c, tab, tg, tr, js, fs);
+        taumol_generic(ib, ig, lay, c, tab, sTm, tg, tr, js, fs);
         interp = true;
     }
     auto src = [&](int off) -> float {
