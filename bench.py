@@ -45,6 +45,8 @@ def parse():
     p.add_argument("--workload", default="fp32", choices=["fp32", "batch", "adjoint"],
                    help="fp32: the FP32-form headline; batch: 48 ragged instances in one launch (FP64 form)")
     p.add_argument("--instances", type=int, default=48)
+    p.add_argument("--batch-form", default="fp64", choices=["fp64", "fp32"],
+                   help="arithmetic form of --workload batch (the batching configuration names FP64)")
     p.add_argument("--irng", type=int, default=0, choices=[0, 1],
                    help="McICA generator of the fused solve: 0 KISS, 1 MT19937 (one stream per call, GCM order)")
     return p.parse_args()
@@ -182,7 +184,9 @@ def run_batch(args):
     from rrtmg_sw_gb300.synthetic import make_columns
     build.build()
     gi.rrtmg_sw_ini(1.004e3)
-    gi.set_form(gi.FORM_FP64)
+    fp32 = args.batch_form == "fp32"
+    form_name = "FP32 form" if fp32 else "FP64 form"
+    gi.set_form(gi.FORM_FP32 if fp32 else gi.FORM_FP64)
     rng = np.random.default_rng(20261203 + 2)
     dev = torch.device("cuda", 0)
     ptr = lambda t: C.cast(C.c_void_p(t.data_ptr()), gi._dp)
@@ -239,12 +243,12 @@ def run_batch(args):
                     "single_columns_per_s": x["sunlit"] / (m1 / 1e3)})
     info = plan.info()
     plan.close()
-    line = {"metric": "sunlit columns/s, 48 ragged instances in one persistent launch (FP64 form)",
+    line = {"metric": "sunlit columns/s, 48 ragged instances in one persistent launch (%s)" % form_name,
             "value": sunlit / (ms / 1e3), "unit": "columns/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup,
-            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if fp32 else "f64", "data": "synthetic",
             "config": {"workload": "%d instances, ncol log-uniform 512..131072, nlay in {40,47,60,72,91,137}, 40%% "
-                                   "night, McICA icld=2, FP64 form" % len(insts),
+                                   "night, McICA icld=2, %s" % (len(insts), form_name),
                        "columns": sum(x["ncol"] for x in insts), "sunlit": sunlit},
             "sum_of_single_calls_ms": sum(p["single_ms"] for p in per),
             "autotuner": info, "instances": per}
@@ -387,6 +391,14 @@ def main():
         ms64 = timed(gi.FORM_FP64, max(2, args.steps // 5), 1)
         res64 = {k: v.cpu().numpy() for k, v in outs.items()}
         err = {k: float(np.max(np.abs(res32[k] - res64[k]))) for k in res32}
+        rms = {k: float(np.sqrt(np.mean((res32[k] - res64[k]) ** 2))) for k in res32}
+        # per level (fluxes, surface first) / per layer (heating rates): max and RMS over columns
+        per_level = {}
+        for k in res32:
+            nl = NLAY if k in ("swhr", "swhrc") else NLAY + 1
+            dk = (res32[k] - res64[k]).reshape((nl, ncol))
+            per_level[k] = {"max": [float("%.3g" % v) for v in np.max(np.abs(dk), axis=1)],
+                            "rms": [float("%.3g" % v) for v in np.sqrt(np.mean(dk * dk, axis=1))]}
     gi.set_form(gi.FORM_FP32)
 
     # irng = 1: the MT19937 generator alone on the call's stream (icld 5: two draws per cell)
@@ -493,7 +505,8 @@ def main():
                    (sum(v.numel() * 8 for v in d.values()) / 1e9)},
         "fp64": None if ms64 is None else {"value": sunlit * world / (ms64 / 1e3), "ms_per_step": ms64,
                                            "speedup_fp32_over_fp64": ms64 / ms32,
-                                           "max_abs_diff_fp32_vs_fp64": err},
+                                           "max_abs_diff_fp32_vs_fp64": err, "rms_diff_fp32_vs_fp64": rms,
+                                           "per_level_diff_fp32_vs_fp64": per_level},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                      "frac": (achieved / peak32) if peak32 else None,
                      "traffic": PROFILED_DRAM_BYTES_PER_COLUMN * ncol if NLAY == 60 else None,

@@ -16,6 +16,14 @@ input preparation (mixing ratios to column amounts :1743-1768, albedo
 (McICA sampling, cloud optics, gas optics, two-stream solve) is left to the
 oracle.  The expected outputs are the committed ``output_rrtm_*`` tables,
 one block per band range.
+
+The five solar-variability runs (``iatm = 1``: their layers come from the
+profile builder ``rrtatm.f``, which is not restated) contribute only what
+does not depend on the layers: their solar records (:1391-1436: juldat,
+sza, isolvar, scon, solcycfrac, solvar) and the top-of-atmosphere row of
+every block.  The downward flux there is the band's solar source times
+cos(sza); for the bands whose source is not interpolated in a species
+ratio at the reference layer it pins the solar-variability factors.
 """
 import json
 import math
@@ -41,6 +49,19 @@ CASES = [
      "output_rrtm_MLS-cld7-imca1-icld5-idcor0"),
     ("MLS-cld7-imca1-icld5-idcor1", "input_rrtm_MLS-cld-imca1-icld5-idcor1", "in_cld_rrtm-cld7", None,
      "output_rrtm_MLS-cld7-imca1-icld5-idcor1"),
+]
+
+SOLVAR_CASES = [
+    ("MLS-clr-sza45-isolvar0_tsi_avg", "input_rrtm_MLS-clr-sza45-isolvar0_tsi_avg",
+     "output_rrtm_MLS-clr-sza45-isolvar0_tsi_avg"),
+    ("MLS-clr-sza45-isolvar1_tsi_max", "input_rrtm_MLS-clr-sza45-isolvar1_tsi_max",
+     "output_rrtm_MLS-clr-sza45-isolvar1_tsi_max"),
+    ("MLS-clr-sza45-isolvar1_tsi_min", "input_rrtm_MLS-clr-sza45-isolvar1_tsi_min",
+     "output_rrtm_MLS-clr-sza45-isolvar1_tsi_min"),
+    ("MLS-clr-sza45-isolvar2_01Jan1950", "input_rrtm_MLS-clr-sza45-isolvar2_01Jan1950",
+     "output_rrtm_MLS-clr-sza45-isolvar2_01Jan1950"),
+    ("MLS-clr-sza45-isolvar3_bndscl_tsi_max", "input_rrtm_MLS-clr-sza45-isolvar3_bndscl_tsi_max",
+     "output_rrtm_MLS-clr-sza45-isolvar3_bndscl_tsi_max"),
 ]
 
 WAVENUM1 = [2600., 3250., 4000., 4650., 5150., 6150., 7700., 8050., 12850., 16000., 22650., 29000., 38000., 820.]
@@ -180,6 +201,34 @@ def read_input(path):
                 albedo=[1.0 - e for e in semiss], idcor=idcor, decorr_con=decorr_con, lat=lat,
                 pavel=pavel, tavel=tavel, pz=pz, tz=tz, coldry=coldry,
                 wkl=[w for lay in wkl for w in lay], dz=dz)
+
+
+def read_solar(path):
+    """Solar records of an iatm = 1 run (:1391-1436) and its surface albedo."""
+    lines = open(path).read().splitlines()
+    k = 0
+    while not lines[k].startswith("$"):
+        k += 1
+    k += 1
+    r = Rec(lines[k]); k += 1
+    r.skip(18); r.i(2); r.skip(29); iatm = r.i(1); r.skip(32); iscat = r.i(1)
+    assert iatm == 1 and iscat == 1
+    # 9020 format (12x, i3, 3x, f7.4, 3x, i2, f10.4, f10.5, 14f10.5)
+    r = Rec(lines[k]); k += 1
+    r.skip(12); juldat = r.i(3); r.skip(3); sza = r.f(7, 4); r.skip(3); isolvar = r.i(2)
+    scon = r.f(10, 4); solcycfrac = r.f(10, 5)
+    solvar = [r.f(10, 5) for _ in range(14)]
+    # 9012 format (11x,i1,2x,i1,14f5.3)
+    r = Rec(lines[k]); k += 1
+    r.skip(11); iemis = r.i(1); r.skip(2); r.i(1)
+    semiss = [r.f(5, 3) for _ in range(14)]
+    if iemis == 0:
+        semiss = [1.0] * 14
+    elif iemis == 1:
+        semiss = [semiss[0]] * 14
+    pi = 2.0 * math.asin(1.0)
+    return dict(juldat=juldat, sza=sza, zenith=math.cos(sza * pi / 180.0), isolvar=isolvar, scon=scon,
+                solcycfrac=solcycfrac, solvar=solvar, albedo=[1.0 - e for e in semiss])
 
 
 def read_cloud(path, nlay):
@@ -323,6 +372,21 @@ def main(ref):
     with open(path, "w") as f:
         json.dump({"source": "RRTMG_SW run_examples_std_atm (iatm=0 runs)", "cases": out}, f)
     print("wrote", path, len(out), "cases")
+    sol = []
+    for name, inp, outp in SOLVAR_CASES:
+        c = read_solar(os.path.join(d, inp))
+        c["name"] = name
+        toa = []
+        for b in read_output(os.path.join(d, outp)):
+            toa.append(dict(istart=b["istart"], iend=b["iend"], p=b["p"][-1], uflx=b["uflx"][-1],
+                            dirdflx=b["dirdflx"][-1], dflx=b["dflx"][-1]))
+        c["toa"] = toa
+        sol.append(c)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "solvar_toa_cases.json")
+    with open(path, "w") as f:
+        json.dump({"source": "RRTMG_SW run_examples_std_atm (iatm=1 runs): solar records and "
+                             "top-of-atmosphere rows", "cases": sol}, f, indent=1)
+    print("wrote", path, len(sol), "cases")
 
 
 if __name__ == "__main__":

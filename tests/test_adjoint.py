@@ -99,7 +99,8 @@ def test_adjoint_is_transpose_of_tangent_linear(gpu, weights):
         dot += ad[k] * d[k]
     scale = max(np.max(np.abs(tl["dJ"])), 1e-300)
     assert np.max(np.abs(dot - tl["dJ"])) / scale <= 1e-9
-    np.testing.assert_allclose(ad["J"], tl["J"], rtol=1e-13)
+    # the weighted objective can cancel (J ~ 0.2 from terms of ~400 W m-2): compare on the terms' scale
+    np.testing.assert_allclose(ad["J"], tl["J"], rtol=1e-13, atol=1e-13 * np.max(np.abs(tl["J"])))
 
 
 def test_stored_and_recomputed_jacobians_agree(gpu):
