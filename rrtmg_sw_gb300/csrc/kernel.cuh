@@ -7,7 +7,7 @@ namespace rrsw {
 
 // levels buffered per reduction round of the g-point sums
 constexpr int KLEV = 4;
-constexpr int KLEV_F32 = 4;
+constexpr int KLEV_F32 = 1;
 __host__ __device__ constexpr int klev_of(size_t rsz) { return rsz == 4 ? KLEV_F32 : KLEV; }
 constexpr int NQ_MAX = 16;
 // g-point sums per level: fu, fd, cu, cd, fddir, cddir; the FP32 form adds
@@ -1036,11 +1036,13 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
 
 }
 
-// FP32 form: 3 resident CTAs per SM (80 registers, ~61 KB shared memory each
-// at 60 layers) hide more latency than 2 CTAs with 128 registers.  MT: fused
-// McICA from the call's MT19937 stream (P.mt) instead of KISS.
+// FP32 form: 4 resident CTAs per SM (72 registers, ~41 KB shared memory each
+// at 60 layers, level sums reduced level by level) hide more latency than 3
+// CTAs with 80 registers and 4-level reductions (147 -> 128 ms at
+// 262 144 x 60) or 2 with 128 registers.
+// MT: fused McICA from the call's MT19937 stream (P.mt) instead of KISS.
 template <typename R, bool MT>
-__global__ void __launch_bounds__(CTA_THREADS, sizeof(R) == 4 ? 3 : 2)
+__global__ void __launch_bounds__(CTA_THREADS, sizeof(R) == 4 ? 4 : 2)
 k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict__ tab64) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     fill_tm<R>(smem_raw);
