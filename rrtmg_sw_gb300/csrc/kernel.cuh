@@ -7,6 +7,10 @@ namespace rrsw {
 
 // levels buffered per reduction round of the g-point sums
 constexpr int KLEV = 4;
+// FP32 form: cells to redo in FP64 queued per column pair (one int each:
+// thread << 12 | layer << 1 | cloudy); cells past the queue are redone by
+// their own thread
+constexpr int REDO_QUEUE = 1024;
 constexpr int KLEV_F32 = 1;
 __host__ __device__ constexpr int klev_of(size_t rsz) { return rsz == 4 ? KLEV_F32 : KLEV; }
 constexpr int NQ_MAX = 16;
@@ -439,6 +443,26 @@ static __device__ __noinline__ CellOpt<float> cell_optics_fp64(const SolveParams
 // the upward adding recurrence (vrtqdr:122-140) from the lowest of them to
 // the top.  sv0 is the thread's scratch column (stride CTA_THREADS per
 // field, NS fields per level); the transmittance slots hold absorptances.
+// A redone cell into its thread's scratch column sv0 (the transmittance
+// slots hold absorptances).
+__device__ inline void store_cell(float* sv0, int NS, int L, int lay, const CellOpt<float>& co, int idelm) {
+    float* sv = sv0 + (size_t)(L - lay) * NS * CTA_THREADS;
+    sv[S_REFC * CTA_THREADS] = co.rc.ref;
+    sv[S_REFDC * CTA_THREADS] = co.rc.refd;
+    sv[S_TRAC * CTA_THREADS] = co.rc.adir;
+    sv[S_TRADC * CTA_THREADS] = co.rc.adif;
+    sv[S_DBTC * CTA_THREADS] = co.zdbtc;
+    sv[S_REF * CTA_THREADS] = co.rt.ref;
+    sv[S_REFD * CTA_THREADS] = co.rt.refd;
+    sv[S_TRA * CTA_THREADS] = co.rt.adir;
+    sv[S_TRAD * CTA_THREADS] = co.rt.adif;
+    sv[S_DBT * CTA_THREADS] = co.zdbt;
+    if (idelm == 0) {
+        sv[S_DBTCN * CTA_THREADS] = co.dbtcn;
+        sv[S_DBTN * CTA_THREADS] = co.dbtn;
+    }
+}
+
 static __device__ __noinline__ void redo_cells_fp64(const SolveParams& P, const Coef<double>& C64, float* sv0, int NS,
                                                     int col, int g, int ib, int igb, bool fused, double cossza,
                                                     const double* __restrict__ tab64, float albp, float albd,
@@ -456,20 +480,7 @@ static __device__ __noinline__ void redo_cells_fp64(const SolveParams& P, const 
         const float mark = at(lay, S_DBTC);
         if (mark < 0.0f) {
             const CellOpt<float> co = cell_optics_fp64(P, C64, col, g, lay, ib, igb, fused, mark < -1.5f, cossza, tab64);
-            at(lay, S_REFC) = co.rc.ref;
-            at(lay, S_REFDC) = co.rc.refd;
-            at(lay, S_TRAC) = co.rc.adir;
-            at(lay, S_TRADC) = co.rc.adif;
-            at(lay, S_DBTC) = co.zdbtc;
-            at(lay, S_REF) = co.rt.ref;
-            at(lay, S_REFD) = co.rt.refd;
-            at(lay, S_TRA) = co.rt.adir;
-            at(lay, S_TRAD) = co.rt.adif;
-            at(lay, S_DBT) = co.zdbt;
-            if (P.idelm == 0) {
-                at(lay, S_DBTCN) = co.dbtcn;
-                at(lay, S_DBTN) = co.dbtn;
-            }
+            store_cell(sv0, NS, L, lay, co, P.idelm);
         }
         {
             const float ref = at(lay, S_REFC), refd = at(lay, S_REFDC), dbt = at(lay, S_DBTC);
@@ -503,7 +514,7 @@ __device__ inline void warp_sum4(R& v) {
 // Shared-memory carve-up of one CTA (two columns); the host sizes the
 // launch with the same function.
 struct Smem {
-    size_t tm, pdp, coef, hrf, pk, misc, kc, ka, omcf, cld, seed, aer, xs, red, flux, total;
+    size_t tm, rq, pdp, coef, hrf, pk, misc, kc, ka, omcf, cld, seed, aer, xs, red, flux, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -515,6 +526,9 @@ __host__ __device__ inline Smem smem_layout(int L, int nq, bool fused, bool aer_
     // FP32 form: taumol descriptors first, at a fixed offset (the batch
     // kernel fills them once and re-lays the rest out per instance)
     if (rsz == sizeof(float)) o = align16(o + NBND * 2 * sizeof(TmSmem));
+    // FP32 form: queue of the cells to redo in FP64
+    m.rq = o;
+    if (rsz == sizeof(float)) o = align16(o + REDO_QUEUE * sizeof(int));
     m.pdp = o;  o = align16(o + COLS_PER_CTA * L * sizeof(double));
     m.coef = o; o = align16(o + COLS_PER_CTA * NFR * L * rsz);
     m.hrf = o;
@@ -556,6 +570,7 @@ __host__ __device__ inline bool stage_aerosol(int iaer) {
 template <typename R>
 struct CtaView {
     const TmSmem* sTm;  // [14][2] FP32 form: taumol descriptors
+    int* sRq;           // [REDO_QUEUE] FP32 form: cells to redo in FP64
     double* sPdp;       // [2][L]
     R* sCoef;           // [2][NFR][L]
     float* sHrf;        // [2][L] FP32 form: heatfac / dp
@@ -577,6 +592,7 @@ __device__ inline CtaView<R> cta_view(unsigned char* smem_raw, const SolveParams
     const Smem M = smem_layout(P.nlay, num_q<R>(P.extra != 0), stages_clouds(P), stage_aerosol<R>(P.iaer), sizeof(R));
     CtaView<R> v;
     v.sTm = (const TmSmem*)(smem_raw + M.tm);
+    v.sRq = (int*)(smem_raw + M.rq);
     v.sPdp = (double*)(smem_raw + M.pdp);
     v.sCoef = (R*)(smem_raw + M.coef);
     v.sHrf = (float*)(smem_raw + M.hrf);
@@ -736,6 +752,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         int lt = 0;
         for (int i = 0; i < L; ++i) lt += (sPk[cc * L + i] >> 30) & 1;
         sMisc[cc] = lt;
+        if (cc == 0) sMisc[2] = 0;  // FP32 form: redo queue length
     }
     __syncthreads();
     const int col = pair_col(P, pair, cc, nmapped);
@@ -812,6 +829,8 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
             if (co.risky) {
                 redo = ci.cloudy ? 2 : 1;
                 if (lay < redo_from) redo_from = lay;
+                const int qi = atomicAdd(sMisc + 2, 1);
+                if (qi < REDO_QUEUE) V.sRq[qi] = (tid << 12) | (lay << 1) | (ci.cloudy ? 1 : 0);
             }
         }
         const RT<R>& rc = co.rc;
@@ -856,6 +875,24 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
     }
 
     if constexpr (sizeof(R) == 4) {
+        // the queued cells, one per thread across the CTA, so the FP64 work
+        // of a warp is dense; then each thread redoes its up-sweep (and any
+        // cell the queue could not hold)
+        __syncthreads();
+        const int nq = min(sMisc[2], REDO_QUEUE);
+        for (int i = tid; i < nq; i += CTA_THREADS) {
+            const int e = V.sRq[i];
+            const int t = e >> 12, lay = (e >> 1) & 2047;
+            const int c2 = t / NGPT, gg = t % NGPT;
+            const int pcol = pair_col(P, pair, c2, nmapped);
+            const Coef<double> Cq{sCoef64 + c2 * NFR * L, sPk + c2 * L, L, sMisc[c2]};
+            double cz = P.coszen[pcol];
+            if (cz < 1.e-10) cz = 1.e-10;
+            const CellOpt<float> co = cell_optics_fp64(P, Cq, pcol, gg, lay, cT.ngb[gg], cT.gib[gg], fused, e & 1, cz,
+                                                       tab64);
+            store_cell(scr + t, NS, L, lay, co, P.idelm);
+        }
+        __syncthreads();
         if (active && redo_from <= L)
             redo_cells_fp64(P, C64, scr + tid, NS, col, g, ib, igb, fused, cossza, tab64, albp, albd, redo_from);
     }
