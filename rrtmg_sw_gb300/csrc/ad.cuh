@@ -362,35 +362,57 @@ __host__ __device__ inline AdSmem ad_smem_layout(int L) {
     return m;
 }
 
-// Dual<5> optics of one cell (pass 1 and the recomputing reverse pass)
+// Optics of one cell with derivatives (pass 1 and the recomputing reverse
+// pass): Dual<5> over (tlay, h2ovmr, o3vmr, clwp, ciwp) for a cloudy cell;
+// a clear cell does not depend on the water paths, so it runs in Dual<3>
+// and its outputs are widened with zero water-path derivatives.
+template <int N>
+__device__ inline void ad_cell_n(const SolveParams& P, const Dual<3>* coef3, const int* pk, int L, int laytrop,
+                                 int col, int lay, int ib, int igb, bool cloudy, const double* cld, double cossza,
+                                 const double* __restrict__ tab64, Dual<5> out[5]) {
+    typedef Dual<N> D;
+    D cf[NFR];
+    for (int f = 0; f < NFR; ++f) {
+        if constexpr (N == 5) cf[f] = widen(coef3[f * L + lay - 1]);
+        else cf[f] = coef3[f * L + lay - 1];
+    }
+    const Coef<D> CN{cf, pk + lay - 1, 1, lay <= laytrop ? 1 : 0};
+    CellIn<D> ci;
+    taumol_g<D>(ib, igb, 1, CN, tab64, ci.taug, ci.taur);
+    aerosol_in<D>(P, col, lay, ib, tab64, ci);
+    ci.cloudy = false;
+    ci.cldf = D(0.0);
+    ci.tc = D(0.0); ci.oc = D(1.0); ci.gc = D(0.0); ci.coc = D(0.0); ci.taor = D(0.0);
+    if constexpr (N == 5) {
+        if (cloudy) {
+            ci.cloudy = true;
+            ci.cldf = D(1.0);
+            D ciwp(cld[0 * L + lay - 1]), clwp(cld[1 * L + lay - 1]);
+            clwp.d[3] = 1.0;
+            ciwp.d[4] = 1.0;
+            const D rei(cld[2 * L + lay - 1]), rel(cld[3 * L + lay - 1]);
+            D tc(0.0), oc(1.0), gc(0.0), fsfc(0.0), taor(0.0), coc(0.0);
+            if (P.tauc) {
+                const size_t kb = (size_t)ib + 14 * ((size_t)col + (size_t)P.ncol * (size_t)(lay - 1));
+                tc = D(P.tauc[kb]); oc = D(P.ssac[kb]); gc = D(P.asmc[kb]); fsfc = D(P.fsfc[kb]);
+            }
+            cldprmc_g<D>(ib, P.inflag, P.iceflag, P.liqflag, D(1.0), ciwp, clwp, rei, rel, fsfc, tc, oc, gc, taor,
+                         coc, tab64, P.err);
+            ci.tc = tc; ci.oc = oc; ci.gc = gc; ci.taor = taor;
+        }
+        cell_total(ci, cossza, out);
+    } else {
+        D o[5];
+        cell_total(ci, cossza, o);
+        for (int k = 0; k < 5; ++k) out[k] = widen(o[k]);
+    }
+}
+
 __device__ inline void ad_cell(const SolveParams& P, const Dual<3>* coef3, const int* pk, int L, int laytrop, int col,
                                int lay, int ib, int igb, bool cloudy, const double* cld, double cossza,
                                const double* __restrict__ tab64, Dual<5> out[5]) {
-    typedef Dual<5> D;
-    D cf5[NFR];
-    for (int f = 0; f < NFR; ++f) cf5[f] = widen(coef3[f * L + lay - 1]);
-    const Coef<D> C5{cf5, pk + lay - 1, 1, lay <= laytrop ? 1 : 0};
-    CellIn<D> ci;
-    taumol_g<D>(ib, igb, 1, C5, tab64, ci.taug, ci.taur);
-    aerosol_in<D>(P, col, lay, ib, tab64, ci);
-    ci.cloudy = cloudy;
-    ci.cldf = D(cloudy ? 1.0 : 0.0);
-    ci.tc = D(0.0); ci.oc = D(1.0); ci.gc = D(0.0); ci.coc = D(0.0); ci.taor = D(0.0);
-    if (cloudy) {
-        D ciwp(cld[0 * L + lay - 1]), clwp(cld[1 * L + lay - 1]);
-        clwp.d[3] = 1.0;
-        ciwp.d[4] = 1.0;
-        const D rei(cld[2 * L + lay - 1]), rel(cld[3 * L + lay - 1]);
-        D tc(0.0), oc(1.0), gc(0.0), fsfc(0.0), taor(0.0), coc(0.0);
-        if (P.tauc) {
-            const size_t kb = (size_t)ib + 14 * ((size_t)col + (size_t)P.ncol * (size_t)(lay - 1));
-            tc = D(P.tauc[kb]); oc = D(P.ssac[kb]); gc = D(P.asmc[kb]); fsfc = D(P.fsfc[kb]);
-        }
-        cldprmc_g<D>(ib, P.inflag, P.iceflag, P.liqflag, D(1.0), ciwp, clwp, rei, rel, fsfc, tc, oc, gc, taor, coc,
-                     tab64, P.err);
-        ci.tc = tc; ci.oc = oc; ci.gc = gc; ci.taor = taor;
-    }
-    cell_total(ci, cossza, out);
+    if (cloudy) ad_cell_n<5>(P, coef3, pk, L, laytrop, col, lay, ib, igb, true, cld, cossza, tab64, out);
+    else ad_cell_n<3>(P, coef3, pk, L, laytrop, col, lay, ib, igb, false, cld, cossza, tab64, out);
 }
 
 __global__ void __launch_bounds__(CTA_THREADS, 1)
