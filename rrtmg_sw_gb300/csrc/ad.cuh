@@ -415,7 +415,7 @@ __device__ inline void ad_cell(const SolveParams& P, const Dual<3>* coef3, const
     else ad_cell_n<3>(P, coef3, pk, L, laytrop, col, lay, ib, igb, false, cld, cossza, tab64, out);
 }
 
-__global__ void __launch_bounds__(CTA_THREADS, 1)
+__global__ void __launch_bounds__(CTA_THREADS, 2)
 k_adjoint(const SolveParams P, const AdParams A, const double* __restrict__ tab64) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = P.nlay;
