@@ -489,14 +489,15 @@ uint64_t mt_stream_length(int icld, int ncol, int nlay) {
     return (icld >= 4 ? 2ull : 1ull) * sc * (uint64_t)nlay;
 }
 
-// Queue one solve on `s`; returns after reading back the device error word.
-int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s, bool nomcica = false) {
+// Queue one solve on `s` (device pointers in a/c) with the given scratch
+// buffer and device error word; nothing is synchronised.
+int enqueue_solve(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s, bool nomcica,
+                  DevBuf& scratch, int* err, int& launches) {
     SolveParams P;
     int rc = make_params(st, a, c, P, nomcica);
     if (rc) return rc;
-    CK(st.errw.ensure(sizeof(int)));
-    P.err = (int*)st.errw.p;
-    int launches = 1;
+    P.err = err;
+    launches = 1;
     if (P.fused && P.icld >= 1 && P.irng) {
         // the call's MT stream, generated in parallel segments, read by the solve
         const uint64_t nr = mt_stream_length(P.icld, P.ncol, P.nlay);
@@ -510,15 +511,166 @@ int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaS
     LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms) : plan_fp64(P, st.num_sms);
     P.slot_elems = slot_elems(P.nlay, P.idelm, fp32);
     const size_t esz = fp32 ? sizeof(float) : sizeof(double);
-    CK(st.scratch.ensure((size_t)li.grid * P.slot_elems * esz));
-    P.scratch = st.scratch.p;
-    CK(cudaMemsetAsync(P.err, 0, sizeof(int), s));
+    CK(scratch.ensure((size_t)li.grid * P.slot_elems * esz));
+    P.scratch = scratch.p;
     if (fp32) CK(launch_solve_fp32(P, (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, li, s));
     else CK(launch_solve_fp64(P, (const double*)st.d_tab64.p, li, s));
+    return RRTMG_SW_OK;
+}
+
+// Queue one solve on `s`; returns after reading back the device error word.
+int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s, bool nomcica = false) {
+    CK(st.errw.ensure(sizeof(int)));
+    int* err = (int*)st.errw.p;
+    CK(cudaMemsetAsync(err, 0, sizeof(int), s));
+    int launches = 0;
+    const int rc = enqueue_solve(st, a, c, s, nomcica, st.scratch, err, launches);
+    if (rc) return rc;
     st.last_launches = launches;
-    CK(cudaMemcpyAsync(st.h_err, P.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(st.h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     return *st.h_err;
+}
+
+// ---------------------------------------------------------------------------
+// Host arrays in column chunks on two streams: a chunk's inputs go in, its
+// solve runs and its outputs come back while the other stream's chunk
+// copies, so most of the transfer time hides behind the solves.  Columns are
+// independent (KISS subcolumn streams are seeded per column), so a chunk is
+// the rrtmg_sw call of its column slices and the results are those of one
+// call; MT streams (irng = 1) depend on ncol and keep the single-call path.
+constexpr int kChunkCols = 16384;  // columns per chunk (even: whole column pairs)
+constexpr int kChunkStreams = 2;
+
+struct ChunkStreams {
+    cudaStream_t s[kChunkStreams] = {nullptr, nullptr};
+    DevBuf scratch[kChunkStreams], err[kChunkStreams];
+    int* h_err = nullptr;  // pinned, one word per stream
+    int device = -1;
+};
+
+ChunkStreams& CS() {
+    static ChunkStreams c;
+    return c;
+}
+
+int solve_host_chunked(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, bool nomcica) {
+    ChunkStreams& cs = CS();
+    if (cs.device != st.device) {
+        for (int i = 0; i < kChunkStreams; ++i) {
+            if (!cs.s[i]) CK(cudaStreamCreateWithFlags(&cs.s[i], cudaStreamNonBlocking));
+        }
+        if (!cs.h_err) CK(cudaMallocHost((void**)&cs.h_err, kChunkStreams * sizeof(int)));
+        cs.device = st.device;
+    }
+    const size_t C = (size_t)a->ncol, L = (size_t)a->nlay, L1 = L + 1;
+    const int icld = (a->icld < 0 || a->icld > 5) ? 2 : a->icld;
+    const int iaer = a->iaer;
+    for (int i = 0; i < kChunkStreams; ++i) {
+        CK(cs.err[i].ensure(sizeof(int)));
+        CK(cudaMemsetAsync(cs.err[i].p, 0, sizeof(int), cs.s[i]));
+    }
+    cudaError_t e = cudaSuccess;
+    int launches = 0;
+    const int nch = (int)((C + kChunkCols - 1) / kChunkCols);
+    for (int ch = 0; ch < nch && e == cudaSuccess; ++ch) {
+        const int si = ch % kChunkStreams;
+        cudaStream_t s = cs.s[si];
+        const size_t c0 = (size_t)ch * kChunkCols, w = std::min((size_t)kChunkCols, C - c0);
+        const std::string pre = "chunk" + std::to_string(si) + ":";
+        // an array with `inner` contiguous elements per column and `outer`
+        // column planes: columns [c0, c0 + w) as a compact (inner, w, outer) slice
+        auto buf = [&](const char* name, size_t n) -> double* {
+            DevBuf& b = st.stage[pre + name];
+            if (e == cudaSuccess) e = b.ensure(n * sizeof(double));
+            return e == cudaSuccess ? (double*)b.p : nullptr;
+        };
+        auto in = [&](const char* name, const double* h, size_t inner, size_t outer) -> const double* {
+            if (!h) return nullptr;
+            double* d = buf(name, inner * w * outer);
+            if (e == cudaSuccess)
+                e = cudaMemcpy2DAsync(d, inner * w * sizeof(double), h + inner * c0, inner * C * sizeof(double),
+                                      inner * w * sizeof(double), outer, cudaMemcpyHostToDevice, s);
+            return d;
+        };
+        auto out = [&](const char* name, double* h, size_t n) -> double* { return h ? buf(name, n) : nullptr; };
+        auto back = [&](double* h, const double* d, size_t outer) {
+            if (h && d && e == cudaSuccess)
+                e = cudaMemcpy2DAsync(h + c0, C * sizeof(double), d, w * sizeof(double), w * sizeof(double), outer,
+                                      cudaMemcpyDeviceToHost, s);
+        };
+        rrtmg_sw_args d = *a;
+        d.ncol = (int32_t)w;
+        d.play = in("play", a->play, 1, L); d.plev = in("plev", a->plev, 1, L1); d.tlay = in("tlay", a->tlay, 1, L);
+        d.tlev = nullptr; d.tsfc = nullptr; d.n2ovmr = nullptr;  // dead inputs in the SW solve
+        d.h2ovmr = in("h2o", a->h2ovmr, 1, L); d.o3vmr = in("o3", a->o3vmr, 1, L);
+        d.co2vmr = in("co2", a->co2vmr, 1, L); d.ch4vmr = in("ch4", a->ch4vmr, 1, L);
+        d.o2vmr = in("o2", a->o2vmr, 1, L);
+        d.asdir = in("asdir", a->asdir, 1, 1); d.asdif = in("asdif", a->asdif, 1, 1);
+        d.aldir = in("aldir", a->aldir, 1, 1); d.aldif = in("aldif", a->aldif, 1, 1);
+        d.coszen = in("coszen", a->coszen, 1, 1);
+        if (icld >= 1 && !c) {
+            d.cldfmcl = in("cldfmcl", a->cldfmcl, NGPT, L); d.taucmcl = in("taucmcl", a->taucmcl, NGPT, L);
+            d.ssacmcl = in("ssacmcl", a->ssacmcl, NGPT, L); d.asmcmcl = in("asmcmcl", a->asmcmcl, NGPT, L);
+            d.fsfcmcl = in("fsfcmcl", a->fsfcmcl, NGPT, L); d.ciwpmcl = in("ciwpmcl", a->ciwpmcl, NGPT, L);
+            d.clwpmcl = in("clwpmcl", a->clwpmcl, NGPT, L);
+            d.reicmcl = in("reicmcl", a->reicmcl, 1, L); d.relqmcl = in("relqmcl", a->relqmcl, 1, L);
+        }
+        rrtmg_sw_clouds dc{};
+        if (c) {
+            dc = *c;
+            dc.cldfrac = in("cldfrac", c->cldfrac, 1, L); dc.ciwp = in("ciwp", c->ciwp, 1, L);
+            dc.clwp = in("clwp", c->clwp, 1, L); dc.rei = in("rei", c->rei, 1, L); dc.rel = in("rel", c->rel, 1, L);
+            dc.tauc = in("tauc", c->tauc, NBND, L); dc.ssac = in("ssac", c->ssac, NBND, L);
+            dc.asmc = in("asmc", c->asmc, NBND, L); dc.fsfc = in("fsfc", c->fsfc, NBND, L);
+            dc.alpha = in("alpha", c->alpha, 1, L);
+        }
+        if (iaer == 10) {
+            d.tauaer = in("tauaer", a->tauaer, 1, NBND * L); d.ssaaer = in("ssaaer", a->ssaaer, 1, NBND * L);
+            d.asmaer = in("asmaer", a->asmaer, 1, NBND * L);
+        }
+        if (iaer == 6) d.ecaer = in("ecaer", a->ecaer, 1, 6 * L);
+        d.swuflx = out("swuflx", a->swuflx, w * L1); d.swdflx = out("swdflx", a->swdflx, w * L1);
+        d.swuflxc = out("swuflxc", a->swuflxc, w * L1); d.swdflxc = out("swdflxc", a->swdflxc, w * L1);
+        d.swhr = out("swhr", a->swhr, w * L); d.swhrc = out("swhrc", a->swhrc, w * L);
+        const char* xn[8] = {"x0", "x1", "x2", "x3", "x4", "x5", "x6", "x7"};
+        double* xh[8] = {a->dirdflux, a->difdflux, a->uvdflx, a->nidflx, a->dirdnuv, a->difdnuv, a->dirdnir,
+                         a->difdnir};
+        double* xd[8];
+        for (int i = 0; i < 8; ++i) xd[i] = out(xn[i], xh[i], w * L1);
+        d.dirdflux = xd[0]; d.difdflux = xd[1]; d.uvdflx = xd[2]; d.nidflx = xd[3];
+        d.dirdnuv = xd[4]; d.difdnuv = xd[5]; d.dirdnir = xd[6]; d.difdnir = xd[7];
+        const char* bn[5] = {"b0", "b1", "b2", "b3", "b4"};
+        double* bh[5] = {a->bndfu, a->bndfd, a->bndfddir, a->bndcu, a->bndcd};
+        double* bd[5];
+        for (int i = 0; i < 5; ++i) bd[i] = out(bn[i], bh[i], w * L1 * NBND);
+        d.bndfu = bd[0]; d.bndfd = bd[1]; d.bndfddir = bd[2]; d.bndcu = bd[3]; d.bndcd = bd[4];
+        if (e != cudaSuccess) break;
+        int nl = 0;
+        const int rc = enqueue_solve(st, &d, c ? &dc : nullptr, s, nomcica, cs.scratch[si], (int*)cs.err[si].p, nl);
+        if (rc) {
+            for (int i = 0; i < kChunkStreams; ++i) cudaStreamSynchronize(cs.s[i]);
+            return rc;
+        }
+        launches += nl;
+        back(a->swuflx, d.swuflx, L1); back(a->swdflx, d.swdflx, L1);
+        back(a->swuflxc, d.swuflxc, L1); back(a->swdflxc, d.swdflxc, L1);
+        back(a->swhr, d.swhr, L); back(a->swhrc, d.swhrc, L);
+        for (int i = 0; i < 8; ++i) back(xh[i], xd[i], L1);
+        for (int i = 0; i < 5; ++i) back(bh[i], bd[i], L1 * NBND);
+    }
+    for (int i = 0; i < kChunkStreams; ++i) {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(cs.h_err + i, cs.err[i].p, sizeof(int), cudaMemcpyDeviceToHost, cs.s[i]);
+    }
+    for (int i = 0; i < kChunkStreams; ++i) {
+        const cudaError_t e2 = cudaStreamSynchronize(cs.s[i]);
+        if (e == cudaSuccess) e = e2;
+    }
+    if (e != cudaSuccess) return cuda_fail(e);
+    st.last_launches = launches;
+    for (int i = 0; i < kChunkStreams; ++i)
+        if (cs.h_err[i]) return cs.h_err[i];
+    return RRTMG_SW_OK;
 }
 
 // Host-array path: stage every array in a named device buffer.
@@ -551,6 +703,8 @@ int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, bool nomcica = 
     if (!st.init) return RRTMG_SW_ENOTINIT;
     int rc = check_args(a);
     if (rc) return rc;
+    const bool mt = c && !nomcica && a->icld >= 1 && c->irng != 0;
+    if (!mt && a->ncol >= 2 * kChunkCols) return solve_host_chunked(st, a, c, nomcica);
     const size_t C = a->ncol, L = a->nlay, CL = C * L, CL1 = C * (L + 1), G = (size_t)NGPT * CL;
     cudaStream_t s = 0;
     Stager sg{st, s};
@@ -1177,6 +1331,16 @@ int rrtmg_sw_finalize_c(void) {
     st.stage.clear();
     if (st.h_err) cudaFreeHost(st.h_err);
     st.h_err = nullptr;
+    ChunkStreams& cs = CS();
+    for (int i = 0; i < kChunkStreams; ++i) {
+        cs.scratch[i].release();
+        cs.err[i].release();
+        if (cs.s[i]) cudaStreamDestroy(cs.s[i]);
+        cs.s[i] = nullptr;
+    }
+    if (cs.h_err) cudaFreeHost(cs.h_err);
+    cs.h_err = nullptr;
+    cs.device = -1;
     st.init = false;
     return RRTMG_SW_OK;
 }
