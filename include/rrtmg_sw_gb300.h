@@ -16,7 +16,9 @@
  *
  * All entry points return 0 on success or one of the RRTMG_SW_E* codes
  * below; rrtmg_sw_errstr_c gives the message the reference would `stop`
- * with.  Outputs are fully overwritten.  The caller owns every array.  The
+ * with.  A call with ncol = 0 does nothing and returns 0, as the
+ * reference's column loop does (a batch instance must have columns).
+ * Outputs are fully overwritten.  The caller owns every array.  The
  * library owns its device tables (rrtmg_sw_ini_c) and a reusable device
  * workspace, released by rrtmg_sw_finalize_c.  Calls are serialised
  * internally; one process drives one GPU.

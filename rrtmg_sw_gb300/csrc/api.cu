@@ -405,8 +405,14 @@ void solar_setup(const State& st, const rrtmg_sw_args* a, SolveParams& P) {
     for (int i = 0; i < 14; ++i) P.adjflux[i] = isolvar < 0 ? adjflx * solvar[i] : adjflx;
 }
 
+// A call with no columns does nothing, as the reference's column loop
+// (rrtmg_sw_rad.f90:640) does; check_args reports it as kEmpty and the
+// entry points return RRTMG_SW_OK.
+constexpr int kEmpty = -1;
+
 int check_args(const rrtmg_sw_args* a) {
-    if (!a || a->ncol <= 0 || a->nlay < 4 || a->nlay > MAX_NLAY) return RRTMG_SW_EARGS;
+    if (a && a->ncol == 0) return kEmpty;
+    if (!a || a->ncol < 0 || a->nlay < 4 || a->nlay > MAX_NLAY) return RRTMG_SW_EARGS;
     const double* req[] = {a->play, a->plev, a->tlay, a->h2ovmr, a->o3vmr, a->co2vmr, a->ch4vmr, a->o2vmr,
                            a->asdir, a->asdif, a->aldir, a->aldif, a->coszen};
     for (const double* p : req)
@@ -702,7 +708,7 @@ int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, bool nomcica = 
     std::lock_guard<std::mutex> lk(st.mu);
     if (!st.init) return RRTMG_SW_ENOTINIT;
     int rc = check_args(a);
-    if (rc) return rc;
+    if (rc) return rc == kEmpty ? RRTMG_SW_OK : rc;
     const bool mt = c && !nomcica && a->icld >= 1 && c->irng != 0;
     if (!mt && a->ncol >= 2 * kChunkCols) return solve_host_chunked(st, a, c, nomcica);
     const size_t C = a->ncol, L = a->nlay, CL = C * L, CL1 = C * (L + 1), G = (size_t)NGPT * CL;
@@ -840,7 +846,8 @@ int solve_ad_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, const rrtmg_
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
     if (!st.init) return RRTMG_SW_ENOTINIT;
-    if (!a || !ad || a->ncol <= 0 || a->nlay < 4 || a->nlay > MAX_NLAY) return RRTMG_SW_EARGS;
+    if (a && ad && a->ncol == 0) return RRTMG_SW_OK;
+    if (!a || !ad || a->ncol < 0 || a->nlay < 4 || a->nlay > MAX_NLAY) return RRTMG_SW_EARGS;
     const double* req[] = {a->play, a->plev, a->tlay, a->h2ovmr, a->o3vmr, a->co2vmr, a->ch4vmr, a->o2vmr,
                            a->asdir, a->asdif, a->aldir, a->aldif, a->coszen};
     for (const double* p : req)
@@ -985,6 +992,7 @@ int batch_plan(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, int 
     long long cols = 0;
     for (int i = 0; i < n; ++i) {
         int rc = check_args(a + i);
+        if (rc == kEmpty) rc = RRTMG_SW_EARGS;  // a batch instance needs columns
         if (!rc) rc = make_params(st, a + i, (c && a[i].icld >= 1) ? c + i : nullptr, P[i]);
         if (!rc && P[i].irng) rc = RRTMG_SW_EIRNG;
         if (rc) { batch_release(bp); return rc; }
@@ -1095,7 +1103,7 @@ int rrtmg_sw_dev_c(const rrtmg_sw_args* a, void* stream) {
     std::lock_guard<std::mutex> lk(st.mu);
     if (!st.init) return RRTMG_SW_ENOTINIT;
     const int rc = check_args(a);
-    if (rc) return rc;
+    if (rc) return rc == kEmpty ? RRTMG_SW_OK : rc;
     return solve_dev(st, a, nullptr, (cudaStream_t)stream);
 }
 
@@ -1110,7 +1118,7 @@ int rrtmg_sw_nomcica_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, voi
     if (!st.init) return RRTMG_SW_ENOTINIT;
     if (!c) return RRTMG_SW_EARGS;
     const int rc = check_args(a);
-    if (rc) return rc;
+    if (rc) return rc == kEmpty ? RRTMG_SW_OK : rc;
     return solve_dev(st, a, c, (cudaStream_t)stream, true);
 }
 
@@ -1120,7 +1128,7 @@ int rrtmg_sw_mcica_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, void*
     if (!st.init) return RRTMG_SW_ENOTINIT;
     if (!c) return RRTMG_SW_EARGS;
     const int rc = check_args(a);
-    if (rc) return rc;
+    if (rc) return rc == kEmpty ? RRTMG_SW_OK : rc;
     return solve_dev(st, a, c, (cudaStream_t)stream);
 }
 
@@ -1129,7 +1137,7 @@ int rrtmg_sw_static_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, void
     std::lock_guard<std::mutex> lk(st.mu);
     if (!st.init) return RRTMG_SW_ENOTINIT;
     const int rc = check_args(a);
-    if (rc) return rc;
+    if (rc) return rc == kEmpty ? RRTMG_SW_OK : rc;
     return solve_static(st, a, c, (cudaStream_t)stream);
 }
 
@@ -1144,7 +1152,8 @@ int mcica_subcol_sw_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t permutes
     if (!st.init) return RRTMG_SW_ENOTINIT;
     if (icld == 0) return RRTMG_SW_OK;                 // mcica:261
     if (icld < 0 || icld > 5) return RRTMG_SW_EICLD;    // mcica:262-264
-    if (ncol <= 0 || nlay < 4 || !play || !cldfrac || !ciwp || !clwp || !rei || !rel) return RRTMG_SW_EARGS;
+    if (ncol == 0) return RRTMG_SW_OK;
+    if (ncol < 0 || nlay < 4 || !play || !cldfrac || !ciwp || !clwp || !rei || !rel) return RRTMG_SW_EARGS;
     if (icld >= 4 && !alpha) return RRTMG_SW_EARGS;
     if (irng != 0) irng = 1;                            // mcica:455
     const size_t C = ncol, L = nlay, CL = C * L, G = (size_t)NGPT * CL;
@@ -1215,7 +1224,8 @@ int get_alpha_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t idcor, double 
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
     if (!st.init) return RRTMG_SW_ENOTINIT;
-    if (ncol <= 0 || nlay < 1 || !dz || !lat || !cldfrac || !alpha) return RRTMG_SW_EARGS;
+    if (ncol == 0) return RRTMG_SW_OK;
+    if (ncol < 0 || nlay < 1 || !dz || !lat || !cldfrac || !alpha) return RRTMG_SW_EARGS;
     const size_t CL = (size_t)ncol * nlay;
     cudaStream_t s = 0;
     Stager sg{st, s};

@@ -238,3 +238,21 @@ def test_invalid_ice_size_reports_reference_error():
     with pytest.raises(gpu.RRTMGError) as ei:
         gpu_call(kw)
     assert ei.value.code == 12 and "ICE GENERALIZED EFFECTIVE SIZE" in str(ei.value)
+
+
+def test_empty_calls_do_nothing():
+    # ncol = 0: the reference's column loop runs no iteration; every entry point returns 0
+    import ctypes as C
+    a = gpu.RrtmgSwArgs()
+    a.ncol, a.nlay, a.icld, a.iaer = 0, 60, 2, 0
+    cl = gpu.RrtmgSwClouds()
+    L = gpu.lib()
+    assert L.rrtmg_sw_c(C.byref(a)) == 0
+    assert L.rrtmg_sw_mcica_c(C.byref(a), C.byref(cl)) == 0
+    assert L.rrtmg_sw_dev_c(C.byref(a), None) == 0
+    assert L.rrtmg_sw_nomcica_c(C.byref(a), C.byref(cl)) == 0
+    null = C.cast(None, gpu._dp)
+    assert L.mcica_subcol_sw_c(0, 60, 2, 112, 0, *([null] * 20)) == 0
+    assert L.get_alpha_c(0, 60, 5, 1, C.c_double(0.0), null, null, 94, null, null) == 0
+    a.ncol = -1
+    assert L.rrtmg_sw_c(C.byref(a)) == 3  # RRTMG_SW_EARGS
