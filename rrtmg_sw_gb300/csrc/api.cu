@@ -539,9 +539,9 @@ int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaS
 }
 
 // ---------------------------------------------------------------------------
-// Host arrays in column chunks on two streams: a chunk's inputs go in, its
-// solve runs and its outputs come back while the other stream's chunk
-// copies, so most of the transfer time hides behind the solves.  Columns are
+// Page-locked host arrays in column chunks on two streams: a chunk's inputs
+// go in, its solve runs and its outputs come back while the other stream's
+// chunk copies, so most of the transfer time hides behind the solves.  Columns are
 // independent (KISS subcolumn streams are seeded per column), so a chunk is
 // the rrtmg_sw call of its column slices and the results are those of one
 // call; MT streams (irng = 1) depend on ncol and keep the single-call path.
@@ -558,6 +558,30 @@ struct ChunkStreams {
 ChunkStreams& CS() {
     static ChunkStreams c;
     return c;
+}
+
+// Whether a host array is page-locked (pinned or registered): only then do
+// asynchronous copies overlap the solves; pageable arrays take one staged
+// copy per array instead.
+bool pinned(const void* p) {
+    if (!p) return true;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+bool all_pinned(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c) {
+    const void* ps[] = {a->play, a->plev, a->tlay, a->h2ovmr, a->o3vmr, a->co2vmr, a->ch4vmr, a->o2vmr, a->asdir,
+                        a->asdif, a->aldir, a->aldif, a->coszen, a->swuflx, a->swdflx, a->swhr, a->swuflxc,
+                        a->swdflxc, a->swhrc};
+    for (const void* p : ps)
+        if (!pinned(p)) return false;
+    if (c && (!pinned(c->cldfrac) || !pinned(c->ciwp) || !pinned(c->clwp))) return false;
+    if (!c && a->icld >= 1 && !pinned(a->taucmcl)) return false;
+    return true;
 }
 
 int solve_host_chunked(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, bool nomcica) {
@@ -710,7 +734,7 @@ int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, bool nomcica = 
     int rc = check_args(a);
     if (rc) return rc == kEmpty ? RRTMG_SW_OK : rc;
     const bool mt = c && !nomcica && a->icld >= 1 && c->irng != 0;
-    if (!mt && a->ncol >= 2 * kChunkCols) return solve_host_chunked(st, a, c, nomcica);
+    if (!mt && a->ncol >= 2 * kChunkCols && all_pinned(a, c)) return solve_host_chunked(st, a, c, nomcica);
     const size_t C = a->ncol, L = a->nlay, CL = C * L, CL1 = C * (L + 1), G = (size_t)NGPT * CL;
     cudaStream_t s = 0;
     Stager sg{st, s};

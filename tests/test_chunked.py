@@ -1,8 +1,9 @@
-"""Host-array calls of 32 768 columns or more run as column chunks on two
-streams (transfers of one chunk overlap the solve of another).  Columns are
-independent, so the outputs must equal those of one device-pointer call on
-the same inputs bit for bit (tolerance 0), in both forms, with fused KISS
-McICA, aerosol, the extra and per-band outputs, and on the non-McICA path.
+"""Host-array calls of 32 768 columns or more on page-locked arrays run as
+column chunks on two streams (transfers of one chunk overlap the solve of
+another).  Columns are independent, so the outputs must equal those of one
+device-pointer call on the same inputs bit for bit (tolerance 0), in both
+forms, with fused KISS McICA, aerosol, the extra and per-band outputs, and
+on the non-McICA path.
 """
 import ctypes as C
 
@@ -27,55 +28,63 @@ def torch():
     gi.set_form(gi.FORM_FP64)
 
 
-def device_call(torch, kw, clouds, nomcica=False):
-    """The same request through rrtmg_sw_mcica_dev_c / rrtmg_sw_nomcica_dev_c (one call)."""
+ARRAYS = ("play", "plev", "tlay", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "o2vmr", "asdir", "asdif", "aldir", "aldif",
+          "coszen")
+
+
+def call(torch, kw, clouds, where, nomcica=False):
+    """The request through the host entry point with pinned arrays (where =
+    "pinned") or through the device entry point (where = "device")."""
     ncol, nlay = kw["ncol"], kw["nlay"]
     dev = torch.device("cuda", torch.cuda.current_device())
     keep = []
 
-    def D(x):
-        t = torch.from_numpy(np.asfortranarray(x).ravel(order="F").copy()).to(dev)
+    def T(x):
+        t = torch.from_numpy(np.asfortranarray(x).ravel(order="F").copy())
+        t = t.pin_memory() if where == "pinned" else t.to(dev)
         keep.append(t)
         return C.cast(C.c_void_p(t.data_ptr()), gi._dp)
 
     a = gi.RrtmgSwArgs()
     a.ncol, a.nlay, a.icld, a.iaer = ncol, nlay, kw["icld"], kw["iaer"]
-    for k in ("play", "plev", "tlay", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "o2vmr", "asdir", "asdif", "aldir",
-              "aldif", "coszen"):
-        setattr(a, k, D(kw[k]))
+    for k in ARRAYS:
+        setattr(a, k, T(kw[k]))
     if kw["iaer"] == 10:
         for k in ("tauaer", "ssaaer", "asmaer"):
-            setattr(a, k, D(kw[k]))
+            setattr(a, k, T(kw[k]))
     a.adjes, a.dyofyr, a.scon, a.isolvar = kw["adjes"], kw["dyofyr"], kw["scon"], kw["isolvar"]
     a.inflgsw, a.iceflgsw, a.liqflgsw = kw["inflgsw"], kw["iceflgsw"], kw["liqflgsw"]
     a.idelm = 1
-    outs = {}
+    shapes = {}
     for k in ("swuflx", "swdflx", "swuflxc", "swdflxc") + gi.EXTRA_OUTPUTS:
-        outs[k] = torch.zeros(ncol * (nlay + 1), dtype=torch.float64, device=dev)
+        shapes[k] = (ncol, nlay + 1)
     for k in ("swhr", "swhrc"):
-        outs[k] = torch.zeros(ncol * nlay, dtype=torch.float64, device=dev)
+        shapes[k] = (ncol, nlay)
     for k in gi.BAND_OUTPUTS:
-        outs[k] = torch.zeros(ncol * (nlay + 1) * 14, dtype=torch.float64, device=dev)
-    for k, v in outs.items():
-        setattr(a, k, C.cast(C.c_void_p(v.data_ptr()), gi._dp))
+        shapes[k] = (ncol, nlay + 1, 14)
+    outs = {}
+    for k, shp in shapes.items():
+        t = torch.zeros(int(np.prod(shp)), dtype=torch.float64)
+        t = t.pin_memory() if where == "pinned" else t.to(dev)
+        outs[k] = t
+        setattr(a, k, C.cast(C.c_void_p(t.data_ptr()), gi._dp))
     cl = gi.RrtmgSwClouds()
     cl.permuteseed, cl.irng = clouds.get("permuteseed", 112), 0
     for k in ("cldfrac", "ciwp", "clwp", "rei", "rel", "tauc", "ssac", "asmc", "fsfc"):
         if clouds.get(k) is not None:
-            setattr(cl, k, D(clouds[k]))
-    s = torch.cuda.current_stream().cuda_stream
-    fn = gi.lib().rrtmg_sw_nomcica_dev_c if nomcica else gi.lib().rrtmg_sw_mcica_dev_c
-    rc = fn(C.byref(a), C.byref(cl), C.c_void_p(s))
+            setattr(cl, k, T(clouds[k]))
+    L = gi.lib()
+    if where == "pinned":
+        rc = (L.rrtmg_sw_nomcica_c if nomcica else L.rrtmg_sw_mcica_c)(C.byref(a), C.byref(cl))
+        launches = L.rrtmg_sw_last_launch_count_c()
+    else:
+        s = torch.cuda.current_stream().cuda_stream
+        rc = (L.rrtmg_sw_nomcica_dev_c if nomcica else L.rrtmg_sw_mcica_dev_c)(C.byref(a), C.byref(cl), C.c_void_p(s))
+        launches = L.rrtmg_sw_last_launch_count_c()
     torch.cuda.synchronize()
     assert rc == 0
-    res = {}
-    for k, v in outs.items():
-        h = v.cpu().numpy()
-        if k in gi.BAND_OUTPUTS:
-            res[k] = h.reshape((ncol, nlay + 1, 14), order="F")
-        else:
-            res[k] = h.reshape((ncol, nlay if k in ("swhr", "swhrc") else nlay + 1), order="F")
-    return res
+    res = {k: outs[k].cpu().numpy().reshape(shp, order="F") for k, shp in shapes.items()}
+    return res, launches
 
 
 @pytest.mark.parametrize("form", ["fp64", "fp32"])
@@ -86,11 +95,11 @@ def test_chunked_host_call_equals_one_device_call(torch, form):
                   rel=c["rel"])
     gi.set_form(gi.FORM_FP64 if form == "fp64" else gi.FORM_FP32)
     try:
-        h = gi.rrtmg_sw(**kw, clouds=clouds, extra=True, bands=True)
-        assert gi.lib().rrtmg_sw_last_launch_count_c() == 3  # one solve per chunk
-        d = device_call(torch, kw, clouds)
+        h, nh = call(torch, kw, clouds, "pinned")
+        d, nd = call(torch, kw, clouds, "device")
     finally:
         gi.set_form(gi.FORM_FP64)
+    assert nh == 3 and nd == 1  # one solve per chunk / one for the whole call
     for k in d:
         np.testing.assert_array_equal(h[k], d[k], err_msg=k)
 
@@ -106,7 +115,8 @@ def test_chunked_nomcica_equals_one_device_call(torch):
                   tauc=rng.uniform(0.0, 8.0, (14, NCOL, NLAY)) * cf[None],
                   ssac=rng.uniform(0.7, 0.999999, (14, NCOL, NLAY)), asmc=rng.uniform(0.5, 0.9, (14, NCOL, NLAY)))
     clouds["fsfc"] = clouds["asmc"] ** 2
-    h = gi.rrtmg_sw(**kw, clouds=clouds, nomcica=True, extra=True, bands=True)
-    d = device_call(torch, kw, clouds, nomcica=True)
+    h, nh = call(torch, kw, clouds, "pinned", nomcica=True)
+    d, _ = call(torch, kw, clouds, "device", nomcica=True)
+    assert nh == 3
     for k in d:
         np.testing.assert_array_equal(h[k], d[k], err_msg=k)
