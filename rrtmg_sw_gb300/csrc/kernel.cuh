@@ -463,6 +463,24 @@ __device__ inline void store_cell(float* sv0, int NS, int L, int lay, const Cell
     }
 }
 
+// Whether a cell redone in FP64 differs from the FP32 values in its
+// scratch column by more than 1e-6 relative in any field (an FP32 choice
+// that went the other way moves a field by ~5e-5 or more; FP32 rounding of
+// the rest stays far below).
+__device__ inline bool cell_changed(const float* sv0, int NS, int L, int lay, const CellOpt<float>& co) {
+    const float* sv = sv0 + (size_t)(L - lay) * NS * CTA_THREADS;
+    const float nv[10] = {co.rc.ref, co.rc.refd, co.rc.adir, co.rc.adif, co.zdbtc,
+                          co.rt.ref, co.rt.refd, co.rt.adir, co.rt.adif, co.zdbt};
+    const int fld[10] = {S_REFC, S_REFDC, S_TRAC, S_TRADC, S_DBTC, S_REF, S_REFD, S_TRA, S_TRAD, S_DBT};
+    bool ch = false;
+#pragma unroll
+    for (int i = 0; i < 10; ++i) {
+        const float o = sv[fld[i] * CTA_THREADS];
+        if (!(fabsf(nv[i] - o) <= 1.0e-6f * fabsf(nv[i]))) ch = true;
+    }
+    return ch;
+}
+
 static __device__ __noinline__ void redo_cells_fp64(const SolveParams& P, const Coef<double>& C64, float* sv0, int NS,
                                                     int col, int g, int ib, int igb, bool fused, double cossza,
                                                     const double* __restrict__ tab64, float albp, float albd,
@@ -528,7 +546,7 @@ __host__ __device__ inline Smem smem_layout(int L, int nq, bool fused, bool aer_
     if (rsz == sizeof(float)) o = align16(o + NBND * 2 * sizeof(TmSmem));
     // FP32 form: queue of the cells to redo in FP64
     m.rq = o;
-    if (rsz == sizeof(float)) o = align16(o + REDO_QUEUE * sizeof(int));
+    if (rsz == sizeof(float)) o = align16(o + (REDO_QUEUE + CTA_THREADS) * sizeof(int));
     m.pdp = o;  o = align16(o + COLS_PER_CTA * L * sizeof(double));
     m.coef = o; o = align16(o + COLS_PER_CTA * NFR * L * rsz);
     m.hrf = o;
@@ -570,7 +588,7 @@ __host__ __device__ inline bool stage_aerosol(int iaer) {
 template <typename R>
 struct CtaView {
     const TmSmem* sTm;  // [14][2] FP32 form: taumol descriptors
-    int* sRq;           // [REDO_QUEUE] FP32 form: cells to redo in FP64
+    int* sRq;           // [REDO_QUEUE] FP32 form: cells to redo in FP64, then [224] replay start per thread
     double* sPdp;       // [2][L]
     R* sCoef;           // [2][NFR][L]
     float* sHrf;        // [2][L] FP32 form: heatfac / dp
@@ -822,15 +840,19 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         const CellOpt<R> co = cell_optics<R>(ci, P.idelm, prmu0, tab, tab64, hrs);
         // FP32 form: a table entry, the conservative switch or the
         // resonance of this cell is too close to call in FP32; it is
-        // marked in the scratch (S_DBTC < 0, -2 if cloudy) and redone
-        // after this pass as the FP64 form does
+        // queued and redone after this pass as the FP64 form does (a cell
+        // past the queue's end is marked in the scratch instead, S_DBTC < 0,
+        // -2 if cloudy, and redone by its own thread)
         int redo = 0;
         if constexpr (sizeof(R) == 4) {
             if (co.risky) {
-                redo = ci.cloudy ? 2 : 1;
-                if (lay < redo_from) redo_from = lay;
                 const int qi = atomicAdd(sMisc + 2, 1);
-                if (qi < REDO_QUEUE) V.sRq[qi] = (tid << 12) | (lay << 1) | (ci.cloudy ? 1 : 0);
+                if (qi < REDO_QUEUE) {
+                    V.sRq[qi] = (tid << 12) | (lay << 1) | (ci.cloudy ? 1 : 0);
+                } else {
+                    redo = ci.cloudy ? 2 : 1;
+                    if (lay < redo_from) redo_from = lay;
+                }
             }
         }
         const RT<R>& rc = co.rc;
@@ -876,8 +898,11 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
 
     if constexpr (sizeof(R) == 4) {
         // the queued cells, one per thread across the CTA, so the FP64 work
-        // of a warp is dense; then each thread redoes its up-sweep (and any
-        // cell the queue could not hold)
+        // of a warp is dense; a redone cell that differs from its FP32 values
+        // replaces them, and its thread goes over its up-sweep again from
+        // there (so does a thread with a cell the queue could not hold)
+        int* sRf = V.sRq + REDO_QUEUE;
+        sRf[tid] = L + 1;
         __syncthreads();
         const int nq = min(sMisc[2], REDO_QUEUE);
         for (int i = tid; i < nq; i += CTA_THREADS) {
@@ -890,11 +915,15 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
             if (cz < 1.e-10) cz = 1.e-10;
             const CellOpt<float> co = cell_optics_fp64(P, Cq, pcol, gg, lay, cT.ngb[gg], cT.gib[gg], fused, e & 1, cz,
                                                        tab64);
-            store_cell(scr + t, NS, L, lay, co, P.idelm);
+            if (cell_changed(scr + t, NS, L, lay, co)) {
+                store_cell(scr + t, NS, L, lay, co, P.idelm);
+                atomicMin(sRf + t, lay);
+            }
         }
         __syncthreads();
-        if (active && redo_from <= L)
-            redo_cells_fp64(P, C64, scr + tid, NS, col, g, ib, igb, fused, cossza, tab64, albp, albd, redo_from);
+        const int from = min(redo_from, sRf[tid]);
+        if (active && from <= L)
+            redo_cells_fp64(P, C64, scr + tid, NS, col, g, ib, igb, fused, cossza, tab64, albp, albd, from);
     }
 
     // ---------------- pass 2: top -> bottom, level fluxes and g sums
