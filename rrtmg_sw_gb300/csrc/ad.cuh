@@ -435,7 +435,7 @@ k_adjoint(const SolveParams P, const AdParams A, const double* __restrict__ tab6
     double* sJ = (double*)(smem_raw + M.jsum);
 
     const int tid = threadIdx.x;
-    const int cc = tid / NGPT, g = tid % NGPT;
+    const int cc = thread_col<double>(tid), g = thread_g<double>(tid);
     const int ib = cT.ngb[g], igb = cT.gib[g];
     const bool nir = ib <= 8 || ib == 13;
     const bool fused = P.fused && P.icld >= 1;
@@ -443,7 +443,7 @@ k_adjoint(const SolveParams P, const AdParams A, const double* __restrict__ tab6
     double* slot = (double*)P.scratch + (size_t)blockIdx.x * P.slot_elems;
     Dual<3>* coef3 = (Dual<3>*)(slot + (size_t)(L + 1) * NA * CTA_THREADS);
     const size_t n = (size_t)P.ncol;
-    const KissJump J = kiss_setup(P, sXs);
+    const KissJump J = kiss_setup(P, sXs, g);
 
     for (int pair = blockIdx.x; pair < P.npairs; pair += gridDim.x) {
         __syncthreads();

@@ -269,6 +269,19 @@ int build_tables(State& st) {
                 if (y >> b & 1u) r ^= T.xs_jump[k - 1][b];
             T.xs_jump[k][j] = r;
         }
+    // thread layout of the solve CTA: warps of whole bands, both columns
+    // of a band side by side (band sizes 2*ng: 12,24,16,16,20,20,4,20,16,12,12,16,12,24)
+    {
+        const int seg[][3] = {  // band, first g in band, count (per column)
+            {2, 0, 8}, {3, 0, 8}, {8, 0, 8}, {11, 0, 8}, {4, 0, 10}, {0, 0, 6}, {5, 0, 10}, {9, 0, 6},
+            {7, 0, 10}, {10, 0, 6}, {1, 0, 12}, {6, 0, 2}, {12, 0, 2}, {13, 0, 12}, {12, 2, 4}};
+        int t = 0, bg0[14], acc = 0;
+        for (int ib = 0; ib < 14; ++ib) { bg0[ib] = acc; acc += kNG[ib]; }
+        for (const auto& sg : seg)
+            for (int cc = 0; cc < 2; ++cc)
+                for (int k = 0; k < sg[2]; ++k) T.thr_cg[t++] = (uint8_t)((cc << 7) | (bg0[sg[0]] + sg[1] + k));
+        if (t != CTA_THREADS) return RRTMG_SW_ETABLES;
+    }
     return RRTMG_SW_OK;
 }
 

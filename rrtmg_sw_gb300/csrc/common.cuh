@@ -59,6 +59,11 @@ struct DevTables {
     int total;                      // blob size
     int8_t ngb[NGPT];               // band index 0..13 of each g-point
     uint8_t gib[NGPT];              // g index within its band, 1-based
+    // FP64 solve and adjoint CTAs: thread -> column slot (bit 7) and g-point
+    // (bits 0-6).  The g-points of a band sit together with both columns'
+    // copies, so a warp spans 2 (at most 3) bands and band-dependent
+    // branches diverge less.
+    uint8_t thr_cg[CTA_THREADS];
     double heatfac, bpade, oneminus;
     float bpade_f, oneminus_f;
     TmRegion tm[NBND][2];

@@ -646,17 +646,33 @@ __device__ inline void fill_tm(unsigned char* smem_raw) {
     }
 }
 
-// McICA stream jump of this thread's subcolumn for parameters P; the
-// xorshift part goes to sXs (one column of M^n per g-point).
-__device__ inline KissJump kiss_setup(const SolveParams& P, uint32_t* sXs) {
+// McICA stream jump of subcolumn g (this thread's) for parameters P; the
+// xorshift parts go to sXs (one column of M^n per g-point, filled by the
+// CTA's first 112 threads).
+__device__ inline KissJump kiss_setup(const SolveParams& P, uint32_t* sXs, int g) {
     KissJump J{1u, 0u, 1u, 1u};
     if (P.fused && P.icld >= 1) {
-        const int g = threadIdx.x % NGPT;
-        const uint64_t off = kiss_offset(P.icld, g, P.nlay, P.permuteseed);
-        J = kiss_jump_consts(off);
-        if (threadIdx.x / NGPT == 0) xorshift_power(off, sXs + g * 32);
+        J = kiss_jump_consts(kiss_offset(P.icld, g, P.nlay, P.permuteseed));
+        if (threadIdx.x < NGPT)
+            xorshift_power(kiss_offset(P.icld, threadIdx.x, P.nlay, P.permuteseed), sXs + threadIdx.x * 32);
     }
     return J;
+}
+
+// Column slot and g-point of solve-CTA thread t.  The FP64 forms (taumol_g
+// runs a different FP64 code path per band) use warps of whole bands from
+// both columns (cT.thr_cg: 2200 -> 1750 ms at 262 144 x 60); the FP32 form
+// (one descriptor-driven taumol path, but cloudy layers that differ by
+// column) is faster with 32 consecutive g-points of one column per warp.
+template <typename R>
+__device__ inline int thread_col(int t) {
+    if constexpr (sizeof(R) == 4) return t / NGPT;
+    else return cT.thr_cg[t] >> 7;
+}
+template <typename R>
+__device__ inline int thread_g(int t) {
+    if constexpr (sizeof(R) == 4) return t % NGPT;
+    else return cT.thr_cg[t] & 127;
 }
 
 // Column of slot c2 of column pair `pair`: consecutive columns, or through
@@ -693,7 +709,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
     R* sRed = V.sRed;
     R* sFlux = V.sFlux;
     const int tid = threadIdx.x;
-    const int cc = tid / NGPT, g = tid % NGPT;
+    const int cc = thread_col<R>(tid), g = thread_g<R>(tid);
     const int ib = cT.ngb[g], igb = cT.gib[g];
     const bool uv = ib >= 9 && ib <= 12;  // bands 25-28 (spcvmc:629)
     const int NS = P.idelm == 0 ? NS_MAX : S_DBTCN;
@@ -848,7 +864,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
             if (co.risky) {
                 const int qi = atomicAdd(sMisc + 2, 1);
                 if (qi < REDO_QUEUE) {
-                    V.sRq[qi] = (tid << 12) | (lay << 1) | (ci.cloudy ? 1 : 0);
+                    V.sRq[qi] = (tid << 20) | (cc << 19) | (g << 12) | (lay << 1) | (ci.cloudy ? 1 : 0);
                 } else {
                     redo = ci.cloudy ? 2 : 1;
                     if (lay < redo_from) redo_from = lay;
@@ -907,8 +923,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         const int nq = min(sMisc[2], REDO_QUEUE);
         for (int i = tid; i < nq; i += CTA_THREADS) {
             const int e = V.sRq[i];
-            const int t = e >> 12, lay = (e >> 1) & 2047;
-            const int c2 = t / NGPT, gg = t % NGPT;
+            const int t = e >> 20, c2 = (e >> 19) & 1, gg = (e >> 12) & 127, lay = (e >> 1) & 2047;
             const int pcol = pair_col(P, pair, c2, nmapped);
             const Coef<double> Cq{sCoef64 + c2 * NFR * L, sPk + c2 * L, L, sMisc[c2]};
             double cz = P.coszen[pcol];
@@ -1014,7 +1029,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         const int slot = (jk - 1) % KL;
 #pragma unroll
         for (int i = 0; i < NQ_MAX; ++i)
-            if (i < NQ) sRed[(slot * NQ + i) * CTA_THREADS + tid] = q[i];
+            if (i < NQ) sRed[(slot * NQ + i) * CTA_THREADS + cc * NGPT + g] = q[i];
         if (slot == KL - 1 || jk == L + 1) {
             __syncthreads();
             const int nlev = slot + 1;
@@ -1113,7 +1128,7 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
     extern __shared__ __align__(16) unsigned char smem_raw[];
     fill_tm<R>(smem_raw);
     const CtaView<R> V = cta_view<R>(smem_raw, P);
-    const KissJump J = kiss_setup(P, V.sXs);  // once per launch
+    const KissJump J = kiss_setup(P, V.sXs, thread_g<R>(threadIdx.x));  // once per launch
     R* scr = (R*)P.scratch + (size_t)blockIdx.x * P.slot_elems;
     for (int pair = blockIdx.x; pair < P.npairs; pair += gridDim.x)
         solve_pair<R, MT>(P, pair, V, J, scr, tab, tab64);
@@ -1159,7 +1174,7 @@ k_solve_batch(const SolveParams* __restrict__ Pb, int ninst, const int* __restri
             }
             __syncthreads();
             V = cta_view<R>(smem_raw, sP);
-            J = kiss_setup(sP, V.sXs);
+            J = kiss_setup(sP, V.sXs, thread_g<R>(threadIdx.x));
             cur = lo;
         }
         R* scr = (R*)sP.scratch + (size_t)blockIdx.x * sP.slot_elems;
