@@ -1388,6 +1388,7 @@ int rrtmg_sw_finalize_c(void) {
     if (cs.h_err) cudaFreeHost(cs.h_err);
     cs.h_err = nullptr;
     cs.device = -1;
+    mt_release_device_tables();
     st.init = false;
     return RRTMG_SW_OK;
 }

@@ -60,6 +60,8 @@ cudaError_t launch_mt_jump(uint32_t seed, uint64_t n, uint32_t* out, int num_sms
 // raw (untempered) words behind outputs offset .. offset+623, on the host;
 // 0 or -1 (offset >= 2^48 or jump tables unavailable)
 int mt_window_host(uint32_t seed, uint64_t offset, uint32_t* window);
+// free the device copies of the jump table (rebuilt on next use)
+void mt_release_device_tables();
 // mcica_subcol_sw from the call's MT stream (irng = 1, GCM order)
 cudaError_t launch_mcica_stream(int ncol, int nlay, int icld, const uint32_t* stream, const double* cldfrac,
                                 const double* ciwp, const double* clwp, const double* tauc, const double* ssac,

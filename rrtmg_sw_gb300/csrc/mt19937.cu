@@ -434,6 +434,12 @@ cudaError_t launch_mt_jump(uint32_t seed, uint64_t n, uint32_t* out, int num_sms
     return cudaGetLastError();
 }
 
+void mt_release_device_tables() {
+    std::lock_guard<std::mutex> lk(mt::g_mu);
+    for (mt::DeviceTable& d : mt::g_dev) cudaFree(d.p);
+    mt::g_dev.clear();
+}
+
 int mt_window_host(uint32_t seed, uint64_t offset, uint32_t* window) {
     const mt::Tables& T = mt::tables();
     if (!T.ok) return -1;
