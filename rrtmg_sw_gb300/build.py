@@ -17,6 +17,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "librrtmg_sw_gb300.so")
+# bounds-check build: every coefficient-table read range-checked into an
+# error word (RRTMG_SW_EBOUNDS), for tests; same sources, -DRRTMG_BOUNDS_CHECK
+LIB_BC = os.path.join(OUT_DIR, "librrtmg_sw_gb300_bc.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           "-I", os.path.join(HERE, "..", "include")]
@@ -40,23 +43,26 @@ def sources():
     return [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", "rrtmg_sw_gb300.h")]
 
 
-def up_to_date():
-    if not os.path.exists(LIB):
+def up_to_date(lib=LIB):
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return all(os.path.getmtime(s) <= t for s in sources())
 
 
-def build(force=False, verbose=False, extra_flags=()):
-    if not force and up_to_date():
-        return LIB
+def build(force=False, verbose=False, extra_flags=(), bounds_check=False):
+    lib = LIB_BC if bounds_check else LIB
+    if not force and up_to_date(lib):
+        return lib
     os.makedirs(OUT_DIR, exist_ok=True)
     cc = nvcc()
+    variant = ["-DRRTMG_BOUNDS_CHECK"] if bounds_check else []
+    suffix = "_bc.o" if bounds_check else ".o"
 
     def compile_one(item):
         src, flags = item
-        obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
-        cmd = [cc, *ARCH, *COMMON, *flags, *extra_flags, "-c", os.path.join(CSRC, src), "-o", obj]
+        obj = os.path.join(OUT_DIR, src.replace(".cu", suffix))
+        cmd = [cc, *ARCH, *COMMON, *flags, *variant, *extra_flags, "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -68,13 +74,13 @@ def build(force=False, verbose=False, extra_flags=()):
 
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(compile_one, UNITS.items()))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s" % r.stderr)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

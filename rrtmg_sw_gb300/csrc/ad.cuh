@@ -167,8 +167,8 @@ __device__ inline double prep_layer_dual(const SolveParams& P, int col, int lay,
     const double plog = ::log(p);
     int jp = (int)(36.0 - 5.0 * (plog + 0.04));
     jp = jp < 1 ? 1 : (jp > 58 ? 58 : jp);
-    const double fp = 5.0 * (tab64[cT.preflog + jp - 1] - plog);
-    const double tr0 = tab64[cT.tref + jp - 1], tr1 = tab64[cT.tref + jp];
+    const double fp = 5.0 * (ldt(tab64, cT.preflog + jp - 1) - plog);
+    const double tr0 = ldt(tab64, cT.tref + jp - 1), tr1 = ldt(tab64, cT.tref + jp);
     int jt = (int)(3.0 + (t.v - tr0) / 15.0);
     jt = jt < 1 ? 1 : (jt > 4 ? 4 : jt);
     const D ft = (t - tr0) / 15.0 - (double)(jt - 3);

@@ -51,7 +51,7 @@ struct State {
     std::vector<double> blob64;
     double mgavgcyc[134], sbavgcyc[134];
     double cpdair = 1.004e3;
-    DevBuf d_tab64, d_tab32, scratch, errw;
+    DevBuf d_tab64, d_tab32, scratch, errw, bounds;
     std::map<std::string, DevBuf> stage;  // host-API staging buffers
     int* h_err = nullptr;                  // pinned
     int form = RRTMG_SW_FORM_FP64;
@@ -294,10 +294,30 @@ int upload(State& st) {
     std::vector<float> b32(st.blob64.begin(), st.blob64.end());
     CK(st.d_tab32.ensure(b32.size() * sizeof(float)));
     CK(cudaMemcpy(st.d_tab32.p, b32.data(), b32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(st.bounds.ensure(sizeof(int)));
+    CK(cudaMemset(st.bounds.p, 0, sizeof(int)));
+    T.bounds_err = (int*)st.bounds.p;
     CK(upload_tables_fp64(T));
     CK(upload_tables_fp32(T));
     CK(upload_tables_ad(T));
     return RRTMG_SW_OK;
+}
+
+// Bounds-check builds: after a completed solve, the table-bounds word (set
+// by the kernels' ldt) turns the call's status into RRTMG_SW_EBOUNDS and is
+// cleared.  Other builds return rc unchanged.
+int bounds_status(State& st, int rc) {
+#ifdef RRTMG_BOUNDS_CHECK
+    int h = 0;
+    if (cudaMemcpy(&h, st.bounds.p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return RRTMG_SW_ECUDA;
+    if (h) {
+        cudaMemset(st.bounds.p, 0, sizeof(int));
+        return RRTMG_SW_EBOUNDS;
+    }
+#else
+    (void)st;
+#endif
+    return rc;
 }
 
 // earth_sun (rrtmg_sw_rad.f90:844-868)
@@ -548,7 +568,7 @@ int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaS
     st.last_launches = launches;
     CK(cudaMemcpyAsync(st.h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    return *st.h_err;
+    return bounds_status(st, *st.h_err);
 }
 
 // ---------------------------------------------------------------------------
@@ -713,7 +733,7 @@ int solve_host_chunked(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds*
     st.last_launches = launches;
     for (int i = 0; i < kChunkStreams; ++i)
         if (cs.h_err[i]) return cs.h_err[i];
-    return RRTMG_SW_OK;
+    return bounds_status(st, RRTMG_SW_OK);
 }
 
 // Host-array path: stage every array in a named device buffer.
@@ -874,7 +894,7 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
     int h_err = 0;  // pageable: the copy completes before the call returns
     CK(cudaMemcpyAsync(&h_err, P.err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    return h_err;
+    return bounds_status(st, h_err);
 }
 
 // ---------------------------------------------------------------------------
@@ -958,7 +978,7 @@ int solve_ad_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, const rrtmg_
     CK(cudaMemcpyAsync(st.h_err, P.err, sizeof(int), cudaMemcpyDeviceToHost, s));
     if (sg.err != cudaSuccess) return cuda_fail(sg.err);
     CK(cudaStreamSynchronize(s));
-    return *st.h_err;
+    return bounds_status(st, *st.h_err);
 }
 
 // ---------------------------------------------------------------------------
@@ -1308,6 +1328,7 @@ const char* rrtmg_sw_errstr_c(int32_t code) {
     case RRTMG_SW_ELAYTROP: return "PROFILE MUST HAVE LAYERS ON BOTH SIDES OF THE 100 HPA SWITCH";
     case RRTMG_SW_EIRNG: return "IRNG = 1 (MT19937) NOT AVAILABLE ON THIS ENTRY POINT";
     case RRTMG_SW_EPARTIAL: return "PARTIAL CLOUD NOT ALLOWED";
+    case RRTMG_SW_EBOUNDS: return "TABLE INDEX OUT OF RANGE (BOUNDS-CHECK BUILD)";
     default: return "UNKNOWN ERROR";
     }
 }
@@ -1344,7 +1365,7 @@ int rrtmg_sw_batch_run_c(void* plan, void* stream) {
     st.last_launches = 2;
     CK(cudaMemcpyAsync(bp->h_err, bp->errw.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    return *bp->h_err;
+    return bounds_status(st, *bp->h_err);
 }
 
 int rrtmg_sw_batch_info_c(void* plan, int32_t* grid, int32_t* deepest_first, float* trial_ms, int32_t* ntrials) {
@@ -1374,6 +1395,7 @@ int rrtmg_sw_finalize_c(void) {
     st.d_tab32.release();
     st.scratch.release();
     st.errw.release();
+    st.bounds.release();
     for (auto& kv : st.stage) kv.second.release();
     st.stage.clear();
     if (st.h_err) cudaFreeHost(st.h_err);

@@ -64,6 +64,9 @@ struct DevTables {
     // copies, so a warp spans 2 (at most 3) bands and band-dependent
     // branches diverge less.
     uint8_t thr_cg[CTA_THREADS];
+    // bounds-check builds (RRTMG_BOUNDS_CHECK): word set to E_BOUNDS when a
+    // table index falls outside the blob
+    int* bounds_err;
     double heatfac, bpade, oneminus;
     float bpade_f, oneminus_f;
     TmRegion tm[NBND][2];
@@ -76,6 +79,21 @@ struct DevTables {
 // its upload function (no relocatable device code needed)
 static __constant__ DevTables cT;
 
+// Table read of element i of a coefficient blob (FP64 or FP32 copy, both
+// cT.total elements).  A bounds-check build (-DRRTMG_BOUNDS_CHECK) tests i
+// against the blob, records E_BOUNDS in cT.bounds_err and reads a clamped
+// element instead of leaving the blob.
+template <typename T>
+__device__ __forceinline__ T ldt(const T* __restrict__ tab, int i) {
+#ifdef RRTMG_BOUNDS_CHECK
+    if (i < 0 || i >= cT.total) {
+        if (cT.bounds_err) atomicCAS(cT.bounds_err, 0, 40);
+        i = i < 0 ? 0 : cT.total - 1;
+    }
+#endif
+    return __ldg(tab + i);
+}
+
 // Error word: first error code wins.
 __device__ inline void set_error(int* err, int code) {
     if (err) atomicCAS(err, 0, code);
@@ -86,7 +104,8 @@ constexpr int MAX_BATCH = 1024;  // instances per batch launch
 // Error codes (mirror include/rrtmg_sw_gb300.h)
 enum {
     E_OK = 0, E_INFLAG1 = 10, E_ICERAD = 11, E_ICEDGE = 12, E_ICEPROP = 13,
-    E_LIQRAD = 14, E_LIQPROP = 15, E_ICLD = 20, E_KISSSEED = 21, E_LAYTROP = 30, E_PARTIAL = 32
+    E_LIQRAD = 14, E_LIQPROP = 15, E_ICLD = 20, E_KISSSEED = 21, E_LAYTROP = 30, E_PARTIAL = 32,
+    E_BOUNDS = 40
 };
 
 }  // namespace rrsw

@@ -61,8 +61,8 @@ __device__ inline void prep_layer(const SolveParams& P, int col, int lay, R* cf,
     const double plog = log(p);
     int jp = (int)DS(36.0, DM(5.0, DA(plog, 0.04)));
     jp = jp < 1 ? 1 : (jp > 58 ? 58 : jp);
-    const double fp = DM(5.0, DS(tab64[cT.preflog + jp - 1], plog));
-    const double tr0 = tab64[cT.tref + jp - 1], tr1 = tab64[cT.tref + jp];
+    const double fp = DM(5.0, DS(ldt(tab64, cT.preflog + jp - 1), plog));
+    const double tr0 = ldt(tab64, cT.tref + jp - 1), tr1 = ldt(tab64, cT.tref + jp);
     int jt = (int)DA(3.0, DS(t, tr0) / 15.0);
     jt = jt < 1 ? 1 : (jt > 4 ? 4 : jt);
     const double ft = DS(DS(t, tr0) / 15.0, (double)(jt - 3));
@@ -152,8 +152,8 @@ __device__ inline void aerosol(const SolveParams& P, int col, int lay, int ib, c
         double t = 0.0, a = 0.0, o = 0.0;
         for (int ia = 0; ia < 6; ++ia) {
             const double ec = P.ecaer[(size_t)col + n * ((size_t)(lay - 1) + nl * (size_t)ia)];
-            const double rt = tab64[cT.rsrtaua + ib + 14 * ia], rp = tab64[cT.rsrpiza + ib + 14 * ia],
-                         ra = tab64[cT.rsrasya + ib + 14 * ia];
+            const double rt = ldt(tab64, cT.rsrtaua + ib + 14 * ia), rp = ldt(tab64, cT.rsrpiza + ib + 14 * ia),
+                         ra = ldt(tab64, cT.rsrasya + ib + 14 * ia);
             t = DA(t, DM(rt, ec));
             o = DA(o, DM(DM(rt, ec), rp));
             a = DA(a, DM(DM(DM(rt, ec), rp), ra));
@@ -322,7 +322,7 @@ __device__ inline float tbl_exp_beam(float x, const float* __restrict__ tab, flo
     const float u = x / (cT.bpade_f + x);
     const float t = 10000.0f * u + 0.5f;
     const int itind = (int)t;
-    const float e = __ldg(tab + cT.exp_tbl + itind);
+    const float e = ldt(tab, cT.exp_tbl + itind);
     const float fr = t - (float)itind;
     if (fminf(fr, 1.0f - fr) < 10000.0f * u * (1.0f - u) * BEAM_EPS) {
         const float bx = cT.bpade_f + x;

@@ -109,7 +109,7 @@ __device__ inline R tbl_exp(R ze1, const R* __restrict__ tab) {
     if (ze1 <= od_lo) return R(1) - ze1 + R(0.5) * ze1 * ze1;
     const R tblind = ze1 / (c_bpade<R>() + ze1);
     const int itind = (int)(R(10000) * tblind + R(0.5));
-    return __ldg(tab + cT.exp_tbl + itind);
+    return ldt(tab, cT.exp_tbl + itind);
 }
 
 // --------------------------------------------------------------- taumol
@@ -145,7 +145,7 @@ __device__ inline Spec<R> spec(R cola, R colb_scaled, R mult, const Coef<R>& c, 
 // k(ind, ig) of a transposed table: [(ind-1)*ng + ig-1]
 template <typename R>
 __device__ inline R K(const TabT<R>* __restrict__ tab, int off, int ng, int ind, int ig) {
-    return R(__ldg(tab + off + (ind - 1) * ng + (ig - 1)));
+    return R(ldt(tab, off + (ind - 1) * ng + (ig - 1)));
 }
 
 template <typename R>
@@ -183,7 +183,7 @@ __device__ inline R selffor(const Coef<R>& c, int lay, const BandOff& B, const T
     return selfterm(c, lay, B, tab, ig) + forterm(c, lay, B, tab, ig);
 }
 template <typename R>
-__device__ inline R V(const TabT<R>* __restrict__ tab, int off, int i) { return R(__ldg(tab + off + i)); }
+__device__ inline R V(const TabT<R>* __restrict__ tab, int off, int i) { return R(ldt(tab, off + i)); }
 
 // Lower/upper table base indices (taumol.f90:326-327, 357-358)
 __device__ inline int ind_lo(int jp, int jt, int nsp, int js) { return ((jp - 1) * 5 + (jt - 1)) * nsp + js; }
@@ -363,40 +363,38 @@ __device__ inline void taumol_generic(int ib, int ig, int lay, const Coef<float>
         const int nsp = d.nsp;
         const int i0 = ((jp * 5 + (jt - 1)) * nsp + js - 1) * ng + ig - 1;
         const int i1 = (((jp + 1) * 5 + (jt1 - 1)) * nsp + js - 1) * ng + ig - 1;
-        const float* k = tab + d.ktab;
         const float gs = 1.0f - fs;
-        const float k0 = gs * f00 * __ldg(k + i0) + fs * f00 * __ldg(k + i0 + ng) +
-                         gs * f10 * __ldg(k + i0 + nsp * ng) + fs * f10 * __ldg(k + i0 + (nsp + 1) * ng);
-        const float k1 = gs * f01 * __ldg(k + i1) + fs * f01 * __ldg(k + i1 + ng) +
-                         gs * f11 * __ldg(k + i1 + nsp * ng) + fs * f11 * __ldg(k + i1 + (nsp + 1) * ng);
+        const float k0 = gs * f00 * ldt(tab, d.ktab + i0) + fs * f00 * ldt(tab, d.ktab + i0 + ng) +
+                         gs * f10 * ldt(tab, d.ktab + i0 + nsp * ng) + fs * f10 * ldt(tab, d.ktab + i0 + (nsp + 1) * ng);
+        const float k1 = gs * f01 * ldt(tab, d.ktab + i1) + fs * f01 * ldt(tab, d.ktab + i1 + ng) +
+                         gs * f11 * ldt(tab, d.ktab + i1 + nsp * ng) + fs * f11 * ldt(tab, d.ktab + i1 + (nsp + 1) * ng);
         tg = speccomb * (k0 + k1);
     } else if (d.kind == 2) {
         const int i0 = (jp * 5 + (jt - 1)) * ng + ig - 1;
         const int i1 = ((jp + 1) * 5 + (jt1 - 1)) * ng + ig - 1;
-        const float* k = tab + d.ktab;
-        const float kk = c.f(F_FAC00, lay) * __ldg(k + i0) + c.f(F_FAC10, lay) * __ldg(k + i0 + ng) +
-                         c.f(F_FAC01, lay) * __ldg(k + i1) + c.f(F_FAC11, lay) * __ldg(k + i1 + ng);
+        const float kk = c.f(F_FAC00, lay) * ldt(tab, d.ktab + i0) + c.f(F_FAC10, lay) * ldt(tab, d.ktab + i0 + ng) +
+                         c.f(F_FAC01, lay) * ldt(tab, d.ktab + i1) + c.f(F_FAC11, lay) * ldt(tab, d.ktab + i1 + ng);
         tg = c.f(F_H2O + d.sa, lay) * d.fac * kk;
     }
     if (d.cont >= 1) {
         const int indf = c.indfor(lay);
-        const float fa = __ldg(tab + t.forref + (indf - 1) * ng + ig - 1), fb = __ldg(tab + t.forref + indf * ng + ig - 1);
+        const float fa = ldt(tab, t.forref + (indf - 1) * ng + ig - 1), fb = ldt(tab, t.forref + indf * ng + ig - 1);
         float cont = c.f(F_FORFAC, lay) * (fa + c.f(F_FORFRAC, lay) * (fb - fa));
         if (d.cont == 1) {
             const int inds = c.indself(lay);
-            const float sa = __ldg(tab + t.selfref + (inds - 1) * ng + ig - 1);
-            const float sb = __ldg(tab + t.selfref + inds * ng + ig - 1);
+            const float sa = ldt(tab, t.selfref + (inds - 1) * ng + ig - 1);
+            const float sb = ldt(tab, t.selfref + inds * ng + ig - 1);
             cont = c.f(F_SELFFAC, lay) * (sa + c.f(F_SELFFRAC, lay) * (sb - sa)) + cont;
         }
         tg += colh2o * cont;
     }
     if (d.minor == 9) tg += 4.35e-4f * c.f(F_O2, lay) / 700.0f;
-    else if (d.minor >= 0) tg += c.f(F_H2O + d.minor, lay) * __ldg(tab + d.mtab + ig - 1);
+    else if (d.minor >= 0) tg += c.f(F_H2O + d.minor, lay) * ldt(tab, d.mtab + ig - 1);
     const float colmol = c.f(F_MOL, lay);
-    if (d.rtype == 0) taur = colmol * __ldg(tab + d.rtab);
-    else if (d.rtype == 1) taur = colmol * __ldg(tab + d.rtab + ig - 1);
+    if (d.rtype == 0) taur = colmol * ldt(tab, d.rtab);
+    else if (d.rtype == 1) taur = colmol * ldt(tab, d.rtab + ig - 1);
     else {
-        const float ra = __ldg(tab + d.rtab + (js - 1) * ng + ig - 1), rb = __ldg(tab + d.rtab + js * ng + ig - 1);
+        const float ra = ldt(tab, d.rtab + (js - 1) * ng + ig - 1), rb = ldt(tab, d.rtab + js * ng + ig - 1);
         taur = colmol * (ra + fs * (rb - ra));
     }
     taug = tg;
@@ -491,8 +489,8 @@ __device__ inline float solar_source_generic(int ib, int ig, const Coef<float>& 
         interp = true;
     }
     auto src = [&](int off) -> float {
-        if (!interp) return __ldg(tab + off + ig - 1);
-        const float a = __ldg(tab + off + (js - 1) * B.ng + ig - 1), b = __ldg(tab + off + js * B.ng + ig - 1);
+        if (!interp) return ldt(tab, off + ig - 1);
+        const float a = ldt(tab, off + (js - 1) * B.ng + ig - 1), b = ldt(tab, off + js * B.ng + ig - 1);
         return a + fs * (b - a);
     };
     if (P.isolvar < 0) {
@@ -538,21 +536,21 @@ __device__ inline void cldprmc_g(int ib, int inflag, int iceflag, int liqflag, R
     double_ extcoice = 0, ssacoice = 0, gice = 0, forwice = 0, extcoliq = 0, ssacoliq = 0, gliq = 0, forwliq = 0;
     double_ coice = 1, coliq = 1;  // 1 - ssacoice, 1 - ssacoliq from the co-albedo tables
     const int jb = ib + 1;  // band column of the Fortran (index, 16:29) LUTs, 1-based
-    auto lut = [&](int off, int n, int index) { return R(__ldg(tab + off + (jb - 1) * n + index - 1)); };
+    auto lut = [&](int off, int n, int index) { return R(ldt(tab, off + (jb - 1) * n + index - 1)); };
     if (ciwp == R(0.0)) {
     } else if (iceflag == 1) {
         if (rei < R(13.0) || rei > R(130.0)) { set_error(err, E_ICERAD); return; }
-        const double_ w2 = R(__ldg(tab + cT.wavenum2 + ib));
+        const double_ w2 = R(ldt(tab, cT.wavenum2 + ib));
         int icx = 0;
         if (w2 > R(1.43e04)) icx = 1;
         else if (w2 > R(7.7e03)) icx = 2;
         else if (w2 > R(5.3e03)) icx = 3;
         else if (w2 > R(4.0e03)) icx = 4;
         else if (w2 >= R(2.5e03)) icx = 5;
-        extcoice = (R(__ldg(tab + cT.abari + icx - 1)) + R(__ldg(tab + cT.bbari + icx - 1)) / rei);
-        ssacoice = R(1.0) - R(__ldg(tab + cT.cbari + icx - 1)) - R(__ldg(tab + cT.dbari + icx - 1)) * rei;
-        coice = R(__ldg(tab + cT.cbari + icx - 1)) + R(__ldg(tab + cT.dbari + icx - 1)) * rei;
-        gice = R(__ldg(tab + cT.ebari + icx - 1)) + R(__ldg(tab + cT.fbari + icx - 1)) * rei;
+        extcoice = (R(ldt(tab, cT.abari + icx - 1)) + R(ldt(tab, cT.bbari + icx - 1)) / rei);
+        ssacoice = R(1.0) - R(ldt(tab, cT.cbari + icx - 1)) - R(ldt(tab, cT.dbari + icx - 1)) * rei;
+        coice = R(ldt(tab, cT.cbari + icx - 1)) + R(ldt(tab, cT.dbari + icx - 1)) * rei;
+        gice = R(ldt(tab, cT.ebari + icx - 1)) + R(ldt(tab, cT.fbari + icx - 1)) * rei;
         if (gice >= R(1.0)) gice = R(1.0) - eps;
         forwice = gice * gice;
         if (extcoice < R(0.0) || ssacoice > R(1.0) || ssacoice < R(0.0) || gice > R(1.0) || gice < R(0.0)) { set_error(err, E_ICEPROP); return; }

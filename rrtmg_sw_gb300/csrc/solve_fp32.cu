@@ -14,7 +14,7 @@ __device__ inline float tbl_exp_om(float x, const float* __restrict__ tab, float
     }
     const float tblind = x / (cT.bpade_f + x);
     const int itind = (int)(10000.0f * tblind + 0.5f);
-    const float e = __ldg(tab + cT.exp_tbl + itind);
+    const float e = ldt(tab, cT.exp_tbl + itind);
     om = 1.0f - e;
     return e;
 }

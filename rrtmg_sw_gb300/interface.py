@@ -85,9 +85,12 @@ def lib():
     """Load the CUDA library; raise if it has not been built."""
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise RuntimeError("librrtmg_sw_gb300.so is not built (run rrtmg_sw_gb300.build.build())")
-        L = C.CDLL(LIB_PATH)
+        # RRTMG_SW_LIB selects another build of the library (e.g. the
+        # bounds-check build, rrtmg_sw_gb300.build.build(bounds_check=True))
+        path = os.environ.get("RRTMG_SW_LIB", LIB_PATH)
+        if not os.path.exists(path):
+            raise RuntimeError("%s is not built (run rrtmg_sw_gb300.build.build())" % path)
+        L = C.CDLL(path)
         L.rrtmg_sw_ini_c.argtypes = [C.c_double]
         L.rrtmg_sw_c.argtypes = [C.POINTER(RrtmgSwArgs)]
         L.rrtmg_sw_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.c_void_p]
