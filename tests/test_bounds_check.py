@@ -3,8 +3,8 @@ is range-checked against the blob and a violation returns RRTMG_SW_EBOUNDS.
 The cases of bounds_cases.py (every form, overlap, RNG, aerosol and cloud
 option, non-McICA, extra and per-band outputs, adjoint) must run clean, and
 its FP64-form results must equal the normal build's bit for bit (the checks
-add no arithmetic; the adjoint to 1e-12 relative); FP32-form results within
-1e-3 W m-2 / K d-1."""
+add no arithmetic; the adjoint, whose gradient sums use atomics, to 1e-8 of
+each field's largest entry); FP32-form results within 1e-3 W m-2 / K d-1."""
 import os
 import subprocess
 import sys
@@ -35,7 +35,9 @@ def test_bounds_check_build_runs_clean(tmp_path):
     for k, v in ref.items():
         if k.startswith("f32"):
             assert np.max(np.abs(bc[k] - v)) <= 1e-3, k
-        elif k.startswith("ad_"):  # the adjoint unit contracts FMAs: compare to 1e-12 of the field
-            assert np.max(np.abs(bc[k] - v)) <= 1e-12 * max(np.max(np.abs(v)), 1e-300), k
+        elif k.startswith("ad_"):
+            # the adjoint unit contracts FMAs and sums gradients with shared-memory
+            # atomics (order varies): compare to 1e-8 of the field's largest entry
+            assert np.max(np.abs(bc[k] - v)) <= 1e-8 * max(np.max(np.abs(v)), 1e-300), k
         else:
             assert np.array_equal(bc[k], v), k
