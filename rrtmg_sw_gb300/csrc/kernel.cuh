@@ -973,6 +973,15 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
             }
             rup = sv[S_RUP * CTA_THREADS]; rupd = sv[S_RUPD * CTA_THREADS];
             if (P.idelm == 0) { dbtcn = sv[S_DBTCN * CTA_THREADS]; dbtn = sv[S_DBTN * CTA_THREADS]; }
+            if constexpr (sizeof(R) == 4) {
+                // the next level's fields into L1 while this level computes and
+                // reduces (the level barriers keep its loads from moving up)
+                if (jk < L) {
+                    const R* nx = sv + (size_t)NS * CTA_THREADS;
+#pragma unroll
+                    for (int f = 0; f < S_DBTCN; ++f) asm volatile("prefetch.global.L1 [%0];" ::"l"(nx + f * CTA_THREADS));
+                }
+            }
         } else {
             rupc = albp; rupdc = albd; rup = albp; rupd = albd;
         }
