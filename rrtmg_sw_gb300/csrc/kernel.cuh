@@ -495,6 +495,10 @@ static __device__ __noinline__ void redo_cells_fp64(const SolveParams& P, const 
         rupd_b = at(from - 1, S_RUPD);
     }
     for (int lay = from; lay <= L; ++lay) {
+        if (lay < L) {  // the next layer's cell fields into L1 while this one is swept
+#pragma unroll
+            for (int f = 0; f < S_DBTCN; ++f) asm volatile("prefetch.global.L1 [%0];" ::"l"(&at(lay + 1, f)));
+        }
         const float mark = at(lay, S_DBTC);
         if (mark < 0.0f) {
             const CellOpt<float> co = cell_optics_fp64(P, C64, col, g, lay, ib, igb, fused, mark < -1.5f, cossza, tab64);
