@@ -74,7 +74,7 @@ def algorithmic_flops_per_column(nlay, cloudy_cells_per_col):
 # DRAM bytes per column of k_solve<float> measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum) in a full capture at 32768 columns x 60 layers; the traffic is
 # per column pair, so a launch's traffic scales with its columns.
-PROFILED_DRAM_BYTES_PER_COLUMN = 28.20e9 / 32768
+PROFILED_DRAM_BYTES_PER_COLUMN = 28.38e9 / 32768
 
 
 def algorithmic_bytes_per_column(nlay):
