@@ -167,7 +167,8 @@ int rrtmg_sw_nomcica_dev_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, voi
  * (any may be NULL); rrtmg_sw_tl_c reads the same arrays as a direction and
  * writes J and dJ = dJ/dx . direction.  store = 1 keeps each cell's local
  * Jacobian from the forward pass (more memory), 0 recomputes it in the
- * reverse pass. */
+ * reverse pass, -1 chooses by memory: stored when that scratch fits in half
+ * of the free device memory; rrtmg_sw_last_ad_store_c reports the choice. */
 typedef struct rrtmg_sw_ad_args {
     double w_toa_up, w_sfc_net, w_hr_sum;
     int32_t store, pad;
@@ -275,6 +276,9 @@ int rrtmg_sw_get_form_c(void);
 
 /* Number of kernels the most recent solve launched (for launch accounting). */
 int rrtmg_sw_last_launch_count_c(void);
+/* Checkpointing of the most recent rrtmg_sw_ad_c / rrtmg_sw_tl_c call:
+ * 1 stored Jacobians, 0 recomputed, -1 none yet. */
+int rrtmg_sw_last_ad_store_c(void);
 
 /* Reference message for an error code; last CUDA error string. */
 const char *rrtmg_sw_errstr_c(int32_t code);

@@ -56,6 +56,7 @@ struct State {
     int* h_err = nullptr;                  // pinned
     int form = RRTMG_SW_FORM_FP64;
     int last_launches = 0;
+    int last_ad_store = -1;  // checkpointing choice of the last adjoint / tangent-linear call
     std::string last_cuda;
 };
 
@@ -939,7 +940,7 @@ int solve_ad_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, const rrtmg_
     // the flux outputs are not written; make_params only records them
     AdParams A{};
     A.w_toa = ad->w_toa_up; A.w_net = ad->w_sfc_net; A.w_hr = ad->w_hr_sum;
-    A.store = ad->store ? 1 : 0;
+    A.store = ad->store > 0 ? 1 : 0;  // store < 0: chosen below from free device memory
     A.tl = tl ? 1 : 0;
     A.J = sg.out("adJ", ad->J, C);
     A.dJ = tl ? sg.out("addJ", ad->dJ, C) : nullptr;
@@ -965,6 +966,15 @@ int solve_ad_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, const rrtmg_
     CK(st.errw.ensure(sizeof(int)));
     P.err = (int*)st.errw.p;
     const int grid = adjoint_grid(P, st.num_sms);
+    if (ad->store < 0) {
+        // stored Jacobians when their scratch fits in half the free memory
+        // (beyond what is already allocated), else recomputed
+        size_t fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot));
+        const size_t need = (size_t)grid * adjoint_slot_elems(P.nlay, 1) * sizeof(double);
+        A.store = need <= st.scratch.bytes + fr / 2 ? 1 : 0;
+    }
+    st.last_ad_store = A.store;
     P.slot_elems = adjoint_slot_elems(P.nlay, A.store);
     CK(st.scratch.ensure((size_t)grid * P.slot_elems * sizeof(double)));
     P.scratch = st.scratch.p;
@@ -1308,6 +1318,8 @@ int rrtmg_sw_set_form_c(int32_t form) {
 int rrtmg_sw_get_form_c(void) { return S().form; }
 
 int rrtmg_sw_last_launch_count_c(void) { return S().last_launches; }
+
+int rrtmg_sw_last_ad_store_c(void) { return S().last_ad_store; }
 
 const char* rrtmg_sw_errstr_c(int32_t code) {
     switch (code) {

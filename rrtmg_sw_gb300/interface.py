@@ -320,7 +320,7 @@ def _ad_call(kw, clouds, weights, store, direction):
             setattr(c, name, _p(keep["c_" + name]))
     d = RrtmgSwAdArgs()
     d.w_toa_up, d.w_sfc_net, d.w_hr_sum = weights
-    d.store = 1 if store else 0
+    d.store = -1 if store == "auto" else (1 if store else 0)
     out = {"J": np.zeros(ncol)}
     if direction is None:
         out.update({k: np.zeros(cl, order="F") for k in AD_LAYER})
@@ -346,7 +346,9 @@ def _ad_call(kw, clouds, weights, store, direction):
 def rrtmg_sw_ad(kw, clouds=None, weights=(1.0, 0.0, 0.0), store=True):
     """Adjoint: J and its gradients (dict keyed by AD_LAYER + AD_SFC) for the
     objective J = w_toa_up*swuflx(top) + w_sfc_net*net flux(sfc) + w_hr_sum*sum(swhr);
-    ``kw`` holds the rrtmg_sw arguments (as for :func:`rrtmg_sw`)."""
+    ``kw`` holds the rrtmg_sw arguments (as for :func:`rrtmg_sw`).  ``store``:
+    True keeps the local Jacobians, False recomputes them, "auto" lets the
+    library choose by free device memory."""
     return _ad_call(kw, clouds, weights, store, None)
 
 

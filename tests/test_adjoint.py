@@ -112,6 +112,18 @@ def test_stored_and_recomputed_jacobians_agree(gpu):
         assert np.max(np.abs(a[k] - b[k])) / scale <= 1e-12, k
 
 
+def test_checkpointing_chosen_by_memory(gpu):
+    # store = "auto" (-1 in the C ABI): the stored Jacobians' scratch of a small
+    # case fits, so they are stored, and the result is that of store=True
+    kw, cl = case(seed=65)
+    a = gpu.rrtmg_sw_ad(kw, cl, (0.5, -1.0, 2.0), store="auto")
+    assert gpu.lib().rrtmg_sw_last_ad_store_c() == 1
+    b = gpu.rrtmg_sw_ad(kw, cl, (0.5, -1.0, 2.0), store=True)
+    for k in ("J",) + gpu.AD_LAYER + gpu.AD_SFC:
+        scale = max(np.max(np.abs(b[k])), 1e-300)
+        assert np.max(np.abs(a[k] - b[k])) / scale <= 1e-12, k
+
+
 def test_smooth_model_is_close_to_the_table_model(gpu):
     kw, cl = case(seed=64, clouds=False)
     ad = gpu.rrtmg_sw_ad(kw, cl, (1.0, 0.0, 0.0))
