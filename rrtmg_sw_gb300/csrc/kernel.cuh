@@ -8,8 +8,9 @@ namespace rrsw {
 // levels buffered per reduction round of the g-point sums
 constexpr int KLEV = 4;
 // FP32 form: cells to redo in FP64 queued per column pair (one int each:
-// thread << 12 | layer << 1 | cloudy); cells past the queue are redone by
-// their own thread
+// thread << 20 | column slot << 19 | g-point << 12 | layer << 1 | cloudy);
+// cells past the queue are marked in
+// the scratch and redone by their own thread
 constexpr int REDO_QUEUE = 1024;
 constexpr int KLEV_F32 = 1;
 __host__ __device__ constexpr int klev_of(size_t rsz) { return rsz == 4 ? KLEV_F32 : KLEV; }
@@ -439,12 +440,9 @@ static __device__ __noinline__ CellOpt<float> cell_optics_fp64(const SolveParams
     return o;
 }
 
-// FP32 form: redo the marked cells of one (column, g-point) in FP64 and
-// the upward adding recurrence (vrtqdr:122-140) from the lowest of them to
-// the top.  sv0 is the thread's scratch column (stride CTA_THREADS per
-// field, NS fields per level); the transmittance slots hold absorptances.
-// A redone cell into its thread's scratch column sv0 (the transmittance
-// slots hold absorptances).
+// A redone cell into its thread's scratch column sv0 (stride CTA_THREADS
+// per field, NS fields per level; the transmittance slots hold
+// absorptances).
 __device__ inline void store_cell(float* sv0, int NS, int L, int lay, const CellOpt<float>& co, int idelm) {
     float* sv = sv0 + (size_t)(L - lay) * NS * CTA_THREADS;
     sv[S_REFC * CTA_THREADS] = co.rc.ref;
@@ -481,6 +479,10 @@ __device__ inline bool cell_changed(const float* sv0, int NS, int L, int lay, co
     return ch;
 }
 
+// FP32 form: the upward adding recurrence (vrtqdr:122-140) of one (column,
+// g-point) again from layer `from` to the top, over cells already redone in
+// FP64 by the CTA's queue, redoing in FP64 any cell still marked in the
+// scratch (one the queue could not hold).
 static __device__ __noinline__ void redo_cells_fp64(const SolveParams& P, const Coef<double>& C64, float* sv0, int NS,
                                                     int col, int g, int ib, int igb, bool fused, double cossza,
                                                     const double* __restrict__ tab64, float albp, float albd,
