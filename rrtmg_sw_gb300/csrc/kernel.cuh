@@ -9,8 +9,8 @@ namespace rrsw {
 constexpr int KLEV = 4;
 // FP32 form: cells to redo in FP64 queued per column pair (one int each:
 // thread << 20 | column slot << 19 | g-point << 12 | layer << 1 | cloudy);
-// cells past the queue are marked in
-// the scratch and redone by their own thread
+// cells past the queue are marked in the scratch and redone by their own
+// thread
 constexpr int REDO_QUEUE = 1024;
 constexpr int KLEV_F32 = 1;
 __host__ __device__ constexpr int klev_of(size_t rsz) { return rsz == 4 ? KLEV_F32 : KLEV; }
