@@ -1,7 +1,7 @@
 """ctypes binding of the FP64 CPU oracle (``liboracle_rrtmg_sw.so``).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of bench.py as the checker for the GPU library.  Nothing in
+CPU-baseline leg of bench.py as the oracle for the GPU library.  Nothing in
 ``rrtmg_sw_gb300`` imports this module.
 """
 import ctypes as C

@@ -1,5 +1,5 @@
 // rrtmg_sw_oracle.cpp -- FP64 CPU restatement of the RRTMG_SW shortwave
-// column solve.  TEST INFRASTRUCTURE ONLY: the checker for the GPU library,
+// column solve.  TEST INFRASTRUCTURE ONLY: the oracle for the GPU library,
 // never part of the product path (see rrtmg_sw_oracle.h).
 //
 // Each routine follows the reference Fortran line by line; the cited

@@ -1,8 +1,8 @@
 /*
  * rrtmg_sw_oracle.h -- FP64 CPU restatement of the RRTMG_SW shortwave solve.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU
- * implementation in rrtmg_sw_gb300/: it is loaded by tests/, by
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the GPU
+ * implementation in rrtmg_sw_gb300/ is tested against: it is loaded by tests/, by
  * __graft_entry__.smoke() and by bench.py's CPU-baseline leg, never by the
  * product path.  It restates, in plain C++ compiled with -ffp-contract=off,
  * the reference Fortran routines cited next to each function in
