@@ -83,6 +83,7 @@ def lib():
         L.orc_setcoef_indices.argtypes = [C.c_int, _dp, _dp, _dp, _dp] + [_ip] * 6
         L.orc_exp_table.argtypes = [_dp]
         L.orc_heatfac.restype = C.c_double
+        L.orc_solar_factors.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int] + [_dp] * 6
         rc = L.orc_init(TABLES.encode(), C.c_double(1.004e3))
         if rc != 0:
             raise RuntimeError("oracle init failed: %d" % rc)
@@ -107,7 +108,10 @@ def _f64(a):
 
 
 def column_mode(case, istart=16, iend=29, nmca=200):
-    """Run one golden column case (dict from tests/golden/std_atm_cases.json)."""
+    """Run one golden column case (dict from tests/golden/std_atm_cases.json).
+
+    Optional keys ``svar`` (f, s, i) and ``svar_bnd`` (3 x 14) carry the
+    solar-variability factors of ``solar_factors``; both default to 1."""
     nlay = case["nlay"]
     keep = []
 
@@ -125,8 +129,9 @@ def column_mode(case, istart=16, iend=29, nmca=200):
     c.inflag, c.iceflag, c.liqflag, c.isolvar = case["inflag"], case["iceflag"], case["liqflag"], case["isolvar"]
     c.istart, c.iend = istart, iend
     c.zenith, c.decorr_con, c.lat = case["zenith"], case["decorr_con"], case["lat"]
-    c.svar_f = c.svar_s = c.svar_i = 1.0
-    c.svar_f_bnd, c.svar_s_bnd, c.svar_i_bnd = arr(ones), arr(ones), arr(ones)
+    c.svar_f, c.svar_s, c.svar_i = case.get("svar", (1.0, 1.0, 1.0))
+    bnd = case.get("svar_bnd", (ones, ones, ones))
+    c.svar_f_bnd, c.svar_s_bnd, c.svar_i_bnd = arr(bnd[0], 14), arr(bnd[1], 14), arr(bnd[2], 14)
     c.adjflux, c.albedo = arr(case["adjflux"], 14), arr(case["albedo"], 14)
     c.pavel, c.tavel = arr(case["pavel"], nlay), arr(case["tavel"], nlay)
     c.pz, c.tz = arr(case["pz"], nlay + 1), arr(case["tz"], nlay + 1)
@@ -144,6 +149,17 @@ def column_mode(case, istart=16, iend=29, nmca=200):
     if rc != 0:
         raise RuntimeError("orc_column_mode failed: %d" % rc)
     return out
+
+
+def solar_factors(isolvar, scon, adjes=1.0, dyofyr=0, indsolvar=None, solcycfrac=None, bndsolvar=None):
+    """Solar-variability factors of one solar record (``orc_solar_factors``):
+    dict with svar (3), svar_bnd (3 x 14) and adjflux (14)."""
+    keep = [None if x is None else _f64(np.atleast_1d(x)) for x in (indsolvar, solcycfrac, bndsolvar)]
+    svar, bnd, adj = np.zeros(3), np.zeros(42), np.zeros(14)
+    rc = lib().orc_solar_factors(isolvar, scon, adjes, dyofyr, *(_p(x) for x in keep), _p(svar), _p(bnd), _p(adj))
+    if rc != 0:
+        raise RuntimeError("orc_solar_factors failed: %d" % rc)
+    return dict(svar=svar, svar_bnd=bnd.reshape(3, 14), adjflux=adj)
 
 
 GCM_INPUTS = ("play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "n2ovmr", "o2vmr",

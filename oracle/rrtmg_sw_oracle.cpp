@@ -1494,6 +1494,31 @@ static void solar_setup(const orc_rrtmg_sw_args* a, Solar& S, double* adjflux) {
     for (int i = 0; i < NBND; ++i) adjflux[i] = isolvar < 0 ? adjflx * solvar[i] : adjflx;
 }
 
+// The column driver's solar settings (rrtmg_sw.1col.f90:1391-1436,1446-1660) are
+// those of inatm_sw for isolvar 0..3: expose them for orc_column_mode.
+int orc_solar_factors(int isolvar, double scon, double adjes, int dyofyr, const double* indsolvar,
+                      const double* solcycfrac, const double* bndsolvar, double* svar, double* svar_bnd,
+                      double* adjflux) {
+    if (!T.ok) return ORC_ERR_NOT_INITIALIZED;
+    orc_rrtmg_sw_args a{};
+    a.isolvar = isolvar;
+    a.scon = scon;
+    a.adjes = adjes;
+    a.dyofyr = dyofyr;
+    a.indsolvar = indsolvar;
+    a.solcycfrac = solcycfrac;
+    a.bndsolvar = bndsolvar;
+    Solar S;
+    solar_setup(&a, S, adjflux);
+    svar[0] = S.svar_f; svar[1] = S.svar_s; svar[2] = S.svar_i;
+    for (int i = 0; i < NBND; ++i) {
+        svar_bnd[i] = S.svar_f_bnd[i];
+        svar_bnd[NBND + i] = S.svar_s_bnd[i];
+        svar_bnd[2 * NBND + i] = S.svar_i_bnd[i];
+    }
+    return ORC_OK;
+}
+
 struct NomcicaClouds {
     const double *cldfr, *taucld, *ssacld, *asmcld, *fsfcld, *cicewp, *cliqwp, *reice, *reliq;
 };

@@ -142,6 +142,16 @@ typedef struct orc_column_case {
 
 int orc_column_mode(const orc_column_case *c);
 
+/* Solar-variability factors of one solar record, for orc_column_mode: the
+ * settings of inatm_sw (rrtmg_sw_rad.f90:1245-1512), which the column driver
+ * repeats for isolvar 0..3 (rrtmg_sw.1col.f90:1391-1436,1446-1660).
+ * indsolvar (2), solcycfrac and bndsolvar (14) may be NULL as in
+ * orc_rrtmg_sw_args.  Outputs: svar = {f, s, i}, svar_bnd = {f[14], s[14],
+ * i[14]}, adjflux (14). */
+int orc_solar_factors(int isolvar, double scon, double adjes, int dyofyr,
+                      const double *indsolvar, const double *solcycfrac, const double *bndsolvar,
+                      double *svar, double *svar_bnd, double *adjflux);
+
 /* Diagnostics of setcoef_sw for parity tests of the integer indices:
  * jp, jt, jt1, indself, indfor (nlay each) and laytrop for one column. */
 int orc_setcoef_indices(int nlay, const double *pavel, const double *tavel,

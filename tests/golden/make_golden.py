@@ -18,12 +18,13 @@ oracle.  The expected outputs are the committed ``output_rrtm_*`` tables,
 one block per band range.
 
 The five solar-variability runs (``iatm = 1``: their layers come from the
-profile builder ``rrtatm.f``, which is not restated) contribute only what
-does not depend on the layers: their solar records (:1391-1436: juldat,
-sza, isolvar, scon, solcycfrac, solvar) and the top-of-atmosphere row of
-every block.  The downward flux there is the band's solar source times
-cos(sza); for the bands whose source is not interpolated in a species
-ratio at the reference layer it pins the solar-variability factors.
+profile builder ``rrtatm.f``) give two fixtures.  ``solvar_toa_cases.json``
+keeps their solar records (:1391-1436: juldat, sza, isolvar, scon,
+solcycfrac, solvar) and the top-of-atmosphere row of every block, which
+does not depend on the layers.  ``std_atm_iatm1_cases.json`` keeps the
+same solar records, the profile-builder records 3.1-3.5 as ``rrtatm.f``
+reads them, and every printed block; the layers themselves are left to
+the oracle's restatement of the profile builder (``oracle/rrtatm.py``).
 """
 import json
 import math
@@ -77,12 +78,11 @@ def fnum(field, d=0):
     if not m:
         raise ValueError("bad numeric field %r" % field)
     sign, ip, dot, fp, ex = m.groups()
+    # one correctly rounded conversion, as a Fortran read makes
     if dot:
-        val = float((ip or "0") + "." + (fp or "0"))
+        val = float("%s.%se%d" % (ip or "0", fp or "0", int(ex) if ex else 0))
     else:
-        val = int(ip + fp) * 10.0 ** (-d)
-    if ex:
-        val = val * 10.0 ** int(ex)
+        val = float("%se%d" % (ip + fp, (int(ex) if ex else 0) - d))
     return -val if sign == "-" else val
 
 
@@ -229,6 +229,68 @@ def read_solar(path):
     pi = 2.0 * math.asin(1.0)
     return dict(juldat=juldat, sza=sza, zenith=math.cos(sza * pi / 180.0), isolvar=isolvar, scon=scon,
                 solcycfrac=solcycfrac, solvar=solvar, albedo=[1.0 - e for e in semiss])
+
+
+def read_iatm1(path):
+    """Control flags (record 1.2, format 9011) and the profile-builder records
+    3.1-3.5 of an iatm = 1 run, as rrtatm.f reads them: ATMPTH record 3.1
+    (rrtatm.f:576-577, format 900) and 3.2 (:786, format 932), boundaries
+    (:830, format 940), NSMDL record 3.4 (format 905) and RDUNIT records 3.5
+    (:3339-3352, formats 900 and 906/905)."""
+    lines = open(path).read().splitlines()
+    k = 0
+    while not lines[k].startswith("$"):
+        k += 1
+    k += 1
+    r = Rec(lines[k]); k += 1
+    r.skip(18); iaer = r.i(2); r.skip(29); iatm = r.i(1); r.skip(32); iscat = r.i(1)
+    r.skip(1); istrm = r.i(1); r.skip(2); iout = r.i(3); r.skip(3); imca = r.i(1); icld = r.i(1)
+    r.skip(3); idelm = r.i(1); icos = r.i(1)
+    assert iatm == 1 and iscat == 1 and istrm == 0 and icos == 0 and icld not in (4, 5)
+    k += 2  # solar record (9020) and surface record (9012), read by read_solar
+    # 900 format (7I5,I2,1X,I2,4F10.3,F10.3)
+    r = Rec(lines[k]); k += 1
+    atm = dict(model=r.i(5), itype=r.i(5), ibmax_b=r.i(5), nozero=r.i(5), noprnt=r.i(5), nmol=r.i(5),
+               ipunch=r.i(5), ifxtyp=r.i(2))
+    r.skip(1)
+    atm.update(munits=r.i(2), re=r.f(10, 3), hspace=r.f(10, 3), xvbar=r.f(10, 3), co2mx=r.f(10, 3),
+               ref_lat=r.f(10, 3))
+    # 932 format (5F10.4,I5,5X,F10.4)
+    r = Rec(lines[k]); k += 1
+    atm.update(h1=r.f(10, 4), h2=r.f(10, 4), angle=r.f(10, 4), range=r.f(10, 4), beta=r.f(10, 4), len=r.i(5))
+    r.skip(5)
+    atm["hobs"] = r.f(10, 4)
+    ibmax = abs(atm["ibmax_b"])
+    bnd = []
+    while len(bnd) < ibmax:
+        r = Rec(lines[k]); k += 1
+        bnd.extend(r.f(10, 3) for _ in range(min(8, ibmax - len(bnd))))
+    atm["bnd"] = bnd
+    assert atm["model"] == 0
+    # 905 format (I5,3A8)
+    r = Rec(lines[k]); k += 1
+    atm["immax_b"] = r.i(5)
+    nmol = atm["nmol"] or 7
+    levels = []
+    for _ in range(abs(atm["immax_b"])):
+        # 900 format (3E10.3,5X,2A1,1X,A1,1X,39A1)
+        r = Rec(lines[k]); k += 1
+        lv = dict(z=r.f(10, 3), p=r.f(10, 3), t=r.f(10, 3))
+        r.skip(5)
+        lv["jcharp"] = r.take(1); lv["jchart"] = r.take(1)
+        r.skip(1)
+        jlong = r.take(1)
+        r.skip(1)
+        lv["jchar"] = r.take(39)[:nmol]
+        wmol = []
+        while len(wmol) < nmol:
+            r = Rec(lines[k]); k += 1
+            width = 15 if jlong == "L" else 10
+            wmol.extend(r.f(width) for _ in range(min(8, nmol - len(wmol))))
+        lv["wmol"] = wmol
+        levels.append(lv)
+    atm["levels"] = levels
+    return dict(iaer=iaer, icld=icld, imca=imca, idelm=idelm, iout=iout), atm
 
 
 def read_cloud(path, nlay):
@@ -387,6 +449,20 @@ def main(ref):
         json.dump({"source": "RRTMG_SW run_examples_std_atm (iatm=1 runs): solar records and "
                              "top-of-atmosphere rows", "cases": sol}, f, indent=1)
     print("wrote", path, len(sol), "cases")
+    full = []
+    for name, inp, outp in SOLVAR_CASES:
+        c = read_solar(os.path.join(d, inp))
+        flags, atm = read_iatm1(os.path.join(d, inp))
+        c.update(flags)
+        c["name"] = name
+        c["atm"] = atm
+        c["expected"] = read_output(os.path.join(d, outp))
+        full.append(c)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "std_atm_iatm1_cases.json")
+    with open(path, "w") as f:
+        json.dump({"source": "RRTMG_SW run_examples_std_atm (iatm=1 runs): solar and profile-builder "
+                             "records, every printed block", "cases": full}, f)
+    print("wrote", path, len(full), "cases")
 
 
 if __name__ == "__main__":

@@ -1,0 +1,137 @@
+"""Pin the oracle on the five iatm = 1 example runs (solar variability).
+
+These runs (run_examples_std_atm/input_rrtm_MLS-clr-sza45-isolvar*) give a
+user profile of 48 levels and 48 layer boundaries in pressure; the column
+driver turns them into 47 layers with the profile builder rrtatm.f
+(rrtmg_sw.1col.f90:1728-1768).  The oracle's restatement of that builder
+(oracle/rrtatm.py) makes the layers from the records in
+tests/golden/std_atm_iatm1_cases.json, the column driver's solar settings
+come from orc_solar_factors, and the oracle's column mode must reproduce
+every printed block of the reference's outputs (broadband and the 14 bands,
+iout = 98) to print precision, as the iatm = 0 runs do
+(test_oracle_golden.py).  A planted error of 1e-6 in the layer amounts
+must break that agreement.
+
+Properties of the builder itself: boundaries given as altitudes or as the
+same levels' pressures give the same layers; an extra boundary inside a
+layer splits its molecular amounts (exponential in altitude) without
+changing their sum; and the inputs outside the restated part raise.
+"""
+import copy
+import json
+import os
+
+import numpy as np
+import pytest
+
+import pyoracle
+import rrtatm
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CASES = json.load(open(os.path.join(HERE, "golden", "std_atm_iatm1_cases.json")))["cases"]
+TOL = {"uflx": 5e-5, "difdflx": 5e-5, "dirdflx": 5e-5, "dflx": 5e-5, "fnet": 5e-7, "htr": 5e-6}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle():
+    pyoracle.init(1.004e3)
+
+
+def column_case(case, lay):
+    """The column driver's inputs for one iatm = 1 run (rrtmg_sw.1col.f90:1391-1436, 1646-1660)."""
+    iso, sv = case["isolvar"], case["solvar"]
+    kw = {}
+    if iso in (1, 2):
+        kw["indsolvar"] = sv[:2]
+    if iso == 1:
+        kw["solcycfrac"] = case["solcycfrac"]
+    if iso in (-1, 3):
+        kw["bndsolvar"] = sv
+    sf = pyoracle.solar_factors(iso, case["scon"], 1.0, case["juldat"], **kw)
+    nl = lay["nlay"]
+    z = [0.0] * nl
+    return dict(nlay=nl, icld=case["icld"], iaer=case["iaer"], idelm=case["idelm"], imca=case["imca"], idcor=0,
+                juldat=case["juldat"], inflag=0, iceflag=0, liqflag=0, isolvar=iso, zenith=case["zenith"],
+                decorr_con=0.0, lat=0.0, svar=tuple(sf["svar"]), svar_bnd=sf["svar_bnd"], adjflux=sf["adjflux"],
+                albedo=case["albedo"], pavel=lay["pavel"], tavel=lay["tavel"], pz=lay["pz"], tz=lay["tz"],
+                coldry=lay["coldry"], wkl=lay["wkl"], dz=z, cldfrac=z, ciwp=z, clwp=z, rei=z, rel=z)
+
+
+def misses(case, lay):
+    """Printed values the oracle misses by more than print precision."""
+    cc = column_case(case, lay)
+    bad = []
+    for b in case["expected"]:
+        out = pyoracle.column_mode(cc, b["istart"], b["iend"])
+        for k, tol in TOL.items():
+            err = np.abs(out[k] - np.array(b[k]))
+            bad += [(b["istart"], b["iend"], k, int(i), float(err[i])) for i in np.nonzero(err > tol + 1e-9)[0]]
+    return bad
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_golden_blocks(case):
+    assert case["icld"] == 0 and case["iaer"] == 0 and len(case["expected"]) == 15
+    lay = rrtatm.readprof_layers(case["atm"])
+    assert lay["nlay"] == 47
+    # the level pressures are the printed pressure column (to its 4 significant digits)
+    np.testing.assert_allclose(lay["pz"], case["expected"][0]["p"], rtol=2e-3)
+    bad = misses(case, lay)
+    assert not bad, bad[:10]
+
+
+def test_planted_layer_error_is_caught():
+    case = CASES[0]
+    lay = rrtatm.readprof_layers(case["atm"])
+    lay["wkl"] = [w * (1.0 + 1e-6) for w in lay["wkl"]]
+    assert len(misses(case, lay)) > 10
+
+
+def altitude_records(atm, extra=()):
+    """The same run with its boundaries given as the levels' altitudes (IBMAX > 0)."""
+    a = copy.deepcopy(atm)
+    z = sorted([lv["z"] for lv in a["levels"]] + list(extra))
+    a["ibmax_b"] = len(z)
+    a["bnd"] = z
+    a["h1"], a["h2"] = z[0], z[-1]
+    return a
+
+
+def test_pressure_and_altitude_boundaries_agree():
+    atm = CASES[0]["atm"]
+    p = rrtatm.readprof_layers(atm)
+    z = rrtatm.readprof_layers(altitude_records(atm))
+    for k in ("pavel", "tavel", "pz", "tz", "coldry", "wkl"):
+        assert p[k] == z[k], k
+
+
+def test_split_layer_keeps_molecular_amounts():
+    atm = CASES[0]["atm"]
+    whole = rrtatm.atmpth(altitude_records(atm))
+    # 25.0-27.5 km is layer 26; a boundary at 26.1 km splits it in two path layers
+    split = rrtatm.atmpth(altitude_records(atm, extra=(26.1,)))
+    assert split["nlayrs"] == whole["nlayrs"] + 1
+    l = [i for i in range(1, whole["nlayrs"] + 1) if whole["altz"][i - 1] == 25.0][0]
+    for k in range(7):
+        a, s = whole["amount"][k], split["amount"][k]
+        assert s[l] + s[l + 1] == pytest.approx(a[l], rel=1e-12)
+        assert s[:l] == a[:l]
+        assert s[l + 2:] == a[l + 1:]
+    assert split["pz"][l] < split["pz"][l - 1] and split["pz"][l] > split["pz"][l + 1]
+
+
+@pytest.mark.parametrize("change", ["model", "between_levels", "unit_code", "slant", "autolayer"])
+def test_unrestated_inputs_raise(change):
+    atm = copy.deepcopy(CASES[0]["atm"])
+    if change == "model":
+        atm["model"] = 2
+    elif change == "between_levels":
+        atm["bnd"][5] = 0.5 * (atm["bnd"][4] + atm["bnd"][5])
+    elif change == "unit_code":
+        atm["levels"][3]["jchar"] = "A1AAAAA"
+    elif change == "slant":
+        atm["range"] = 10.0
+    else:
+        atm["ibmax_b"] = 0
+    with pytest.raises(NotImplementedError):
+        rrtatm.atmpth(atm)

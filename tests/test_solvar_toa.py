@@ -1,8 +1,11 @@
 """Solar variability (isolvar 0-3) pinned at the top of the atmosphere.
 
 The five iatm = 1 example runs take their layers from the profile builder
-rrtatm.f, which is not restated, so their full tables cannot be reproduced.
-Their top-of-atmosphere rows can: the downward flux there is the band's
+rrtatm.f; the oracle reproduces their full tables from its restatement of
+that builder (test_rrtatm_golden.py).  The GCM interface takes layers, not
+profile records, so the GPU library is checked here where the tables do
+not depend on the layers, their top-of-atmosphere rows: the downward flux
+there is the band's
 solar source times cos(sza) (rrtmg_sw_spcvmc.f90:349-356, the taumol ssi
 terms, e.g. rrtmg_sw_taumol.f90:364-378), with the facular, sunspot and
 quiet-sun factors of the solar-variability options (rrtmg_sw_rad.f90:
