@@ -1,13 +1,13 @@
 """Solar variability (isolvar 0-3) pinned at the top of the atmosphere.
 
 The five iatm = 1 example runs take their layers from the profile builder
-rrtatm.f; the oracle reproduces their full tables from its restatement of
-that builder (test_rrtatm_golden.py).  The GCM interface takes layers, not
-profile records, so the GPU library is checked here where the tables do
-not depend on the layers, their top-of-atmosphere rows: the downward flux
-there is the band's
-solar source times cos(sza) (rrtmg_sw_spcvmc.f90:349-356, the taumol ssi
-terms, e.g. rrtmg_sw_taumol.f90:364-378), with the facular, sunspot and
+rrtatm.f; their full tables are reproduced from the oracle's restatement of
+that builder (test_rrtatm_golden.py, and test_gcm_golden.py through the GPU
+library).  This test isolates the solar-variability settings where the
+tables do not depend on the layers, the top-of-atmosphere rows: the
+downward flux there is the band's solar source times cos(sza)
+(rrtmg_sw_spcvmc.f90:349-356, the taumol ssi terms, e.g.
+rrtmg_sw_taumol.f90:364-378), with the facular, sunspot and
 quiet-sun factors of the solar-variability options (rrtmg_sw_rad.f90:
 1327-1496).  Bands 16, 20, 23, 25, 26, 27 and 29 take their source without
 interpolation in a gas ratio, so their rows do not depend on the layers at
