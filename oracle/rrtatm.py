@@ -339,7 +339,6 @@ def _alayer(a, path, j, sinai, cosai, cpath, sh, gamma):
     cosai1 = cosai
     if (1.0 - sinai) < EPSILN:
         raise NotImplementedError("near-horizontal rays are not restated")
-    y3 = 0.0
     x1 = -r1 * cosai1
     ratio1 = r1 / radrfd(h1, sh, gamma)
     dsdx1 = 1.0 / (1.0 - ratio1 * sinai1 ** 2)
