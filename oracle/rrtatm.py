@@ -10,12 +10,13 @@ back its layer pressures, temperatures, level values and molecular column
 amounts.  This module restates the part of that program an RRTM input can
 reach: a user-supplied profile (``MODEL = 0``), the vertical path that
 ``ATMPTH`` forces (``ANGLE = 0``, ``rrtatm.f:787``), layer boundaries given
-as altitudes or as pressures on the profile's levels, and the refracted-ray
-integration of ``RFPATH``/``ALAYER`` with the Curtis-Godson averages of
-``FPACK``.  Everything else raises ``NotImplementedError`` (the six built-in
-model atmospheres, automatic layering, boundaries between pressure levels,
-slant paths), never a silent approximation.  Arithmetic is IEEE double,
-as the reference is built (``-r8``); sums run in the reference's order.
+as altitudes or as pressures, the hydrostatic altitudes of ``CMPALT`` for
+profiles on pressure levels and boundary pressures between levels, and the
+refracted-ray integration of ``RFPATH``/``ALAYER`` with the Curtis-Godson
+averages of ``FPACK``.  Everything else raises ``NotImplementedError`` (the
+six built-in model atmospheres, automatic layering, slant paths), never a
+silent approximation.  Arithmetic is IEEE double, as the reference is built
+(``-r8``); sums run in the reference's order.
 """
 import math
 
@@ -133,10 +134,64 @@ def convrt(p, t, junit, wmol, nmol, co2mx):
     return den
 
 
-def nsmdl(levels, nmol, co2mx, immax_b):
-    """User-supplied profile (NSMDL rrtatm.f:3048-3168, RDUNIT :3223-3399)."""
-    if immax_b < 0:
-        raise NotImplementedError("profile on pressure levels: altitudes from CMPALT are not restated")
+def cmpalt(pm, tm, denw, ref_z, ref_lat, re_):
+    """Altitudes (km) of pressure levels by the hydrostatic equation with a
+    moist-air compressibility factor (CMPALT, rrtatm.f:7800-7918): pm in mb,
+    tm in K, denw the water vapour number densities, ref_z the first level's
+    altitude, gravity at ref_lat falling off as (RE / (RE + z))**2."""
+    ca0, ca1, ca2 = 1.58123E-6, -2.9331E-8, 1.1043E-10
+    cb0, cb1 = 5.707E-6, -2.051E-8
+    cc0, cc1 = 1.9898E-4, -2.376E-6
+    cd, ce = 1.83E-11, -0.0765E-8
+    xmass_h2o, xmass_dry = 0.018015, 0.0289654
+    rgas, btz = 8.31441, 1.380662E-23
+    n = len(pm)
+    g0 = 9.80612 - 0.02586 * math.cos(2.0 * PI * ref_lat / 180.0)
+    xmass_ratio = xmass_h2o / xmass_dry
+    h2o_mixrat, comp_factor = [0.0] * n, [0.0] * n
+    for j in range(n):
+        dt = tm[j] - 273.15
+        total_air = pm[j] * 1.0E-4 / (btz * tm[j])
+        dry_air = total_air - denw[j]
+        h2o_mixrat[j] = denw[j] / dry_air
+        chim = xmass_ratio * h2o_mixrat[j]
+        comp_factor[j] = (1. - (pm[j] * 100 / tm[j]) *
+                          (ca0 + ca1 * dt + ca2 * dt ** 2 + (cb0 + cb1 * dt) * chim + (cc0 + cc1 * dt) * chim ** 2) +
+                          (cd + ce * chim ** 2) * (pm[j] * 100. / tm[j]) ** 2)
+    ztemp = [0.0] * n
+    zmdl = [0.0] * n
+    ztemp[0] = ref_z * 1000.0
+    zmdl[0] = ref_z
+    for i in range(n - 1):
+        gave = g0 * (re_ / (re_ + ztemp[i] / 1000.0)) ** 2
+        y = math.log(pm[i + 1] / pm[i])
+        if y != 0.0:
+            chi0 = h2o_mixrat[i]
+            dchi = (h2o_mixrat[i + 1] - h2o_mixrat[i]) / y
+            t0 = tm[i]
+            dt = (tm[i + 1] - tm[i]) / y
+            c1 = t0 + t0 * chi0
+            c2 = t0 * dchi + dt * chi0 + dt
+            c3 = dt * dchi
+            b = 1 + xmass_ratio * chi0
+            a = xmass_ratio * dchi
+            alpha = a / b
+            if abs(alpha * y) >= 0.01:
+                raise ValueError("LAYER TOO THICK")
+            xint_tot = c1 * y + 0.5 * (c2 - c1 * alpha) * y ** 2 + 0.3333 * (c3 - c2 * alpha + c1 * alpha ** 2) * y ** 3
+            xint_tot = -xint_tot * rgas / (xmass_dry * gave * b)
+            ztemp[i + 1] = ztemp[i] + xint_tot * comp_factor[i]
+            zmdl[i + 1] = ztemp[i + 1] / 1000.
+        else:
+            ztemp[i + 1] = zmdl[i] * 1000.0
+            zmdl[i + 1] = zmdl[i]
+    return zmdl
+
+
+def nsmdl(levels, nmol, co2mx, immax_b, ref_lat, re_):
+    """User-supplied profile (NSMDL rrtatm.f:3048-3168, RDUNIT :3223-3399);
+    a profile on pressure levels (IMMAX < 0) takes its altitudes from CMPALT,
+    starting at the first level's altitude."""
     zmdl, pm, tm, denm = [], [], [], []
     for lv in levels:
         junitp, junitt = jou(lv["jcharp"]), jou(lv["jchart"])
@@ -149,6 +204,8 @@ def nsmdl(levels, nmol, co2mx, immax_b):
         pm.append(p)
         tm.append(t)
         denm.append(convrt(p, t, junit, list(lv["wmol"][:nmol]), nmol, co2mx))
+    if immax_b < 0:
+        zmdl = cmpalt(pm, tm, [d[0] for d in denm], zmdl[0], ref_lat, re_)
     for im in range(1, len(zmdl)):
         if zmdl[im] <= zmdl[im - 1]:
             raise ValueError("INPUT ALTITUDES NOT IN ASCENDING ORDER")
@@ -214,10 +271,12 @@ class _Atm:
         return sclhtd(self.zmdl[i1], self.zmdl[i2], self.rfndxm[i1], self.rfndxm[i2])
 
 
-def _pressure_to_altitude(a, pval):
-    """Altitude of a boundary given as a pressure on a profile level (ATMPTH
-    loop 160 and its H1/H2 twins, rrtatm.f:872-1080).  A pressure between
-    levels needs the hydrostatic CMPALT, which is not restated."""
+def _pressure_to_altitude(a, pval, ref_lat):
+    """Altitude and temperature of a boundary given as a pressure (ATMPTH
+    loop 160 and its H1/H2 twins, rrtatm.f:872-1080).  Between two profile
+    levels the altitude blends the log-pressure interpolation with a CMPALT
+    step from the level below, weighted by the cube of the log-pressure
+    fraction."""
     lip = a.immax
     for cand in range(2, a.immax + 1):
         if pval > a.pm[cand]:
@@ -227,7 +286,19 @@ def _pressure_to_altitude(a, pval):
         return a.zmdl[lip - 1], a.tm[lip - 1]
     if pval == a.pm[lip]:
         return a.zmdl[lip], a.tm[lip]
-    raise NotImplementedError("boundary pressure %g between profile levels (CMPALT) is not restated" % pval)
+    lpm = math.log(a.pm[lip] / a.pm[lip - 1])
+    lp = math.log(pval / a.pm[lip - 1])
+    hip = (a.zmdl[lip] - a.zmdl[lip - 1]) / lpm
+    zint = a.zmdl[lip - 1] + hip * lp
+    tip = (a.tm[lip] - a.tm[lip - 1]) / lpm
+    t2 = a.tm[lip - 1] + tip * lp
+    wvip = (a.denm[lip][0] - a.denm[lip - 1][0]) / lpm
+    wv2 = a.denm[lip - 1][0] + wvip * lp
+    z2 = cmpalt([a.pm[lip - 1], pval], [a.tm[lip - 1], t2], [a.denm[lip - 1][0], wv2], a.zmdl[lip - 1], ref_lat,
+                a.re)[1]
+    ratp = lp / lpm
+    w = ratp ** 3
+    return w * zint + (1 - w) * z2, t2
 
 
 def _amerge(a, h1, h2, hmin, len_, zbnd):
@@ -474,7 +545,8 @@ def atmpth(atm):
     if ibmax_b < 0 and any(bnd[i] >= bnd[i - 1] for i in range(1, ibmax)):
         raise ValueError("PBND not descending")
     # MDLATM (rrtatm.f:2919-3047) with the user profile of NSMDL
-    zmdl, pm, tm, denm = nsmdl(atm["levels"], nmol, atm["co2mx"], atm["immax_b"])
+    ref_lat = atm["ref_lat"] if atm["ref_lat"] != 0 else 45.
+    zmdl, pm, tm, denm = nsmdl(atm["levels"], nmol, atm["co2mx"], atm["immax_b"], ref_lat, re_)
     ispace = 1
     for i, z in enumerate(zmdl):
         if hspace + 0.001 > z:
@@ -484,9 +556,11 @@ def atmpth(atm):
     zmax = a.zmdl[a.immax]
     # layer boundaries and path ends given as pressures (:866-1080)
     if ibmax_b < 0:
-        zbnd = [None] + [_pressure_to_altitude(a, p)[0] for p in bnd]
-        h1 = _pressure_to_altitude(a, h1)[0]
-        h2 = _pressure_to_altitude(a, h2)[0]
+        zbnd = [None] + [_pressure_to_altitude(a, p, ref_lat)[0] for p in bnd]
+        h1 = _pressure_to_altitude(a, h1, ref_lat)[0]
+        h2 = _pressure_to_altitude(a, h2, ref_lat)[0]
+        if h1 < 0.0 or h2 < 0.0:
+            raise ValueError("COMPUTED ALTITUDE VALUE OF H1/H2 IS NEGATIVE")
     else:
         zbnd = [None] + list(bnd)
     if zbnd[1] < a.zmdl[1]:

@@ -14,8 +14,11 @@ must break that agreement.
 
 Properties of the builder itself: boundaries given as altitudes or as the
 same levels' pressures give the same layers; an extra boundary inside a
-layer splits its molecular amounts (exponential in altitude) without
-changing their sum; and the inputs outside the restated part raise.
+layer, given as an altitude or as a pressure between levels, splits its
+molecular amounts (exponential in altitude) without changing their sum;
+the hydrostatic altitudes (CMPALT) of the run's pressures stay near its
+given altitudes, and a profile on pressure levels equals the same profile
+on those altitudes; the inputs outside the restated part raise.
 """
 import copy
 import json
@@ -120,13 +123,51 @@ def test_split_layer_keeps_molecular_amounts():
     assert split["pz"][l] < split["pz"][l - 1] and split["pz"][l] > split["pz"][l + 1]
 
 
-@pytest.mark.parametrize("change", ["model", "between_levels", "unit_code", "slant", "autolayer"])
+def test_cmpalt_heights_of_the_example_profile():
+    # the run's profile gives both altitudes and pressures: the hydrostatic
+    # altitudes of its pressures stay within 0.5 % of the given ones
+    atm = CASES[0]["atm"]
+    z, p, t, den = rrtatm.nsmdl(atm["levels"], 7, 0.0, 48, 45.0, 6371.23)
+    zc = rrtatm.cmpalt(p, t, [d[0] for d in den], z[0], 45.0, 6371.23)
+    assert zc[0] == z[0]
+    assert all(abs(a - b) <= 0.005 * b + 0.01 for a, b in zip(zc, z))
+    assert all(zc[i] > zc[i - 1] for i in range(1, len(zc)))
+
+
+def test_pressure_level_profile_takes_cmpalt_heights():
+    atm = CASES[0]["atm"]
+    onp = copy.deepcopy(atm)
+    onp["immax_b"] = -atm["immax_b"]
+    z, p, t, den = rrtatm.nsmdl(atm["levels"], 7, 0.0, 48, 45.0, 6371.23)
+    zc = rrtatm.cmpalt(p, t, [d[0] for d in den], z[0], 45.0, 6371.23)
+    onz = copy.deepcopy(atm)
+    for lv, h in zip(onz["levels"], zc):
+        lv["z"] = h
+    a, b = rrtatm.readprof_layers(onp), rrtatm.readprof_layers(onz)
+    for k in ("pavel", "tavel", "pz", "tz", "coldry", "wkl", "altz"):
+        assert a[k] == b[k], k
+
+
+def test_boundary_between_pressure_levels():
+    atm = CASES[0]["atm"]
+    split = copy.deepcopy(atm)
+    i = split["bnd"].index(19.07)
+    split["bnd"].insert(i, 23.0)
+    split["ibmax_b"] = -(abs(atm["ibmax_b"]) + 1)
+    whole, part = rrtatm.atmpth(atm), rrtatm.atmpth(split)
+    assert part["nlayrs"] == whole["nlayrs"] + 1
+    l = [k for k in range(1, whole["nlayrs"] + 1) if whole["pz"][k - 1] == 27.7][0]
+    assert part["pz"][l] == pytest.approx(23.0, rel=5e-3)
+    assert part["pz"][l - 1] == 27.7 and part["pz"][l + 1] == 19.07
+    for k in range(7):
+        assert part["amount"][k][l] + part["amount"][k][l + 1] == pytest.approx(whole["amount"][k][l], rel=1e-12)
+
+
+@pytest.mark.parametrize("change", ["model", "unit_code", "slant", "autolayer"])
 def test_unrestated_inputs_raise(change):
     atm = copy.deepcopy(CASES[0]["atm"])
     if change == "model":
         atm["model"] = 2
-    elif change == "between_levels":
-        atm["bnd"][5] = 0.5 * (atm["bnd"][4] + atm["bnd"][5])
     elif change == "unit_code":
         atm["levels"][3]["jchar"] = "A1AAAAA"
     elif change == "slant":
