@@ -6,8 +6,7 @@ example runs.  Here the same runs go through the GCM call sequence,
 get_alpha -> mcica_subcol_sw -> rrtmg_sw (rrtmg_sw_rad.f90:99-111), or the
 non-McICA rrtmg_sw (rrtmg_sw_rad.nomcica.f90:97-109): the oracle's, and the
 GPU library's FP64 form (print precision) and FP32 form (0.05 W m-2,
-0.01 K/day).  15 of the 16 runs map onto those arguments; MLS-clr-sza65 has
-a different albedo in each band and stays with the column mode.
+0.01 K/day), all 16 runs.
 
 A column-driver case becomes GCM arguments as follows.
   - The driver takes column amounts (coldry, wkl in molecules cm-2), while
@@ -20,7 +19,10 @@ A column-driver case becomes GCM arguments as follows.
     the driver's own level pressures, htr(i-1) = (fnet(i) - fnet(i-1)) *
     heatfac / (pz(i-1) - pz(i)) (rrtmg_sw.1col.f90:811-821, 1799).
   - Albedo 1 - semiss: bands 16-24 and 29 take aldir/aldif, 25-28
-    asdir/asdif (rrtmg_sw_rad.f90:673-683).
+    asdir/asdif (rrtmg_sw_rad.f90:673-683).  MLS-clr-sza65 gives a
+    different albedo in each band: it runs once per band with that band's
+    albedo everywhere and keeps that band's fluxes (the bands do not
+    interact in the solve), its broadband fluxes summed over the bands.
   - McICA runs average 200 samples, sample ims drawn with the Mersenne
     Twister seeded (ims + 1) * 112 (mcica_subcol_gen_sw.1col.f90:255,
     rrtmg_sw.1col.f90:524); the samples are the columns of one call.  With
@@ -50,11 +52,7 @@ UV = slice(9, 13)       # bands 25-28
 
 def column_cases():
     """Column-driver cases (layers, solar settings, expected blocks) that map onto the GCM call."""
-    out = []
-    for c in STD:
-        if c["name"] == "MLS-clr-sza65":
-            continue
-        out.append(dict(c))
+    out = [dict(c) for c in STD]
     for c in IATM1:
         d = dict(c)
         d["solar_record"] = True
@@ -84,8 +82,16 @@ def solar_args(case):
     return kw
 
 
-def gcm_arguments(case, ncol):
-    """rrtmg_sw arguments (Fortran-ordered arrays) for ncol copies of one column-driver case."""
+def maps_albedo(case):
+    """Whether the case's band albedos fit the GCM's near-IR / UV pair."""
+    alb = np.array(case["albedo"])
+    nir = np.concatenate([alb[:9], alb[13:]])
+    return bool(np.all(nir == nir[0]) and np.all(alb[UV] == alb[UV][0]))
+
+
+def gcm_arguments(case, ncol, albedo=None):
+    """rrtmg_sw arguments (Fortran-ordered arrays) for ncol copies of one
+    column-driver case; ``albedo`` replaces all four surface albedos."""
     nl = case["nlay"]
     pz = np.array(case["pz"])
     coldry = np.array(case["coldry"])
@@ -99,8 +105,11 @@ def gcm_arguments(case, ncol):
     for l in range(nl - 1, -1, -1):
         plev[l] = plev[l + 1] + dp[l]
     alb = np.array(case["albedo"])
-    nir = np.concatenate([alb[:9], alb[13:]])
-    assert np.all(nir == nir[0]) and np.all(alb[UV] == alb[UV][0]), "per-band albedo does not map"
+    if albedo is None:
+        assert maps_albedo(case), "per-band albedo does not map"
+        uv, nir = alb[UV][0], alb[0]
+    else:
+        uv = nir = albedo
 
     def cl(x):
         return np.tile(np.asarray(x, dtype=np.float64), (ncol, 1))
@@ -112,7 +121,7 @@ def gcm_arguments(case, ncol):
     kw = dict(ncol=ncol, nlay=nl, icld=case["icld"], iaer=case["iaer"], play=cl(case["pavel"]), plev=cl(plev),
               tlay=cl(case["tavel"]), tlev=cl(tz), tsfc=col(tz[0]), h2ovmr=cl(vmr[:, 0]), o3vmr=cl(vmr[:, 2]),
               co2vmr=cl(vmr[:, 1]), ch4vmr=cl(vmr[:, 5]), n2ovmr=cl(vmr[:, 3]), o2vmr=cl(vmr[:, 6]),
-              asdir=col(alb[UV][0]), asdif=col(alb[UV][0]), aldir=col(nir[0]), aldif=col(nir[0]),
+              asdir=col(uv), asdif=col(uv), aldir=col(nir), aldif=col(nir),
               coszen=col(case["zenith"]), inflgsw=case["inflag"], iceflgsw=case["iceflag"],
               liqflgsw=case["liqflag"], idelm=case["idelm"])
     kw.update(solar_args(case))
@@ -185,6 +194,27 @@ def blocks(case, res, heatfac, plev=None):
     return got
 
 
+def run_case(case, run):
+    """``run(case, albedo) -> (outputs, plev)`` once, or once per band when
+    the albedos do not fit the GCM's pair: each band's fluxes from the run
+    with its albedo, broadband fluxes summed over bands, no solver heating
+    rate."""
+    if maps_albedo(case):
+        return run(case, None)
+    res = None
+    for ib, a in enumerate(case["albedo"]):
+        r, plev = run(case, a)
+        if res is None:
+            res = {k: np.array(r[k]) for k in ("bndfu", "bndfd", "bndfddir")}
+            res["swhr"] = np.full(np.shape(r["swhr"]), np.nan)
+        for k in ("bndfu", "bndfd", "bndfddir"):
+            res[k][:, :, ib] = r[k][:, :, ib]
+    res["swuflx"] = res["bndfu"].sum(axis=2)
+    res["swdflx"] = res["bndfd"].sum(axis=2)
+    res["dirdflux"] = res["bndfddir"].sum(axis=2)
+    return res, plev
+
+
 def misses(case, got, tol):
     bad = []
     for b in case["expected"]:
@@ -217,9 +247,9 @@ def fortran(x):
     return np.asarray(x, dtype=np.float64).ravel(order="F")
 
 
-def oracle_run(case):
+def oracle_run(case, albedo=None):
     ncol = NMCA if case["imca"] == 1 and case["icld"] >= 1 else 1
-    kw = gcm_arguments(case, ncol)
+    kw = gcm_arguments(case, ncol, albedo)
     nl = case["nlay"]
     inp = {k: fortran(kw[k]) for k in pyoracle.GCM_INPUTS + pyoracle.AER_INPUTS}
     solar = {k: kw[k] for k in ("adjes", "dyofyr", "scon", "isolvar", "bndsolvar", "indsolvar", "solcycfrac")
@@ -258,7 +288,7 @@ def heatfac():
 
 @pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
 def test_oracle_gcm_path(case, heatfac):
-    res, plev = oracle_run(case)
+    res, plev = run_case(case, oracle_run)
     bad = misses(case, blocks(case, res, heatfac), TOL)
     assert not bad, bad[:10]
     # the solver's own heating rate, rescaled to the driver's pressure thicknesses
@@ -277,9 +307,9 @@ def gpu():
     gi.set_form(gi.FORM_FP64)
 
 
-def gpu_run(gi, case):
+def gpu_run(gi, case, albedo=None):
     ncol = NMCA if case["imca"] == 1 and case["icld"] >= 1 else 1
-    kw = gcm_arguments(case, ncol)
+    kw = gcm_arguments(case, ncol, albedo)
     nl = case["nlay"]
     clouds = None
     nomcica = case["icld"] >= 1 and case["imca"] == 0
@@ -315,17 +345,17 @@ def gpu_run(gi, case):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("form", ["fp64", "fp32"])
-def test_gpu_gcm_path(gpu, form, heatfac):
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_gpu_gcm_path(gpu, form, case, heatfac):
     gpu.set_form(gpu.FORM_FP64 if form == "fp64" else gpu.FORM_FP32)
     try:
-        for case in CASES:
-            res, plev = gpu_run(gpu, case)
-            if form == "fp64":
-                bad = misses(case, blocks(case, res, heatfac), TOL)
-            else:
-                # FP32 fluxes are rounded to ~1e-7 of their size, which a difference over a
-                # 0.001 hPa layer turns into 0.1 K/day: the solver's own heating rate is checked
-                bad = misses(case, blocks(case, res, heatfac, plev), TOL32)
-            assert not bad, (case["name"], bad[:10])
+        res, plev = run_case(case, lambda c, a: gpu_run(gpu, c, a))
     finally:
         gpu.set_form(gpu.FORM_FP64)
+    if form == "fp64":
+        bad = misses(case, blocks(case, res, heatfac), TOL)
+    else:
+        # FP32 fluxes are rounded to ~1e-7 of their size, which a difference over a
+        # 0.001 hPa layer turns into 0.1 K/day: the solver's own heating rate is checked
+        bad = misses(case, blocks(case, res, heatfac, plev), TOL32)
+    assert not bad, bad[:10]
