@@ -8,14 +8,17 @@ With ``iatm = 1`` the column driver (``rrtmg_sw.1col.f90:1728-1768``) calls
 ``RRTATM`` (``rrtatm.f:5-205``), the LBLRTM atmosphere program, and reads
 back its layer pressures, temperatures, level values and molecular column
 amounts.  This module restates the part of that program an RRTM input can
-reach: a user-supplied profile (``MODEL = 0``), the vertical path that
-``ATMPTH`` forces (``ANGLE = 0``, ``rrtatm.f:787``), layer boundaries given
-as altitudes or as pressures, the hydrostatic altitudes of ``CMPALT`` for
-profiles on pressure levels and boundary pressures between levels, and the
-refracted-ray integration of ``RFPATH``/``ALAYER`` with the Curtis-Godson
-averages of ``FPACK``.  Everything else raises ``NotImplementedError`` (the
-six built-in model atmospheres, automatic layering, slant paths), never a
-silent approximation.  Arithmetic is IEEE double, as the reference is built
+reach: a user-supplied profile (``MODEL = 0``, unit codes 1-6 filled from
+the built-in atmospheres) or one of the six built-in model atmospheres
+(``MODEL`` 1-6, data extracted by oracle/extract_afgl.py); the vertical path
+that ``ATMPTH`` forces (``ANGLE = 0``, ``rrtatm.f:787``); layer boundaries
+given as altitudes or as pressures, with the hydrostatic altitudes of
+``CMPALT`` for profiles on pressure levels and boundary pressures between
+levels; and the refracted-ray integration of ``RFPATH``/``ALAYER`` with the
+Curtis-Godson averages of ``FPACK``.  Everything else raises ``NotImplementedError``
+(automatic layering, slant paths, unit codes 1-6 on pressure levels, trace
+species beyond the seventh from the model atmospheres), never a silent
+approximation.  Arithmetic is IEEE double, as the reference is built
 (``-r8``); sums run in the reference's order.
 """
 import math
@@ -134,6 +137,97 @@ def convrt(p, t, junit, wmol, nmol, co2mx):
     return den
 
 
+_AFGL = None
+
+
+def afgl():
+    """The six built-in model atmospheres (rrtatm.f BLOCK DATA MLATMB,
+    extracted by oracle/extract_afgl.py): alt (50), p and t (6 x 50), amol
+    (6 x 8 x 50: ppmv of H2O, CO2, O3, N2O, CO, CH4, O2, then air cm-3)."""
+    global _AFGL
+    if _AFGL is None:
+        import json
+        import os
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "afgl_atmospheres.json")) as f:
+            _AFGL = json.load(f)
+    return _AFGL
+
+
+def mdlatm_builtin(mdl, nmol, co2mx):
+    """Levels of built-in model atmosphere ``mdl`` (MDLATM, rrtatm.f:2919-3047):
+    water relative to the tabulated air density, the other species relative
+    to dry air, CO2 scaled to co2mx ppmv when that is given."""
+    if nmol > 7:
+        raise NotImplementedError("trace species 8+ of the model atmospheres (/TRAC/) are not restated")
+    d = afgl()
+    m = mdl - 1
+    co2rat = 1.
+    if co2mx > 0.:
+        co2rat = co2mx / 330.
+    zmdl, pm, tm, denm = [], [], [], []
+    for i in range(50):
+        amol = [d["amol"][m][k][i] for k in range(8)]
+        den1 = amol[0] * amol[7] * 1.0E-6
+        dryair = amol[7] - den1
+        den = [amol[k] * 1.0E-6 * dryair for k in range(nmol)]
+        if nmol > 1:
+            den[1] = den[1] * co2rat
+        zmdl.append(d["alt"][i])
+        pm.append(d["p"][m][i])
+        tm.append(d["t"][m][i])
+        denm.append(den)
+    return zmdl, pm, tm, denm
+
+
+def defalt(z, p, t, junitp, junitt, junit, wmol, nmol):
+    """Values taken from a built-in model atmosphere for unit codes 1-6
+    (DEFALT, rrtatm.f:3487-3680): 4-point Lagrange interpolation in altitude
+    of ln p, t and the mixing ratios (ppmv), which then carry unit code 10.
+    Returns (p, t, junit, wmol)."""
+    d = afgl()
+    alt = [None] + d["alt"]
+    im50 = 50
+    i2 = im50
+    for im in range(2, im50 + 1):
+        if alt[im] >= z:
+            i2 = im
+            break
+    i1, i0, i3 = i2 - 1, i2 - 2, i2 + 1
+    if i0 < 1:
+        i0, i1, i2, i3 = i1, i2, i3, i3 + 1
+    elif i3 > im50:
+        if z > alt[im50]:
+            raise ValueError("DEFAULT Z")
+        i3, i2, i1 = i2, i1, i0
+        i0 = i1 - 1
+    z0, z1, z2, z3 = alt[i0], alt[i1], alt[i2], alt[i3]
+    den1 = (z0 - z1) * (z0 - z2) * (z0 - z3)
+    den2 = (z1 - z2) * (z1 - z3) * (z1 - z0)
+    den3 = (z2 - z3) * (z2 - z0) * (z2 - z1)
+    den4 = (z3 - z0) * (z3 - z1) * (z3 - z2)
+    a1 = ((z - z1) * (z - z2) * (z - z3)) / den1
+    a2 = ((z - z2) * (z - z3) * (z - z0)) / den2
+    a3 = ((z - z3) * (z - z0) * (z - z1)) / den3
+    a4 = ((z - z0) * (z - z1) * (z - z2)) / den4
+
+    def val(x):
+        return a1 * x[i0 - 1] + a2 * x[i1 - 1] + a3 * x[i2 - 1] + a4 * x[i3 - 1]
+
+    if junitp <= 6:
+        p = math.exp(val([math.log(v) for v in d["p"][junitp - 1]]))
+    if junitt <= 6:
+        t = val(d["t"][junitt - 1])
+    junit, wmol = list(junit), list(wmol)
+    for k in range(nmol):
+        if junit[k] > 6:
+            continue
+        if k >= 7:
+            raise NotImplementedError("trace species 8+ of the model atmospheres (/TRAC/) are not restated")
+        wmol[k] = val(d["amol"][junit[k] - 1][k])
+        junit[k] = 10
+    return p, t, junit, wmol
+
+
 def cmpalt(pm, tm, denw, ref_z, ref_lat, re_):
     """Altitudes (km) of pressure levels by the hydrostatic equation with a
     moist-air compressibility factor (CMPALT, rrtatm.f:7800-7918): pm in mb,
@@ -196,14 +290,17 @@ def nsmdl(levels, nmol, co2mx, immax_b, ref_lat, re_):
     for lv in levels:
         junitp, junitt = jou(lv["jcharp"]), jou(lv["jchart"])
         junit = [jou(c) for c in lv["jchar"][:nmol].ljust(nmol)]
-        if min([junitp, junitt] + junit) <= 6:
-            raise NotImplementedError("unit codes 1-6 take values from the built-in model atmospheres (DEFALT)")
         p = check(lv["p"], junitp, 1)
         t = check(lv["t"], junitt, 2)
+        wmol = list(lv["wmol"][:nmol])
+        if min([junitp, junitt] + junit) <= 6:
+            if immax_b < 0:
+                raise NotImplementedError("unit codes 1-6 on pressure levels (DEFALT_P) are not restated")
+            p, t, junit, wmol = defalt(lv["z"], p, t, junitp, junitt, junit, wmol, nmol)
         zmdl.append(lv["z"])
         pm.append(p)
         tm.append(t)
-        denm.append(convrt(p, t, junit, list(lv["wmol"][:nmol]), nmol, co2mx))
+        denm.append(convrt(p, t, junit, wmol, nmol, co2mx))
     if immax_b < 0:
         zmdl = cmpalt(pm, tm, [d[0] for d in denm], zmdl[0], ref_lat, re_)
     for im in range(1, len(zmdl)):
@@ -527,11 +624,11 @@ def atmpth(atm):
     nmol = atm["nmol"] or KMXNOM
     nozero = 1
     xvbar = 1.0
-    if model != 0:
-        raise NotImplementedError("built-in model atmospheres (MODEL 1-6, BLOCK DATA MLATMB) are not restated")
+    if not 0 <= model <= 6:
+        raise ValueError("CARD 3.1: MODEL out of range")
     re_ = atm["re"]
     if re_ == 0.0:
-        re_ = 6371.23
+        re_ = {1: 6378.39, 4: 6356.91, 5: 6356.91}.get(model, 6371.23)
     hspace = atm["hspace"] if atm["hspace"] != 0. else 100.
     # record 3.2 (:786-795): RRTM sets ANGLE = 0
     h1, h2 = atm["h1"], atm["h2"]
@@ -546,7 +643,10 @@ def atmpth(atm):
         raise ValueError("PBND not descending")
     # MDLATM (rrtatm.f:2919-3047) with the user profile of NSMDL
     ref_lat = atm["ref_lat"] if atm["ref_lat"] != 0 else 45.
-    zmdl, pm, tm, denm = nsmdl(atm["levels"], nmol, atm["co2mx"], atm["immax_b"], ref_lat, re_)
+    if model == 0:
+        zmdl, pm, tm, denm = nsmdl(atm["levels"], nmol, atm["co2mx"], atm["immax_b"], ref_lat, re_)
+    else:
+        zmdl, pm, tm, denm = mdlatm_builtin(model, nmol, atm["co2mx"])
     ispace = 1
     for i, z in enumerate(zmdl):
         if hspace + 0.001 > z:

@@ -18,7 +18,10 @@ layer, given as an altitude or as a pressure between levels, splits its
 molecular amounts (exponential in altitude) without changing their sum;
 the hydrostatic altitudes (CMPALT) of the run's pressures stay near its
 given altitudes, and a profile on pressure levels equals the same profile
-on those altitudes; the inputs outside the restated part raise.
+on those altitudes; the run's profile is the built-in mid-latitude summer
+atmosphere, so unit codes taking its values give the same layers, and the
+built-in atmosphere itself (MODEL = 2) the same pressures and temperatures;
+the inputs outside the restated part raise.
 """
 import copy
 import json
@@ -163,13 +166,64 @@ def test_boundary_between_pressure_levels():
         assert part["amount"][k][l] + part["amount"][k][l + 1] == pytest.approx(whole["amount"][k][l], rel=1e-12)
 
 
-@pytest.mark.parametrize("change", ["model", "unit_code", "slant", "autolayer"])
+def test_unit_codes_take_the_model_atmosphere():
+    # the run's profile is the mid-latitude summer atmosphere (model 2) at its
+    # 48 lowest levels: unit code 2 for the temperatures and all seven species
+    # (DEFALT at the model's own altitudes) must give the same layers
+    atm = CASES[0]["atm"]
+    coded = copy.deepcopy(atm)
+    for lv in coded["levels"]:
+        lv["jchart"] = "2"
+        lv["jchar"] = "2222222"
+        lv["t"], lv["wmol"] = 0.0, [0.0] * 7
+    a, b = rrtatm.readprof_layers(atm), rrtatm.readprof_layers(coded)
+    for k in a:
+        assert a[k] == b[k], k
+
+
+def test_model_atmosphere_interpolation_between_levels():
+    # 4-point Lagrange interpolation in altitude: a cubic through the four
+    # neighbouring levels of the model's table
+    d = rrtatm.afgl()
+    z = 2.6
+    p, t, junit, wmol = rrtatm.defalt(z, 0.0, 0.0, 2, 2, [2] * 7, [0.0] * 7, 7)
+    i = [1, 2, 3, 4]
+    for got, tab, log in [(t, d["t"][1], False), (p, d["p"][1], True)] + \
+            [(wmol[k], d["amol"][1][k], False) for k in range(7)]:
+        y = np.log([tab[j] for j in i]) if log else [tab[j] for j in i]
+        ref = np.polyval(np.polyfit([d["alt"][j] for j in i], y, 3), z)
+        assert (np.log(got) if log else got) == pytest.approx(ref, rel=1e-9, abs=1e-12)
+    assert junit == [10] * 7
+
+
+def test_builtin_model_atmosphere():
+    # MODEL = 2 takes the same levels from the built-in table but densities
+    # from its tabulated air density (MDLATM) rather than the ideal gas
+    # (CONVRT): pressures and temperatures agree exactly, amounts to 1e-3,
+    # and the printed tables to a few hundredths
+    case = CASES[0]
+    atm = copy.deepcopy(case["atm"])
+    atm["model"] = 2
+    a, b = rrtatm.readprof_layers(case["atm"]), rrtatm.readprof_layers(atm)
+    for k in ("pavel", "tavel", "pz", "tz"):
+        assert a[k] == b[k], k
+    np.testing.assert_allclose(b["wkl"], a["wkl"], rtol=1e-3)
+    cc = column_case(case, b)
+    for blk in case["expected"]:
+        out = pyoracle.column_mode(cc, blk["istart"], blk["iend"])
+        for k in ("uflx", "dflx", "dirdflx", "difdflx", "fnet", "htr"):
+            assert np.max(np.abs(out[k] - np.array(blk[k]))) <= 0.05, (blk["istart"], k)
+
+
+@pytest.mark.parametrize("change", ["trace_species", "codes_on_pressure_levels", "slant", "autolayer"])
 def test_unrestated_inputs_raise(change):
     atm = copy.deepcopy(CASES[0]["atm"])
-    if change == "model":
+    if change == "trace_species":
         atm["model"] = 2
-    elif change == "unit_code":
-        atm["levels"][3]["jchar"] = "A1AAAAA"
+        atm["nmol"] = 8
+    elif change == "codes_on_pressure_levels":
+        atm["immax_b"] = -atm["immax_b"]
+        atm["levels"][3]["jchar"] = "A2AAAAA"
     elif change == "slant":
         atm["range"] = 10.0
     else:
