@@ -16,9 +16,8 @@ given as altitudes or as pressures, with the hydrostatic altitudes of
 ``CMPALT`` for profiles on pressure levels and boundary pressures between
 levels; and the refracted-ray integration of ``RFPATH``/``ALAYER`` with the
 Curtis-Godson averages of ``FPACK``.  Everything else raises ``NotImplementedError``
-(automatic layering, slant paths, unit codes 1-6 on pressure levels, trace
-species beyond the seventh from the model atmospheres), never a silent
-approximation.  Arithmetic is IEEE double, as the reference is built
+(automatic layering, slant paths, trace species beyond the seventh from the
+model atmospheres), never a silent approximation.  Arithmetic is IEEE double, as the reference is built
 (``-r8``); sums run in the reference's order.
 """
 import math
@@ -228,6 +227,55 @@ def defalt(z, p, t, junitp, junitt, junit, wmol, nmol):
     return p, t, junit, wmol
 
 
+def defalt_p(p, t, junitt, junit, wmol, nmol):
+    """Unit codes 1-6 on a profile given on pressure levels (DEFALT_P,
+    rrtatm.f:3681-3874): for each model, 4-point Lagrange interpolation in
+    ln p on that model's own pressures of the temperature and mixing ratios
+    (ppmv) that name it.  The pressure itself is kept.  Returns (t, junit, wmol)."""
+    d = afgl()
+    xlog_p = math.log(p)
+    junit, wmol = list(junit), list(wmol)
+    for j in range(1, 7):
+        pm = [None] + d["p"][j - 1]
+        lvl_50 = 50
+        i2 = lvl_50
+        for lvl in range(2, lvl_50 + 1):
+            if p >= pm[lvl]:
+                i2 = lvl
+                break
+        i1, i0, i3 = i2 - 1, i2 - 2, i2 + 1
+        if i0 < 1:
+            i0, i1, i2, i3 = i1, i2, i3, i3 + 1
+        elif i3 > lvl_50:
+            if p <= pm[lvl_50]:
+                raise ValueError("DEFAULT P")
+            i3, i2, i1 = i2, i1, i0
+            i0 = i1 - 1
+        p0, p1, p2, p3 = (math.log(pm[i]) for i in (i0, i1, i2, i3))
+        den1 = (p0 - p1) * (p0 - p2) * (p0 - p3)
+        den2 = (p1 - p2) * (p1 - p3) * (p1 - p0)
+        den3 = (p2 - p3) * (p2 - p0) * (p2 - p1)
+        den4 = (p3 - p0) * (p3 - p1) * (p3 - p2)
+        a1 = ((xlog_p - p1) * (xlog_p - p2) * (xlog_p - p3)) / den1
+        a2 = ((xlog_p - p2) * (xlog_p - p3) * (xlog_p - p0)) / den2
+        a3 = ((xlog_p - p3) * (xlog_p - p0) * (xlog_p - p1)) / den3
+        a4 = ((xlog_p - p0) * (xlog_p - p1) * (xlog_p - p2)) / den4
+
+        def val(x):
+            return a1 * x[i0 - 1] + a2 * x[i1 - 1] + a3 * x[i2 - 1] + a4 * x[i3 - 1]
+
+        if junitt == j:
+            t = val(d["t"][j - 1])
+        for k in range(nmol):
+            if junit[k] != j:
+                continue
+            if k >= 7:
+                raise NotImplementedError("trace species 8+ of the model atmospheres (/TRAC/) are not restated")
+            wmol[k] = val(d["amol"][j - 1][k])
+            junit[k] = 10
+    return t, junit, wmol
+
+
 def cmpalt(pm, tm, denw, ref_z, ref_lat, re_):
     """Altitudes (km) of pressure levels by the hydrostatic equation with a
     moist-air compressibility factor (CMPALT, rrtatm.f:7800-7918): pm in mb,
@@ -295,8 +343,9 @@ def nsmdl(levels, nmol, co2mx, immax_b, ref_lat, re_):
         wmol = list(lv["wmol"][:nmol])
         if min([junitp, junitt] + junit) <= 6:
             if immax_b < 0:
-                raise NotImplementedError("unit codes 1-6 on pressure levels (DEFALT_P) are not restated")
-            p, t, junit, wmol = defalt(lv["z"], p, t, junitp, junitt, junit, wmol, nmol)
+                t, junit, wmol = defalt_p(p, t, junitt, junit, wmol, nmol)
+            else:
+                p, t, junit, wmol = defalt(lv["z"], p, t, junitp, junitt, junit, wmol, nmol)
         zmdl.append(lv["z"])
         pm.append(p)
         tm.append(t)

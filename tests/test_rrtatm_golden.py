@@ -196,6 +196,32 @@ def test_model_atmosphere_interpolation_between_levels():
     assert junit == [10] * 7
 
 
+def test_unit_codes_on_pressure_levels():
+    # DEFALT_P at the model's own pressures returns its table values: a
+    # profile on pressure levels with unit code 2 equals the same profile
+    # with the values written out
+    atm = copy.deepcopy(CASES[0]["atm"])
+    atm["immax_b"] = -atm["immax_b"]
+    coded = copy.deepcopy(atm)
+    for lv in coded["levels"]:
+        lv["jchart"] = "2"
+        lv["jchar"] = "2222222"
+        lv["t"], lv["wmol"] = 0.0, [0.0] * 7
+    a, b = rrtatm.readprof_layers(atm), rrtatm.readprof_layers(coded)
+    for k in a:
+        assert a[k] == b[k], k
+    # between the model's pressures: a cubic in ln p through the four neighbours
+    d = rrtatm.afgl()
+    p = 700.0
+    t, junit, wmol = rrtatm.defalt_p(p, 0.0, 2, [2] * 7, [0.0] * 7, 7)
+    i = [2, 3, 4, 5]
+    x = np.log([d["p"][1][j] for j in i])
+    for got, tab in [(t, d["t"][1])] + [(wmol[k], d["amol"][1][k]) for k in range(7)]:
+        ref = np.polyval(np.polyfit(x, [tab[j] for j in i], 3), np.log(p))
+        assert got == pytest.approx(ref, rel=1e-9, abs=1e-12)
+    assert junit == [10] * 7
+
+
 def test_builtin_model_atmosphere():
     # MODEL = 2 takes the same levels from the built-in table but densities
     # from its tabulated air density (MDLATM) rather than the ideal gas
@@ -215,15 +241,12 @@ def test_builtin_model_atmosphere():
             assert np.max(np.abs(out[k] - np.array(blk[k]))) <= 0.05, (blk["istart"], k)
 
 
-@pytest.mark.parametrize("change", ["trace_species", "codes_on_pressure_levels", "slant", "autolayer"])
+@pytest.mark.parametrize("change", ["trace_species", "slant", "autolayer"])
 def test_unrestated_inputs_raise(change):
     atm = copy.deepcopy(CASES[0]["atm"])
     if change == "trace_species":
         atm["model"] = 2
         atm["nmol"] = 8
-    elif change == "codes_on_pressure_levels":
-        atm["immax_b"] = -atm["immax_b"]
-        atm["levels"][3]["jchar"] = "A2AAAAA"
     elif change == "slant":
         atm["range"] = 10.0
     else:
