@@ -21,7 +21,11 @@
  * Outputs are fully overwritten.  The caller owns every array.  The
  * library owns its device tables (rrtmg_sw_ini_c) and a reusable device
  * workspace, released by rrtmg_sw_finalize_c.  Calls are serialised
- * internally; one process drives one GPU.
+ * internally; one process drives one GPU: every entry point that uses the
+ * device returns RRTMG_SW_ENOTINIT when the current device is not the one
+ * rrtmg_sw_ini_c loaded the tables on.  Host-array entry points run on a
+ * non-blocking stream of the library's own and return when their outputs
+ * are back in host memory.
  */
 #ifndef RRTMG_SW_GB300_H
 #define RRTMG_SW_GB300_H
@@ -125,7 +129,10 @@ int rrtmg_sw_ini_c(double cpdair);
 /* rrtmg_sw (rrtmg_sw_rad.f90:99-841) with host arrays: copies inputs to the
  * device, solves every column, copies the outputs back.  icld outside 0..5
  * becomes 2 and iaer outside {0,6,10} becomes 0 (rrtmg_sw_rad.f90:589,597;
- * icld 4/5 are accepted). */
+ * icld 4/5 are accepted).  Any nlay from 1 to 1000 is accepted; the profile
+ * must have layers on both sides of the 100 hPa switch (RRTMG_SW_ELAYTROP),
+ * and KISS subcolumns (fused McICA, irng = 0) need nlay >= 4
+ * (RRTMG_SW_EKISSSEED), as their seeds come from the bottom four layers. */
 int rrtmg_sw_c(const rrtmg_sw_args *a);
 
 /* Same, all array pointers are device pointers; work is queued on `stream`
@@ -216,11 +223,19 @@ int rrtmg_sw_batch_free_c(void *plan);
  *   - The first call on each device looks up the area's address once
  *     (cudaGetSymbolAddress with that device current) and loads the module
  *     that holds it; make that first call before any stream capture.
- *   - Limit: the area must hold one scratch slot per SM.  A slot is
- *     nlay * (16 with idelm = 0, else 14) * 224 values of the form's type
- *     (the FP32 form adds 60 * nlay floats), so 256 MiB takes nlay <= 138
- *     (FP32) or <= 70 (FP64) with idelm = 1 on a 152-SM GPU.  Larger
- *     requests return RRTMG_SW_ESCRATCH, nothing runs.
+ *     rrtmg_sw_finalize_c forgets the address, so a later first call looks
+ *     it up again.
+ *   - Memory: with lazy CUDA module loading (the default since CUDA 12) the
+ *     area is reserved on a device when that first call loads its module;
+ *     with CUDA_MODULE_LOADING=EAGER every device the process creates a
+ *     context on reserves the 256 MiB at context creation, even if this
+ *     entry point is never called.
+ *   - Limit: the area must hold one scratch slot per SM, or per column pair
+ *     when the call has fewer pairs than SMs.  A slot is nlay * (16 with
+ *     idelm = 0, else 14) * 224 values of the form's type (the FP32 form
+ *     adds 60 * nlay floats), so 256 MiB takes nlay <= 138 (FP32) or <= 70
+ *     (FP64) with idelm = 1 on a 152-SM GPU and at least 304 columns.
+ *     Larger requests return RRTMG_SW_ESCRATCH, nothing runs.
  *     Fewer resident CTAs than rrtmg_sw_dev_c may run when the slots that
  *     fit are fewer than its grid; results are identical, only slower.
  *   - Nothing needs to start at zero: every scratch value is written before
@@ -270,7 +285,9 @@ int get_alpha_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t idcor, double 
                 const double *dz, const double *lat, int32_t juldat, const double *cldfrac,
                 double *alpha);
 
-/* Select the arithmetic form used by subsequent solves (default FP64). */
+/* Select the arithmetic form used by subsequent solves (default FP64).  The
+ * switch takes the library's lock, so a solve in progress on another thread
+ * finishes in the form it started with. */
 int rrtmg_sw_set_form_c(int32_t form);
 int rrtmg_sw_get_form_c(void);
 

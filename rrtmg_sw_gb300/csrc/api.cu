@@ -54,6 +54,9 @@ struct State {
     DevBuf d_tab64, d_tab32, scratch, errw, bounds;
     std::map<std::string, DevBuf> stage;  // host-API staging buffers
     int* h_err = nullptr;                  // pinned
+    // host-array calls run on this non-blocking stream (not the legacy
+    // default stream, which would serialise against every stream of the host)
+    cudaStream_t host_stream = nullptr;
     int form = RRTMG_SW_FORM_FP64;
     int last_launches = 0;
     int last_ad_store = -1;  // checkpointing choice of the last adjoint / tangent-linear call
@@ -74,6 +77,17 @@ int cuda_fail(cudaError_t e) {
         cudaError_t e_ = (x);                 \
         if (e_ != cudaSuccess) return cuda_fail(e_); \
     } while (0)
+
+// Every entry point that touches the device first checks that the tables
+// were loaded (rrtmg_sw_ini_c) and that the current device is the one they
+// were loaded on: the tables and the workspace live on that GPU, and a
+// kernel launched on another would read them from the wrong device.
+int ready(const State& st) {
+    if (!st.init) return RRTMG_SW_ENOTINIT;
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    return dev == st.device ? RRTMG_SW_OK : RRTMG_SW_ENOTINIT;
+}
 
 std::string table_path() {
     if (const char* env = std::getenv("RRTMG_SW_TABLES")) return env;
@@ -444,9 +458,15 @@ void solar_setup(const State& st, const rrtmg_sw_args* a, SolveParams& P) {
 // entry points return RRTMG_SW_OK.
 constexpr int kEmpty = -1;
 
+// Any nlay >= 1 is accepted here, as the reference's driver accepts it; the
+// KISS subcolumn seed reads the bottom four layer pressures
+// (mcica_subcol_gen_sw.f90:470-478), so make_params requires nlay >= 4 for
+// the fused McICA path with irng = 0 only (RRTMG_SW_EKISSSEED), and a profile without
+// layers on both sides of the 100 hPa switch is reported by the solve
+// (RRTMG_SW_ELAYTROP).
 int check_args(const rrtmg_sw_args* a) {
     if (a && a->ncol == 0) return kEmpty;
-    if (!a || a->ncol < 0 || a->nlay < 4 || a->nlay > MAX_NLAY) return RRTMG_SW_EARGS;
+    if (!a || a->ncol < 0 || a->nlay < 1 || a->nlay > MAX_NLAY) return RRTMG_SW_EARGS;
     const double* req[] = {a->play, a->plev, a->tlay, a->h2ovmr, a->o3vmr, a->co2vmr, a->ch4vmr, a->o2vmr,
                            a->asdir, a->asdif, a->aldir, a->aldif, a->coszen};
     for (const double* p : req)
@@ -492,6 +512,7 @@ int make_params(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, Sol
     }
     if (c && !nomcica && P.icld >= 1) {
         P.irng = c->irng != 0 ? 1 : 0;  // mcica:455
+        if (P.irng == 0 && P.nlay < 4) return RRTMG_SW_EKISSSEED;  // seeds from the bottom four layers
         P.permuteseed = c->permuteseed;
         P.cldfrac = c->cldfrac; P.ciwp = c->ciwp; P.clwp = c->clwp; P.rei = c->rei; P.rel = c->rel;
         P.tauc = c->tauc; P.ssac = c->ssac; P.asmc = c->asmc; P.fsfc = c->fsfc; P.alpha = c->alpha;
@@ -764,13 +785,14 @@ struct Stager {
 int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, bool nomcica = false) {
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
-    if (!st.init) return RRTMG_SW_ENOTINIT;
-    int rc = check_args(a);
+    int rc = ready(st);
+    if (rc) return rc;
+    rc = check_args(a);
     if (rc) return rc == kEmpty ? RRTMG_SW_OK : rc;
     const bool mt = c && !nomcica && a->icld >= 1 && c->irng != 0;
     if (!mt && a->ncol >= 2 * kChunkCols && all_pinned(a, c)) return solve_host_chunked(st, a, c, nomcica);
     const size_t C = a->ncol, L = a->nlay, CL = C * L, CL1 = C * (L + 1), G = (size_t)NGPT * CL;
-    cudaStream_t s = 0;
+    cudaStream_t s = st.host_stream;
     Stager sg{st, s};
     rrtmg_sw_args d = *a;
     d.play = sg.in("play", a->play, CL); d.plev = sg.in("plev", a->plev, CL1); d.tlay = sg.in("tlay", a->tlay, CL);
@@ -838,7 +860,11 @@ int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, bool nomcica = 
 // never need clearing (every slot value is written before it is read); the
 // error word is cleared on the stream by each call.  One area per device, so
 // two solves on it at once would race; calls are serialised by State::mu and
-// each call waits for its kernel.
+// each call waits for its kernel.  The area belongs to this library's CUDA
+// module: with lazy module loading (the CUDA 12+ default) a device reserves
+// it when the module is first used there; with CUDA_MODULE_LOADING=EAGER every
+// device a process creates a context on reserves it at context creation,
+// whether or not the entry point is ever called.
 constexpr size_t kStaticScratchBytes = size_t(256) << 20;
 constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
@@ -882,7 +908,9 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
     P.slot_elems = slot_elems(P.nlay, P.idelm, fp32);
     const size_t slot_bytes = P.slot_elems * (fp32 ? sizeof(float) : sizeof(double));
     const size_t slots = kStaticScratchBytes / slot_bytes;
-    if (slots < (size_t)st.num_sms) return RRTMG_SW_ESCRATCH;
+    // one slot per SM, or per column pair when the call has fewer pairs
+    const size_t need = (size_t)std::min(li.grid, st.num_sms);
+    if (slots < need) return RRTMG_SW_ESCRATCH;
     if ((size_t)li.grid > slots) li.grid = (int)slots;
     StaticArea area;
     CK(static_area(dev, area));
@@ -903,9 +931,10 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
 int solve_ad_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, const rrtmg_sw_ad_args* ad, bool tl) {
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
-    if (!st.init) return RRTMG_SW_ENOTINIT;
+    const int rr = ready(st);
+    if (rr) return rr;
     if (a && ad && a->ncol == 0) return RRTMG_SW_OK;
-    if (!a || !ad || a->ncol < 0 || a->nlay < 4 || a->nlay > MAX_NLAY) return RRTMG_SW_EARGS;
+    if (!a || !ad || a->ncol < 0 || a->nlay < 1 || a->nlay > MAX_NLAY) return RRTMG_SW_EARGS;
     const double* req[] = {a->play, a->plev, a->tlay, a->h2ovmr, a->o3vmr, a->co2vmr, a->ch4vmr, a->o2vmr,
                            a->asdir, a->asdif, a->aldir, a->aldif, a->coszen};
     for (const double* p : req)
@@ -913,7 +942,7 @@ int solve_ad_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, const rrtmg_
     const int icld = (a->icld < 0 || a->icld > 5) ? 2 : a->icld;
     if (icld >= 1 && !c) return RRTMG_SW_EARGS;
     const size_t C = a->ncol, L = a->nlay, CL = C * L, CL1 = C * (L + 1);
-    cudaStream_t s = 0;
+    cudaStream_t s = st.host_stream;
     Stager sg{st, s};
     rrtmg_sw_args d = *a;
     d.play = sg.in("play", a->play, CL); d.plev = sg.in("plev", a->plev, CL1); d.tlay = sg.in("tlay", a->tlay, CL);
@@ -1151,6 +1180,7 @@ int rrtmg_sw_ini_c(double cpdair) {
         const int rc = build_tables(st);
         if (rc) return rc;
         CK(cudaMallocHost((void**)&st.h_err, sizeof(int)));
+        CK(cudaStreamCreateWithFlags(&st.host_stream, cudaStreamNonBlocking));
     }
     const int rc = upload(st);
     if (rc) return rc;
@@ -1168,7 +1198,7 @@ int rrtmg_sw_mcica_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c) {
 int rrtmg_sw_dev_c(const rrtmg_sw_args* a, void* stream) {
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
-    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (const int r0 = ready(st)) return r0;
     const int rc = check_args(a);
     if (rc) return rc == kEmpty ? RRTMG_SW_OK : rc;
     return solve_dev(st, a, nullptr, (cudaStream_t)stream);
@@ -1182,7 +1212,7 @@ int rrtmg_sw_nomcica_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c) {
 int rrtmg_sw_nomcica_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, void* stream) {
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
-    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (const int r0 = ready(st)) return r0;
     if (!c) return RRTMG_SW_EARGS;
     const int rc = check_args(a);
     if (rc) return rc == kEmpty ? RRTMG_SW_OK : rc;
@@ -1192,7 +1222,7 @@ int rrtmg_sw_nomcica_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, voi
 int rrtmg_sw_mcica_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, void* stream) {
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
-    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (const int r0 = ready(st)) return r0;
     if (!c) return RRTMG_SW_EARGS;
     const int rc = check_args(a);
     if (rc) return rc == kEmpty ? RRTMG_SW_OK : rc;
@@ -1202,7 +1232,7 @@ int rrtmg_sw_mcica_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, void*
 int rrtmg_sw_static_dev_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, void* stream) {
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
-    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (const int r0 = ready(st)) return r0;
     const int rc = check_args(a);
     if (rc) return rc == kEmpty ? RRTMG_SW_OK : rc;
     return solve_static(st, a, c, (cudaStream_t)stream);
@@ -1216,15 +1246,16 @@ int mcica_subcol_sw_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t permutes
                       double* ssacmcl, double* asmcmcl, double* fsfcmcl) {
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
-    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (const int r0 = ready(st)) return r0;
     if (icld == 0) return RRTMG_SW_OK;                 // mcica:261
     if (icld < 0 || icld > 5) return RRTMG_SW_EICLD;    // mcica:262-264
     if (ncol == 0) return RRTMG_SW_OK;
-    if (ncol < 0 || nlay < 4 || !play || !cldfrac || !ciwp || !clwp || !rei || !rel) return RRTMG_SW_EARGS;
+    if (ncol < 0 || nlay < 1 || !play || !cldfrac || !ciwp || !clwp || !rei || !rel) return RRTMG_SW_EARGS;
+    if (irng == 0 && nlay < 4) return RRTMG_SW_EKISSSEED;  // KISS seeds from the bottom four layers (mcica:470-478)
     if (icld >= 4 && !alpha) return RRTMG_SW_EARGS;
     if (irng != 0) irng = 1;                            // mcica:455
     const size_t C = ncol, L = nlay, CL = C * L, G = (size_t)NGPT * CL;
-    cudaStream_t s = 0;
+    cudaStream_t s = st.host_stream;
     Stager sg{st, s};
     const double* d_play = sg.in("m_play", play, CL);
     const double* d_cf = sg.in("m_cf", cldfrac, CL);
@@ -1278,7 +1309,7 @@ int rrtmg_sw_mt_window_c(int32_t seed, uint64_t offset, uint32_t* window) {
 int rrtmg_sw_mt_stream_dev_c(int32_t seed, uint64_t n, uint32_t* out, int32_t log_seg, void* stream) {
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
-    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (const int r0 = ready(st)) return r0;
     if (!out || log_seg > 40) return RRTMG_SW_EARGS;
     CK(launch_mt_jump((uint32_t)seed, n, out, st.num_sms, log_seg, (cudaStream_t)stream));
     st.last_launches = n ? 2 : 0;
@@ -1290,11 +1321,11 @@ int get_alpha_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t idcor, double 
                 const double* lat, int32_t juldat, const double* cldfrac, double* alpha) {
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
-    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (const int r0 = ready(st)) return r0;
     if (ncol == 0) return RRTMG_SW_OK;
     if (ncol < 0 || nlay < 1 || !dz || !lat || !cldfrac || !alpha) return RRTMG_SW_EARGS;
     const size_t CL = (size_t)ncol * nlay;
-    cudaStream_t s = 0;
+    cudaStream_t s = st.host_stream;
     Stager sg{st, s};
     const double* d_dz = sg.in("a_dz", dz, CL);
     const double* d_lat = sg.in("a_lat", lat, (size_t)ncol);
@@ -1309,13 +1340,21 @@ int get_alpha_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t idcor, double 
     return RRTMG_SW_OK;
 }
 
+// The form is read by each solve while it holds the library mutex, so a
+// switch waits for a call in progress and never changes it half way.
 int rrtmg_sw_set_form_c(int32_t form) {
     if (form != RRTMG_SW_FORM_FP64 && form != RRTMG_SW_FORM_FP32) return RRTMG_SW_EARGS;
-    S().form = form;
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    st.form = form;
     return RRTMG_SW_OK;
 }
 
-int rrtmg_sw_get_form_c(void) { return S().form; }
+int rrtmg_sw_get_form_c(void) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    return st.form;
+}
 
 int rrtmg_sw_last_launch_count_c(void) { return S().last_launches; }
 
@@ -1328,7 +1367,7 @@ const char* rrtmg_sw_errstr_c(int32_t code) {
     case RRTMG_SW_ETABLES: return "COEFFICIENT TABLE FILE MISSING OR CORRUPT";
     case RRTMG_SW_EARGS: return "INVALID ARGUMENTS";
     case RRTMG_SW_ECUDA: return "CUDA ERROR";
-    case RRTMG_SW_ESCRATCH: return "REQUEST EXCEEDS THE 256 MIB STATIC SCRATCH (ONE SLOT PER SM)";
+    case RRTMG_SW_ESCRATCH: return "REQUEST EXCEEDS THE 256 MIB STATIC SCRATCH (ONE SLOT PER SM OR COLUMN PAIR)";
     case RRTMG_SW_EINFLAG1: return "INFLAG = 1 OPTION NOT AVAILABLE WITH MCICA";
     case RRTMG_SW_EICERAD: return "ICE RADIUS OUT OF BOUNDS";
     case RRTMG_SW_EICEDGE: return "ICE GENERALIZED EFFECTIVE SIZE OUT OF BOUNDS";
@@ -1358,7 +1397,7 @@ int rrtmg_sw_tl_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, const rrtmg_
 int rrtmg_sw_batch_plan_c(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, int32_t n, void* stream, void** plan) {
     State& st = S();
     std::lock_guard<std::mutex> lk(st.mu);
-    if (!st.init) return RRTMG_SW_ENOTINIT;
+    if (const int r0 = ready(st)) return r0;
     if (!a || !plan) return RRTMG_SW_EARGS;
     BatchPlan* bp = nullptr;
     const int rc = batch_plan(st, a, c, n, (cudaStream_t)stream, &bp);
@@ -1372,6 +1411,9 @@ int rrtmg_sw_batch_run_c(void* plan, void* stream) {
     BatchPlan* bp = (BatchPlan*)plan;
     if (!st.init) return RRTMG_SW_ENOTINIT;
     if (!bp) return RRTMG_SW_EARGS;
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev != bp->device) return RRTMG_SW_ENOTINIT;  // the plan's graph and buffers live on its device
     cudaStream_t s = (cudaStream_t)stream;
     CK(cudaGraphLaunch(bp->exec, s));
     st.last_launches = 2;
@@ -1412,6 +1454,11 @@ int rrtmg_sw_finalize_c(void) {
     st.stage.clear();
     if (st.h_err) cudaFreeHost(st.h_err);
     st.h_err = nullptr;
+    if (st.host_stream) cudaStreamDestroy(st.host_stream);
+    st.host_stream = nullptr;
+    // a later rrtmg_sw_ini_c (after a cudaDeviceReset, say) looks the static
+    // area's address up again
+    for (StaticArea& sa : g_static_area) sa = StaticArea{};
     ChunkStreams& cs = CS();
     for (int i = 0; i < kChunkStreams; ++i) {
         cs.scratch[i].release();
