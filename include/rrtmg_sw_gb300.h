@@ -116,7 +116,9 @@ enum {
     RRTMG_SW_ELAYTROP = 30,    /* profile without layers on both sides of the ~100 hPa switch */
     RRTMG_SW_EIRNG = 31,       /* irng = 1 (MT19937) on the static, batch or TL/AD entry points */
     RRTMG_SW_EPARTIAL = 32,    /* rrtmg_sw_rad.nomcica.f90:619-621  PARTIAL CLOUD NOT ALLOWED */
-    RRTMG_SW_EBOUNDS = 40      /* bounds-check build only: a table index left its coefficient blob */
+    RRTMG_SW_EBOUNDS = 40,     /* bounds-check build only: a table index left its coefficient blob */
+    RRTMG_SW_ETIMEOUT = 41     /* FP32 form, tiled kernel: a wait between its warps gave up after seconds
+                                  (the kernel ends with this code instead of hanging; outputs invalid) */
 };
 
 /* rrtmg_sw_ini (rrtmg_sw_init.f90:47-173): load the 112-g-point tables

@@ -53,7 +53,13 @@ struct State {
     double cpdair = 1.004e3;
     DevBuf d_tab64, d_tab32, scratch, errw, bounds;
     std::map<std::string, DevBuf> stage;  // host-API staging buffers
-    int* h_err = nullptr;                  // pinned
+    int* h_err = nullptr;                  // pinned: [0] error word, [1] tiled-kernel overflow count
+    // diagnostics, from the environment at each rrtmg_sw_ini_c: RRTMG_SW_TILED=1
+    // puts the FP32 form on the tiled kernel; RRTMG_SW_TILE_QCAP=n
+    // lowers the tiled kernel's capacity of FP64 cells per column pair (tests
+    // of its fallback)
+    bool no_tiled = false;
+    int tile_qcap = 0;
     // host-array calls run on this non-blocking stream (not the legacy
     // default stream, which would serialise against every stream of the host)
     cudaStream_t host_stream = nullptr;
@@ -550,10 +556,18 @@ uint64_t mt_stream_length(int icld, int ncol, int nlay) {
     return (icld >= 4 ? 2ull : 1ull) * sc * (uint64_t)nlay;
 }
 
+// Bytes of a launch's scratch before the tiled kernel's overflow list, and
+// the list's size for npairs column pairs (count word + pair indices).
+size_t ovf_offset(size_t slots_bytes) { return (slots_bytes + 255) & ~(size_t)255; }
+size_t ovf_bytes(int npairs) { return (size_t)(npairs + 1) * sizeof(int); }
+
 // Queue one solve on `s` (device pointers in a/c) with the given scratch
-// buffer and device error word; nothing is synchronised.
+// buffer and device error word; nothing is synchronised.  Pout / liout
+// receive the parameters and launch shape (the tiled FP32 kernel's overflow
+// list is read by the caller).
 int enqueue_solve(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s, bool nomcica,
-                  DevBuf& scratch, int* err, int& launches) {
+                  DevBuf& scratch, int* err, int& launches, SolveParams* Pout = nullptr,
+                  LaunchInfo* liout = nullptr, bool allow_tiled = true) {
     SolveParams P;
     int rc = make_params(st, a, c, P, nomcica);
     if (rc) return rc;
@@ -569,27 +583,96 @@ int enqueue_solve(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, c
         launches += 2;
     }
     const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
-    LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms) : plan_fp64(P, st.num_sms);
-    P.slot_elems = slot_elems(P.nlay, P.idelm, fp32);
-    const size_t esz = fp32 ? sizeof(float) : sizeof(double);
-    CK(scratch.ensure((size_t)li.grid * P.slot_elems * esz));
+    LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms, allow_tiled && !st.no_tiled) : plan_fp64(P, st.num_sms);
+    if (!fp32) li.slot_bytes = slot_elems(P.nlay, P.idelm, false) * sizeof(double);
+    P.slot_elems = li.slot_bytes / (fp32 ? sizeof(float) : sizeof(double));
+    const size_t off = ovf_offset((size_t)li.grid * li.slot_bytes);
+    CK(scratch.ensure(li.tiled ? off + ovf_bytes(P.npairs) : (size_t)li.grid * li.slot_bytes));
     P.scratch = scratch.p;
+    if (li.tiled) {
+        P.tovfcount = (int*)((char*)scratch.p + off);
+        P.tovf = P.tovfcount + 1;
+        P.tovfcap = P.npairs;
+        P.tile_qcap = st.tile_qcap;
+        CK(cudaMemsetAsync(P.tovfcount, 0, sizeof(int), s));
+    }
     if (fp32) CK(launch_solve_fp32(P, (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, li, s));
     else CK(launch_solve_fp64(P, (const double*)st.d_tab64.p, li, s));
+    if (Pout) *Pout = P;
+    if (liout) *liout = li;
     return RRTMG_SW_OK;
 }
 
-// Queue one solve on `s`; returns after reading back the device error word.
-int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s, bool nomcica = false) {
+// The tiled FP32 kernel listed `count` column pairs whose FP64 cells
+// exceeded its capacities (their outputs are not final): solve them again
+// with the scratch-based kernel (k_solve<float>, whose FP64 redo has no such
+// limit) through its column map, on the same stream.  With more pairs than
+// the list holds, every pair is solved again.  `colmap` is device memory for
+// 2 * count + 1 ints; `scratch(bytes)` returns device scratch of that size
+// (the tiled launch must have finished: its scratch is reused).
+template <typename ScratchFn>
+int tiled_fallback(State& st, const SolveParams& Pt, int count, cudaStream_t s, int* colmap, ScratchFn scratch,
+                   int& launches) {
+    SolveParams P = Pt;
+    if (count <= Pt.tovfcap) {
+        std::vector<int> pairs(count);
+        CK(cudaMemcpyAsync(pairs.data(), Pt.tovf, count * sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        std::sort(pairs.begin(), pairs.end());
+        std::vector<int> cols(2 * (size_t)count + 1);
+        for (int i = 0; i < count; ++i)
+            for (int c2 = 0; c2 < COLS_PER_CTA; ++c2) {
+                const int k = COLS_PER_CTA * pairs[i] + c2;
+                cols[COLS_PER_CTA * i + c2] = k < P.ncol ? k : P.ncol;  // ncol: empty slot
+            }
+        cols[2 * (size_t)count] = 2 * count;
+        CK(cudaMemcpyAsync(colmap, cols.data(), cols.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+        P.colmap = colmap;
+        P.mapcount = colmap + 2 * (size_t)count;
+        P.npairs = count;
+    }
+    P.tovf = nullptr;
+    P.tovfcount = nullptr;
+    P.tovfcap = 0;
+    LaunchInfo li = plan_fp32(P, st.num_sms, false);
+    void* sp = scratch((size_t)li.grid * li.slot_bytes);
+    if (!sp) return RRTMG_SW_ESCRATCH;
+    P.scratch = sp;
+    P.slot_elems = li.slot_bytes / sizeof(float);
+    CK(launch_solve_fp32(P, (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, li, s));
+    launches += 1;
+    return RRTMG_SW_OK;
+}
+
+// Queue one solve on `s`; returns after reading back the device error word
+// (and, after the tiled FP32 kernel, after solving again any column pairs it
+// could not finish).
+int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s, bool nomcica = false,
+              bool allow_tiled = true) {
     CK(st.errw.ensure(sizeof(int)));
     int* err = (int*)st.errw.p;
     CK(cudaMemsetAsync(err, 0, sizeof(int), s));
     int launches = 0;
-    const int rc = enqueue_solve(st, a, c, s, nomcica, st.scratch, err, launches);
+    SolveParams P;
+    LaunchInfo li;
+    const int rc = enqueue_solve(st, a, c, s, nomcica, st.scratch, err, launches, &P, &li, allow_tiled);
     if (rc) return rc;
-    st.last_launches = launches;
+    st.h_err[1] = 0;
     CK(cudaMemcpyAsync(st.h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (li.tiled) CK(cudaMemcpyAsync(st.h_err + 1, P.tovfcount, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (li.tiled && st.h_err[0] == 0 && st.h_err[1] > 0) {
+        DevBuf& cm = st.stage["tovf_colmap"];
+        CK(cm.ensure((2 * (size_t)std::min(st.h_err[1], P.tovfcap) + 1) * sizeof(int)));
+        const int r2 = tiled_fallback(st, P, st.h_err[1], s, (int*)cm.p, [&](size_t b) -> void* {
+            return st.scratch.ensure(b) == cudaSuccess ? st.scratch.p : nullptr;
+        }, launches);
+        if (r2) return r2;
+        CK(cudaMemcpyAsync(st.h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    st.last_launches = launches;
     return bounds_status(st, *st.h_err);
 }
 
@@ -601,12 +684,17 @@ int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaS
 // the rrtmg_sw call of its column slices and the results are those of one
 // call; MT streams (irng = 1) depend on ncol and keep the single-call path.
 constexpr int kChunkCols = 16384;  // columns per chunk (even: whole column pairs)
+// a chunk's tiled solve left column pairs for the scratch-based kernel: the
+// chunked call is repeated as one call without the tiled kernel
+constexpr int kRetryUntiled = -2;
 constexpr int kChunkStreams = 2;
 
 struct ChunkStreams {
     cudaStream_t s[kChunkStreams] = {nullptr, nullptr};
     DevBuf scratch[kChunkStreams], err[kChunkStreams];
     int* h_err = nullptr;  // pinned, one word per stream
+    int* h_ovf = nullptr;  // pinned, the tiled kernel's overflow count of each chunk
+    int ovf_cap = 0;
     int device = -1;
 };
 
@@ -658,6 +746,14 @@ int solve_host_chunked(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds*
     cudaError_t e = cudaSuccess;
     int launches = 0;
     const int nch = (int)((C + kChunkCols - 1) / kChunkCols);
+    if (cs.ovf_cap < nch) {
+        if (cs.h_ovf) cudaFreeHost(cs.h_ovf);
+        cs.h_ovf = nullptr;
+        cs.ovf_cap = 0;
+        CK(cudaMallocHost((void**)&cs.h_ovf, nch * sizeof(int)));
+        cs.ovf_cap = nch;
+    }
+    for (int ch = 0; ch < nch; ++ch) cs.h_ovf[ch] = 0;
     for (int ch = 0; ch < nch && e == cudaSuccess; ++ch) {
         const int si = ch % kChunkStreams;
         cudaStream_t s = cs.s[si];
@@ -732,11 +828,16 @@ int solve_host_chunked(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds*
         d.bndfu = bd[0]; d.bndfd = bd[1]; d.bndfddir = bd[2]; d.bndcu = bd[3]; d.bndcd = bd[4];
         if (e != cudaSuccess) break;
         int nl = 0;
-        const int rc = enqueue_solve(st, &d, c ? &dc : nullptr, s, nomcica, cs.scratch[si], (int*)cs.err[si].p, nl);
+        SolveParams Pc;
+        LaunchInfo lic;
+        const int rc = enqueue_solve(st, &d, c ? &dc : nullptr, s, nomcica, cs.scratch[si], (int*)cs.err[si].p, nl,
+                                     &Pc, &lic);
         if (rc) {
             for (int i = 0; i < kChunkStreams; ++i) cudaStreamSynchronize(cs.s[i]);
             return rc;
         }
+        // the chunk's overflow count, read before the next chunk on this stream reuses the scratch
+        if (lic.tiled) e = cudaMemcpyAsync(cs.h_ovf + ch, Pc.tovfcount, sizeof(int), cudaMemcpyDeviceToHost, s);
         launches += nl;
         back(a->swuflx, d.swuflx, L1); back(a->swdflx, d.swdflx, L1);
         back(a->swuflxc, d.swuflxc, L1); back(a->swdflxc, d.swdflxc, L1);
@@ -755,6 +856,8 @@ int solve_host_chunked(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds*
     st.last_launches = launches;
     for (int i = 0; i < kChunkStreams; ++i)
         if (cs.h_err[i]) return cs.h_err[i];
+    for (int ch = 0; ch < nch; ++ch)
+        if (cs.h_ovf[ch] > 0) return kRetryUntiled;  // rare: the caller solves the call again in one piece
     return bounds_status(st, RRTMG_SW_OK);
 }
 
@@ -790,7 +893,12 @@ int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, bool nomcica = 
     rc = check_args(a);
     if (rc) return rc == kEmpty ? RRTMG_SW_OK : rc;
     const bool mt = c && !nomcica && a->icld >= 1 && c->irng != 0;
-    if (!mt && a->ncol >= 2 * kChunkCols && all_pinned(a, c)) return solve_host_chunked(st, a, c, nomcica);
+    bool allow_tiled = true;
+    if (!mt && a->ncol >= 2 * kChunkCols && all_pinned(a, c)) {
+        rc = solve_host_chunked(st, a, c, nomcica);
+        if (rc != kRetryUntiled) return rc;
+        allow_tiled = false;
+    }
     const size_t C = a->ncol, L = a->nlay, CL = C * L, CL1 = C * (L + 1), G = (size_t)NGPT * CL;
     cudaStream_t s = st.host_stream;
     Stager sg{st, s};
@@ -840,7 +948,7 @@ int solve_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, bool nomcica = 
     for (int i = 0; i < 5; ++i) bd[i] = sg.out(bn[i], bh[i], 14 * CL1);
     d.bndfu = bd[0]; d.bndfd = bd[1]; d.bndfddir = bd[2]; d.bndcu = bd[3]; d.bndcd = bd[4];
     if (sg.err != cudaSuccess) return cuda_fail(sg.err);
-    rc = solve_dev(st, &d, c ? &dc : nullptr, s, nomcica);
+    rc = solve_dev(st, &d, c ? &dc : nullptr, s, nomcica, allow_tiled);
     if (rc) return rc;
     sg.back(a->swuflx, d.swuflx, CL1); sg.back(a->swdflx, d.swdflx, CL1);
     sg.back(a->swuflxc, d.swuflxc, CL1); sg.back(a->swdflxc, d.swdflxc, CL1);
@@ -894,6 +1002,13 @@ cudaError_t static_area(int dev, StaticArea& out) {
     return cudaSuccess;
 }
 
+// The last kStaticTail bytes of the static area hold the tiled FP32
+// kernel's overflow list (a count and up to kStaticOvfCap column pairs) and
+// the column map of their second solve; slots come from the rest.
+constexpr int kStaticOvfCap = 4096;
+constexpr size_t kStaticTail = (((size_t)(1 + kStaticOvfCap) + (2 * (size_t)kStaticOvfCap + 1)) * sizeof(int) +
+                                255) & ~(size_t)255;
+
 int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s) {
     int dev = -1;
     CK(cudaGetDevice(&dev));
@@ -904,26 +1019,47 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
     if (rc) return rc;
     if (P.irng) return RRTMG_SW_EIRNG;  // the MT stream needs a device buffer
     const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
-    LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms) : plan_fp64(P, st.num_sms);
-    P.slot_elems = slot_elems(P.nlay, P.idelm, fp32);
-    const size_t slot_bytes = P.slot_elems * (fp32 ? sizeof(float) : sizeof(double));
-    const size_t slots = kStaticScratchBytes / slot_bytes;
+    LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms, !st.no_tiled) : plan_fp64(P, st.num_sms);
+    if (!fp32) li.slot_bytes = slot_elems(P.nlay, P.idelm, false) * sizeof(double);
+    const size_t avail = kStaticScratchBytes - kStaticTail;
+    const size_t slots = avail / li.slot_bytes;
     // one slot per SM, or per column pair when the call has fewer pairs
     const size_t need = (size_t)std::min(li.grid, st.num_sms);
     if (slots < need) return RRTMG_SW_ESCRATCH;
     if ((size_t)li.grid > slots) li.grid = (int)slots;
+    P.slot_elems = li.slot_bytes / (fp32 ? sizeof(float) : sizeof(double));
     StaticArea area;
     CK(static_area(dev, area));
     P.scratch = area.scratch;
     P.err = area.err;
+    int* tail = (int*)((char*)area.scratch + avail);
+    if (li.tiled) {
+        P.tovfcount = tail;
+        P.tovf = tail + 1;
+        P.tovfcap = std::min(P.npairs, kStaticOvfCap);
+        P.tile_qcap = st.tile_qcap;
+        CK(cudaMemsetAsync(P.tovfcount, 0, sizeof(int), s));
+    }
     CK(cudaMemsetAsync(P.err, 0, sizeof(int), s));
     if (fp32) CK(launch_solve_fp32(P, (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, li, s));
     else CK(launch_solve_fp64(P, (const double*)st.d_tab64.p, li, s));
-    st.last_launches = 1;
-    int h_err = 0;  // pageable: the copy completes before the call returns
-    CK(cudaMemcpyAsync(&h_err, P.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    int launches = 1;
+    int h[2] = {0, 0};  // pageable: the copies complete before the calls return
+    CK(cudaMemcpyAsync(&h[0], P.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (li.tiled) CK(cudaMemcpyAsync(&h[1], P.tovfcount, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    return bounds_status(st, h_err);
+    if (li.tiled && h[0] == 0 && h[1] > 0) {
+        // column pairs the tiled kernel left: the scratch-based kernel, in the
+        // same area (its column map after the overflow list)
+        const int r2 = tiled_fallback(st, P, h[1], s, tail + 1 + kStaticOvfCap,
+                                      [&](size_t b) -> void* { return b <= avail ? area.scratch : nullptr; },
+                                      launches);
+        if (r2) return r2;
+        CK(cudaMemcpyAsync(&h[0], P.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    st.last_launches = launches;
+    return bounds_status(st, h[0]);
 }
 
 // ---------------------------------------------------------------------------
@@ -1179,8 +1315,14 @@ int rrtmg_sw_ini_c(double cpdair) {
         CK(cudaDeviceGetAttribute(&st.num_sms, cudaDevAttrMultiProcessorCount, dev));
         const int rc = build_tables(st);
         if (rc) return rc;
-        CK(cudaMallocHost((void**)&st.h_err, sizeof(int)));
+        CK(cudaMallocHost((void**)&st.h_err, 2 * sizeof(int)));
         CK(cudaStreamCreateWithFlags(&st.host_stream, cudaStreamNonBlocking));
+    }
+    {
+        const char* t = std::getenv("RRTMG_SW_TILED");
+        st.no_tiled = !(t && std::strcmp(t, "1") == 0);
+        const char* q = std::getenv("RRTMG_SW_TILE_QCAP");
+        st.tile_qcap = q ? std::atoi(q) : 0;
     }
     const int rc = upload(st);
     if (rc) return rc;
@@ -1380,6 +1522,7 @@ const char* rrtmg_sw_errstr_c(int32_t code) {
     case RRTMG_SW_EIRNG: return "IRNG = 1 (MT19937) NOT AVAILABLE ON THIS ENTRY POINT";
     case RRTMG_SW_EPARTIAL: return "PARTIAL CLOUD NOT ALLOWED";
     case RRTMG_SW_EBOUNDS: return "TABLE INDEX OUT OF RANGE (BOUNDS-CHECK BUILD)";
+    case RRTMG_SW_ETIMEOUT: return "WAIT BETWEEN THE WARPS OF THE TILED SOLVE TIMED OUT";
     default: return "UNKNOWN ERROR";
     }
 }
@@ -1468,6 +1611,9 @@ int rrtmg_sw_finalize_c(void) {
     }
     if (cs.h_err) cudaFreeHost(cs.h_err);
     cs.h_err = nullptr;
+    if (cs.h_ovf) cudaFreeHost(cs.h_ovf);
+    cs.h_ovf = nullptr;
+    cs.ovf_cap = 0;
     cs.device = -1;
     mt_release_device_tables();
     st.init = false;

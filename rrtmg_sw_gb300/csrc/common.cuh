@@ -105,7 +105,7 @@ constexpr int MAX_BATCH = 1024;  // instances per batch launch
 enum {
     E_OK = 0, E_INFLAG1 = 10, E_ICERAD = 11, E_ICEDGE = 12, E_ICEPROP = 13,
     E_LIQRAD = 14, E_LIQPROP = 15, E_ICLD = 20, E_KISSSEED = 21, E_LAYTROP = 30, E_PARTIAL = 32,
-    E_BOUNDS = 40
+    E_BOUNDS = 40, E_TIMEOUT = 41
 };
 
 }  // namespace rrsw

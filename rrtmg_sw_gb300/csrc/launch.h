@@ -12,6 +12,8 @@ namespace rrsw {
 struct LaunchInfo {
     int grid;            // CTAs (persistent: each loops over column pairs)
     size_t smem;         // dynamic shared memory per CTA
+    bool tiled = false;  // FP32 form: the tiled kernel (layer R/T in shared memory)
+    size_t slot_bytes = 0;  // global scratch per CTA
 };
 
 // FP64 form
@@ -20,7 +22,8 @@ LaunchInfo plan_fp64(const SolveParams& P, int num_sms);
 cudaError_t launch_solve_fp64(const SolveParams& P, const double* tab, const LaunchInfo& li, cudaStream_t s);
 // FP32 form
 cudaError_t upload_tables_fp32(const DevTables& t);
-LaunchInfo plan_fp32(const SolveParams& P, int num_sms);
+// allow_tiled = false keeps the scratch-based kernel (k_solve<float>)
+LaunchInfo plan_fp32(const SolveParams& P, int num_sms, bool allow_tiled = true);
 cudaError_t launch_solve_fp32(const SolveParams& P, const float* tab, const double* tab64, const LaunchInfo& li,
                               cudaStream_t s);
 // batch of instances (device array of SolveParams, sunlit lists built by

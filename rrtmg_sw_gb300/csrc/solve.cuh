@@ -48,6 +48,14 @@ struct SolveParams {
     size_t slot_elems;
     int *err;
     const uint32_t* mt;  // irng 1: tempered MT words of the call's stream (subcolumn, column, layer order)
+    // tiled FP32 kernel: column pairs with more FP64 cells than its capacities
+    // (list of pair indices, its length and capacity); the caller solves them
+    // again with the scratch-based kernel.  tile_qcap > 0 lowers the capacity
+    // of FP64 cells per pair (tests of that path).
+    int* tovf;
+    int* tovfcount;
+    int tovfcap;
+    int tile_qcap;
 };
 
 // Tangent-linear / adjoint request (solve_ad.cu): objective weights and

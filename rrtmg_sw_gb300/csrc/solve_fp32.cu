@@ -1,6 +1,7 @@
 // solve_fp32.cu -- FP32 form of the solve (FMA contraction allowed).
 #include "kernel.cuh"
 #include "launch.h"
+#include "tiled.cuh"
 
 namespace rrsw {
 
@@ -146,8 +147,26 @@ __device__ __noinline__ RT<float> reftra_g<float>(float zto1, float zw, float zc
 
 cudaError_t upload_tables_fp32(const DevTables& t) { return cudaMemcpyToSymbol(cT, &t, sizeof(DevTables)); }
 
-LaunchInfo plan_fp32(const SolveParams& P, int num_sms) {
+LaunchInfo plan_fp32(const SolveParams& P, int num_sms, bool allow_tiled) {
     LaunchInfo li;
+    static int smem_optin = -1;
+    if (smem_optin < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    if (allow_tiled && tiled_supports(P, (size_t)smem_optin)) {
+        // one CTA per SM, persistent over the column pairs
+        const bool fused = P.fused && P.icld >= 1, nomc = P.nomcica && P.icld >= 1;
+        li.tiled = true;
+        li.smem = tiled_smem(P.nlay, P.extra ? 16 : 8, fused, fused || nomc).total;
+        const auto kern = P.mt ? k_solve_tiled<true> : k_solve_tiled<false>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
+        li.grid = num_sms < P.npairs ? num_sms : P.npairs;
+        if (li.grid < 1) li.grid = 1;
+        li.slot_bytes = tiled_glob(P.nlay).total;
+        return li;
+    }
     li.smem = smem_layout(P.nlay, num_q<float>(P.extra != 0), stages_clouds(P),
                           stage_aerosol<float>(P.iaer), sizeof(float)).total;
     const auto kern = P.mt ? k_solve<float, true> : k_solve<float, false>;
@@ -158,13 +177,19 @@ LaunchInfo plan_fp32(const SolveParams& P, int num_sms) {
     li.grid = num_sms * per_sm;
     if (li.grid > P.npairs) li.grid = P.npairs;
     if (li.grid < 1) li.grid = 1;
+    li.slot_bytes = slot_elems(P.nlay, P.idelm, true) * sizeof(float);
     return li;
 }
 
 cudaError_t launch_solve_fp32(const SolveParams& P, const float* tab, const double* tab64, const LaunchInfo& li,
                               cudaStream_t s) {
-    if (P.mt) k_solve<float, true><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab64);
-    else k_solve<float, false><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab64);
+    if (li.tiled) {
+        if (P.mt) k_solve_tiled<true><<<li.grid, T_THREADS, li.smem, s>>>(P, tab, tab64);
+        else k_solve_tiled<false><<<li.grid, T_THREADS, li.smem, s>>>(P, tab, tab64);
+    } else {
+        if (P.mt) k_solve<float, true><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab64);
+        else k_solve<float, false><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab64);
+    }
     return cudaGetLastError();
 }
 

@@ -1,0 +1,1010 @@
+// tiled.cuh -- FP32 form of the solve with every layer's reflectance and
+// transmittance kept on chip.  Included by solve_fp32.cu (FMA contraction,
+// approximate FP32 division).
+//
+// One persistent CTA per SM works through column pairs.  A pair's 224
+// subcolumns (column x g-point) are cut into 7 tiles of 32.  A tile holds,
+// for its 32 subcolumns and every layer, the clear and total layer
+// reflectance, absorptance and direct transmittance of spcvmc_sw /
+// reftra_sw (rrtmg_sw_spcvmc.f90:442-585, rrtmg_sw_reftra.f90:151-326) in
+// shared memory, two tiles double-buffered.  Warp roles:
+//
+//   optics warps (T_OPT): per pair, setcoef (FP64) into shared memory, the
+//     McICA subcolumn masks (one walk per subcolumn), the solar source; then
+//     per tile the cells (g-point, layer) -- gas optics, clouds, aerosol,
+//     delta scaling, the two-stream layer solution -- layer rows taken from
+//     a shared counter, the 32 subcolumns of a row in one warp (32
+//     consecutive g-points: coalesced table reads).
+//   adding warp (1): per tile, the vertical adding method of vrtqdr_sw
+//     (rrtmg_sw_vrtqdr.f90:122-169), one lane per subcolumn: up-sweep from
+//     the surface (upward albedos kept in shared memory), down-sweep with the
+//     weighted level fluxes written into the tile slots it has just read;
+//     then the g-point sums of spcvmc_sw (:607-655), one lane per level, off
+//     the sweeps' dependency chain.
+//   FP64 warp (1): redoes in FP64 the cells whose FP32 discrete choices
+//     (transmittance table entry, conservative switch, resonance) are too
+//     close to call, for the whole pair at once (FP64 runs at a small
+//     fraction of the FP32 rate, so its cells are processed 32 at a time).
+//
+// A subcolumn with such a cell is left out of its tile's sums; its R/T
+// column is copied aside (global, per CTA) and swept again with the FP64
+// cells once the FP64 warp is done, its contribution added before the
+// pair's outputs are written (one pair later, so the wait is hidden).
+// Handoffs use mbarriers (tile full / empty, pair done, pair redone) whose
+// waits give up after ~2^33 cycles with an error code instead of hanging.
+// A pair with more such cells than the capacities below is listed for the
+// caller, which solves it again with the scratch-based kernel
+// (k_solve<float>).
+#pragma once
+
+#include "kernel.cuh"
+
+#ifndef RRSW_TILED_OPT
+#define RRSW_TILED_OPT 14
+#endif
+
+namespace rrsw {
+
+constexpr int TW = 32;                                   // subcolumns per tile
+constexpr int TILES = COLS_PER_CTA * NGPT / TW;          // 7 tiles per pair
+constexpr int T_OPT = RRSW_TILED_OPT;                    // optics warps
+constexpr int T_REDO = T_OPT;                            // FP64 warp index
+constexpr int T_ADD = T_OPT + 1;                         // adding warp index
+constexpr int T_THREADS = (T_OPT + 2) * 32;
+constexpr int T_QCAP = 128;                              // FP64 cells per pair
+constexpr int T_RCAP = 64;                               // subcolumns with such cells per pair
+constexpr int T_NF = 10;                                 // tile fields per cell
+constexpr int T_MAXL = 64;                               // layers (two mask words per subcolumn)
+enum { TF_REFC, TF_REFDC, TF_ADIRC, TF_ADIFC, TF_DBTC, TF_REF, TF_REFD, TF_ADIR, TF_ADIF, TF_DBT };
+enum { TB_FULL0, TB_FULL1, TB_EMPTY0, TB_EMPTY1, TB_PAIR0, TB_PAIR1, TB_REDO0, TB_REDO1, TB_N };
+// control words in shared memory
+enum { TC_ROW0, TC_ROW1, TC_QN0, TC_QN1, TC_RN0, TC_RN1, TC_ABORT, TC_LT0, TC_LT1, TC_ACT0, TC_ACT1,
+       TC_OVF0, TC_OVF1, TC_N };
+
+// Shared-memory carve-up of the tiled kernel; the host sizes the launch with
+// the same function.
+struct TSmem {
+    size_t bar, ctl, tm, tile, rup, coef, pk, hrf, mu, cld, mask, kc, ka, omcf, seed, sub, risky, queue, recof,
+        flux, scr, total;
+};
+
+__host__ __device__ inline TSmem tiled_smem(int L, int nq, bool fused, bool cloud_stage) {
+    TSmem m;
+    size_t o = 0;
+    m.bar = o;   o = align16(o + TB_N * sizeof(unsigned long long));
+    m.ctl = o;   o = align16(o + TC_N * sizeof(int));
+    m.tm = o;    o = align16(o + NBND * 2 * sizeof(TmSmem));
+    m.tile = o;  o = align16(o + (size_t)2 * T_NF * L * TW * sizeof(float));
+    m.rup = o;   o = align16(o + (size_t)4 * L * TW * sizeof(float));
+    m.coef = o;  o = align16(o + (size_t)COLS_PER_CTA * NFR * L * sizeof(float));
+    m.pk = o;    o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(int));
+    m.hrf = o;   o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(float));
+    m.mu = o;    o = align16(o + (size_t)COLS_PER_CTA * sizeof(float));
+    m.cld = m.mask = m.kc = m.ka = m.omcf = m.seed = o;
+    if (cloud_stage) { m.cld = o; o = align16(o + (size_t)COLS_PER_CTA * 4 * L * sizeof(float)); }
+    if (fused) {
+        m.mask = o; o = align16(o + (size_t)COLS_PER_CTA * NGPT * 2 * sizeof(uint32_t));
+        m.kc = o;   o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(long long));
+        m.ka = o;   o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(long long));
+        m.omcf = o; o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(double));
+        m.seed = o; o = align16(o + (size_t)COLS_PER_CTA * 4 * sizeof(uint32_t));
+    }
+    m.sub = o;   o = align16(o + (size_t)2 * 3 * COLS_PER_CTA * NGPT * sizeof(float));   // [par][zinc,albp,albd][224]
+    m.risky = o; o = align16(o + (size_t)2 * TILES * sizeof(uint32_t));
+    m.queue = o; o = align16(o + (size_t)2 * T_QCAP * sizeof(int));
+    m.recof = o; o = align16(o + (size_t)2 * COLS_PER_CTA * NGPT * sizeof(short));
+    m.flux = o;  o = align16(o + (size_t)2 * COLS_PER_CTA * nq * (L + 1) * sizeof(float));
+    // adding warp: surface-level sums and lane keys of a tile, reduction
+    // scratch of the set-aside subcolumns (rows 6-7 hold 64-bit keys)
+    m.scr = o;   o = align16(o + (size_t)16 * TW * sizeof(float));
+    m.total = o;
+    return m;
+}
+
+// Per-CTA global area of the tiled kernel (bytes): KISS jump columns, the
+// aerosol staged in FP32, and per pair parity the FP64 layer coefficients,
+// the layer thicknesses, the FP64 cells and the set-aside subcolumns.
+struct TGlob {
+    size_t xs, aer, par, coef64, pk, lt, pdp, corr, rec, rec_stride, par_stride, total;
+};
+
+__host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+__host__ __device__ inline TGlob tiled_glob(int L) {
+    TGlob g;
+    size_t o = 0;
+    g.xs = o;   o = align256(o + (size_t)NGPT * 32 * sizeof(uint32_t));
+    g.aer = o;  o = align256(o + (size_t)COLS_PER_CTA * 3 * NBND * L * sizeof(float));
+    g.par = o;
+    size_t p = 0;
+    g.coef64 = p; p = align256(p + (size_t)COLS_PER_CTA * NFR * L * sizeof(double));
+    g.pk = p;     p = align256(p + (size_t)COLS_PER_CTA * L * sizeof(int));
+    g.lt = p;     p = align256(p + (size_t)COLS_PER_CTA * sizeof(int));
+    g.pdp = p;    p = align256(p + (size_t)COLS_PER_CTA * L * sizeof(double));
+    g.corr = p;   p = align256(p + (size_t)T_QCAP * T_NF * sizeof(float));
+    // record: s, column slot, zinc, albp, albd, pad[3], then T_NF x L fields
+    g.rec_stride = align256((8 + (size_t)T_NF * L) * sizeof(float));
+    g.rec = p;    p = align256(p + (size_t)T_RCAP * g.rec_stride);
+    g.par_stride = p;
+    o += 2 * p;
+    g.total = o;
+    return g;
+}
+
+// ------------------------------------------------------------- mbarriers
+__device__ inline uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ inline void mbar_init(unsigned long long* b, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+
+__device__ inline void mbar_arrive(unsigned long long* b) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_addr(b))
+                 : "memory");
+}
+
+__device__ inline bool mbar_test(unsigned long long* b, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for the completion of the phase of parity `parity`.  Gives up after
+// ~2^33 cycles (seconds; a tile takes microseconds): records E_TIMEOUT and
+// the CTA's abort flag, after which every later wait returns at once, so a
+// fault in the handoff ends the kernel with an error instead of a hang.
+__device__ inline void mbar_wait(unsigned long long* b, unsigned parity, volatile int* abort, int* err) {
+    if (*abort) return;
+    const long long t0 = clock64();
+    while (!mbar_test(b, parity)) {
+        if (*abort) return;
+        if (clock64() - t0 > (1ll << 33)) {
+            *abort = 1;
+            set_error(err, E_TIMEOUT);
+            return;
+        }
+    }
+}
+
+// named barrier of the optics warps only
+__device__ inline void opt_sync() { asm volatile("bar.sync 1, %0;" ::"n"(T_OPT * 32) : "memory"); }
+
+// ------------------------------------------------------------- helpers
+struct TileView {
+    unsigned long long* bar;
+    int* ctl;
+    const TmSmem* tm;
+    float* tile;      // [2][T_NF][L][TW]
+    float* rup;       // [4][L][TW]
+    float* coef;      // [2][NFR][L]
+    int* pk;          // [2][L]
+    float* hrf;       // [2][L]
+    float* mu;        // [2]
+    float* cld;       // [2][4][L]
+    uint32_t* mask;   // [224][2]
+    long long* kc;    // [2][L]
+    long long* ka;    // [2][L]
+    double* omcf;     // [2][L]
+    uint32_t* seed;   // [2][4]
+    float* sub;       // [2][3][224]
+    uint32_t* risky;  // [2][TILES]
+    int* queue;       // [2][T_QCAP]
+    short* recof;     // [2][224]
+    float* flux;      // [2][2][NQ][L+1]
+    float* scr;       // [16][TW]
+};
+
+__device__ inline TileView tile_view(unsigned char* raw, const TSmem& M) {
+    TileView v;
+    v.bar = (unsigned long long*)(raw + M.bar);
+    v.ctl = (int*)(raw + M.ctl);
+    v.tm = (const TmSmem*)(raw + M.tm);
+    v.tile = (float*)(raw + M.tile);
+    v.rup = (float*)(raw + M.rup);
+    v.coef = (float*)(raw + M.coef);
+    v.pk = (int*)(raw + M.pk);
+    v.hrf = (float*)(raw + M.hrf);
+    v.mu = (float*)(raw + M.mu);
+    v.cld = (float*)(raw + M.cld);
+    v.mask = (uint32_t*)(raw + M.mask);
+    v.kc = (long long*)(raw + M.kc);
+    v.ka = (long long*)(raw + M.ka);
+    v.omcf = (double*)(raw + M.omcf);
+    v.seed = (uint32_t*)(raw + M.seed);
+    v.sub = (float*)(raw + M.sub);
+    v.risky = (uint32_t*)(raw + M.risky);
+    v.queue = (int*)(raw + M.queue);
+    v.recof = (short*)(raw + M.recof);
+    v.flux = (float*)(raw + M.flux);
+    v.scr = (float*)(raw + M.scr);
+    return v;
+}
+
+// tile field f of layer index i (0 = surface layer), lane l
+__device__ inline float& tfield(float* tb, int L, int f, int i, int l) { return tb[((size_t)f * L + i) * TW + l]; }
+
+// ---------------------------------------------------------- adding method
+// State of the down-sweep of one subcolumn, clear and total sky, plus the
+// absorption of the layer above the current level for the heating rate.
+struct DownState {
+    float tdbtc, tdnc, rdndc, tdbt, tdn, rdnd;
+    float absc, abst, adifc_up, adift_up;
+};
+
+__device__ inline void down_init(DownState& s) {
+    s.tdbtc = s.tdnc = s.tdbt = s.tdn = 1.0f;
+    s.rdndc = s.rdnd = 0.0f;
+    s.absc = s.abst = s.adifc_up = s.adift_up = 0.0f;
+}
+
+// Fluxes at a level whose upward albedos (below it) are rupc..rupd (vrtqdr:
+// 163-169), weighted by zinc: q = fu, fd, cu, cd, direct total / clear,
+// absorption of the layer above the level (total, clear; its lower face's
+// upward flux added here).  cdif / fdif are returned for the layer step.
+__device__ inline void level_q(const DownState& s, float rupc, float rupdc, float rup, float rupd, float zinc,
+                               float* q, float& cdif, float& fdif) {
+    const float zrc = 1.0f / (1.0f - s.rdndc * rupdc);
+    const float cu = (s.tdbtc * rupc + (s.tdnc - s.tdbtc) * rupdc) * zrc;
+    cdif = (s.tdnc - s.tdbtc + s.tdbtc * rupc * s.rdndc) * zrc;
+    const float cd = s.tdbtc + cdif;
+    const float zrt = 1.0f / (1.0f - s.rdnd * rupd);
+    const float fu = (s.tdbt * rup + (s.tdn - s.tdbt) * rupd) * zrt;
+    fdif = (s.tdn - s.tdbt + s.tdbt * rup * s.rdnd) * zrt;
+    const float fd = s.tdbt + fdif;
+    q[0] = zinc * fu;
+    q[1] = zinc * fd;
+    q[2] = zinc * cu;
+    q[3] = zinc * cd;
+    q[4] = zinc * s.tdbt;
+    q[5] = zinc * s.tdbtc;
+    q[6] = zinc * (s.abst + fu * s.adift_up);
+    q[7] = zinc * (s.absc + cu * s.adifc_up);
+}
+
+// Through one layer downward (vrtqdr:144-159, direct beam spcvmc:575-585);
+// the layer's absorption is carried to the next level.
+__device__ inline void layer_down(DownState& s, const float* f, float cdif, float fdif) {
+    const float refc = f[TF_REFC], refdc = f[TF_REFDC], adirc = f[TF_ADIRC], adifc = f[TF_ADIFC], dbtc = f[TF_DBTC];
+    const float ref = f[TF_REF], refd = f[TF_REFD], adirt = f[TF_ADIR], adift = f[TF_ADIF], dbt = f[TF_DBT];
+    const float trac = 1.0f - refc - adirc, tradc = 1.0f - refdc - adifc;
+    const float tra = 1.0f - ref - adirt, trad = 1.0f - refd - adift;
+    s.abst = s.tdbt * adirt + fdif * adift;
+    s.absc = s.tdbtc * adirc + cdif * adifc;
+    s.adift_up = adift;
+    s.adifc_up = adifc;
+    const float zr1 = 1.0f / (1.0f - refdc * s.rdndc);
+    const float tdnc_n = s.tdbtc * trac + (tradc * ((s.tdnc - s.tdbtc) + s.tdbtc * refc * s.rdndc)) * zr1;
+    s.rdndc = refdc + tradc * tradc * s.rdndc * zr1;
+    s.tdnc = tdnc_n;
+    const float zr2 = 1.0f / (1.0f - refd * s.rdnd);
+    const float tdn_n = s.tdbt * tra + (trad * ((s.tdn - s.tdbt) + s.tdbt * ref * s.rdnd)) * zr2;
+    s.rdnd = refd + trad * trad * s.rdnd * zr2;
+    s.tdn = tdn_n;
+    s.tdbtc = dbtc * s.tdbtc;
+    s.tdbt = dbt * s.tdbt;
+}
+
+// One up-sweep step through a layer (vrtqdr:122-140).
+__device__ inline void up_step(const float* f, float& rupc, float& rupdc, float& rup, float& rupd) {
+    {
+        const float ref = f[TF_REFC], refd = f[TF_REFDC], dbt = f[TF_DBTC];
+        const float tra = 1.0f - ref - f[TF_ADIRC], trad = 1.0f - refd - f[TF_ADIFC];
+        const float zr = 1.0f / (1.0f - rupdc * refd);
+        const float r = ref + (trad * ((tra - dbt) * rupdc + dbt * rupc)) * zr;
+        rupdc = refd + trad * trad * rupdc * zr;
+        rupc = r;
+    }
+    {
+        const float ref = f[TF_REF], refd = f[TF_REFD], dbt = f[TF_DBT];
+        const float tra = 1.0f - ref - f[TF_ADIR], trad = 1.0f - refd - f[TF_ADIF];
+        const float zr = 1.0f / (1.0f - rupd * refd);
+        const float r = ref + (trad * ((tra - dbt) * rupd + dbt * rup)) * zr;
+        rupd = refd + trad * trad * rupd * zr;
+        rup = r;
+    }
+}
+
+// ------------------------------------------------------------ the kernel
+struct TCtx {
+    TileView V;
+    TGlob G;
+    unsigned char* glob;  // this CTA's global area
+    int L, nmapped, qcap, nlocal;
+    bool fused, nomc, cstage;
+    volatile int* abort;
+};
+
+__device__ inline unsigned char* tpar(const TCtx& X, int par) {
+    return X.glob + X.G.par + (size_t)par * X.G.par_stride;
+}
+__device__ inline float* trec(const TCtx& X, int par, int r) {
+    return (float*)(tpar(X, par) + X.G.rec + (size_t)r * X.G.rec_stride);
+}
+__device__ inline int tpair(int lp) { return blockIdx.x + lp * gridDim.x; }
+
+// ---- optics warps: per-pair preparation.  setcoef (FP64, explicit
+// roundings) into shared memory and its FP64 copy for the FP64 warp, McICA
+// thresholds, cloud and aerosol inputs; then per column laytrop; then per
+// subcolumn the solar source, the albedos and the McICA mask bits.
+template <bool MT>
+__device__ void tiled_prep(const SolveParams& P, const TCtx& X, int lp, const KissJump& J,
+                           const double* __restrict__ tab64, const float* __restrict__ tab) {
+    const TileView& V = X.V;
+    const int L = X.L, par = lp & 1, pair = tpair(lp), otid = threadIdx.x;
+    const size_t n = (size_t)P.ncol;
+    unsigned char* pb = tpar(X, par);
+    double* coef64 = (double*)(pb + X.G.coef64);
+    int* pkg = (int*)(pb + X.G.pk);
+    int* ltg = (int*)(pb + X.G.lt);
+    double* pdpg = (double*)(pb + X.G.pdp);
+    float* aer = (float*)(X.glob + X.G.aer);
+    for (int it = otid; it < COLS_PER_CTA * L; it += T_OPT * 32) {
+        const int c2 = it / L, lay = it % L + 1, i = lay - 1;
+        const int pcol = pair_col(P, pair, c2, X.nmapped);
+        prep_layer<float>(P, pcol, lay, V.coef + c2 * NFR * L, V.pk + c2 * L, pdpg + c2 * L, L, tab64,
+                          coef64 + c2 * NFR * L);
+        pkg[c2 * L + i] = V.pk[c2 * L + i];
+        V.hrf[c2 * L + i] = (float)(cT.heatfac / pdpg[c2 * L + i]);
+        const bool real = pcol < P.ncol;
+        const size_t kl = (size_t)pcol + n * (size_t)i;
+        if (X.fused) {
+            double cf = real ? P.cldfrac[kl] : 0.0;
+            if (cf < 1.0e-20) cf = 0.0;
+            const double omcf = DS(1.0, cf);
+            V.omcf[c2 * L + i] = omcf;
+            if constexpr (MT) {
+                V.kc[c2 * L + i] = mt_threshold(omcf);
+                V.ka[c2 * L + i] = (P.icld >= 4 && real) ? mt_threshold(P.alpha[kl]) : 0ll;
+            } else {
+                V.kc[c2 * L + i] = kiss_threshold(omcf);
+                V.ka[c2 * L + i] = (P.icld >= 4 && real) ? kiss_threshold(P.alpha[kl]) : 0ll;
+            }
+            if (lay == 1) {
+                uint32_t* sd = V.seed + c2 * 4;
+                if (real && !MT) {
+                    const double p1 = DM(P.play[pcol], 1.e2), p2 = DM(P.play[pcol + n], 1.e2);
+                    if (p1 < p2) set_error(P.err, E_KISSSEED);
+                    sd[0] = kiss_seed(p1);
+                    sd[1] = kiss_seed(p2);
+                    sd[2] = kiss_seed(DM(P.play[pcol + 2 * n], 1.e2));
+                    sd[3] = kiss_seed(DM(P.play[pcol + 3 * n], 1.e2));
+                } else {
+                    sd[0] = sd[1] = sd[2] = sd[3] = 1u;
+                }
+            }
+        }
+        if (X.nomc) {
+            // spcvrt_sw takes clear or overcast layers only (rrtmg_sw_rad.nomcica.f90:617-621)
+            const double cf = real ? P.cldfrac[kl] : 0.0;
+            if (cf > 1.e-6 && cf < 1.0 - 1.e-6) set_error(P.err, E_PARTIAL);
+        }
+        if (X.cstage) {
+            float* cd = V.cld + c2 * 4 * L;
+            cd[0 * L + i] = real ? (float)P.ciwp[kl] : 0.0f;
+            cd[1 * L + i] = real ? (float)P.clwp[kl] : 0.0f;
+            cd[2 * L + i] = real ? (float)P.rei[kl] : 0.0f;
+            cd[3 * L + i] = real ? (float)P.rel[kl] : 0.0f;
+        }
+        if (P.iaer != 0) {
+            for (int b = 0; b < NBND; ++b) {
+                double ta = 0.0, oa = 1.0, ga = 0.0;
+                if (real) aerosol(P, pcol, lay, b, tab64, ta, oa, ga);
+                float* ad = aer + c2 * 3 * NBND * L;
+                ad[(0 * NBND + b) * L + i] = (float)ta;
+                ad[(1 * NBND + b) * L + i] = (float)DS(1.0, oa);  // co-albedo, formed in FP64
+                ad[(2 * NBND + b) * L + i] = (float)ga;
+            }
+        }
+    }
+    opt_sync();
+    if (otid < COLS_PER_CTA) {
+        const int c2 = otid;
+        int lt = 0;
+        for (int i = 0; i < L; ++i) lt += (V.pk[c2 * L + i] >> 30) & 1;
+        const int pcol = pair_col(P, pair, c2, X.nmapped);
+        int act = pcol < P.ncol;
+        if (act && (lt < 1 || lt >= L)) {
+            set_error(P.err, E_LAYTROP);
+            act = 0;
+        }
+        V.ctl[TC_LT0 + c2] = lt;
+        V.ctl[TC_ACT0 + c2] = act;
+        ltg[c2] = lt;
+        double cz = act ? P.coszen[pcol] : 1.0;
+        if (cz < 1.e-10) cz = 1.e-10;
+        V.mu[c2] = (float)cz;
+    }
+    opt_sync();
+    if (otid < COLS_PER_CTA * NGPT) {
+        const int s = otid, c2 = s / NGPT, g = s % NGPT;
+        const int ib = cT.ngb[g], igb = cT.gib[g];
+        const int pcol = pair_col(P, pair, c2, X.nmapped);
+        const bool act = V.ctl[TC_ACT0 + c2] != 0;
+        float zinc = 0.0f, albp = 0.0f, albd = 0.0f;
+        if (act) {
+            const bool nir = ib <= 8 || ib == 13;
+            albp = (float)(nir ? P.aldir[pcol] : P.asdir[pcol]);
+            albd = (float)(nir ? P.aldif[pcol] : P.asdif[pcol]);
+            const Coef<float> C{V.coef + c2 * NFR * L, V.pk + c2 * L, L, V.ctl[TC_LT0 + c2]};
+            // zincflx = adjflux * ssi * prmu0 (spcvmc:349-356)
+            const float src = solar_source_generic(ib, igb, C, P, tab, V.tm);
+            zinc = float(P.adjflux[ib]) * src * V.mu[c2];
+        }
+        float* sub = V.sub + par * 3 * COLS_PER_CTA * NGPT;
+        sub[s] = zinc;
+        sub[COLS_PER_CTA * NGPT + s] = albp;
+        sub[2 * COLS_PER_CTA * NGPT + s] = albd;
+        if (X.fused) {
+            uint32_t w0 = 0u, w1 = 0u;
+            if (act) {
+                McicaMask<MT> mc;
+                Kiss k0{1u, 1u, 1u, 1u};
+                if constexpr (!MT) k0 = kiss_start(V.seed + c2 * 4, J, (const uint32_t*)(X.glob + X.G.xs) + g * 32);
+                mc.start(k0, P.icld, MT ? P.mt + mt_offset(P.icld, g, pcol, P.ncol, L) : nullptr);
+                for (int lay = 1; lay <= L; ++lay) {
+                    const int i = lay - 1;
+                    if (mc.step(lay, V.kc[c2 * L + i], V.ka[c2 * L + i], V.omcf[c2 * L + i])) {
+                        if (i < 32) w0 |= 1u << i;
+                        else w1 |= 1u << (i - 32);
+                    }
+                }
+            }
+            V.mask[s * 2] = w0;
+            V.mask[s * 2 + 1] = w1;
+        }
+    }
+    opt_sync();
+}
+
+// ---- optics warps: the cells of tile t of pair lp into buffer b
+__device__ void tiled_optics(const SolveParams& P, const TCtx& X, int lp, int t, int b,
+                             const float* __restrict__ tab, const double* __restrict__ tab64) {
+    const TileView& V = X.V;
+    const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
+    float* tb = V.tile + (size_t)b * T_NF * L * TW;
+    const int s = TW * t + lane, c2 = s / NGPT, g = s % NGPT;
+    const int ib = cT.ngb[g], igb = cT.gib[g];
+    const int pcol = pair_col(P, pair, c2, X.nmapped);
+    const bool act = V.ctl[TC_ACT0 + c2] != 0;
+    const Coef<float> C{V.coef + c2 * NFR * L, V.pk + c2 * L, L, V.ctl[TC_LT0 + c2]};
+    const float zinc = V.sub[par * 3 * COLS_PER_CTA * NGPT + s];
+    const float mu = V.mu[c2];
+    const float* aer = (const float*)(X.glob + X.G.aer) + c2 * 3 * NBND * L;
+    const float* cld = X.cstage ? V.cld + c2 * 4 * L : nullptr;
+    while (true) {
+        int r = 0;
+        if (lane == 0) r = atomicAdd(&V.ctl[TC_ROW0 + b], 1);
+        r = __shfl_sync(0xffffffffu, r, 0);
+        if (r >= L) break;
+        const int lay = r + 1;
+        float f[T_NF] = {0.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 0.f, 1.f};
+        if (act) {
+            float taug, taur, fs;
+            int js;
+            taumol_generic(ib, igb, lay, C, tab, V.tm, taug, taur, js, fs);
+            CellIn<float> ci;
+            ci.taug = taug;
+            ci.taur = taur;
+            if (P.iaer != 0) {
+                ci.rta = aer[(0 * NBND + ib) * L + r];
+                ci.rcoa = aer[(1 * NBND + ib) * L + r];
+                ci.roa = 1.0f - ci.rcoa;
+                ci.rga = aer[(2 * NBND + ib) * L + r];
+            } else {
+                ci.rta = 0.0f; ci.roa = 1.0f; ci.rga = 0.0f; ci.rcoa = 0.0f;
+            }
+            bool cloudy = false;
+            if (X.fused) cloudy = (V.mask[s * 2 + (r >> 5)] >> (r & 31)) & 1u;
+            cloud_in<float>(P, pcol, g, lay, ib, X.fused, cloudy, cld, ci, tab);
+            const float hrs = zinc * V.hrf[c2 * L + r];
+            const CellOpt<float> co = cell_optics<float>(ci, 1, mu, tab, tab64, hrs);
+            f[TF_REFC] = co.rc.ref; f[TF_REFDC] = co.rc.refd; f[TF_ADIRC] = co.rc.adir; f[TF_ADIFC] = co.rc.adif;
+            f[TF_DBTC] = co.zdbtc;
+            f[TF_REF] = co.rt.ref; f[TF_REFD] = co.rt.refd; f[TF_ADIR] = co.rt.adir; f[TF_ADIF] = co.rt.adif;
+            f[TF_DBT] = co.zdbt;
+            if (co.risky) {
+                // an FP32 choice too close to call: the FP64 warp redoes the
+                // cell, and the subcolumn is swept apart from its tile
+                const int q = atomicAdd(&V.ctl[TC_QN0 + par], 1);
+                if (q < X.qcap) V.queue[par * T_QCAP + q] = (s << 12) | (lay << 1) | (ci.cloudy ? 1 : 0);
+                atomicOr(&V.risky[par * TILES + t], 1u << lane);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < T_NF; ++k) tfield(tb, L, k, r, lane) = f[k];
+    }
+}
+
+// ---- FP64 warp: the pair's queued cells, 32 at a time
+__device__ void tiled_redo(const SolveParams& P, const TCtx& X, int lp, const double* __restrict__ tab64) {
+    const TileView& V = X.V;
+    const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
+    unsigned char* pb = tpar(X, par);
+    const double* coef64 = (const double*)(pb + X.G.coef64);
+    const int* pkg = (const int*)(pb + X.G.pk);
+    const int* ltg = (const int*)(pb + X.G.lt);
+    float* corr = (float*)(pb + X.G.corr);
+    const int qn = min(V.ctl[TC_QN0 + par], X.qcap);
+    for (int k = lane; k < qn; k += 32) {
+        const int e = V.queue[par * T_QCAP + k];
+        const int s = e >> 12, lay = (e >> 1) & 127, c2 = s / NGPT, g = s % NGPT;
+        const int pcol = pair_col(P, pair, c2, X.nmapped);
+        const Coef<double> C64{coef64 + c2 * NFR * L, pkg + c2 * L, L, ltg[c2]};
+        double cz = P.coszen[pcol];
+        if (cz < 1.e-10) cz = 1.e-10;
+        const CellOpt<float> co =
+            cell_optics_fp64(P, C64, pcol, g, lay, cT.ngb[g], cT.gib[g], X.fused, (e & 1) != 0, cz, tab64);
+        float* o = corr + k * T_NF;
+        o[TF_REFC] = co.rc.ref; o[TF_REFDC] = co.rc.refd; o[TF_ADIRC] = co.rc.adir; o[TF_ADIFC] = co.rc.adif;
+        o[TF_DBTC] = co.zdbtc;
+        o[TF_REF] = co.rt.ref; o[TF_REFD] = co.rt.refd; o[TF_ADIR] = co.rt.adir; o[TF_ADIF] = co.rt.adif;
+        o[TF_DBT] = co.zdbt;
+    }
+}
+
+// ---- adding warp: the vertical sweeps of tile t (buffer b) of pair lp
+template <int NQ>
+__device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, int b) {
+    const TileView& V = X.V;
+    const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
+    const size_t n = (size_t)P.ncol, L1 = (size_t)L + 1;
+    float* tb = V.tile + (size_t)b * T_NF * L * TW;
+    const int s = TW * t + lane, c2 = s / NGPT, g = s % NGPT;
+    const int ib = cT.ngb[g];
+    const bool uv = ib >= 9 && ib <= 12;  // bands 25-28 (spcvmc:629)
+    const float* sub = V.sub + par * 3 * COLS_PER_CTA * NGPT;
+    const float zinc = sub[s], albp = sub[COLS_PER_CTA * NGPT + s], albd = sub[2 * COLS_PER_CTA * NGPT + s];
+    const bool act = V.ctl[TC_ACT0 + c2] != 0;
+    const bool risky = (V.risky[par * TILES + t] >> lane) & 1u;
+    const bool use = act && !risky;
+    float* R = V.rup;
+    // up-sweep from the surface (vrtqdr:122-140), the next layer's fields
+    // loaded while this one is swept
+    float rupc = albp, rupdc = albd, rup = albp, rupd = albd;
+    float f[T_NF], fn[T_NF];
+#pragma unroll
+    for (int k = 0; k < T_NF; ++k) f[k] = tfield(tb, L, k, 0, lane);
+    for (int i = 0; i < L; ++i) {
+        const int in = i + 1 < L ? i + 1 : i;
+#pragma unroll
+        for (int k = 0; k < T_NF; ++k) fn[k] = tfield(tb, L, k, in, lane);
+        up_step(f, rupc, rupdc, rup, rupd);
+        R[(0 * L + i) * TW + lane] = rupc;
+        R[(1 * L + i) * TW + lane] = rupdc;
+        R[(2 * L + i) * TW + lane] = rup;
+        R[(3 * L + i) * TW + lane] = rupd;
+#pragma unroll
+        for (int k = 0; k < T_NF; ++k) f[k] = fn[k];
+    }
+    // subcolumns with FP64 cells: their R/T column is set aside for the
+    // pair's second sweep, and they stay out of this tile's sums
+    const unsigned rm = __ballot_sync(0xffffffffu, act && risky);
+    if (rm) {
+        const int base = V.ctl[TC_RN0 + par];
+        const int idx = base + __popc(rm & ((1u << lane) - 1u));
+        if (act && risky && idx < T_RCAP) {
+            float* rp = trec(X, par, idx);
+            rp[0] = (float)s;
+            rp[1] = (float)c2;
+            rp[2] = zinc;
+            rp[3] = albp;
+            rp[4] = albd;
+            for (int k = 0; k < T_NF; ++k)
+                for (int i = 0; i < L; ++i) rp[8 + k * L + i] = tfield(tb, L, k, i, lane);
+            V.recof[par * COLS_PER_CTA * NGPT + s] = (short)idx;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            const int nb = base + __popc(rm);
+            V.ctl[TC_RN0 + par] = nb;
+            if (nb > T_RCAP) V.ctl[TC_OVF0 + par] = 1;
+        }
+        __syncwarp();
+    }
+    // down-sweep: the 8 weighted fluxes of level i+1 replace the fields of
+    // layer i, which were read just before (level 0, the surface, goes to scr)
+    DownState st;
+    down_init(st);
+    float q[8], rr[4], rn[4];
+#pragma unroll
+    for (int k = 0; k < T_NF; ++k) f[k] = tfield(tb, L, k, L - 1, lane);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) rr[k] = R[(k * L + L - 1) * TW + lane];
+    for (int i = L - 1; i >= 0; --i) {
+        const int in = i > 0 ? i - 1 : 0;
+#pragma unroll
+        for (int k = 0; k < T_NF; ++k) fn[k] = tfield(tb, L, k, in, lane);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) rn[k] = R[(k * L + in) * TW + lane];
+        float cdif, fdif;
+        level_q(st, rr[0], rr[1], rr[2], rr[3], zinc, q, cdif, fdif);
+        layer_down(st, f, cdif, fdif);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) tfield(tb, L, k, i, lane) = use ? q[k] : 0.0f;
+#pragma unroll
+        for (int k = 0; k < T_NF; ++k) f[k] = fn[k];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) rr[k] = rn[k];
+    }
+    {
+        float cdif, fdif;
+        level_q(st, albp, albd, albp, albd, zinc, q, cdif, fdif);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) V.scr[k * TW + lane] = use ? q[k] : 0.0f;
+    int* key = (int*)(V.scr + 8 * TW);
+    key[lane] = c2 * 16 + ib;
+    const unsigned uvm = __ballot_sync(0xffffffffu, uv);
+    __syncwarp();
+    // g-point sums, one lane per level; lanes of the tile's two columns (tile
+    // 3 holds the end of column 0 and the start of column 1) summed apart
+    const int c0 = (TW * t) / NGPT;
+    const int cb = ((TW * t + TW - 1) / NGPT == c0) ? TW : NGPT * (c0 + 1) - TW * t;  // first lane of column 1
+    for (int v = lane; v <= L; v += 32) {
+        const float* src = v ? tb + (size_t)(v - 1) * TW : V.scr;
+        const int stride = v ? L * TW : TW;
+        float a0[8], a1[8], e0[8], e1[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a0[k] = a1[k] = e0[k] = e1[k] = 0.0f;
+        for (int m = 0; m < TW; ++m) {
+            const int j = (m + lane) & 31;  // rotated: the lanes read 32 different banks
+            const bool lo = j < cb;
+            const bool u = (uvm >> j) & 1u;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const float x = src[k * stride + j];
+                if (lo) a0[k] += x;
+                else a1[k] += x;
+            }
+            if constexpr (NQ > 8) {
+                // UV (bands 25-28) / near-IR split of fd, cd and the direct fluxes
+                const float x1 = src[1 * stride + j], x3 = src[3 * stride + j];
+                const float x4 = src[4 * stride + j], x5 = src[5 * stride + j];
+                const int o = u ? 0 : 4;
+                float* e = lo ? e0 : e1;
+                e[o] += x1; e[o + 1] += x3; e[o + 2] += x4; e[o + 3] += x5;
+            }
+        }
+        float* F0 = V.flux + ((size_t)(par * COLS_PER_CTA + c0) * NQ) * L1;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) F0[k * L1 + v] += a0[k];
+        if constexpr (NQ > 8) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) F0[(8 + k) * L1 + v] += e0[k];
+        }
+        if (cb < TW) {
+            float* F1 = F0 + (size_t)NQ * L1;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) F1[k * L1 + v] += a1[k];
+            if constexpr (NQ > 8) {
+#pragma unroll
+                for (int k = 0; k < 8; ++k) F1[(8 + k) * L1 + v] += e1[k];
+            }
+        }
+        if (P.bands) {
+            // per-band fluxes (the band loop of spcvmc:619-630): lanes of one
+            // (column, band) in order, added to the FP64 outputs (zeroed at
+            // the pair's first tile)
+            const int qb[5] = {0, 1, 4, 2, 3};  // fu, fd, fddir, cu, cd
+            int j = 0;
+            while (j < TW) {
+                const int kj = key[j];
+                float a[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+                int e = j;
+                for (; e < TW && key[e] == kj; ++e)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) a[k] += src[qb[k] * stride + e];
+                const int pc = pair_col(P, pair, kj >> 4, X.nmapped);
+                if (pc < P.ncol) {
+                    const size_t idx = (size_t)pc + n * ((size_t)v + L1 * (size_t)(kj & 15));
+#pragma unroll
+                    for (int k = 0; k < 5; ++k)
+                        if (P.bout[k]) P.bout[k][idx] += (double)a[k];
+                }
+                j = e;
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// ---- adding warp: sweeps of the set-aside subcolumns r0 .. r0+31 of pair lp
+// (their FP64 cells already patched in), added to the pair's level sums
+template <int NQ>
+__device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r0, int rn) {
+    const TileView& V = X.V;
+    const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
+    const size_t n = (size_t)P.ncol, L1 = (size_t)L + 1;
+    const int r = r0 + lane;
+    const bool on = r < rn;
+    const float* rp = trec(X, par, on ? r : r0);
+    const int s = (int)rp[0], c2 = (int)rp[1], g = s % NGPT, ib = cT.ngb[g];
+    const bool uv = ib >= 9 && ib <= 12;
+    const float zinc = on ? rp[2] : 0.0f, albp = rp[3], albd = rp[4];
+    const int pcol = pair_col(P, pair, c2, X.nmapped);
+    const float* fl = rp + 8;
+    float* R = V.rup;
+    float rupc = albp, rupdc = albd, rup = albp, rupd = albd;
+    for (int i = 0; i < L; ++i) {
+        float f[T_NF];
+#pragma unroll
+        for (int k = 0; k < T_NF; ++k) f[k] = fl[k * L + i];
+        up_step(f, rupc, rupdc, rup, rupd);
+        R[(0 * L + i) * TW + lane] = rupc;
+        R[(1 * L + i) * TW + lane] = rupdc;
+        R[(2 * L + i) * TW + lane] = rup;
+        R[(3 * L + i) * TW + lane] = rupd;
+    }
+    const unsigned m0 = __ballot_sync(0xffffffffu, on && c2 == 0);
+    const unsigned m1 = __ballot_sync(0xffffffffu, on && c2 == 1);
+    DownState st;
+    down_init(st);
+    float q[16];
+    for (int i = L - 1; i >= -1; --i) {
+        float cdif, fdif;
+        if (i >= 0) {
+            float f[T_NF];
+#pragma unroll
+            for (int k = 0; k < T_NF; ++k) f[k] = fl[k * L + i];
+            level_q(st, R[(0 * L + i) * TW + lane], R[(1 * L + i) * TW + lane], R[(2 * L + i) * TW + lane],
+                    R[(3 * L + i) * TW + lane], zinc, q, cdif, fdif);
+            layer_down(st, f, cdif, fdif);
+        } else {
+            level_q(st, albp, albd, albp, albd, zinc, q, cdif, fdif);
+        }
+        if constexpr (NQ > 8) {
+            const int o = uv ? 8 : 12, z = uv ? 12 : 8;
+            const float x1 = q[1], x3 = q[3], x4 = q[4], x5 = q[5];
+            q[o] = x1; q[o + 1] = x3; q[o + 2] = x4; q[o + 3] = x5;
+            q[z] = q[z + 1] = q[z + 2] = q[z + 3] = 0.0f;
+        }
+        const int l = i + 1;
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) V.scr[k * TW + lane] = on ? q[k] : 0.0f;
+        __syncwarp();
+        if (lane < 2 * NQ) {
+            // one lane per (column, quantity), subcolumns in record order
+            const int c = lane / NQ, k = lane % NQ;
+            unsigned m = c ? m1 : m0;
+            if (m) {
+                float v = 0.0f;
+                while (m) {
+                    const int j = __ffs(m) - 1;
+                    m &= m - 1;
+                    v += V.scr[k * TW + j];
+                }
+                V.flux[((size_t)(par * COLS_PER_CTA + c) * NQ + k) * L1 + l] += v;
+            }
+        }
+        __syncwarp();
+        if (P.bands) {
+            const float bv[5] = {q[0], q[1], q[4], q[2], q[3]};
+#pragma unroll
+            for (int k = 0; k < 5; ++k) V.scr[k * TW + lane] = on ? bv[k] : 0.0f;
+            long long* key = (long long*)(V.scr + 6 * TW);
+            key[lane] = on && pcol < P.ncol ? (long long)((size_t)pcol + n * ((size_t)l + L1 * (size_t)ib)) : -1ll;
+            __syncwarp();
+            if (lane < 5 && P.bout[lane]) {
+                // records in order, one lane per output array
+                for (int j = 0; j < TW; ++j)
+                    if (key[j] >= 0) P.bout[lane][key[j]] += (double)V.scr[lane * TW + j];
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// ---- adding warp: pair lp's set-aside subcolumns, outputs, reset
+template <int NQ>
+__device__ void tiled_finish(const SolveParams& P, const TCtx& X, int lp) {
+    const TileView& V = X.V;
+    const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
+    const size_t n = (size_t)P.ncol;
+    mbar_wait(&V.bar[TB_REDO0 + par], (lp >> 1) & 1, X.abort, P.err);
+    const int qn = V.ctl[TC_QN0 + par], rn = V.ctl[TC_RN0 + par];
+    const bool ovf = qn > X.qcap || V.ctl[TC_OVF0 + par] != 0;
+    if (!ovf && rn > 0) {
+        const float* corr = (const float*)(tpar(X, par) + X.G.corr);
+        for (int k = lane; k < qn; k += 32) {
+            const int e = V.queue[par * T_QCAP + k];
+            const int s = e >> 12, lay = (e >> 1) & 127;
+            const int r = V.recof[par * COLS_PER_CTA * NGPT + s];
+            if (r >= 0 && r < T_RCAP) {
+                float* rp = trec(X, par, r) + 8;
+#pragma unroll
+                for (int f = 0; f < T_NF; ++f) rp[f * L + lay - 1] = corr[k * T_NF + f];
+            }
+        }
+        __syncwarp();
+        for (int r0 = 0; r0 < rn; r0 += TW) tiled_records<NQ>(P, X, lp, r0, rn);
+    }
+    if (ovf && lane == 0 && P.tovfcount) {
+        // too many FP64 cells for the capacities: the caller solves the pair again
+        const int k = atomicAdd(P.tovfcount, 1);
+        if (k < P.tovfcap) P.tovf[k] = pair;
+    }
+    // outputs (level 0 = surface)
+    const double* pdpg = (const double*)(tpar(X, par) + X.G.pdp);
+    constexpr int QX = 8;
+    for (int it = lane; it < COLS_PER_CTA * (L + 1); it += 32) {
+        const int c2 = it / (L + 1), l = it % (L + 1);
+        const int ocol = pair_col(P, pair, c2, X.nmapped);
+        if (ocol >= P.ncol) continue;
+        const float* F = V.flux + (size_t)(par * COLS_PER_CTA + c2) * NQ * (L + 1);
+        const size_t o = (size_t)ocol + n * (size_t)l;
+        const double fu = (double)F[0 * (L + 1) + l], fd = (double)F[1 * (L + 1) + l];
+        P.swuflx[o] = fu;
+        P.swdflx[o] = fd;
+        P.swuflxc[o] = (double)F[2 * (L + 1) + l];
+        P.swdflxc[o] = (double)F[3 * (L + 1) + l];
+        if (l < L) {
+            double hr = 0.0, hrc = 0.0;
+            if (l < L - 1) {
+                // summed layer absorption (= net-flux divergence) (rrtmg_sw_rad.f90:829-836)
+                const double zdpgcp = cT.heatfac / pdpg[c2 * L + l];
+                hr = (double)F[6 * (L + 1) + l] * zdpgcp;
+                hrc = (double)F[7 * (L + 1) + l] * zdpgcp;
+            }
+            P.swhr[o] = hr;
+            P.swhrc[o] = hrc;
+        }
+        if constexpr (NQ > 8) {
+            const double fddir = (double)F[4 * (L + 1) + l];
+            const double uvfd = (double)F[(QX + 0) * (L + 1) + l], uvfddir = (double)F[(QX + 2) * (L + 1) + l];
+            const double nifd = (double)F[(QX + 4) * (L + 1) + l], nifddir = (double)F[(QX + 6) * (L + 1) + l];
+            const double vals[8] = {fddir, DS(fd, fddir), uvfd, nifd, uvfddir, DS(uvfd, uvfddir), nifddir,
+                                    DS(nifd, nifddir)};
+            for (int x = 0; x < 8; ++x)
+                if (P.xout[x]) P.xout[x][o] = vals[x];
+        }
+    }
+    __syncwarp();
+    // this parity's per-pair state, ready for pair lp + 2
+    float* F = V.flux + (size_t)par * COLS_PER_CTA * NQ * (L + 1);
+    for (int k = lane; k < COLS_PER_CTA * NQ * (L + 1); k += 32) F[k] = 0.0f;
+    for (int k = lane; k < COLS_PER_CTA * NGPT; k += 32) V.recof[par * COLS_PER_CTA * NGPT + k] = -1;
+    if (lane < TILES) V.risky[par * TILES + lane] = 0u;
+    if (lane == 0) {
+        V.ctl[TC_QN0 + par] = 0;
+        V.ctl[TC_RN0 + par] = 0;
+        V.ctl[TC_OVF0 + par] = 0;
+    }
+    __syncwarp();
+}
+
+// ---- adding warp: the pair's per-band outputs start at zero
+__device__ void tiled_zero_bands(const SolveParams& P, const TCtx& X, int lp) {
+    const int L = X.L, pair = tpair(lp), lane = threadIdx.x & 31;
+    const size_t n = (size_t)P.ncol, L1 = (size_t)L + 1;
+    for (int it = lane; it < COLS_PER_CTA * (L + 1) * NBND; it += 32) {
+        const int c2 = it / ((L + 1) * NBND), rem = it % ((L + 1) * NBND), l = rem % (L + 1), b = rem / (L + 1);
+        const int pcol = pair_col(P, pair, c2, X.nmapped);
+        if (pcol >= P.ncol) continue;
+        const size_t o = (size_t)pcol + n * ((size_t)l + L1 * (size_t)b);
+        for (int k = 0; k < 5; ++k)
+            if (P.bout[k]) P.bout[k][o] = 0.0;
+    }
+    __syncwarp();
+}
+
+template <bool MT>
+__global__ void __launch_bounds__(T_THREADS, 1)
+k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* __restrict__ tab64) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L = P.nlay;
+    const int NQ = P.extra ? 16 : 8;
+    TCtx X;
+    X.fused = P.fused && P.icld >= 1;
+    X.nomc = P.nomcica && P.icld >= 1;
+    X.cstage = X.fused || X.nomc;
+    const TSmem M = tiled_smem(L, NQ, X.fused, X.cstage);
+    X.V = tile_view(smem_raw, M);
+    X.G = tiled_glob(L);
+    X.glob = (unsigned char*)P.scratch + (size_t)blockIdx.x * P.slot_elems * sizeof(float);
+    X.L = L;
+    X.nmapped = P.colmap ? *P.mapcount : 0;
+    X.qcap = (P.tile_qcap > 0 && P.tile_qcap < T_QCAP) ? P.tile_qcap : T_QCAP;
+    X.nlocal = (int)blockIdx.x < P.npairs ? (P.npairs - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    X.abort = (volatile int*)&X.V.ctl[TC_ABORT];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    TmSmem* tm = (TmSmem*)X.V.tm;
+    for (int i = tid; i < NBND * 2; i += T_THREADS) {
+        TmSmem d;
+        d.r = cT.tm[i / 2][i % 2];
+        d.selfref = cT.b[i / 2].selfref;
+        d.forref = cT.b[i / 2].forref;
+        d.ng = cT.b[i / 2].ng;
+        d.pad = 0;
+        tm[i] = d;
+    }
+    for (int i = tid; i < TC_N; i += T_THREADS) X.V.ctl[i] = 0;
+    for (int i = tid; i < 2 * TILES; i += T_THREADS) X.V.risky[i] = 0u;
+    for (int i = tid; i < 2 * COLS_PER_CTA * NGPT; i += T_THREADS) X.V.recof[i] = -1;
+    for (int i = tid; i < 2 * COLS_PER_CTA * NQ * (L + 1); i += T_THREADS) X.V.flux[i] = 0.0f;
+    if (tid == 0) {
+        mbar_init(&X.V.bar[TB_FULL0], T_OPT);
+        mbar_init(&X.V.bar[TB_FULL1], T_OPT);
+        mbar_init(&X.V.bar[TB_EMPTY0], 1);
+        mbar_init(&X.V.bar[TB_EMPTY1], 1);
+        mbar_init(&X.V.bar[TB_PAIR0], T_OPT);
+        mbar_init(&X.V.bar[TB_PAIR1], T_OPT);
+        mbar_init(&X.V.bar[TB_REDO0], 1);
+        mbar_init(&X.V.bar[TB_REDO1], 1);
+    }
+    // KISS: the xorshift part of each subcolumn's stream jump (depends on g)
+    if (X.fused && !MT && tid < NGPT)
+        xorshift_power(kiss_offset(P.icld, tid, L, P.permuteseed), (uint32_t*)(X.glob + X.G.xs) + tid * 32);
+    __syncthreads();
+    if (warp < T_OPT) {
+        KissJump J{1u, 0u, 1u, 1u};
+        if (X.fused && !MT && tid < COLS_PER_CTA * NGPT)
+            J = kiss_jump_consts(kiss_offset(P.icld, tid % NGPT, L, P.permuteseed));
+        for (int lp = 0; lp < X.nlocal; ++lp) {
+            opt_sync();  // the previous pair's cells are all written
+            tiled_prep<MT>(P, X, lp, J, tab64, tab);
+            for (int t = 0; t < TILES; ++t) {
+                const int T = TILES * lp + t, b = T & 1;
+                if (T >= 2) mbar_wait(&X.V.bar[TB_EMPTY0 + b], ((T - 2) >> 1) & 1, X.abort, P.err);
+                tiled_optics(P, X, lp, t, b, tab, tab64);
+                __syncwarp();
+                __threadfence_block();
+                if (lane == 0) {
+                    mbar_arrive(&X.V.bar[TB_FULL0 + b]);
+                    if (t == TILES - 1) mbar_arrive(&X.V.bar[TB_PAIR0 + (lp & 1)]);
+                }
+            }
+        }
+    } else if (warp == T_REDO) {
+        for (int lp = 0; lp < X.nlocal; ++lp) {
+            mbar_wait(&X.V.bar[TB_PAIR0 + (lp & 1)], (lp >> 1) & 1, X.abort, P.err);
+            tiled_redo(P, X, lp, tab64);
+            __syncwarp();
+            __threadfence_block();
+            if (lane == 0) mbar_arrive(&X.V.bar[TB_REDO0 + (lp & 1)]);
+        }
+    } else {
+        int pend = -1;
+        for (int lp = 0; lp < X.nlocal; ++lp) {
+            if (P.bands) tiled_zero_bands(P, X, lp);
+            for (int t = 0; t < TILES; ++t) {
+                const int T = TILES * lp + t, b = T & 1;
+                mbar_wait(&X.V.bar[TB_FULL0 + b], (T >> 1) & 1, X.abort, P.err);
+                if (NQ > 8) tiled_sweep<16>(P, X, lp, t, b);
+                else tiled_sweep<8>(P, X, lp, t, b);
+                __syncwarp();
+                if (lane == 0) {
+                    X.V.ctl[TC_ROW0 + b] = 0;
+                    __threadfence_block();
+                    mbar_arrive(&X.V.bar[TB_EMPTY0 + b]);
+                }
+                __syncwarp();
+                // the previous pair is finished while this one's tiles come in
+                if (pend >= 0 && t == 1) {
+                    if (NQ > 8) tiled_finish<16>(P, X, pend);
+                    else tiled_finish<8>(P, X, pend);
+                    pend = -1;
+                }
+            }
+            pend = lp;
+        }
+        if (pend >= 0) {
+            if (NQ > 8) tiled_finish<16>(P, X, pend);
+            else tiled_finish<8>(P, X, pend);
+        }
+    }
+}
+
+// Whether the tiled kernel takes a call: FP32 form, delta-scaled direct
+// fluxes (idelm = 1), at most T_MAXL layers whose tiles fit in shared
+// memory, no batch column map.
+__host__ inline bool tiled_supports(const SolveParams& P, size_t smem_max) {
+    if (P.idelm != 1 || P.nlay > T_MAXL || P.colmap) return false;
+    const bool fused = P.fused && P.icld >= 1, nomc = P.nomcica && P.icld >= 1;
+    return tiled_smem(P.nlay, P.extra ? 16 : 8, fused, fused || nomc).total <= smem_max;
+}
+
+}  // namespace rrsw

@@ -9,6 +9,7 @@ night columns are zero in the batch and within 1e-6 of zero in the single
 call (the reference clamps mu0 to 1e-10).
 """
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -26,11 +27,16 @@ SHAPES = ((37, 40), (512, 47), (1000, 60), (64, 72), (200, 91), (3, 137))
 
 @pytest.fixture(scope="module")
 def torch():
+    # the batch launch runs the scratch-based kernels, so the single calls it
+    # is compared with bit for bit use them too (RRTMG_SW_TILED=0)
     t = pytest.importorskip("torch")
     from rrtmg_sw_gb300 import build
     build.build()
+    os.environ["RRTMG_SW_TILED"] = "0"
     gi.rrtmg_sw_ini(1.004e3)
     yield t
+    os.environ.pop("RRTMG_SW_TILED", None)
+    gi.rrtmg_sw_ini(1.004e3)
     gi.set_form(gi.FORM_FP64)
 
 
