@@ -282,6 +282,16 @@ int mcica_subcol_sw_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t permutes
 int rrtmg_sw_mt_window_c(int32_t seed, uint64_t offset, uint32_t *window);
 int rrtmg_sw_mt_stream_dev_c(int32_t seed, uint64_t n, uint32_t *out, int32_t log_seg, void *stream);
 
+/* setcoef_sw's integer outputs (rrtmg_sw_setcoef.f90:158-200) for the
+ * layers of a GCM call, as the solve kernels of both forms compute them (the
+ * same device routine, after inatm_sw's layer amounts,
+ * rrtmg_sw_rad.f90:1527-1586): jp, jt, jt1, indself, indfor (ncol,nlay) and
+ * laytrop (ncol), host arrays.  Only the state inputs of `a` are read (play,
+ * plev, tlay and the gas mixing ratios).  A diagnostic for checking the
+ * table indices bit for bit against another implementation. */
+int rrtmg_sw_setcoef_c(const rrtmg_sw_args *a, int32_t *jp, int32_t *jt, int32_t *jt1, int32_t *indself,
+                       int32_t *indfor, int32_t *laytrop);
+
 /* get_alpha (mcica_subcol_gen_sw.f90:66-178), host arrays. */
 int get_alpha_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t idcor, double decorr_con,
                 const double *dz, const double *lat, int32_t juldat, const double *cldfrac,
@@ -295,6 +305,24 @@ int rrtmg_sw_get_form_c(void);
 
 /* Number of kernels the most recent solve launched (for launch accounting). */
 int rrtmg_sw_last_launch_count_c(void);
+/* Kernel of the most recent solve's main launch: RRTMG_SW_KERNEL_FP64, the
+ * FP32 form's scratch-based kernel (RRTMG_SW_KERNEL_FP32) or its tiled kernel
+ * (RRTMG_SW_KERNEL_FP32_TILED: nlay <= 64, idelm = 1, shared memory
+ * permitting); -1 before the first solve. */
+#define RRTMG_SW_KERNEL_FP64 0
+#define RRTMG_SW_KERNEL_FP32 1
+#define RRTMG_SW_KERNEL_FP32_TILED 2
+int rrtmg_sw_last_kernel_c(void);
+/* Counters of the FP32 form over the most recent solve through
+ * rrtmg_sw_c / rrtmg_sw_mcica_c / their _dev_ forms (zeros for the FP64
+ * form): stats[0] cells whose FP32 optics were too close to a discrete
+ * choice of the reference (table entry, conservative switch, resonance)
+ * and were redone in FP64; stats[1] of those, cells past the scratch-based
+ * kernel's redo queue (redone by their own thread); stats[2] column pairs
+ * the tiled kernel handed back to the scratch-based kernel (capacity of
+ * FP64 cells exceeded); stats[3] subcolumns the tiled kernel swept a
+ * second time for their FP64 cells. */
+int rrtmg_sw_last_fp32_stats_c(int64_t* stats);
 /* Checkpointing of the most recent rrtmg_sw_ad_c / rrtmg_sw_tl_c call:
  * 1 stored Jacobians, 0 recomputed, -1 none yet. */
 int rrtmg_sw_last_ad_store_c(void);

@@ -81,6 +81,7 @@ def lib():
         L.orc_mt_real.argtypes = [C.c_int, C.c_int, _dp]
         L.orc_kiss_real.argtypes = [C.c_int32] * 4 + [C.c_int, _dp]
         L.orc_setcoef_indices.argtypes = [C.c_int, _dp, _dp, _dp, _dp] + [_ip] * 6
+        L.orc_gcm_setcoef_indices.argtypes = [C.c_int, C.c_int] + [_dp] * 9 + [_ip] * 6
         L.orc_exp_table.argtypes = [_dp]
         L.orc_heatfac.restype = C.c_double
         L.orc_solar_factors.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int] + [_dp] * 6
@@ -273,6 +274,22 @@ def setcoef_indices(pavel, tavel, coldry, wkl):
     lib().orc_setcoef_indices(nlay, *[_p(x) for x in ins], *[o.ctypes.data_as(_ip) for o in outs],
                               lt.ctypes.data_as(_ip))
     return dict(zip(("jp", "jt", "jt1", "indself", "indfor"), outs), laytrop=int(lt[0]))
+
+
+def gcm_setcoef_indices(kw):
+    """setcoef_sw indices (jp, jt, jt1, indself, indfor: (ncol, nlay); laytrop: (ncol)) of the
+    GCM-interface inputs in ``kw`` (rrtmg_sw keyword arrays), after inatm_sw's layer amounts."""
+    ncol, nlay = kw["ncol"], kw["nlay"]
+    ins = [_f64(np.asarray(kw[k]).ravel(order="F")) for k in
+           ("play", "plev", "tlay", "h2ovmr", "co2vmr", "o3vmr", "n2ovmr", "ch4vmr", "o2vmr")]
+    outs = [np.zeros(ncol * nlay, dtype=np.int32) for _ in range(5)]
+    lt = np.zeros(ncol, dtype=np.int32)
+    rc = lib().orc_gcm_setcoef_indices(ncol, nlay, *[_p(x) for x in ins], *[o.ctypes.data_as(_ip) for o in outs],
+                                       lt.ctypes.data_as(_ip))
+    assert rc == 0, rc
+    res = {k: o.reshape((ncol, nlay), order="F") for k, o in zip(("jp", "jt", "jt1", "indself", "indfor"), outs)}
+    res["laytrop"] = lt
+    return res
 
 
 def exp_table():

@@ -1366,6 +1366,42 @@ int orc_setcoef_indices(int nlay, const double* pavel, const double* tavel, cons
     return ORC_OK;
 }
 
+// setcoef_sw indices of GCM-interface columns: inatm_sw's layer amounts
+// (rrtmg_sw_rad.f90:1527-1586, as in rrtmg_sw_impl below), then setcoef.
+// Outputs (ncol, nlay) in column-major order, laytrop (ncol).
+int orc_gcm_setcoef_indices(int ncol, int nlay, const double* play, const double* plev, const double* tlay,
+                            const double* h2ovmr, const double* co2vmr, const double* o3vmr, const double* n2ovmr,
+                            const double* ch4vmr, const double* o2vmr, int32_t* jp, int32_t* jt, int32_t* jt1,
+                            int32_t* indself, int32_t* indfor, int32_t* laytrop) {
+    if (!T.ok) return ORC_ERR_NOT_INITIALIZED;
+    const double amd = 28.9660, amw = 18.0160, avogad = 6.02214199e+23, grav = 9.8066;
+    for (int iplon = 0; iplon < ncol; ++iplon) {
+        std::vector<double> pavel(nlay), tavel(nlay), pz(nlay + 1), coldry(nlay), wkl(7 * nlay, 0.0);
+        pz[0] = plev[iplon];
+        for (int l = 1; l <= nlay; ++l) {
+            const size_t k = iplon + (size_t)ncol * (l - 1);
+            pavel[l - 1] = play[k];
+            tavel[l - 1] = tlay[k];
+            pz[l] = plev[iplon + (size_t)ncol * l];
+            double* w = &wkl[7 * (l - 1)];
+            w[0] = h2ovmr[k]; w[1] = co2vmr[k]; w[2] = o3vmr[k]; w[3] = n2ovmr[k]; w[5] = ch4vmr[k]; w[6] = o2vmr[k];
+            const double amm = (1.0 - w[0]) * amd + w[0] * amw;
+            coldry[l - 1] = (pz[l - 1] - pz[l]) * 1.e3 * avogad / (1.e2 * grav * amm * (1.0 + w[0]));
+        }
+        for (int l = 1; l <= nlay; ++l)
+            for (int m = 0; m < 7; ++m) wkl[7 * (l - 1) + m] = coldry[l - 1] * wkl[7 * (l - 1) + m];
+        Coef c;
+        setcoef(nlay, pavel.data(), tavel.data(), coldry.data(), wkl.data(), c);
+        for (int l = 1; l <= nlay; ++l) {
+            const size_t k = iplon + (size_t)ncol * (l - 1);
+            jp[k] = c.jp[l]; jt[k] = c.jt[l]; jt1[k] = c.jt1[l];
+            indself[k] = c.indself[l]; indfor[k] = c.indfor[l];
+        }
+        laytrop[iplon] = c.laytrop;
+    }
+    return ORC_OK;
+}
+
 // earth_sun (rrtmg_sw_rad.f90:844-868)
 static double earth_sun(int idn) {
     const double gamma = 2.0 * T.pi * (idn - 1) / 365.0;

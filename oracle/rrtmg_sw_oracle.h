@@ -158,6 +158,12 @@ int orc_setcoef_indices(int nlay, const double *pavel, const double *tavel,
                         const double *coldry, const double *wkl,
                         int32_t *jp, int32_t *jt, int32_t *jt1,
                         int32_t *indself, int32_t *indfor, int32_t *laytrop);
+/* setcoef_sw indices of GCM-interface columns (inatm_sw amounts first);
+ * outputs (ncol, nlay) column-major, laytrop (ncol) */
+int orc_gcm_setcoef_indices(int ncol, int nlay, const double* play, const double* plev, const double* tlay,
+                            const double* h2ovmr, const double* co2vmr, const double* o3vmr, const double* n2ovmr,
+                            const double* ch4vmr, const double* o2vmr, int32_t* jp, int32_t* jt, int32_t* jt1,
+                            int32_t* indself, int32_t* indfor, int32_t* laytrop);
 
 /* exp_tbl (0:10000) as built by rrtmg_sw_ini, for tests. */
 int orc_exp_table(double *out10001);

@@ -54,6 +54,9 @@ struct State {
     DevBuf d_tab64, d_tab32, scratch, errw, bounds;
     std::map<std::string, DevBuf> stage;  // host-API staging buffers
     int* h_err = nullptr;                  // pinned: [0] error word, [1] tiled-kernel overflow count
+    unsigned long long* h_stats = nullptr;  // pinned: the FP32 form's counters of the last solve
+    DevBuf statsw;                         // their device copy
+    long long last_stats[4] = {0, 0, 0, 0};
     // diagnostics, from the environment at each rrtmg_sw_ini_c: RRTMG_SW_TILED=1
     // puts the FP32 form on the tiled kernel; RRTMG_SW_TILE_QCAP=n
     // lowers the tiled kernel's capacity of FP64 cells per column pair (tests
@@ -65,6 +68,7 @@ struct State {
     cudaStream_t host_stream = nullptr;
     int form = RRTMG_SW_FORM_FP64;
     int last_launches = 0;
+    int last_kernel = -1;  // RRTMG_SW_KERNEL_* of the most recent solve's main launch
     int last_ad_store = -1;  // checkpointing choice of the last adjoint / tangent-linear call
     std::string last_cuda;
 };
@@ -567,11 +571,12 @@ size_t ovf_bytes(int npairs) { return (size_t)(npairs + 1) * sizeof(int); }
 // list is read by the caller).
 int enqueue_solve(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaStream_t s, bool nomcica,
                   DevBuf& scratch, int* err, int& launches, SolveParams* Pout = nullptr,
-                  LaunchInfo* liout = nullptr, bool allow_tiled = true) {
+                  LaunchInfo* liout = nullptr, bool allow_tiled = true, unsigned long long* stats = nullptr) {
     SolveParams P;
     int rc = make_params(st, a, c, P, nomcica);
     if (rc) return rc;
     P.err = err;
+    P.stats = stats;
     launches = 1;
     if (P.fused && P.icld >= 1 && P.irng) {
         // the call's MT stream, generated in parallel segments, read by the solve
@@ -584,6 +589,7 @@ int enqueue_solve(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, c
     }
     const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
     LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms, allow_tiled && !st.no_tiled) : plan_fp64(P, st.num_sms);
+    st.last_kernel = !fp32 ? RRTMG_SW_KERNEL_FP64 : li.tiled ? RRTMG_SW_KERNEL_FP32_TILED : RRTMG_SW_KERNEL_FP32;
     if (!fp32) li.slot_bytes = slot_elems(P.nlay, P.idelm, false) * sizeof(double);
     P.slot_elems = li.slot_bytes / (fp32 ? sizeof(float) : sizeof(double));
     const size_t off = ovf_offset((size_t)li.grid * li.slot_bytes);
@@ -656,7 +662,10 @@ int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaS
     int launches = 0;
     SolveParams P;
     LaunchInfo li;
-    const int rc = enqueue_solve(st, a, c, s, nomcica, st.scratch, err, launches, &P, &li, allow_tiled);
+    CK(st.statsw.ensure(4 * sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(st.statsw.p, 0, 4 * sizeof(unsigned long long), s));
+    const int rc = enqueue_solve(st, a, c, s, nomcica, st.scratch, err, launches, &P, &li, allow_tiled,
+                                 (unsigned long long*)st.statsw.p);
     if (rc) return rc;
     st.h_err[1] = 0;
     CK(cudaMemcpyAsync(st.h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -672,6 +681,9 @@ int solve_dev(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cudaS
         CK(cudaMemcpyAsync(st.h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
     }
+    CK(cudaMemcpyAsync(st.h_stats, st.statsw.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < 4; ++i) st.last_stats[i] = (long long)st.h_stats[i];
     st.last_launches = launches;
     return bounds_status(st, *st.h_err);
 }
@@ -754,6 +766,9 @@ int solve_host_chunked(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds*
         cs.ovf_cap = nch;
     }
     for (int ch = 0; ch < nch; ++ch) cs.h_ovf[ch] = 0;
+    CK(st.statsw.ensure(4 * sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(st.statsw.p, 0, 4 * sizeof(unsigned long long), cs.s[0]));
+    CK(cudaStreamSynchronize(cs.s[0]));  // zeroed before either stream's first solve
     for (int ch = 0; ch < nch && e == cudaSuccess; ++ch) {
         const int si = ch % kChunkStreams;
         cudaStream_t s = cs.s[si];
@@ -831,7 +846,7 @@ int solve_host_chunked(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds*
         SolveParams Pc;
         LaunchInfo lic;
         const int rc = enqueue_solve(st, &d, c ? &dc : nullptr, s, nomcica, cs.scratch[si], (int*)cs.err[si].p, nl,
-                                     &Pc, &lic);
+                                     &Pc, &lic, true, (unsigned long long*)st.statsw.p);
         if (rc) {
             for (int i = 0; i < kChunkStreams; ++i) cudaStreamSynchronize(cs.s[i]);
             return rc;
@@ -853,6 +868,9 @@ int solve_host_chunked(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds*
         if (e == cudaSuccess) e = e2;
     }
     if (e != cudaSuccess) return cuda_fail(e);
+    CK(cudaMemcpyAsync(st.h_stats, st.statsw.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, cs.s[0]));
+    CK(cudaStreamSynchronize(cs.s[0]));
+    for (int i = 0; i < 4; ++i) st.last_stats[i] = (long long)st.h_stats[i];
     st.last_launches = launches;
     for (int i = 0; i < kChunkStreams; ++i)
         if (cs.h_err[i]) return cs.h_err[i];
@@ -1316,6 +1334,7 @@ int rrtmg_sw_ini_c(double cpdair) {
         const int rc = build_tables(st);
         if (rc) return rc;
         CK(cudaMallocHost((void**)&st.h_err, 2 * sizeof(int)));
+        CK(cudaMallocHost((void**)&st.h_stats, 4 * sizeof(unsigned long long)));
         CK(cudaStreamCreateWithFlags(&st.host_stream, cudaStreamNonBlocking));
     }
     {
@@ -1443,6 +1462,58 @@ int mcica_subcol_sw_c(int32_t ncol, int32_t nlay, int32_t icld, int32_t permutes
     return RRTMG_SW_OK;
 }
 
+int rrtmg_sw_setcoef_c(const rrtmg_sw_args* a, int32_t* jp, int32_t* jt, int32_t* jt1, int32_t* indself,
+                       int32_t* indfor, int32_t* laytrop) {
+    State& st = S();
+    std::lock_guard<std::mutex> lk(st.mu);
+    if (const int r0 = ready(st)) return r0;
+    if (a && a->ncol == 0) return RRTMG_SW_OK;
+    if (!a || a->ncol < 0 || a->nlay < 1 || a->nlay > MAX_NLAY || !jp || !jt || !jt1 || !indself || !indfor ||
+        !laytrop)
+        return RRTMG_SW_EARGS;
+    const double* req[] = {a->play, a->plev, a->tlay, a->h2ovmr, a->o3vmr, a->co2vmr, a->ch4vmr, a->o2vmr};
+    for (const double* p : req)
+        if (!p) return RRTMG_SW_EARGS;
+    const size_t C = a->ncol, L = a->nlay, CL = C * L;
+    cudaStream_t s = st.host_stream;
+    Stager sg{st, s};
+    SolveParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.ncol = a->ncol;
+    P.nlay = a->nlay;
+    P.play = sg.in("play", a->play, CL); P.plev = sg.in("plev", a->plev, C * (L + 1));
+    P.tlay = sg.in("tlay", a->tlay, CL); P.h2ovmr = sg.in("h2o", a->h2ovmr, CL);
+    P.o3vmr = sg.in("o3", a->o3vmr, CL); P.co2vmr = sg.in("co2", a->co2vmr, CL);
+    P.ch4vmr = sg.in("ch4", a->ch4vmr, CL); P.o2vmr = sg.in("o2", a->o2vmr, CL);
+    if (sg.err != cudaSuccess) return cuda_fail(sg.err);
+    DevBuf& cf = st.stage["sc_cf"];
+    DevBuf& pk = st.stage["sc_pk"];
+    DevBuf& pdp = st.stage["sc_pdp"];
+    CK(cf.ensure(CL * NFR * sizeof(double)));
+    CK(pk.ensure(CL * sizeof(int)));
+    CK(pdp.ensure(CL * sizeof(double)));
+    CK(launch_setcoef(P, (const double*)st.d_tab64.p, (double*)cf.p, (int*)pk.p, (double*)pdp.p, s));
+    st.last_launches = 1;
+    std::vector<int> h(CL);
+    CK(cudaMemcpyAsync(h.data(), pk.p, CL * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (size_t c = 0; c < C; ++c) {
+        int lt = 0;
+        for (size_t l = 0; l < L; ++l) {
+            const int w = h[c * L + l];
+            const size_t o = c + C * l;  // (ncol, nlay), column-major
+            jp[o] = w & 0xff;
+            jt[o] = (w >> 8) & 0xf;
+            jt1[o] = (w >> 12) & 0xf;
+            indself[o] = (w >> 16) & 0xff;
+            indfor[o] = (w >> 24) & 0xf;
+            lt += (w >> 30) & 1;
+        }
+        laytrop[c] = lt;
+    }
+    return RRTMG_SW_OK;
+}
+
 int rrtmg_sw_mt_window_c(int32_t seed, uint64_t offset, uint32_t* window) {
     if (!window) return RRTMG_SW_EARGS;
     return mt_window_host((uint32_t)seed, offset, window) == 0 ? RRTMG_SW_OK : RRTMG_SW_EARGS;
@@ -1499,6 +1570,12 @@ int rrtmg_sw_get_form_c(void) {
 }
 
 int rrtmg_sw_last_launch_count_c(void) { return S().last_launches; }
+int rrtmg_sw_last_kernel_c(void) { return S().last_kernel; }
+int rrtmg_sw_last_fp32_stats_c(int64_t* stats) {
+    if (!stats) return RRTMG_SW_EARGS;
+    for (int i = 0; i < 4; ++i) stats[i] = S().last_stats[i];
+    return RRTMG_SW_OK;
+}
 
 int rrtmg_sw_last_ad_store_c(void) { return S().last_ad_store; }
 
@@ -1592,11 +1669,14 @@ int rrtmg_sw_finalize_c(void) {
     st.d_tab32.release();
     st.scratch.release();
     st.errw.release();
+    st.statsw.release();
     st.bounds.release();
     for (auto& kv : st.stage) kv.second.release();
     st.stage.clear();
     if (st.h_err) cudaFreeHost(st.h_err);
     st.h_err = nullptr;
+    if (st.h_stats) cudaFreeHost(st.h_stats);
+    st.h_stats = nullptr;
     if (st.host_stream) cudaStreamDestroy(st.host_stream);
     st.host_stream = nullptr;
     // a later rrtmg_sw_ini_c (after a cudaDeviceReset, say) looks the static

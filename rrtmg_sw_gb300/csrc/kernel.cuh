@@ -927,6 +927,10 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         sRf[tid] = L + 1;
         __syncthreads();
         const int nq = min(sMisc[2], REDO_QUEUE);
+        if (tid == 0 && P.stats) {
+            atomicAdd(P.stats, (unsigned long long)sMisc[2]);
+            if (sMisc[2] > REDO_QUEUE) atomicAdd(P.stats + 1, (unsigned long long)(sMisc[2] - REDO_QUEUE));
+        }
         for (int i = tid; i < nq; i += CTA_THREADS) {
             const int e = V.sRq[i];
             const int t = e >> 20, c2 = (e >> 19) & 1, gg = (e >> 12) & 127, lay = (e >> 1) & 2047;

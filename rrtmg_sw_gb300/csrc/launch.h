@@ -47,6 +47,10 @@ cudaError_t launch_adjoint(const SolveParams& P, const AdParams& A, const double
 // scratch elements (of the form's type) per CTA slot
 size_t slot_elems(int nlay, int idelm, bool fp32);
 
+// setcoef_sw indices of every (column, layer) through the solve's prep_layer:
+// cf (ncol x NFR x nlay), pk and pdp (ncol x nlay), column-major by column
+cudaError_t launch_setcoef(const SolveParams& P, const double* tab64, double* cf, int* pk, double* pdp,
+                           cudaStream_t s);
 // get_alpha (mcica_subcol_gen_sw.f90:66-178) on the device
 cudaError_t launch_get_alpha(int ncol, int nlay, int icld, int idcor, double decorr_con, const double* dz,
                              const double* lat, int juldat, const double* cldfrac, double* alpha, cudaStream_t s);

@@ -56,6 +56,11 @@ struct SolveParams {
     int* tovfcount;
     int tovfcap;
     int tile_qcap;
+    // FP32 form's counters (nullptr: not kept): [0] cells redone in FP64,
+    // [1] of those past the scratch kernel's queue (redone by their own
+    // thread), [2] column pairs the tiled kernel handed back, [3] subcolumns
+    // the tiled kernel swept a second time for their FP64 cells
+    unsigned long long* stats;
 };
 
 // Tangent-linear / adjoint request (solve_ad.cu): objective weights and

@@ -204,4 +204,26 @@ cudaError_t launch_mcica_stream(int ncol, int nlay, int icld, const uint32_t* st
     return cudaGetLastError();
 }
 
+
+// setcoef_sw's integer outputs as the solve computes them: one thread per
+// (column, layer) through prep_layer, the routine both forms' kernels call;
+// pk (ncol, nlay) holds the packed jp | jt<<8 | jt1<<12 | indself<<16 |
+// indfor<<24 | below-100-hPa<<30 word.
+static __global__ void __launch_bounds__(256) k_setcoef(const SolveParams P, const double* __restrict__ tab64,
+                                                        double* cf, int* pk, double* pdp) {
+    const size_t n = (size_t)P.ncol, L = (size_t)P.nlay;
+    const size_t it = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= n * L) return;
+    const int col = (int)(it % n), lay = (int)(it / n) + 1;
+    int* pc = pk + (size_t)col * L;
+    prep_layer<double>(P, col, lay, cf + (size_t)col * NFR * L, pc, pdp + (size_t)col * L, (int)L, tab64);
+}
+
+cudaError_t launch_setcoef(const SolveParams& P, const double* tab64, double* cf, int* pk, double* pdp,
+                           cudaStream_t s) {
+    const size_t n = (size_t)P.ncol * P.nlay;
+    k_setcoef<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, tab64, cf, pk, pdp);
+    return cudaGetLastError();
+}
+
 }  // namespace rrsw

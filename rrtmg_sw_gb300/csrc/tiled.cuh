@@ -15,32 +15,33 @@
 //     delta scaling, the two-stream layer solution -- layer rows taken from
 //     a shared counter, the 32 subcolumns of a row in one warp (32
 //     consecutive g-points: coalesced table reads).
-//   adding warp (1): per tile, the vertical adding method of vrtqdr_sw
-//     (rrtmg_sw_vrtqdr.f90:122-169), one lane per subcolumn: up-sweep from
-//     the surface (upward albedos kept in shared memory), down-sweep with the
-//     weighted level fluxes written into the tile slots it has just read;
-//     then the g-point sums of spcvmc_sw (:607-655), one lane per level, off
-//     the sweeps' dependency chain.
+//   adding warps (2): per tile, the vertical adding method of vrtqdr_sw
+//     (rrtmg_sw_vrtqdr.f90:122-169), one lane per subcolumn, one warp for
+//     the clear sky and one for the total sky (the two recurrences are
+//     independent): up-sweep from the surface (upward albedos kept in shared
+//     memory), down-sweep with the weighted level fluxes written into the
+//     tile slots the warp has just read; then the g-point sums of spcvmc_sw
+//     (:607-655), one lane per level, half of the levels per warp.
 //   FP64 warp (1): redoes in FP64 the cells whose FP32 discrete choices
 //     (transmittance table entry, conservative switch, resonance) are too
 //     close to call, for the whole pair at once (FP64 runs at a small
-//     fraction of the FP32 rate, so its cells are processed 32 at a time).
+//     fraction of the FP32 rate, so its cells are processed 32 at a time);
+//     then finishes the pair (below) and writes its outputs.
 //
 // A subcolumn with such a cell is left out of its tile's sums; its R/T
 // column is copied aside (global, per CTA) and swept again with the FP64
-// cells once the FP64 warp is done, its contribution added before the
-// pair's outputs are written (one pair later, so the wait is hidden).
-// Handoffs use mbarriers (tile full / empty, pair done, pair redone) whose
-// waits give up after ~2^33 cycles with an error code instead of hanging.
-// A pair with more such cells than the capacities below is listed for the
-// caller, which solves it again with the scratch-based kernel
-// (k_solve<float>).
+// cells by the FP64 warp, its contribution added before the pair's outputs
+// are written.  Handoffs use mbarriers (tile full / empty, pair produced,
+// pair swept, pair finished) whose waits give up after ~2^33 cycles with an
+// error code instead of hanging.  A pair with more such cells than the
+// capacities below is listed for the caller, which solves it again with the
+// scratch-based kernel (k_solve<float>).
 #pragma once
 
 #include "kernel.cuh"
 
 #ifndef RRSW_TILED_OPT
-#define RRSW_TILED_OPT 14
+#define RRSW_TILED_OPT 13
 #endif
 
 namespace rrsw {
@@ -49,14 +50,16 @@ constexpr int TW = 32;                                   // subcolumns per tile
 constexpr int TILES = COLS_PER_CTA * NGPT / TW;          // 7 tiles per pair
 constexpr int T_OPT = RRSW_TILED_OPT;                    // optics warps
 constexpr int T_REDO = T_OPT;                            // FP64 warp index
-constexpr int T_ADD = T_OPT + 1;                         // adding warp index
-constexpr int T_THREADS = (T_OPT + 2) * 32;
+constexpr int T_ADDC = T_OPT + 1;                        // adding warp, clear sky
+constexpr int T_ADDT = T_OPT + 2;                        // adding warp, total sky
+constexpr int T_THREADS = (T_OPT + 3) * 32;
 constexpr int T_QCAP = 128;                              // FP64 cells per pair
 constexpr int T_RCAP = 64;                               // subcolumns with such cells per pair
 constexpr int T_NF = 10;                                 // tile fields per cell
 constexpr int T_MAXL = 64;                               // layers (two mask words per subcolumn)
 enum { TF_REFC, TF_REFDC, TF_ADIRC, TF_ADIFC, TF_DBTC, TF_REF, TF_REFD, TF_ADIR, TF_ADIF, TF_DBT };
-enum { TB_FULL0, TB_FULL1, TB_EMPTY0, TB_EMPTY1, TB_PAIR0, TB_PAIR1, TB_REDO0, TB_REDO1, TB_N };
+enum { TB_FULL0, TB_FULL1, TB_EMPTY0, TB_EMPTY1, TB_PAIR0, TB_PAIR1, TB_SWEPT0, TB_SWEPT1, TB_FIN0, TB_FIN1,
+       TB_N };
 // control words in shared memory
 enum { TC_ROW0, TC_ROW1, TC_QN0, TC_QN1, TC_RN0, TC_RN1, TC_ABORT, TC_LT0, TC_LT1, TC_ACT0, TC_ACT1,
        TC_OVF0, TC_OVF1, TC_N };
@@ -65,7 +68,7 @@ enum { TC_ROW0, TC_ROW1, TC_QN0, TC_QN1, TC_RN0, TC_RN1, TC_ABORT, TC_LT0, TC_LT
 // the same function.
 struct TSmem {
     size_t bar, ctl, tm, tile, rup, coef, pk, hrf, mu, cld, mask, kc, ka, omcf, seed, sub, risky, queue, recof,
-        flux, scr, total;
+        flux, scr, scr2, total;
 };
 
 __host__ __device__ inline TSmem tiled_smem(int L, int nq, bool fused, bool cloud_stage) {
@@ -94,9 +97,10 @@ __host__ __device__ inline TSmem tiled_smem(int L, int nq, bool fused, bool clou
     m.queue = o; o = align16(o + (size_t)2 * T_QCAP * sizeof(int));
     m.recof = o; o = align16(o + (size_t)2 * COLS_PER_CTA * NGPT * sizeof(short));
     m.flux = o;  o = align16(o + (size_t)2 * COLS_PER_CTA * nq * (L + 1) * sizeof(float));
-    // adding warp: surface-level sums and lane keys of a tile, reduction
-    // scratch of the set-aside subcolumns (rows 6-7 hold 64-bit keys)
+    // adding warps: surface-level sums and lane keys of a tile
     m.scr = o;   o = align16(o + (size_t)16 * TW * sizeof(float));
+    // FP64 warp: reduction scratch of the set-aside subcolumns (rows 6-7: 64-bit keys)
+    m.scr2 = o;  o = align16(o + (size_t)16 * TW * sizeof(float));
     m.total = o;
     return m;
 }
@@ -105,7 +109,7 @@ __host__ __device__ inline TSmem tiled_smem(int L, int nq, bool fused, bool clou
 // aerosol staged in FP32, and per pair parity the FP64 layer coefficients,
 // the layer thicknesses, the FP64 cells and the set-aside subcolumns.
 struct TGlob {
-    size_t xs, aer, par, coef64, pk, lt, pdp, corr, rec, rec_stride, par_stride, total;
+    size_t xs, rrup, aer, par, coef64, pk, lt, pdp, corr, rec, rec_stride, par_stride, total;
 };
 
 __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -114,6 +118,7 @@ __host__ __device__ inline TGlob tiled_glob(int L) {
     TGlob g;
     size_t o = 0;
     g.xs = o;   o = align256(o + (size_t)NGPT * 32 * sizeof(uint32_t));
+    g.rrup = o; o = align256(o + (size_t)4 * L * TW * sizeof(float));   // FP64 warp: record sweeps' albedos
     g.aer = o;  o = align256(o + (size_t)COLS_PER_CTA * 3 * NBND * L * sizeof(float));
     g.par = o;
     size_t p = 0;
@@ -170,8 +175,9 @@ __device__ inline void mbar_wait(unsigned long long* b, unsigned parity, volatil
     }
 }
 
-// named barrier of the optics warps only
+// named barriers: the optics warps; the two adding warps
 __device__ inline void opt_sync() { asm volatile("bar.sync 1, %0;" ::"n"(T_OPT * 32) : "memory"); }
+__device__ inline void add_sync() { asm volatile("bar.sync 2, 64;" ::: "memory"); }
 
 // ------------------------------------------------------------- helpers
 struct TileView {
@@ -195,7 +201,8 @@ struct TileView {
     int* queue;       // [2][T_QCAP]
     short* recof;     // [2][224]
     float* flux;      // [2][2][NQ][L+1]
-    float* scr;       // [16][TW]
+    float* scr;       // [16][TW] adding warps
+    float* scr2;      // [16][TW] FP64 warp
 };
 
 __device__ inline TileView tile_view(unsigned char* raw, const TSmem& M) {
@@ -221,6 +228,7 @@ __device__ inline TileView tile_view(unsigned char* raw, const TSmem& M) {
     v.recof = (short*)(raw + M.recof);
     v.flux = (float*)(raw + M.flux);
     v.scr = (float*)(raw + M.scr);
+    v.scr2 = (float*)(raw + M.scr2);
     return v;
 }
 
@@ -228,84 +236,58 @@ __device__ inline TileView tile_view(unsigned char* raw, const TSmem& M) {
 __device__ inline float& tfield(float* tb, int L, int f, int i, int l) { return tb[((size_t)f * L + i) * TW + l]; }
 
 // ---------------------------------------------------------- adding method
-// State of the down-sweep of one subcolumn, clear and total sky, plus the
-// absorption of the layer above the current level for the heating rate.
-struct DownState {
-    float tdbtc, tdnc, rdndc, tdbt, tdn, rdnd;
-    float absc, abst, adifc_up, adift_up;
+// One sky's layer fields in a tile: reflectance, diffuse reflectance,
+// absorptance (direct, diffuse incidence), direct transmittance; the clear
+// sky's at TF_REFC, the total sky's at TF_REF.
+constexpr int SKY_BASE[2] = {TF_REFC, TF_REF};
+
+// State of one sky's down-sweep of one subcolumn, plus the absorption of the
+// layer above the current level for the heating rate.
+struct Down1 {
+    float tdbt, tdn, rdnd, abs, adif_up;
 };
 
-__device__ inline void down_init(DownState& s) {
-    s.tdbtc = s.tdnc = s.tdbt = s.tdn = 1.0f;
-    s.rdndc = s.rdnd = 0.0f;
-    s.absc = s.abst = s.adifc_up = s.adift_up = 0.0f;
+__device__ inline void down1_init(Down1& s) {
+    s.tdbt = s.tdn = 1.0f;
+    s.rdnd = s.abs = s.adif_up = 0.0f;
 }
 
-// Fluxes at a level whose upward albedos (below it) are rupc..rupd (vrtqdr:
-// 163-169), weighted by zinc: q = fu, fd, cu, cd, direct total / clear,
-// absorption of the layer above the level (total, clear; its lower face's
-// upward flux added here).  cdif / fdif are returned for the layer step.
-__device__ inline void level_q(const DownState& s, float rupc, float rupdc, float rup, float rupd, float zinc,
-                               float* q, float& cdif, float& fdif) {
-    const float zrc = 1.0f / (1.0f - s.rdndc * rupdc);
-    const float cu = (s.tdbtc * rupc + (s.tdnc - s.tdbtc) * rupdc) * zrc;
-    cdif = (s.tdnc - s.tdbtc + s.tdbtc * rupc * s.rdndc) * zrc;
-    const float cd = s.tdbtc + cdif;
-    const float zrt = 1.0f / (1.0f - s.rdnd * rupd);
-    const float fu = (s.tdbt * rup + (s.tdn - s.tdbt) * rupd) * zrt;
-    fdif = (s.tdn - s.tdbt + s.tdbt * rup * s.rdnd) * zrt;
-    const float fd = s.tdbt + fdif;
-    q[0] = zinc * fu;
-    q[1] = zinc * fd;
-    q[2] = zinc * cu;
-    q[3] = zinc * cd;
-    q[4] = zinc * s.tdbt;
-    q[5] = zinc * s.tdbtc;
-    q[6] = zinc * (s.abst + fu * s.adift_up);
-    q[7] = zinc * (s.absc + cu * s.adifc_up);
+// Fluxes at a level whose upward albedos (below it) are rup, rupd (vrtqdr:
+// 163-169), weighted by zinc: q = up, down, direct down, absorption of the
+// layer above the level (its lower face's upward flux added here); dif is
+// the diffuse down flux, for the layer step.
+__device__ inline void level1(const Down1& s, float rup, float rupd, float zinc, float* q, float& dif) {
+    const float zr = 1.0f / (1.0f - s.rdnd * rupd);
+    const float u = (s.tdbt * rup + (s.tdn - s.tdbt) * rupd) * zr;
+    dif = (s.tdn - s.tdbt + s.tdbt * rup * s.rdnd) * zr;
+    q[0] = zinc * u;
+    q[1] = zinc * (s.tdbt + dif);
+    q[2] = zinc * s.tdbt;
+    q[3] = zinc * (s.abs + u * s.adif_up);
 }
 
 // Through one layer downward (vrtqdr:144-159, direct beam spcvmc:575-585);
-// the layer's absorption is carried to the next level.
-__device__ inline void layer_down(DownState& s, const float* f, float cdif, float fdif) {
-    const float refc = f[TF_REFC], refdc = f[TF_REFDC], adirc = f[TF_ADIRC], adifc = f[TF_ADIFC], dbtc = f[TF_DBTC];
-    const float ref = f[TF_REF], refd = f[TF_REFD], adirt = f[TF_ADIR], adift = f[TF_ADIF], dbt = f[TF_DBT];
-    const float trac = 1.0f - refc - adirc, tradc = 1.0f - refdc - adifc;
-    const float tra = 1.0f - ref - adirt, trad = 1.0f - refd - adift;
-    s.abst = s.tdbt * adirt + fdif * adift;
-    s.absc = s.tdbtc * adirc + cdif * adifc;
-    s.adift_up = adift;
-    s.adifc_up = adifc;
-    const float zr1 = 1.0f / (1.0f - refdc * s.rdndc);
-    const float tdnc_n = s.tdbtc * trac + (tradc * ((s.tdnc - s.tdbtc) + s.tdbtc * refc * s.rdndc)) * zr1;
-    s.rdndc = refdc + tradc * tradc * s.rdndc * zr1;
-    s.tdnc = tdnc_n;
-    const float zr2 = 1.0f / (1.0f - refd * s.rdnd);
-    const float tdn_n = s.tdbt * tra + (trad * ((s.tdn - s.tdbt) + s.tdbt * ref * s.rdnd)) * zr2;
-    s.rdnd = refd + trad * trad * s.rdnd * zr2;
+// f = the sky's 5 fields.  The layer's absorption is carried to the next level.
+__device__ inline void down1(Down1& s, const float* f, float dif) {
+    const float ref = f[0], refd = f[1], adir = f[2], adif = f[3], dbt = f[4];
+    const float tra = 1.0f - ref - adir, trad = 1.0f - refd - adif;
+    s.abs = s.tdbt * adir + dif * adif;
+    s.adif_up = adif;
+    const float zr = 1.0f / (1.0f - refd * s.rdnd);
+    const float tdn_n = s.tdbt * tra + (trad * ((s.tdn - s.tdbt) + s.tdbt * ref * s.rdnd)) * zr;
+    s.rdnd = refd + trad * trad * s.rdnd * zr;
     s.tdn = tdn_n;
-    s.tdbtc = dbtc * s.tdbtc;
     s.tdbt = dbt * s.tdbt;
 }
 
-// One up-sweep step through a layer (vrtqdr:122-140).
-__device__ inline void up_step(const float* f, float& rupc, float& rupdc, float& rup, float& rupd) {
-    {
-        const float ref = f[TF_REFC], refd = f[TF_REFDC], dbt = f[TF_DBTC];
-        const float tra = 1.0f - ref - f[TF_ADIRC], trad = 1.0f - refd - f[TF_ADIFC];
-        const float zr = 1.0f / (1.0f - rupdc * refd);
-        const float r = ref + (trad * ((tra - dbt) * rupdc + dbt * rupc)) * zr;
-        rupdc = refd + trad * trad * rupdc * zr;
-        rupc = r;
-    }
-    {
-        const float ref = f[TF_REF], refd = f[TF_REFD], dbt = f[TF_DBT];
-        const float tra = 1.0f - ref - f[TF_ADIR], trad = 1.0f - refd - f[TF_ADIF];
-        const float zr = 1.0f / (1.0f - rupd * refd);
-        const float r = ref + (trad * ((tra - dbt) * rupd + dbt * rup)) * zr;
-        rupd = refd + trad * trad * rupd * zr;
-        rup = r;
-    }
+// One up-sweep step of one sky through a layer (vrtqdr:122-140).
+__device__ inline void up1(const float* f, float& rup, float& rupd) {
+    const float ref = f[0], refd = f[1], dbt = f[4];
+    const float tra = 1.0f - ref - f[2], trad = 1.0f - refd - f[3];
+    const float zr = 1.0f / (1.0f - rupd * refd);
+    const float r = ref + (trad * ((tra - dbt) * rupd + dbt * rup)) * zr;
+    rupd = refd + trad * trad * rupd * zr;
+    rup = r;
 }
 
 // ------------------------------------------------------------ the kernel
@@ -546,143 +528,152 @@ __device__ void tiled_redo(const SolveParams& P, const TCtx& X, int lp, const do
     }
 }
 
-// ---- adding warp: the vertical sweeps of tile t (buffer b) of pair lp
-template <int NQ>
+// Where a tile keeps the 8 weighted fluxes of a level after the sweeps:
+// level v >= 1 in the slots of layer v-1 that the sweeps have read (clear
+// sky in fields 0-3, total sky in fields 5-8), the surface level in rows of
+// scr.  Order of q: fu, fd, cu, cd, direct total, direct clear, absorption
+// total, absorption clear.
+__device__ __forceinline__ int q_total(int k) { return k < 4 ? ((k >> 1) & 1) == 0 : (k & 1) == 0; }
+__device__ __forceinline__ int q_comp(int k) { return k < 4 ? (k & 1) : (k < 6 ? 2 : 3); }
+__device__ __forceinline__ int q_slot(int k) { return (q_total(k) ? TF_REF : TF_REFC) + q_comp(k); }
+__device__ __forceinline__ int q_srow(int k) { return (q_total(k) ? 4 : 0) + q_comp(k); }
+
+// ---- adding warps: the vertical sweeps of tile t (buffer b) of pair lp,
+// sky SKY (0 clear, 1 total); then the g-point sums of half the levels
+template <int SKY, int NQ>
 __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, int b) {
     const TileView& V = X.V;
     const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
     const size_t n = (size_t)P.ncol, L1 = (size_t)L + 1;
+    constexpr int F0 = SKY_BASE[SKY];
     float* tb = V.tile + (size_t)b * T_NF * L * TW;
     const int s = TW * t + lane, c2 = s / NGPT, g = s % NGPT;
     const int ib = cT.ngb[g];
-    const bool uv = ib >= 9 && ib <= 12;  // bands 25-28 (spcvmc:629)
     const float* sub = V.sub + par * 3 * COLS_PER_CTA * NGPT;
     const float zinc = sub[s], albp = sub[COLS_PER_CTA * NGPT + s], albd = sub[2 * COLS_PER_CTA * NGPT + s];
     const bool act = V.ctl[TC_ACT0 + c2] != 0;
     const bool risky = (V.risky[par * TILES + t] >> lane) & 1u;
     const bool use = act && !risky;
-    float* R = V.rup;
-    // up-sweep from the surface (vrtqdr:122-140), the next layer's fields
-    // loaded while this one is swept
-    float rupc = albp, rupdc = albd, rup = albp, rupd = albd;
-    float f[T_NF], fn[T_NF];
-#pragma unroll
-    for (int k = 0; k < T_NF; ++k) f[k] = tfield(tb, L, k, 0, lane);
-    for (int i = 0; i < L; ++i) {
-        const int in = i + 1 < L ? i + 1 : i;
-#pragma unroll
-        for (int k = 0; k < T_NF; ++k) fn[k] = tfield(tb, L, k, in, lane);
-        up_step(f, rupc, rupdc, rup, rupd);
-        R[(0 * L + i) * TW + lane] = rupc;
-        R[(1 * L + i) * TW + lane] = rupdc;
-        R[(2 * L + i) * TW + lane] = rup;
-        R[(3 * L + i) * TW + lane] = rupd;
-#pragma unroll
-        for (int k = 0; k < T_NF; ++k) f[k] = fn[k];
-    }
-    // subcolumns with FP64 cells: their R/T column is set aside for the
-    // pair's second sweep, and they stay out of this tile's sums
+    // subcolumns with FP64 cells: each warp copies its sky's fields aside
+    // for the pair's second sweep; they stay out of this tile's sums
     const unsigned rm = __ballot_sync(0xffffffffu, act && risky);
     if (rm) {
         const int base = V.ctl[TC_RN0 + par];
         const int idx = base + __popc(rm & ((1u << lane) - 1u));
         if (act && risky && idx < T_RCAP) {
             float* rp = trec(X, par, idx);
-            rp[0] = (float)s;
-            rp[1] = (float)c2;
-            rp[2] = zinc;
-            rp[3] = albp;
-            rp[4] = albd;
-            for (int k = 0; k < T_NF; ++k)
+            for (int k = F0; k < F0 + 5; ++k)
                 for (int i = 0; i < L; ++i) rp[8 + k * L + i] = tfield(tb, L, k, i, lane);
-            V.recof[par * COLS_PER_CTA * NGPT + s] = (short)idx;
+            if (SKY == 1) {
+                rp[0] = (float)s;
+                rp[1] = (float)c2;
+                rp[2] = zinc;
+                rp[3] = albp;
+                rp[4] = albd;
+                V.recof[par * COLS_PER_CTA * NGPT + s] = (short)idx;
+            }
         }
-        __syncwarp();
-        if (lane == 0) {
+        add_sync();  // both warps have read the record count
+        if (SKY == 1 && lane == 0) {
             const int nb = base + __popc(rm);
             V.ctl[TC_RN0 + par] = nb;
             if (nb > T_RCAP) V.ctl[TC_OVF0 + par] = 1;
         }
-        __syncwarp();
     }
-    // down-sweep: the 8 weighted fluxes of level i+1 replace the fields of
-    // layer i, which were read just before (level 0, the surface, goes to scr)
-    DownState st;
-    down_init(st);
-    float q[8], rr[4], rn[4];
+    float* R = V.rup + (size_t)2 * SKY * L * TW;  // [2][L][TW]: rup, rupd of this sky
+    // up-sweep from the surface (vrtqdr:122-140), the next layer's fields
+    // loaded while this one is swept
+    float ru = albp, rud = albd;
+    float f[5], fn[5];
 #pragma unroll
-    for (int k = 0; k < T_NF; ++k) f[k] = tfield(tb, L, k, L - 1, lane);
+    for (int k = 0; k < 5; ++k) f[k] = tfield(tb, L, F0 + k, 0, lane);
+    for (int i = 0; i < L; ++i) {
+        const int in = i + 1 < L ? i + 1 : i;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) rr[k] = R[(k * L + L - 1) * TW + lane];
+        for (int k = 0; k < 5; ++k) fn[k] = tfield(tb, L, F0 + k, in, lane);
+        up1(f, ru, rud);
+        R[i * TW + lane] = ru;
+        R[(L + i) * TW + lane] = rud;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] = fn[k];
+    }
+    // down-sweep: this sky's 4 weighted fluxes of level i+1 replace its
+    // first 4 fields of layer i, read just before
+    Down1 st;
+    down1_init(st);
+    float q[4], rr[2], rn[2], dif;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) f[k] = tfield(tb, L, F0 + k, L - 1, lane);
+    rr[0] = R[(L - 1) * TW + lane];
+    rr[1] = R[(2 * L - 1) * TW + lane];
     for (int i = L - 1; i >= 0; --i) {
         const int in = i > 0 ? i - 1 : 0;
 #pragma unroll
-        for (int k = 0; k < T_NF; ++k) fn[k] = tfield(tb, L, k, in, lane);
+        for (int k = 0; k < 5; ++k) fn[k] = tfield(tb, L, F0 + k, in, lane);
+        rn[0] = R[in * TW + lane];
+        rn[1] = R[(L + in) * TW + lane];
+        level1(st, rr[0], rr[1], zinc, q, dif);
+        down1(st, f, dif);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) rn[k] = R[(k * L + in) * TW + lane];
-        float cdif, fdif;
-        level_q(st, rr[0], rr[1], rr[2], rr[3], zinc, q, cdif, fdif);
-        layer_down(st, f, cdif, fdif);
+        for (int k = 0; k < 4; ++k) tfield(tb, L, F0 + k, i, lane) = use ? q[k] : 0.0f;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) tfield(tb, L, k, i, lane) = use ? q[k] : 0.0f;
-#pragma unroll
-        for (int k = 0; k < T_NF; ++k) f[k] = fn[k];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) rr[k] = rn[k];
+        for (int k = 0; k < 5; ++k) f[k] = fn[k];
+        rr[0] = rn[0];
+        rr[1] = rn[1];
     }
-    {
-        float cdif, fdif;
-        level_q(st, albp, albd, albp, albd, zinc, q, cdif, fdif);
-    }
+    level1(st, albp, albd, zinc, q, dif);  // surface
 #pragma unroll
-    for (int k = 0; k < 8; ++k) V.scr[k * TW + lane] = use ? q[k] : 0.0f;
+    for (int k = 0; k < 4; ++k) V.scr[(4 * SKY + k) * TW + lane] = use ? q[k] : 0.0f;
     int* key = (int*)(V.scr + 8 * TW);
-    key[lane] = c2 * 16 + ib;
+    if (SKY == 1) key[lane] = c2 * 16 + ib;
+    const bool uv = ib >= 9 && ib <= 12;  // bands 25-28 (spcvmc:629)
     const unsigned uvm = __ballot_sync(0xffffffffu, uv);
-    __syncwarp();
-    // g-point sums, one lane per level; lanes of the tile's two columns (tile
-    // 3 holds the end of column 0 and the start of column 1) summed apart
+    add_sync();  // both skies' fluxes of every level are in place
+    // g-point sums, one lane per level, levels split between the two warps;
+    // lanes of the tile's two columns (tile 3 holds the end of column 0 and
+    // the start of column 1) summed apart
     const int c0 = (TW * t) / NGPT;
     const int cb = ((TW * t + TW - 1) / NGPT == c0) ? TW : NGPT * (c0 + 1) - TW * t;  // first lane of column 1
-    for (int v = lane; v <= L; v += 32) {
+    for (int v = lane + 32 * SKY; v <= L; v += 64) {
         const float* src = v ? tb + (size_t)(v - 1) * TW : V.scr;
         const int stride = v ? L * TW : TW;
+        int slot[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) slot[k] = (v ? q_slot(k) : q_srow(k)) * stride;
         float a0[8], a1[8], e0[8], e1[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) a0[k] = a1[k] = e0[k] = e1[k] = 0.0f;
         for (int m = 0; m < TW; ++m) {
             const int j = (m + lane) & 31;  // rotated: the lanes read 32 different banks
             const bool lo = j < cb;
-            const bool u = (uvm >> j) & 1u;
+            float x[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                const float x = src[k * stride + j];
-                if (lo) a0[k] += x;
-                else a1[k] += x;
+                x[k] = src[slot[k] + j];
+                if (lo) a0[k] += x[k];
+                else a1[k] += x[k];
             }
             if constexpr (NQ > 8) {
                 // UV (bands 25-28) / near-IR split of fd, cd and the direct fluxes
-                const float x1 = src[1 * stride + j], x3 = src[3 * stride + j];
-                const float x4 = src[4 * stride + j], x5 = src[5 * stride + j];
-                const int o = u ? 0 : 4;
+                const int o = ((uvm >> j) & 1u) ? 0 : 4;
                 float* e = lo ? e0 : e1;
-                e[o] += x1; e[o + 1] += x3; e[o + 2] += x4; e[o + 3] += x5;
+                e[o] += x[1]; e[o + 1] += x[3]; e[o + 2] += x[4]; e[o + 3] += x[5];
             }
         }
-        float* F0 = V.flux + ((size_t)(par * COLS_PER_CTA + c0) * NQ) * L1;
+        float* Fl0 = V.flux + ((size_t)(par * COLS_PER_CTA + c0) * NQ) * L1;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) F0[k * L1 + v] += a0[k];
+        for (int k = 0; k < 8; ++k) Fl0[k * L1 + v] += a0[k];
         if constexpr (NQ > 8) {
 #pragma unroll
-            for (int k = 0; k < 8; ++k) F0[(8 + k) * L1 + v] += e0[k];
+            for (int k = 0; k < 8; ++k) Fl0[(8 + k) * L1 + v] += e0[k];
         }
         if (cb < TW) {
-            float* F1 = F0 + (size_t)NQ * L1;
+            float* Fl1 = Fl0 + (size_t)NQ * L1;
 #pragma unroll
-            for (int k = 0; k < 8; ++k) F1[k * L1 + v] += a1[k];
+            for (int k = 0; k < 8; ++k) Fl1[k * L1 + v] += a1[k];
             if constexpr (NQ > 8) {
 #pragma unroll
-                for (int k = 0; k < 8; ++k) F1[(8 + k) * L1 + v] += e1[k];
+                for (int k = 0; k < 8; ++k) Fl1[(8 + k) * L1 + v] += e1[k];
             }
         }
         if (P.bands) {
@@ -697,7 +688,7 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
                 int e = j;
                 for (; e < TW && key[e] == kj; ++e)
 #pragma unroll
-                    for (int k = 0; k < 5; ++k) a[k] += src[qb[k] * stride + e];
+                    for (int k = 0; k < 5; ++k) a[k] += src[slot[qb[k]] + e];
                 const int pc = pair_col(P, pair, kj >> 4, X.nmapped);
                 if (pc < P.ncol) {
                     const size_t idx = (size_t)pc + n * ((size_t)v + L1 * (size_t)(kj & 15));
@@ -712,10 +703,11 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
     __syncwarp();
 }
 
-// ---- adding warp: sweeps of the set-aside subcolumns r0 .. r0+31 of pair lp
-// (their FP64 cells already patched in), added to the pair's level sums
+// ---- FP64 warp: sweeps of the set-aside subcolumns r0 .. r0+31 of pair lp
+// (their FP64 cells already patched in), added to the pair's level sums;
+// R: 4 x L x TW albedo scratch, scr: 16 x TW reduction scratch
 template <int NQ>
-__device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r0, int rn) {
+__device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r0, int rn, float* R, float* scr) {
     const TileView& V = X.V;
     const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
     const size_t n = (size_t)P.ncol, L1 = (size_t)L + 1;
@@ -727,13 +719,16 @@ __device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r
     const float zinc = on ? rp[2] : 0.0f, albp = rp[3], albd = rp[4];
     const int pcol = pair_col(P, pair, c2, X.nmapped);
     const float* fl = rp + 8;
-    float* R = V.rup;
     float rupc = albp, rupdc = albd, rup = albp, rupd = albd;
     for (int i = 0; i < L; ++i) {
-        float f[T_NF];
+        float fc[5], ft[5];
 #pragma unroll
-        for (int k = 0; k < T_NF; ++k) f[k] = fl[k * L + i];
-        up_step(f, rupc, rupdc, rup, rupd);
+        for (int k = 0; k < 5; ++k) {
+            fc[k] = fl[(TF_REFC + k) * L + i];
+            ft[k] = fl[(TF_REF + k) * L + i];
+        }
+        up1(fc, rupc, rupdc);
+        up1(ft, rup, rupd);
         R[(0 * L + i) * TW + lane] = rupc;
         R[(1 * L + i) * TW + lane] = rupdc;
         R[(2 * L + i) * TW + lane] = rup;
@@ -741,30 +736,37 @@ __device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r
     }
     const unsigned m0 = __ballot_sync(0xffffffffu, on && c2 == 0);
     const unsigned m1 = __ballot_sync(0xffffffffu, on && c2 == 1);
-    DownState st;
-    down_init(st);
+    Down1 sc, stt;
+    down1_init(sc);
+    down1_init(stt);
     float q[16];
     for (int i = L - 1; i >= -1; --i) {
-        float cdif, fdif;
+        float qc[4], qt[4], difc, dift;
         if (i >= 0) {
-            float f[T_NF];
+            float fc[5], ft[5];
 #pragma unroll
-            for (int k = 0; k < T_NF; ++k) f[k] = fl[k * L + i];
-            level_q(st, R[(0 * L + i) * TW + lane], R[(1 * L + i) * TW + lane], R[(2 * L + i) * TW + lane],
-                    R[(3 * L + i) * TW + lane], zinc, q, cdif, fdif);
-            layer_down(st, f, cdif, fdif);
+            for (int k = 0; k < 5; ++k) {
+                fc[k] = fl[(TF_REFC + k) * L + i];
+                ft[k] = fl[(TF_REF + k) * L + i];
+            }
+            level1(sc, R[(0 * L + i) * TW + lane], R[(1 * L + i) * TW + lane], zinc, qc, difc);
+            level1(stt, R[(2 * L + i) * TW + lane], R[(3 * L + i) * TW + lane], zinc, qt, dift);
+            down1(sc, fc, difc);
+            down1(stt, ft, dift);
         } else {
-            level_q(st, albp, albd, albp, albd, zinc, q, cdif, fdif);
+            level1(sc, albp, albd, zinc, qc, difc);
+            level1(stt, albp, albd, zinc, qt, dift);
         }
+        q[0] = qt[0]; q[1] = qt[1]; q[2] = qc[0]; q[3] = qc[1];
+        q[4] = qt[2]; q[5] = qc[2]; q[6] = qt[3]; q[7] = qc[3];
         if constexpr (NQ > 8) {
             const int o = uv ? 8 : 12, z = uv ? 12 : 8;
-            const float x1 = q[1], x3 = q[3], x4 = q[4], x5 = q[5];
-            q[o] = x1; q[o + 1] = x3; q[o + 2] = x4; q[o + 3] = x5;
+            q[o] = q[1]; q[o + 1] = q[3]; q[o + 2] = q[4]; q[o + 3] = q[5];
             q[z] = q[z + 1] = q[z + 2] = q[z + 3] = 0.0f;
         }
         const int l = i + 1;
 #pragma unroll
-        for (int k = 0; k < NQ; ++k) V.scr[k * TW + lane] = on ? q[k] : 0.0f;
+        for (int k = 0; k < NQ; ++k) scr[k * TW + lane] = on ? q[k] : 0.0f;
         __syncwarp();
         if (lane < 2 * NQ) {
             // one lane per (column, quantity), subcolumns in record order
@@ -775,7 +777,7 @@ __device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r
                 while (m) {
                     const int j = __ffs(m) - 1;
                     m &= m - 1;
-                    v += V.scr[k * TW + j];
+                    v += scr[k * TW + j];
                 }
                 V.flux[((size_t)(par * COLS_PER_CTA + c) * NQ + k) * L1 + l] += v;
             }
@@ -784,27 +786,27 @@ __device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r
         if (P.bands) {
             const float bv[5] = {q[0], q[1], q[4], q[2], q[3]};
 #pragma unroll
-            for (int k = 0; k < 5; ++k) V.scr[k * TW + lane] = on ? bv[k] : 0.0f;
-            long long* key = (long long*)(V.scr + 6 * TW);
+            for (int k = 0; k < 5; ++k) scr[k * TW + lane] = on ? bv[k] : 0.0f;
+            long long* key = (long long*)(scr + 6 * TW);
             key[lane] = on && pcol < P.ncol ? (long long)((size_t)pcol + n * ((size_t)l + L1 * (size_t)ib)) : -1ll;
             __syncwarp();
             if (lane < 5 && P.bout[lane]) {
                 // records in order, one lane per output array
                 for (int j = 0; j < TW; ++j)
-                    if (key[j] >= 0) P.bout[lane][key[j]] += (double)V.scr[lane * TW + j];
+                    if (key[j] >= 0) P.bout[lane][key[j]] += (double)scr[lane * TW + j];
             }
             __syncwarp();
         }
     }
 }
 
-// ---- adding warp: pair lp's set-aside subcolumns, outputs, reset
+// ---- FP64 warp: pair lp's set-aside subcolumns, outputs, reset (after both
+// adding warps have summed the pair's last tile)
 template <int NQ>
 __device__ void tiled_finish(const SolveParams& P, const TCtx& X, int lp) {
     const TileView& V = X.V;
     const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
     const size_t n = (size_t)P.ncol;
-    mbar_wait(&V.bar[TB_REDO0 + par], (lp >> 1) & 1, X.abort, P.err);
     const int qn = V.ctl[TC_QN0 + par], rn = V.ctl[TC_RN0 + par];
     const bool ovf = qn > X.qcap || V.ctl[TC_OVF0 + par] != 0;
     if (!ovf && rn > 0) {
@@ -820,7 +822,15 @@ __device__ void tiled_finish(const SolveParams& P, const TCtx& X, int lp) {
             }
         }
         __syncwarp();
-        for (int r0 = 0; r0 < rn; r0 += TW) tiled_records<NQ>(P, X, lp, r0, rn);
+        float* R = (float*)(X.glob + X.G.rrup);
+        for (int r0 = 0; r0 < rn; r0 += TW) tiled_records<NQ>(P, X, lp, r0, rn, R, V.scr2);
+    }
+    if (lane == 0 && P.stats) {
+        if (ovf) atomicAdd(P.stats + 2, 1ull);
+        else {
+            atomicAdd(P.stats, (unsigned long long)qn);
+            atomicAdd(P.stats + 3, (unsigned long long)rn);
+        }
     }
     if (ovf && lane == 0 && P.tovfcount) {
         // too many FP64 cells for the capacities: the caller solves the pair again
@@ -928,12 +938,14 @@ k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* 
     if (tid == 0) {
         mbar_init(&X.V.bar[TB_FULL0], T_OPT);
         mbar_init(&X.V.bar[TB_FULL1], T_OPT);
-        mbar_init(&X.V.bar[TB_EMPTY0], 1);
-        mbar_init(&X.V.bar[TB_EMPTY1], 1);
+        mbar_init(&X.V.bar[TB_EMPTY0], 2);
+        mbar_init(&X.V.bar[TB_EMPTY1], 2);
         mbar_init(&X.V.bar[TB_PAIR0], T_OPT);
         mbar_init(&X.V.bar[TB_PAIR1], T_OPT);
-        mbar_init(&X.V.bar[TB_REDO0], 1);
-        mbar_init(&X.V.bar[TB_REDO1], 1);
+        mbar_init(&X.V.bar[TB_SWEPT0], 2);
+        mbar_init(&X.V.bar[TB_SWEPT1], 2);
+        mbar_init(&X.V.bar[TB_FIN0], 1);
+        mbar_init(&X.V.bar[TB_FIN1], 1);
     }
     // KISS: the xorshift part of each subcolumn's stream jump (depends on g)
     if (X.fused && !MT && tid < NGPT)
@@ -944,6 +956,8 @@ k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* 
         if (X.fused && !MT && tid < COLS_PER_CTA * NGPT)
             J = kiss_jump_consts(kiss_offset(P.icld, tid % NGPT, L, P.permuteseed));
         for (int lp = 0; lp < X.nlocal; ++lp) {
+            // pair lp - 2 is finished: its parity's per-pair state is free
+            if (lp >= 2) mbar_wait(&X.V.bar[TB_FIN0 + (lp & 1)], ((lp - 2) >> 1) & 1, X.abort, P.err);
             opt_sync();  // the previous pair's cells are all written
             tiled_prep<MT>(P, X, lp, J, tab64, tab);
             for (int t = 0; t < TILES; ++t) {
@@ -960,40 +974,42 @@ k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* 
         }
     } else if (warp == T_REDO) {
         for (int lp = 0; lp < X.nlocal; ++lp) {
-            mbar_wait(&X.V.bar[TB_PAIR0 + (lp & 1)], (lp >> 1) & 1, X.abort, P.err);
+            const int par = lp & 1;
+            mbar_wait(&X.V.bar[TB_PAIR0 + par], (lp >> 1) & 1, X.abort, P.err);
             tiled_redo(P, X, lp, tab64);
             __syncwarp();
+            mbar_wait(&X.V.bar[TB_SWEPT0 + par], (lp >> 1) & 1, X.abort, P.err);
+            if (NQ > 8) tiled_finish<16>(P, X, lp);
+            else tiled_finish<8>(P, X, lp);
             __threadfence_block();
-            if (lane == 0) mbar_arrive(&X.V.bar[TB_REDO0 + (lp & 1)]);
+            if (lane == 0) mbar_arrive(&X.V.bar[TB_FIN0 + par]);
         }
     } else {
-        int pend = -1;
+        const int sky = warp == T_ADDT ? 1 : 0;
         for (int lp = 0; lp < X.nlocal; ++lp) {
-            if (P.bands) tiled_zero_bands(P, X, lp);
+            const int par = lp & 1;
+            // pair lp - 2 is finished: its level sums and set-aside state are free
+            if (lp >= 2) mbar_wait(&X.V.bar[TB_FIN0 + par], ((lp - 2) >> 1) & 1, X.abort, P.err);
+            if (P.bands && sky == 1) tiled_zero_bands(P, X, lp);
             for (int t = 0; t < TILES; ++t) {
                 const int T = TILES * lp + t, b = T & 1;
                 mbar_wait(&X.V.bar[TB_FULL0 + b], (T >> 1) & 1, X.abort, P.err);
-                if (NQ > 8) tiled_sweep<16>(P, X, lp, t, b);
-                else tiled_sweep<8>(P, X, lp, t, b);
+                if (sky) {
+                    if (NQ > 8) tiled_sweep<1, 16>(P, X, lp, t, b);
+                    else tiled_sweep<1, 8>(P, X, lp, t, b);
+                } else {
+                    if (NQ > 8) tiled_sweep<0, 16>(P, X, lp, t, b);
+                    else tiled_sweep<0, 8>(P, X, lp, t, b);
+                }
                 __syncwarp();
                 if (lane == 0) {
-                    X.V.ctl[TC_ROW0 + b] = 0;
+                    if (sky == 1) X.V.ctl[TC_ROW0 + b] = 0;
                     __threadfence_block();
                     mbar_arrive(&X.V.bar[TB_EMPTY0 + b]);
+                    if (t == TILES - 1) mbar_arrive(&X.V.bar[TB_SWEPT0 + par]);
                 }
                 __syncwarp();
-                // the previous pair is finished while this one's tiles come in
-                if (pend >= 0 && t == 1) {
-                    if (NQ > 8) tiled_finish<16>(P, X, pend);
-                    else tiled_finish<8>(P, X, pend);
-                    pend = -1;
-                }
             }
-            pend = lp;
-        }
-        if (pend >= 0) {
-            if (NQ > 8) tiled_finish<16>(P, X, pend);
-            else tiled_finish<8>(P, X, pend);
         }
     }
 }

@@ -110,6 +110,7 @@ def lib():
         L.mcica_subcol_sw_c.argtypes = [C.c_int32] * 5 + [_dp] * 11 + [_dp] * 9
         L.get_alpha_c.argtypes = [C.c_int32] * 4 + [C.c_double, _dp, _dp, C.c_int32, _dp, _dp]
         L.rrtmg_sw_set_form_c.argtypes = [C.c_int32]
+        L.rrtmg_sw_setcoef_c.argtypes = [C.POINTER(RrtmgSwArgs)] + [C.POINTER(C.c_int32)] * 6
         L.rrtmg_sw_mt_window_c.argtypes = [C.c_int32, C.c_uint64, C.POINTER(C.c_uint32)]
         L.rrtmg_sw_mt_stream_dev_c.argtypes = [C.c_int32, C.c_uint64, C.c_void_p, C.c_int32, C.c_void_p]
         L.rrtmg_sw_errstr_c.restype = C.c_char_p
@@ -405,3 +406,39 @@ class BatchPlan:
 
 def last_launch_count():
     return lib().rrtmg_sw_last_launch_count_c()
+
+
+KERNEL_FP64, KERNEL_FP32, KERNEL_FP32_TILED = 0, 1, 2
+
+
+def last_kernel():
+    """Kernel of the most recent solve's main launch (KERNEL_*; -1 before any)."""
+    return lib().rrtmg_sw_last_kernel_c()
+
+
+def last_fp32_stats():
+    """FP32 form's counters of the most recent solve: cells redone in FP64,
+    of those past the scratch kernel's queue, column pairs the tiled kernel
+    handed back, subcolumns the tiled kernel swept a second time."""
+    out = (C.c_int64 * 4)()
+    _check(lib().rrtmg_sw_last_fp32_stats_c(out))
+    return dict(redone_cells=out[0], past_queue=out[1], pairs_handed_back=out[2], subcolumns_swept_twice=out[3])
+
+
+def setcoef_indices(ncol, nlay, play, plev, tlay, h2ovmr, o3vmr, co2vmr, ch4vmr, o2vmr, **_):
+    """setcoef_sw's indices (rrtmg_sw_setcoef.f90:158-200) as the solve kernels compute them:
+    dict of jp, jt, jt1, indself, indfor (ncol, nlay) and laytrop (ncol), int32."""
+    cl = (ncol, nlay)
+    keep = [_f(play, cl), _f(plev, (ncol, nlay + 1)), _f(tlay, cl), _f(h2ovmr, cl), _f(o3vmr, cl),
+            _f(co2vmr, cl), _f(ch4vmr, cl), _f(o2vmr, cl)]
+    a = RrtmgSwArgs()
+    a.ncol, a.nlay = ncol, nlay
+    for k, v in zip(("play", "plev", "tlay", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "o2vmr"), keep):
+        setattr(a, k, v.ctypes.data_as(_dp))
+    outs = {k: np.zeros(cl, dtype=np.int32, order="F") for k in ("jp", "jt", "jt1", "indself", "indfor")}
+    lt = np.zeros(ncol, dtype=np.int32)
+    ip = lambda x: x.ctypes.data_as(C.POINTER(C.c_int32))
+    _check(lib().rrtmg_sw_setcoef_c(C.byref(a), *[ip(outs[k]) for k in ("jp", "jt", "jt1", "indself", "indfor")],
+                                    ip(lt)))
+    outs["laytrop"] = lt
+    return outs

@@ -1,11 +1,12 @@
 """The FP32 form's tiled kernel (layer R/T in shared memory, vertical adding
-by one warp per tile of 32 subcolumns, FP64 cells redone by a dedicated
-warp) against the FP64 oracle and against the scratch-based FP32 kernel.
+by two warps, clear and total sky, per tile of 32 subcolumns, FP64 cells
+redone by a dedicated warp) against the FP64 oracle and against the scratch-based FP32 kernel.
 
 Tolerances: |dF| <= 0.05 W m-2 and |dHR| <= 0.01 K/day against the oracle
 (the FP32 form's bounds); against the scratch-based FP32 kernel, which makes
 the same discrete choices, 1e-3 W m-2 and 1e-4 K/day.  The library chooses
-the kernel for nlay <= 64 with idelm = 1; RRTMG_SW_TILED=0 (read at
+the kernel for nlay <= 64 with idelm = 1 when its shared memory fits (every
+case here asserts which kernel ran); RRTMG_SW_TILED=0 (read at
 rrtmg_sw_ini_c) keeps the scratch-based kernel, and RRTMG_SW_TILE_QCAP
 lowers the tiled kernel's capacity of FP64 cells per column pair so that its
 fallback (pairs solved again by the scratch-based kernel) runs.
@@ -60,12 +61,17 @@ def case(ncol, nlay, seed, icld, iaer=0):
     return c, clouds, alpha
 
 
-def run_fp32(c, clouds, icld, iaer, bands=False):
+def run_fp32(c, clouds, icld, iaer, bands=False, extra=False, tiled=None):
     gpu.set_form(gpu.FORM_FP32)
     try:
-        res = gpu.rrtmg_sw(**gcm_inputs(c, icld=icld, iaer=iaer), clouds=clouds, extra=True, bands=bands)
+        res = gpu.rrtmg_sw(**gcm_inputs(c, icld=icld, iaer=iaer), clouds=clouds, extra=extra, bands=bands)
     finally:
         gpu.set_form(gpu.FORM_FP64)
+    if not isinstance(res, dict):
+        res = dict(zip(("swuflx", "swdflx", "swhr", "swuflxc", "swdflxc", "swhrc"), res))
+    if tiled is not None:
+        want = gpu.KERNEL_FP32_TILED if tiled else gpu.KERNEL_FP32
+        assert gpu.last_kernel() == want, (gpu.last_kernel(), want)
     return res
 
 
@@ -99,7 +105,7 @@ def check_bounds(g, o, fl=0.05, hr=0.01):
 def test_tiled_against_oracle(icld, iaer):
     set_env(tiled=True)
     c, clouds, alpha = case(300, 60, 20261220 + icld + iaer, icld, iaer)
-    g = run_fp32(c, clouds, icld, iaer)
+    g = run_fp32(c, clouds, icld, iaer, tiled=True)
     assert gpu.lib().rrtmg_sw_last_launch_count_c() == 1
     check_bounds(g, oracle(c, icld, iaer, alpha))
 
@@ -108,16 +114,16 @@ def test_tiled_against_oracle(icld, iaer):
 def test_tiled_layer_counts_odd_ncol(nlay):
     set_env(tiled=True)
     c, clouds, alpha = case(37, nlay, 7000 + nlay, 2)
-    check_bounds(run_fp32(c, clouds, 2, 0), oracle(c, 2, 0, alpha))
+    check_bounds(run_fp32(c, clouds, 2, 0, tiled=True), oracle(c, 2, 0, alpha))
 
 
 def test_tiled_matches_scratch_kernel_with_outputs():
     # extra (direct/diffuse, UV/NIR) and per-band outputs, tiled vs scratch-based FP32 kernel
     c, clouds, alpha = case(256, 60, 20261230, 5)
     set_env(tiled=False)
-    ref = run_fp32(c, clouds, 5, 0, bands=True)
+    ref = run_fp32(c, clouds, 5, 0, bands=True, extra=True, tiled=False)
     set_env(tiled=True)
-    got = run_fp32(c, clouds, 5, 0, bands=True)
+    got = run_fp32(c, clouds, 5, 0, bands=True, extra=True, tiled=True)
     for k in FLUX + tuple(gpu.EXTRA_OUTPUTS) + tuple(gpu.BAND_OUTPUTS):
         assert np.max(np.abs(got[k] - ref[k])) <= 1e-3, (k, float(np.max(np.abs(got[k] - ref[k]))))
     for k in HR:
@@ -127,8 +133,11 @@ def test_tiled_matches_scratch_kernel_with_outputs():
 def test_tiled_is_deterministic():
     set_env(tiled=True)
     c, clouds, alpha = case(500, 60, 20261231, 5)
-    a = run_fp32(c, clouds, 5, 0)
-    b = run_fp32(c, clouds, 5, 0)
+    a = run_fp32(c, clouds, 5, 0, extra=True, tiled=True)
+    b = run_fp32(c, clouds, 5, 0, extra=True, tiled=True)
+    st = gpu.last_fp32_stats()
+    # cloudy columns have FP64 cells; none handed back at full capacity
+    assert st["redone_cells"] > 0 and st["subcolumns_swept_twice"] > 0 and st["pairs_handed_back"] == 0, st
     for k in FLUX + HR:
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
 
@@ -138,7 +147,19 @@ def test_tiled_overflow_fallback():
     # second time by the scratch-based kernel
     c, clouds, alpha = case(400, 60, 20261232, 5)
     set_env(tiled=True, qcap=1)
-    g = run_fp32(c, clouds, 5, 0)
+    g = run_fp32(c, clouds, 5, 0, tiled=True)
     assert gpu.lib().rrtmg_sw_last_launch_count_c() == 2
+    st = gpu.last_fp32_stats()
+    assert st["pairs_handed_back"] > 0 and st["redone_cells"] > 0, st
     check_bounds(g, oracle(c, 5, 0, alpha))
     set_env(tiled=True)
+
+
+def test_tiled_shared_memory_limit():
+    # 64 layers: the clear-sky kernel fits in shared memory, the McICA one
+    # (subcolumn masks and cloud staging) does not and runs the scratch kernel
+    set_env(tiled=True)
+    c, clouds, alpha = case(41, 64, 7064, 2)
+    check_bounds(run_fp32(c, clouds, 2, 0, tiled=False), oracle(c, 2, 0, alpha))
+    c, clouds, alpha = case(41, 64, 7065, 0)
+    check_bounds(run_fp32(c, None, 0, 0, tiled=True), oracle(c, 0, 0, None))
