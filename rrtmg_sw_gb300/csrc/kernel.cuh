@@ -170,21 +170,36 @@ __device__ inline void aerosol(const SolveParams& P, int col, int lay, int ib, c
     }
 }
 
-// Whether the FP32 estimate of 1 - zwo (reftra:183-188) is too close to the
-// 5e-7 switch to trust its branch.  The window is an error bound from the
-// FP32 optics: 2e-6 relative on the co-albedo and on the asymmetry.  Near
-// zg = 0.5, where the reference's q = zg / (1 - zg) reaches 1, 1 - zwo
-// falls steeply with zg and the window widens accordingly.
-__device__ inline bool near_conservative_edge(float zw, float zco, float zg) {
-    if (zg == 1.0f || !(zw > 0.0f)) return false;
-    const float r = one_minus_zwo(zw, zco, zg);
+// FP32 form: 1 - zwo of reftra:183-186 from the co-albedo (zwo = zw / (1 -
+// zco q^2), q = zg / (1 - zg); 1 where the reference leaves zwo = 0), and
+// in `edge` whether that estimate is too close to the 5e-7 switch to trust
+// its branch.  The window is an error bound from the FP32 optics: 2e-6
+// relative on the co-albedo and on the asymmetry.  Near zg = 0.5, where q
+// reaches 1, 1 - zwo falls steeply with zg and the window widens
+// accordingly.  With den >= 1/4 and zg <= 0.9 the window is below
+// 0.0544 |zco| + 1e-13, so cells farther than 0.0631 |zco| + 1e-12 from the
+// switch skip its evaluation.
+__device__ inline float conservative_test(float zw, float zco, float zg, bool& edge) {
+    edge = false;
+    if (zg == 1.0f) return zw > 0.0f ? zco : 1.0f;
+    if (!(zw > 0.0f)) return 1.0f;
     const float q = zg / (1.0f - zg);
-    const float den = 1.0f - zco * q * q;
-    if (den == 0.0f) return true;
-    const float d_dg = 2.0f * zco * q * (1.0f - zco) / (den * den * (1.0f - zg) * (1.0f - zg));
-    const float d_dco = fabsf(1.0f - q * q) / (den * den);
+    const float q2 = q * q;
+    const float den = 1.0f - zco * q2;
+    if (den == 0.0f) {
+        edge = true;
+        return 1.0f;
+    }
+    const float rden = 1.0f / den;
+    const float r = zco * (1.0f - q2) * rden;
+    const float dist = fabsf(r - 5.0e-7f);
+    if (den >= 0.25f && zg <= 0.9f && dist > 0.0631f * fabsf(zco) + 1.0e-12f) return r;
+    const float rd2 = rden * rden, opq = 1.0f + q;  // 1 + q = 1 / (1 - zg)
+    const float d_dg = 2.0f * zco * q * (1.0f - zco) * rd2 * opq * opq;
+    const float d_dco = fabsf(1.0f - q2) * rd2;
     const float tol = d_dg * (2.0e-6f * fabsf(zg) + 1.0e-9f) + d_dco * 2.0e-6f * zco + 1.0e-13f;
-    return fabsf(r - 5.0e-7f) <= tol;
+    edge = dist <= tol;
+    return r;
 }
 
 // Optical inputs of one (g-point, layer) cell: gas and Rayleigh depths,

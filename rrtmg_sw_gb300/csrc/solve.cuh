@@ -744,18 +744,6 @@ __device__ inline RT<double> reftra_g<double>(double zto1, double zw, double zco
     return reftra_fp64(zto1, zw, zg, prmuz, tab);
 }
 
-// 1 - zwo of reftra:183-186 from the co-albedo (zwo = zw / (1 - zco q^2),
-// q = zg / (1 - zg)); returns 1 when the reference leaves zwo = 0.
-template <typename R>
-__device__ inline R one_minus_zwo(R zw, R zco, R zg) {
-    if (zg == R(1)) return zw > R(0) ? zco : R(1);
-    const R q = zg / (R(1) - zg);
-    const R q2 = q * q;
-    const R denom = R(1) - zco * q2;
-    if (!(zw > R(0) && denom != R(0))) return R(1);
-    return zco * (R(1) - q2) / denom;
-}
-
 // ------------------------------------------------------------------ KISS
 // KISS generator (mcica_subcol_gen_sw.f90:721-753).  Subcolumn g of a
 // column consumes the column's stream from position n = permuteseed +

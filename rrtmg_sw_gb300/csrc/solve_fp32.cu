@@ -47,9 +47,15 @@ __device__ inline float tbl_exp_om(float x, const float* __restrict__ tab, float
 // |zrpp| < RESONANCE_TOL zw, or with |zrpp| < RESONANCE_WIDE and a table
 // lookup too close to an entry edge to be sure of, are flagged risky; the
 // caller then recomputes the cell as the FP64 form does.  So are cells
-// whose conservative switch is too close.
+// whose conservative switch is too close.  The edge window near resonance
+// is RESONANCE_EPS relative in the lookup's argument, about four times the
+// FP32 optical depth's own error: strongly absorbing clear layers under a
+// sun near 60 degrees (k ~ 2, mu0 ~ 0.5) sit at resonance, and with a
+// narrower window (5e-7) a flipped entry there moved one UV layer's heating
+// rate by 0.01 K/day.
 constexpr float RESONANCE_TOL = 2.0e-3f;
 constexpr float RESONANCE_WIDE = 5.0e-2f;
+constexpr float RESONANCE_EPS = 2.0e-6f;
 constexpr float CLOUD_EDGE_EPS = 2.0e-7f;  // window of the cloudy total-sky lookups
 
 // Whether exp(-x) from the table could come from the neighbouring entry
@@ -64,7 +70,7 @@ __device__ inline bool entry_edge(float x, float eps) {
 }
 
 template <>
-__device__ __noinline__ RT<float> reftra_g<float>(float zto1, float zw, float zco, float zg, float prmuz,
+__device__ __forceinline__ RT<float> reftra_g<float>(float zto1, float zw, float zco, float zg, float prmuz,
                                            const float* __restrict__ tab, const double* __restrict__ tab64,
                                            int force) {
     RT<float> o;
@@ -76,10 +82,11 @@ __device__ __noinline__ RT<float> reftra_g<float>(float zto1, float zw, float zc
     const float zgamma4 = 1.0f - zgamma3;
     // zwo >= zwcrit  <=>  1 - zwo <= 5e-7  (reftra:183-188)
     (void)tab64;
-    const bool cons = one_minus_zwo(zw, zco, zg) <= 5.0e-7f;
+    bool edge;
+    const bool cons = conservative_test(zw, zco, zg, edge) <= 5.0e-7f;
     o.adir = 0.0f;
     o.adif = 0.0f;
-    o.risky = near_conservative_edge(zw, zco, zg);
+    o.risky = edge;
     if (cons) {
         // conservative scattering (reftra:191-228); ptra = 1 - pref and
         // ptrad = 1 - prefd written without the subtraction; no absorption
@@ -119,7 +126,7 @@ __device__ __noinline__ RT<float> reftra_g<float>(float zto1, float zw, float zc
     // force = 1 (cloudy total sky): a neighbouring table entry moves pref/ptra
     // of a thick layer enough to show in the fluxes, so every lookup is tested
     if ((force == 1 || fabsf(zrpp) < RESONANCE_WIDE) && !o.risky) {
-        const float eps = fabsf(zrpp) < RESONANCE_WIDE ? 5.0e-7f : CLOUD_EDGE_EPS;
+        const float eps = fabsf(zrpp) < RESONANCE_WIDE ? RESONANCE_EPS : CLOUD_EDGE_EPS;
         o.risky = entry_edge(fminf(zrk * zto1, 500.0f), eps) || entry_edge(fminf(zto1 / prmuz, 500.0f), eps);
     }
     const float p1 = om1 / zem1;  // zep1 - 1

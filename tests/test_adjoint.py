@@ -129,3 +129,51 @@ def test_smooth_model_is_close_to_the_table_model(gpu):
     ad = gpu.rrtmg_sw_ad(kw, cl, (1.0, 0.0, 0.0))
     res = gpu.rrtmg_sw(**kw, extra=True)
     np.testing.assert_allclose(ad["J"], res["swuflx"][:, -1], atol=0.5)
+
+
+def config4_subset(ncol=256):
+    """The first `ncol` columns of the 65 536-column x 60-layer McICA set the
+    adjoint is timed on (icld=2, seed 20261203 + 4, model top 0.01 hPa)."""
+    c = make_columns(65536, 60, 20261203 + 4, clouds=True)
+    c = {k: (v[:ncol] if isinstance(v, np.ndarray) and v.shape[:1] == (65536,) else v) for k, v in c.items()}
+    kw = gcm_inputs(c, icld=2, iaer=0)
+    cl = dict(permuteseed=112, irng=0, cldfrac=c["cldfrac"], ciwp=c["ciwp"], clwp=c["clwp"], rei=c["rei"],
+              rel=c["rel"])
+    return kw, cl
+
+
+@pytest.mark.parametrize("weights", [(1.0, 0.0, 0.0), (0.0, 1.0, 0.0)])
+def test_config4_subset_tangent_linear_matches_central_differences(gpu, weights):
+    # 256 columns x 60 layers: FD with relative step 1e-6 within 1e-6 of the
+    # largest |dJ|.  The heating-rate sum is left to the transpose check below:
+    # with this set's 0.01 hPa top its FD quotient is dominated by the FP64
+    # rounding of J (see the module docstring).
+    kw, cl = config4_subset()
+    d = direction(kw, cl, 17)
+    tl = gpu.rrtmg_sw_tl(kw, d, cl, weights)
+    h = 1.e-6
+
+    def J(step):
+        k2, c2 = shifted(kw, cl, d, step)
+        return gpu.rrtmg_sw_tl(k2, {}, c2, weights)["J"]
+
+    fd = (J(h) - J(-h)) / (2.0 * h)
+    scale = max(np.max(np.abs(fd)), 1e-300)
+    err = np.max(np.abs(tl["dJ"] - fd)) / scale
+    assert err <= 1e-6, err
+
+
+def test_config4_subset_adjoint_is_transpose_of_tangent_linear(gpu):
+    kw, cl = config4_subset()
+    weights = (0.5, -1.0, 2.0)
+    d = direction(kw, cl, 18)
+    tl = gpu.rrtmg_sw_tl(kw, d, cl, weights)
+    for store in (True, False):
+        ad = gpu.rrtmg_sw_ad(kw, cl, weights, store=store)
+        dot = np.zeros(kw["ncol"])
+        for k in gpu.AD_LAYER:
+            dot += np.sum(ad[k] * d[k], axis=1)
+        for k in gpu.AD_SFC:
+            dot += ad[k] * d[k]
+        scale = max(np.max(np.abs(tl["dJ"])), 1e-300)
+        assert np.max(np.abs(dot - tl["dJ"])) / scale <= 1e-9, store
