@@ -243,6 +243,9 @@ def run_adjoint(args):
         return min(ts) * 1e3
 
     fwd = best(lambda: gi.rrtmg_sw(**kw, clouds=cl))
+    gi.set_form(gi.FORM_FP32)
+    fwd32 = best(lambda: gi.rrtmg_sw(**kw, clouds=cl))
+    gi.set_form(gi.FORM_FP64)
     d = {k: np.ones_like(kw["tlay"]) for k in gi.AD_LAYER}
     tl = best(lambda: gi.rrtmg_sw_tl(kw, d, cl, w))
     ad_s = best(lambda: gi.rrtmg_sw_ad(kw, cl, w, store=True))
@@ -254,11 +257,13 @@ def run_adjoint(args):
     except Exception:
         pass
     slot = lambda fields: ((NLAY + 1) * fields * 224 + 2 * 15 * NLAY * 4) * 8
-    line = {"metric": "adjoint cost relative to the FP64 forward (host-array calls, end to end)",
+    line = {"metric": "adjoint cost relative to the FP64 forward it differentiates (host-array calls, end to end)",
             "value": ad_s / fwd, "unit": "x forward", "n_gpus": 1, "higher_is_better": False,
             "config": {"workload": "%d columns x %d layers, McICA icld=2, objective TOA up + sfc net + HR sum"
                                    % (ncol, NLAY)},
-            "forward_fp64_ms": fwd, "tangent_linear_ms": tl, "adjoint_store_ms": ad_s, "adjoint_recompute_ms": ad_r,
+            "forward_fp64_ms": fwd, "forward_fp32_ms": fwd32, "tangent_linear_ms": tl, "adjoint_store_ms": ad_s,
+            "adjoint_recompute_ms": ad_r, "adjoint_store_vs_fp64_forward": ad_s / fwd,
+            "adjoint_store_vs_fp32_forward": ad_s / fwd32, "adjoint_recompute_vs_fp64_forward": ad_r / fwd,
             "scratch_bytes_store": slot(45) * sms, "scratch_bytes_recompute": slot(20) * sms}
     print(json.dumps(line))
 

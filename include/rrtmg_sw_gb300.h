@@ -234,10 +234,13 @@ int rrtmg_sw_batch_free_c(void *plan);
  *     entry point is never called.
  *   - Limit: the area must hold one scratch slot per SM, or per column pair
  *     when the call has fewer pairs than SMs.  A slot is nlay * (16 with
- *     idelm = 0, else 14) * 224 values of the form's type (the FP32 form
- *     adds 60 * nlay floats), so 256 MiB takes nlay <= 138 (FP32) or <= 70
- *     (FP64) with idelm = 1 on a 152-SM GPU and at least 304 columns.
- *     Larger requests return RRTMG_SW_ESCRATCH, nothing runs.
+ *     idelm = 0, else 14) * 224 values of the form's type, so 256 MiB
+ *     takes nlay <= 140 (FP32) or <= 70 (FP64) with idelm = 1 on a 152-SM
+ *     GPU and at least 304 columns.  Larger requests return
+ *     RRTMG_SW_ESCRATCH, nothing runs.  The FP32 form's tiled kernel needs
+ *     instead its per-SM areas plus one prepared block per column pair
+ *     (about 16 KB at 60 layers); calls whose blocks do not fit take the
+ *     scratch-based kernel.
  *     Fewer resident CTAs than rrtmg_sw_dev_c may run when the slots that
  *     fit are fewer than its grid; results are identical, only slower.
  *   - Nothing needs to start at zero: every scratch value is written before
@@ -288,7 +291,10 @@ int rrtmg_sw_mt_stream_dev_c(int32_t seed, uint64_t n, uint32_t *out, int32_t lo
  * rrtmg_sw_rad.f90:1527-1586): jp, jt, jt1, indself, indfor (ncol,nlay) and
  * laytrop (ncol), host arrays.  Only the state inputs of `a` are read (play,
  * plev, tlay and the gas mixing ratios).  A diagnostic for checking the
- * table indices bit for bit against another implementation. */
+ * table indices bit for bit against another implementation.  Computed as
+ * the current arithmetic form computes them: the FP32 form's setcoef (FP32
+ * arithmetic, each index re-evaluated in FP64 where its FP32 value is within
+ * 1e-4 of an integer or threshold) returns the FP64 form's indices. */
 int rrtmg_sw_setcoef_c(const rrtmg_sw_args *a, int32_t *jp, int32_t *jt, int32_t *jt1, int32_t *indself,
                        int32_t *indfor, int32_t *laytrop);
 

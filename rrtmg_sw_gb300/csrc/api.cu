@@ -57,8 +57,9 @@ struct State {
     unsigned long long* h_stats = nullptr;  // pinned: the FP32 form's counters of the last solve
     DevBuf statsw;                         // their device copy
     long long last_stats[4] = {0, 0, 0, 0};
-    // diagnostics, from the environment at each rrtmg_sw_ini_c: RRTMG_SW_TILED=1
-    // puts the FP32 form on the tiled kernel; RRTMG_SW_TILE_QCAP=n
+    // from the environment at each rrtmg_sw_ini_c: RRTMG_SW_TILED=0 keeps the
+    // FP32 form on the scratch-based kernel (the tiled kernel is the default
+    // where it applies); RRTMG_SW_TILE_QCAP=n
     // lowers the tiled kernel's capacity of FP64 cells per column pair (tests
     // of its fallback)
     bool no_tiled = false;
@@ -592,15 +593,19 @@ int enqueue_solve(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, c
     st.last_kernel = !fp32 ? RRTMG_SW_KERNEL_FP64 : li.tiled ? RRTMG_SW_KERNEL_FP32_TILED : RRTMG_SW_KERNEL_FP32;
     if (!fp32) li.slot_bytes = slot_elems(P.nlay, P.idelm, false) * sizeof(double);
     P.slot_elems = li.slot_bytes / (fp32 ? sizeof(float) : sizeof(double));
-    const size_t off = ovf_offset((size_t)li.grid * li.slot_bytes);
+    // tiled: per-CTA areas, then the pairs' prepared blocks, then the overflow list
+    const size_t off_prep = ovf_offset((size_t)li.grid * li.slot_bytes);
+    const size_t off = ovf_offset(off_prep + (size_t)P.npairs * li.prep_bytes);
     CK(scratch.ensure(li.tiled ? off + ovf_bytes(P.npairs) : (size_t)li.grid * li.slot_bytes));
     P.scratch = scratch.p;
     if (li.tiled) {
+        P.tprep = (char*)scratch.p + off_prep;
         P.tovfcount = (int*)((char*)scratch.p + off);
         P.tovf = P.tovfcount + 1;
         P.tovfcap = P.npairs;
         P.tile_qcap = st.tile_qcap;
         CK(cudaMemsetAsync(P.tovfcount, 0, sizeof(int), s));
+        launches += 1;  // the preparation kernel
     }
     if (fp32) CK(launch_solve_fp32(P, (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, li, s));
     else CK(launch_solve_fp64(P, (const double*)st.d_tab64.p, li, s));
@@ -1037,9 +1042,14 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
     if (rc) return rc;
     if (P.irng) return RRTMG_SW_EIRNG;  // the MT stream needs a device buffer
     const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
-    LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms, !st.no_tiled) : plan_fp64(P, st.num_sms);
-    if (!fp32) li.slot_bytes = slot_elems(P.nlay, P.idelm, false) * sizeof(double);
     const size_t avail = kStaticScratchBytes - kStaticTail;
+    LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms, !st.no_tiled) : plan_fp64(P, st.num_sms);
+    // the tiled kernel's prepared blocks (one per pair) must fit beside its
+    // per-CTA areas; larger calls take the scratch-based kernel
+    const size_t off_prep = (((size_t)li.grid * li.slot_bytes) + 255) & ~(size_t)255;
+    if (li.tiled && off_prep + (size_t)P.npairs * li.prep_bytes > avail) li = plan_fp32(P, st.num_sms, false);
+    st.last_kernel = !fp32 ? RRTMG_SW_KERNEL_FP64 : li.tiled ? RRTMG_SW_KERNEL_FP32_TILED : RRTMG_SW_KERNEL_FP32;
+    if (!fp32) li.slot_bytes = slot_elems(P.nlay, P.idelm, false) * sizeof(double);
     const size_t slots = avail / li.slot_bytes;
     // one slot per SM, or per column pair when the call has fewer pairs
     const size_t need = (size_t)std::min(li.grid, st.num_sms);
@@ -1052,6 +1062,7 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
     P.err = area.err;
     int* tail = (int*)((char*)area.scratch + avail);
     if (li.tiled) {
+        P.tprep = (char*)area.scratch + off_prep;
         P.tovfcount = tail;
         P.tovf = tail + 1;
         P.tovfcap = std::min(P.npairs, kStaticOvfCap);
@@ -1061,7 +1072,7 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
     CK(cudaMemsetAsync(P.err, 0, sizeof(int), s));
     if (fp32) CK(launch_solve_fp32(P, (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, li, s));
     else CK(launch_solve_fp64(P, (const double*)st.d_tab64.p, li, s));
-    int launches = 1;
+    int launches = li.tiled ? 2 : 1;
     int h[2] = {0, 0};  // pageable: the copies complete before the calls return
     CK(cudaMemcpyAsync(&h[0], P.err, sizeof(int), cudaMemcpyDeviceToHost, s));
     if (li.tiled) CK(cudaMemcpyAsync(&h[1], P.tovfcount, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1339,7 +1350,7 @@ int rrtmg_sw_ini_c(double cpdair) {
     }
     {
         const char* t = std::getenv("RRTMG_SW_TILED");
-        st.no_tiled = !(t && std::strcmp(t, "1") == 0);
+        st.no_tiled = t && std::strcmp(t, "0") == 0;
         const char* q = std::getenv("RRTMG_SW_TILE_QCAP");
         st.tile_qcap = q ? std::atoi(q) : 0;
     }
@@ -1492,7 +1503,11 @@ int rrtmg_sw_setcoef_c(const rrtmg_sw_args* a, int32_t* jp, int32_t* jt, int32_t
     CK(cf.ensure(CL * NFR * sizeof(double)));
     CK(pk.ensure(CL * sizeof(int)));
     CK(pdp.ensure(CL * sizeof(double)));
-    CK(launch_setcoef(P, (const double*)st.d_tab64.p, (double*)cf.p, (int*)pk.p, (double*)pdp.p, s));
+    if (st.form == RRTMG_SW_FORM_FP32)
+        CK(launch_setcoef_f32(P, (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, (float*)cf.p, (int*)pk.p,
+                              (double*)pdp.p, s));
+    else
+        CK(launch_setcoef(P, (const double*)st.d_tab64.p, (double*)cf.p, (int*)pk.p, (double*)pdp.p, s));
     st.last_launches = 1;
     std::vector<int> h(CL);
     CK(cudaMemcpyAsync(h.data(), pk.p, CL * sizeof(int), cudaMemcpyDeviceToHost, s));

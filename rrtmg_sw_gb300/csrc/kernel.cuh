@@ -34,11 +34,13 @@ __device__ inline double DS(double a, double b) { return __dsub_rn(a, b); }
 
 // inatm_sw (rrtmg_sw_rad.f90:1527-1586) and setcoef_sw
 // (rrtmg_sw_setcoef.f90:158-301) for one (column, layer), in FP64 with
-// explicit roundings so both arithmetic forms see identical indices.
+// explicit roundings so both arithmetic forms see identical indices.  The
+// results go to index `at` of the [NFR][L] / [L] arrays (default lay - 1).
 template <typename R>
 __device__ inline void prep_layer(const SolveParams& P, int col, int lay, R* cf, int* pk, double* pdp,
-                                  int L, const double* __restrict__ tab64, double* cf64 = nullptr) {
-    const int i = lay - 1;
+                                  int L, const double* __restrict__ tab64, double* cf64 = nullptr, int at = -1) {
+    const int li = lay - 1;
+    const int i = at >= 0 ? at : li;
     if (col >= P.ncol) {
         for (int f = 0; f < NFR; ++f) cf[f * L + i] = R(0);
         if (cf64)
@@ -48,7 +50,7 @@ __device__ inline void prep_layer(const SolveParams& P, int col, int lay, R* cf,
         return;
     }
     const size_t n = (size_t)P.ncol;
-    const size_t k = (size_t)col + n * (size_t)i;
+    const size_t k = (size_t)col + n * (size_t)li;
     const double p = P.play[k], t = P.tlay[k];
     const double pzb = P.plev[k], pzt = P.plev[k + n];
     const double h2o = P.h2ovmr[k];
@@ -137,6 +139,108 @@ __device__ inline void prep_layer(const SolveParams& P, int col, int lay, R* cf,
     cf[F_FORFRAC * L + i] = (R)forfrac;
     cf[F_PDP * L + i] = (R)pdp[i];
     pk[i] = jp | (jt << 8) | (jt1 << 12) | (indself << 16) | (indfor << 24) | (low << 30);
+}
+
+// FP32 form: inatm_sw + setcoef_sw for one (column, layer) in FP32, with the
+// FP64 form's table indices.  Every index (jp, jt, jt1, indself, indfor,
+// the laytrop test) is the integer part of an expression, or a comparison;
+// where the FP32 value lies within IDX_EPS of the integer or of the
+// threshold (its own error is below 2e-5), the expression is evaluated again
+// in FP64 exactly as prep_layer does.  The pressure thickness stays FP64
+// (the top layers are thin differences of level pressures).
+constexpr float IDX_EPS = 1.0e-4f;
+
+__device__ inline bool near_int(float x) { return fabsf(x - rintf(x)) < IDX_EPS; }
+
+__device__ inline void prep_layer_f32(const SolveParams& P, int col, int lay, float* cf, int* pk, double* pdp,
+                                      int L, const float* __restrict__ tab, const double* __restrict__ tab64) {
+    // explicit roundings (no FMA contraction), so every kernel that inlines
+    // this gets the same coefficients bit for bit
+    auto M = [](float a, float b) { return __fmul_rn(a, b); };
+    auto A = [](float a, float b) { return __fadd_rn(a, b); };
+    auto S = [](float a, float b) { return __fsub_rn(a, b); };
+    auto D = [](float a, float b) { return __fdiv_rn(a, b); };
+    const int i = lay - 1;
+    if (col >= P.ncol) {
+        for (int f = 0; f < NFR; ++f) cf[f * L + i] = 0.0f;
+        pk[i] = 1 | (1 << 8) | (1 << 12) | (1 << 16) | (1 << 24);
+        pdp[i] = 1.0;
+        return;
+    }
+    const size_t n = (size_t)P.ncol;
+    const size_t k = (size_t)col + n * (size_t)i;
+    const double pd = P.play[k], td = P.tlay[k];
+    const double dp = DS(P.plev[k], P.plev[k + n]);
+    pdp[i] = dp;
+    const float p = (float)pd, t = (float)td, h2o = (float)P.h2ovmr[k];
+    const float amd = 28.9660f, amw = 18.0160f;
+    // 1e3 * avogad / (1e2 * grav)
+    const float cfac = (float)(1.e3 * 6.02214199e+23 / (1.e2 * 9.8066));
+    const float amm = A(M(S(1.0f, h2o), amd), M(h2o, amw));
+    const float coldry = D(M((float)dp, cfac), M(amm, A(1.0f, h2o)));
+    const float w0 = M(coldry, h2o), w1 = M(coldry, (float)P.co2vmr[k]), w2 = M(coldry, (float)P.o3vmr[k]);
+    const float w5 = M(coldry, (float)P.ch4vmr[k]), w6 = M(coldry, (float)P.o2vmr[k]);
+    const float plog = logf(p);
+    const float xjp = S(36.0f, M(5.0f, A(plog, 0.04f)));
+    int jp = near_int(xjp) ? (int)DS(36.0, DM(5.0, DA(log(pd), 0.04))) : (int)xjp;
+    jp = jp < 1 ? 1 : (jp > 58 ? 58 : jp);
+    const float fp = M(5.0f, S(ldt(tab, cT.preflog + jp - 1), plog));
+    const float tr0 = ldt(tab, cT.tref + jp - 1), tr1 = ldt(tab, cT.tref + jp);
+    const double tr0d = ldt(tab64, cT.tref + jp - 1), tr1d = ldt(tab64, cT.tref + jp);
+    const float q0 = D(S(t, tr0), 15.0f), q1 = D(S(t, tr1), 15.0f);
+    const float xjt = A(3.0f, q0), xjt1 = A(3.0f, q1);
+    int jt = near_int(xjt) ? (int)DA(3.0, DS(td, tr0d) / 15.0) : (int)xjt;
+    jt = jt < 1 ? 1 : (jt > 4 ? 4 : jt);
+    int jt1 = near_int(xjt1) ? (int)DA(3.0, DS(td, tr1d) / 15.0) : (int)xjt1;
+    jt1 = jt1 < 1 ? 1 : (jt1 > 4 ? 4 : jt1);
+    const float ft = S(q0, (float)(jt - 3));
+    const float ft1 = S(q1, (float)(jt1 - 3));
+    const float water = h2o;  // w0 / coldry
+    const float scalefac = D(M(p, 296.0f / 1013.0f), t);
+    const bool low = fabsf(plog - 4.56f) < IDX_EPS ? log(pd) > 4.56 : plog > 4.56f;
+    float forfac, forfrac, selffac, selffrac;
+    int indfor, indself;
+    forfac = D(scalefac, A(1.0f, water));
+    if (low) {
+        const float f1 = D(S(332.0f, t), 36.0f);
+        indfor = near_int(f1) ? (int)(DS(332.0, td) / 36.0) : (int)f1;
+        indfor = indfor < 1 ? 1 : (indfor > 2 ? 2 : indfor);
+        forfrac = S(f1, (float)indfor);
+        selffac = M(water, forfac);
+        const float f2 = D(S(t, 188.0f), 7.2f);
+        indself = (near_int(f2) ? (int)(DS(td, 188.0) / 7.2) : (int)f2) - 7;
+        indself = indself < 1 ? 1 : (indself > 9 ? 9 : indself);
+        selffrac = S(f2, (float)(indself + 7));
+    } else {
+        indfor = 3;
+        forfrac = S(D(S(t, 188.0f), 36.0f), 1.0f);
+        selffac = 0.0f;
+        selffrac = 0.0f;
+        indself = 0;
+    }
+    const float colh2o = M(1.e-20f, w0);
+    float colco2 = M(1.e-20f, w1), colo3 = M(1.e-20f, w2), colch4 = M(1.e-20f, w5), colo2 = M(1.e-20f, w6);
+    const float colmol = A(M(1.e-20f, coldry), colh2o);
+    if (colco2 == 0.0f) colco2 = M(1.e-32f, coldry);
+    if (colch4 == 0.0f) colch4 = M(1.e-32f, coldry);
+    if (colo2 == 0.0f) colo2 = M(1.e-32f, coldry);
+    const float compfp = S(1.0f, fp);
+    cf[F_FAC10 * L + i] = M(compfp, ft);
+    cf[F_FAC00 * L + i] = M(compfp, S(1.0f, ft));
+    cf[F_FAC11 * L + i] = M(fp, ft1);
+    cf[F_FAC01 * L + i] = M(fp, S(1.0f, ft1));
+    cf[F_H2O * L + i] = colh2o;
+    cf[F_CO2 * L + i] = colco2;
+    cf[F_O3 * L + i] = colo3;
+    cf[F_CH4 * L + i] = colch4;
+    cf[F_O2 * L + i] = colo2;
+    cf[F_MOL * L + i] = colmol;
+    cf[F_SELFFAC * L + i] = selffac;
+    cf[F_SELFFRAC * L + i] = selffrac;
+    cf[F_FORFAC * L + i] = forfac;
+    cf[F_FORFRAC * L + i] = forfrac;
+    cf[F_PDP * L + i] = (float)dp;
+    pk[i] = jp | (jt << 8) | (jt1 << 12) | (indself << 16) | (indfor << 24) | ((low ? 1 : 0) << 30);
 }
 
 // Aerosol optical properties of band ib at (column, layer): iaer = 10 reads
@@ -326,14 +430,19 @@ __device__ inline void cloud_in(const SolveParams& P, int col, int g, int lay, i
 // risky when it sits so close to the edge between two table entries that
 // the FP64 form may take the other one, and the step would move this
 // layer's heating rate by more than BEAM_HR_TOL K/day (hrs = incident flux
-// * heatfac / dp).  The window assumes BEAM_EPS relative uncertainty in the
-// FP32 optical depth.
+// * heatfac / dp) or the g-point's direct flux below the layer by more than
+// BEAM_F_TOL W/m2 (zinc = the g-point's incident flux): in thick, hazy
+// layers near the surface a step moves the surface flux far more than the
+// layer's heating rate, and steps of many layers add up there.  The window
+// assumes BEAM_EPS relative uncertainty in the FP32 optical depth.
 constexpr float BEAM_EPS = 5.0e-7f;
 constexpr float BEAM_HR_TOL = 2.0e-3f;
+constexpr float BEAM_F_TOL = 1.0e-3f;
 // The direct-beam lookup of tbl_exp (x > od_lo: u = x / (bpade + x), entry
 // int(1e4 u + 0.5)) together with beam_risky's test, sharing its division:
-// the window 1e4 b x / (b + x)^2 * BEAM_EPS is 1e4 u (1 - u) * BEAM_EPS.
-__device__ inline float tbl_exp_beam(float x, const float* __restrict__ tab, float hrs, bool& risky) {
+// the window 1e4 b x / (b + x)^2 * BEAM_EPS is 1e4 u (1 - u) * BEAM_EPS, and
+// one entry's step in exp(-x) is e (b + x)^2 / (1e4 b).
+__device__ inline float tbl_exp_beam(float x, const float* __restrict__ tab, float hrs, float zinc, bool& risky) {
     if (x <= 0.06f) return 1.0f - x + 0.5f * x * x;
     const float u = x / (cT.bpade_f + x);
     const float t = 10000.0f * u + 0.5f;
@@ -342,7 +451,8 @@ __device__ inline float tbl_exp_beam(float x, const float* __restrict__ tab, flo
     const float fr = t - (float)itind;
     if (fminf(fr, 1.0f - fr) < 10000.0f * u * (1.0f - u) * BEAM_EPS) {
         const float bx = cT.bpade_f + x;
-        if (hrs * e * bx * bx / (cT.bpade_f * 10000.0f) > BEAM_HR_TOL) risky = true;
+        const float de = e * bx * bx / (cT.bpade_f * 10000.0f);
+        if (hrs * de > BEAM_HR_TOL || zinc * de > BEAM_F_TOL) risky = true;
     }
     return e;
 }
@@ -353,7 +463,7 @@ __device__ inline float tbl_exp_beam(float x, const float* __restrict__ tab, flo
 // FP32 form also carries the co-albedo and flags risky cells.
 template <typename R>
 __device__ inline CellOpt<R> cell_optics(const CellIn<R>& ci, int idelm, R prmu0, const R* __restrict__ tab,
-                                         const double* __restrict__ tab64, float hrs) {
+                                         const double* __restrict__ tab64, float hrs, float zinc = 0.0f) {
     CellOpt<R> o;
     o.risky = false;
     o.dbtcn = o.dbtn = R(0);
@@ -382,7 +492,7 @@ __device__ inline CellOpt<R> cell_optics(const CellIn<R>& ci, int idelm, R prmu0
     const R xc = ztauc / prmu0;
     if constexpr (sizeof(R) == 4) {
         bool br = false;
-        o.zdbtc = tbl_exp_beam(xc, tab, hrs, br);
+        o.zdbtc = tbl_exp_beam(xc, tab, hrs, zinc, br);
         o.risky = o.rc.risky || br;
     } else {
         o.zdbtc = tbl_exp<R>(xc, tab);
@@ -412,7 +522,7 @@ __device__ inline CellOpt<R> cell_optics(const CellIn<R>& ci, int idelm, R prmu0
         const R xo = ztauo / prmu0;
         R zdbtmo;
         bool bro = false;
-        if constexpr (sizeof(R) == 4) zdbtmo = tbl_exp_beam(xo, tab, hrs, bro);
+        if constexpr (sizeof(R) == 4) zdbtmo = tbl_exp_beam(xo, tab, hrs, zinc, bro);
         else zdbtmo = tbl_exp<R>(xo, tab);
         o.zdbt = zclear * o.zdbtc + zcloud * zdbtmo;
         if constexpr (sizeof(R) == 4) {
@@ -430,9 +540,10 @@ __device__ inline CellOpt<R> cell_optics(const CellIn<R>& ci, int idelm, R prmu0
 static __device__ __noinline__ CellOpt<float> cell_optics_fp64(const SolveParams& P, const Coef<double>& C64, int col,
                                                                int g, int lay, int ib, int igb, bool fused,
                                                                bool cloudy, double cossza,
-                                                               const double* __restrict__ tab64) {
+                                                               const double* __restrict__ tab64, int clay = -1) {
+    // clay: the layer's index in C64 (C64 may hold this layer alone)
     CellIn<double> ci;
-    taumol_g<double>(ib, igb, lay, C64, tab64, ci.taug, ci.taur);
+    taumol_g<double>(ib, igb, clay >= 1 ? clay : lay, C64, tab64, ci.taug, ci.taur);
     aerosol_in(P, col, lay, ib, tab64, ci);
     cloud_in<double>(P, col, g, lay, ib, fused, cloudy, nullptr, ci, tab64);
     const CellOpt<double> d = cell_optics<double>(ci, P.idelm, cossza, tab64, tab64, 0.0f);
@@ -494,11 +605,26 @@ __device__ inline bool cell_changed(const float* sv0, int NS, int L, int lay, co
     return ch;
 }
 
+// FP32 form: the FP64 form's coefficients of one layer of one column (setcoef
+// again, in FP64), as a Coef whose only layer is layer 1; cell_optics_fp64
+// takes it with clay = 1.  The FP32 form keeps no FP64 copy of its
+// coefficients: the few cells it redoes per column pair recompute theirs.
+struct Coef64At {
+    double cf[NFR];
+    int pk;
+};
+__device__ inline Coef<double> coef64_at(const SolveParams& P, int col, int lay, int laytrop,
+                                         const double* __restrict__ tab64, Coef64At& b) {
+    double pdpv;
+    prep_layer<double>(P, col, lay, b.cf, &b.pk, &pdpv, 1, tab64, nullptr, 0);
+    return Coef<double>{b.cf, &b.pk, 1, lay <= laytrop ? 1 : 0};
+}
+
 // FP32 form: the upward adding recurrence (vrtqdr:122-140) of one (column,
 // g-point) again from layer `from` to the top, over cells already redone in
 // FP64 by the CTA's queue, redoing in FP64 any cell still marked in the
 // scratch (one the queue could not hold).
-static __device__ __noinline__ void redo_cells_fp64(const SolveParams& P, const Coef<double>& C64, float* sv0, int NS,
+static __device__ __noinline__ void redo_cells_fp64(const SolveParams& P, int laytrop, float* sv0, int NS,
                                                     int col, int g, int ib, int igb, bool fused, double cossza,
                                                     const double* __restrict__ tab64, float albp, float albd,
                                                     int from) {
@@ -518,7 +644,10 @@ static __device__ __noinline__ void redo_cells_fp64(const SolveParams& P, const 
         }
         const float mark = at(lay, S_DBTC);
         if (mark < 0.0f) {
-            const CellOpt<float> co = cell_optics_fp64(P, C64, col, g, lay, ib, igb, fused, mark < -1.5f, cossza, tab64);
+            Coef64At b;
+            const Coef<double> C64 = coef64_at(P, col, lay, laytrop, tab64, b);
+            const CellOpt<float> co =
+                cell_optics_fp64(P, C64, col, g, lay, ib, igb, fused, mark < -1.5f, cossza, tab64, 1);
             store_cell(sv0, NS, L, lay, co, P.idelm);
         }
         {
@@ -734,19 +863,20 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
     const int ib = cT.ngb[g], igb = cT.gib[g];
     const bool uv = ib >= 9 && ib <= 12;  // bands 25-28 (spcvmc:629)
     const int NS = P.idelm == 0 ? NS_MAX : S_DBTCN;
-    // FP32 form: the FP64 layer coefficients [2][NFR][L] follow the level fields of the slot
-    double* sCoef64 = (double*)(scr + (size_t)L * NS * CTA_THREADS);
     const size_t n = (size_t)P.ncol;
     const int nmapped = P.colmap ? *P.mapcount : 0;
     (void)nomc;
     __syncthreads();
-    // ---------------- prep: one (column, layer) per item, FP64
+    // ---------------- prep: one (column, layer) per item; FP64 in the FP64
+    // form, FP32 with the FP64 form's indices in the FP32 form
     for (int it = tid; it < COLS_PER_CTA * L; it += CTA_THREADS) {
         const int c2 = it / L, lay = it % L + 1;
         const int pcol = pair_col(P, pair, c2, nmapped);
         constexpr bool f32 = sizeof(R) == 4;
-        prep_layer<R>(P, pcol, lay, sCoef + c2 * NFR * L, sPk + c2 * L, sPdp + c2 * L, L, tab64,
-                      f32 ? sCoef64 + c2 * NFR * L : nullptr);
+        if constexpr (f32)
+            prep_layer_f32(P, pcol, lay, sCoef + c2 * NFR * L, sPk + c2 * L, sPdp + c2 * L, L, tab, tab64);
+        else
+            prep_layer<R>(P, pcol, lay, sCoef + c2 * NFR * L, sPk + c2 * L, sPdp + c2 * L, L, tab64);
         if (f32) sHrf[c2 * L + lay - 1] = (float)(cT.heatfac / sPdp[c2 * L + lay - 1]);
         const bool real = pcol < P.ncol;
         const size_t kl = (size_t)pcol + n * (size_t)(lay - 1);
@@ -812,7 +942,6 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
     __syncthreads();
     const int col = pair_col(P, pair, cc, nmapped);
     const Coef<R> C{sCoef + cc * NFR * L, sPk + cc * L, L, sMisc[cc]};
-    const Coef<double> C64{sCoef64 + cc * NFR * L, sPk + cc * L, L, sMisc[cc]};
     bool active = col < P.ncol;
     if (active && (C.laytrop < 1 || C.laytrop >= L)) {
         set_error(P.err, E_LAYTROP);
@@ -874,7 +1003,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
             cloudy = mc.step(lay, sKc[cc * L + lay - 1], sKa[cc * L + lay - 1], sOmcf[cc * L + lay - 1]);
         cloud_in<R>(P, col, g, lay, ib, fused, cloudy, cld, ci, tab);
         const R hrs = zinc * sHrf[cc * L + lay - 1];
-        const CellOpt<R> co = cell_optics<R>(ci, P.idelm, prmu0, tab, tab64, hrs);
+        const CellOpt<R> co = cell_optics<R>(ci, P.idelm, prmu0, tab, tab64, hrs, (float)zinc);
         // FP32 form: a table entry, the conservative switch or the
         // resonance of this cell is too close to call in FP32; it is
         // queued and redone after this pass as the FP64 form does (a cell
@@ -950,11 +1079,12 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
             const int e = V.sRq[i];
             const int t = e >> 20, c2 = (e >> 19) & 1, gg = (e >> 12) & 127, lay = (e >> 1) & 2047;
             const int pcol = pair_col(P, pair, c2, nmapped);
-            const Coef<double> Cq{sCoef64 + c2 * NFR * L, sPk + c2 * L, L, sMisc[c2]};
+            Coef64At b;
+            const Coef<double> Cq = coef64_at(P, pcol, lay, sMisc[c2], tab64, b);
             double cz = P.coszen[pcol];
             if (cz < 1.e-10) cz = 1.e-10;
             const CellOpt<float> co = cell_optics_fp64(P, Cq, pcol, gg, lay, cT.ngb[gg], cT.gib[gg], fused, e & 1, cz,
-                                                       tab64);
+                                                       tab64, 1);
             if (cell_changed(scr + t, NS, L, lay, co)) {
                 store_cell(scr + t, NS, L, lay, co, P.idelm);
                 atomicMin(sRf + t, lay);
@@ -963,7 +1093,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         __syncthreads();
         const int from = min(redo_from, sRf[tid]);
         if (active && from <= L)
-            redo_cells_fp64(P, C64, scr + tid, NS, col, g, ib, igb, fused, cossza, tab64, albp, albd, from);
+            redo_cells_fp64(P, C.laytrop, scr + tid, NS, col, g, ib, igb, fused, cossza, tab64, albp, albd, from);
     }
 
     // ---------------- pass 2: top -> bottom, level fluxes and g sums

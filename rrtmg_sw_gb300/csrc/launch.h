@@ -14,6 +14,10 @@ struct LaunchInfo {
     size_t smem;         // dynamic shared memory per CTA
     bool tiled = false;  // FP32 form: the tiled kernel (layer R/T in shared memory)
     size_t slot_bytes = 0;  // global scratch per CTA
+    // tiled kernel: its preparation kernel's grid and shared memory, and the
+    // bytes of one pair's prepared block (P.tprep holds npairs of them)
+    int prep_grid = 0;
+    size_t prep_smem = 0, prep_bytes = 0;
 };
 
 // FP64 form
@@ -22,6 +26,9 @@ LaunchInfo plan_fp64(const SolveParams& P, int num_sms);
 cudaError_t launch_solve_fp64(const SolveParams& P, const double* tab, const LaunchInfo& li, cudaStream_t s);
 // FP32 form
 cudaError_t upload_tables_fp32(const DevTables& t);
+// setcoef of the FP32 form (FP32 arithmetic, the FP64 form's indices) over all (column, layer)
+cudaError_t launch_setcoef_f32(const SolveParams& P, const float* tab, const double* tab64, float* cf, int* pk,
+                               double* pdp, cudaStream_t s);
 // allow_tiled = false keeps the scratch-based kernel (k_solve<float>)
 LaunchInfo plan_fp32(const SolveParams& P, int num_sms, bool allow_tiled = true);
 cudaError_t launch_solve_fp32(const SolveParams& P, const float* tab, const double* tab64, const LaunchInfo& li,

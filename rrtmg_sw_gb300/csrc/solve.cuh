@@ -61,6 +61,8 @@ struct SolveParams {
     // thread), [2] column pairs the tiled kernel handed back, [3] subcolumns
     // the tiled kernel swept a second time for their FP64 cells
     unsigned long long* stats;
+    // tiled FP32 kernel: the pairs' prepared blocks (written by k_tiled_prep)
+    void* tprep;
 };
 
 // Tangent-linear / adjoint request (solve_ad.cu): objective weights and

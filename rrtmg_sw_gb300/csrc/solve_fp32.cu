@@ -152,6 +152,26 @@ __device__ __forceinline__ RT<float> reftra_g<float>(float zto1, float zw, float
     return o;
 }
 
+// setcoef of the FP32 form for every (column, layer): the diagnostic export
+// of its table indices (rrtmg_sw_setcoef_c)
+static __global__ void __launch_bounds__(256) k_setcoef_f32(const SolveParams P, const float* __restrict__ tab,
+                                                            const double* __restrict__ tab64, float* cf, int* pk,
+                                                            double* pdp) {
+    const size_t n = (size_t)P.ncol, L = (size_t)P.nlay;
+    const size_t it = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= n * L) return;
+    const int col = (int)(it % n), lay = (int)(it / n) + 1;
+    prep_layer_f32(P, col, lay, cf + (size_t)col * NFR * L, pk + (size_t)col * L, pdp + (size_t)col * L, (int)L,
+                   tab, tab64);
+}
+
+cudaError_t launch_setcoef_f32(const SolveParams& P, const float* tab, const double* tab64, float* cf, int* pk,
+                               double* pdp, cudaStream_t s) {
+    const size_t n = (size_t)P.ncol * P.nlay;
+    k_setcoef_f32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, tab, tab64, cf, pk, pdp);
+    return cudaGetLastError();
+}
+
 cudaError_t upload_tables_fp32(const DevTables& t) { return cudaMemcpyToSymbol(cT, &t, sizeof(DevTables)); }
 
 LaunchInfo plan_fp32(const SolveParams& P, int num_sms, bool allow_tiled) {
@@ -167,11 +187,20 @@ LaunchInfo plan_fp32(const SolveParams& P, int num_sms, bool allow_tiled) {
         const bool fused = P.fused && P.icld >= 1, nomc = P.nomcica && P.icld >= 1;
         li.tiled = true;
         li.smem = tiled_smem(P.nlay, P.extra ? 16 : 8, fused, fused || nomc).total;
-        const auto kern = P.mt ? k_solve_tiled<true> : k_solve_tiled<false>;
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
+        cudaFuncSetAttribute(k_solve_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
         li.grid = num_sms < P.npairs ? num_sms : P.npairs;
         if (li.grid < 1) li.grid = 1;
         li.slot_bytes = tiled_glob(P.nlay).total;
+        // the preparation kernel: persistent over the pairs at the occupancy it reaches
+        li.prep_smem = tiled_prep_smem(P.nlay).total;
+        li.prep_bytes = tiled_prep_layout(P.nlay, fused, fused || nomc, P.iaer != 0).total;
+        const auto prep = P.mt ? k_tiled_prep<true> : k_tiled_prep<false>;
+        cudaFuncSetAttribute(prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.prep_smem);
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prep, CTA_THREADS, li.prep_smem);
+        if (per_sm < 1) per_sm = 1;
+        li.prep_grid = num_sms * per_sm < P.npairs ? num_sms * per_sm : P.npairs;
+        if (li.prep_grid < 1) li.prep_grid = 1;
         return li;
     }
     li.smem = smem_layout(P.nlay, num_q<float>(P.extra != 0), stages_clouds(P),
@@ -191,8 +220,9 @@ LaunchInfo plan_fp32(const SolveParams& P, int num_sms, bool allow_tiled) {
 cudaError_t launch_solve_fp32(const SolveParams& P, const float* tab, const double* tab64, const LaunchInfo& li,
                               cudaStream_t s) {
     if (li.tiled) {
-        if (P.mt) k_solve_tiled<true><<<li.grid, T_THREADS, li.smem, s>>>(P, tab, tab64);
-        else k_solve_tiled<false><<<li.grid, T_THREADS, li.smem, s>>>(P, tab, tab64);
+        if (P.mt) k_tiled_prep<true><<<li.prep_grid, CTA_THREADS, li.prep_smem, s>>>(P, tab, tab64);
+        else k_tiled_prep<false><<<li.prep_grid, CTA_THREADS, li.prep_smem, s>>>(P, tab, tab64);
+        k_solve_tiled<<<li.grid, T_THREADS, li.smem, s>>>(P, tab, tab64);
     } else {
         if (P.mt) k_solve<float, true><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab64);
         else k_solve<float, false><<<li.grid, CTA_THREADS, li.smem, s>>>(P, tab, tab64);

@@ -10,9 +10,8 @@ namespace rrsw {
 cudaError_t upload_tables_fp64(const DevTables& t) { return cudaMemcpyToSymbol(cT, &t, sizeof(DevTables)); }
 
 size_t slot_elems(int nlay, int idelm, bool fp32) {
-    const size_t fields = (size_t)nlay * (size_t)(idelm == 0 ? NS_MAX : S_DBTCN) * CTA_THREADS;
-    // the FP32 form also keeps the FP64 layer coefficients of its two columns
-    return fp32 ? fields + 2 * (size_t)COLS_PER_CTA * NFR * nlay : fields;
+    (void)fp32;  // the same level fields in both forms (elements of the form's type)
+    return (size_t)nlay * (size_t)(idelm == 0 ? NS_MAX : S_DBTCN) * CTA_THREADS;
 }
 
 LaunchInfo plan_fp64(const SolveParams& P, int num_sms) {

@@ -9,9 +9,8 @@
 // reftra_sw (rrtmg_sw_spcvmc.f90:442-585, rrtmg_sw_reftra.f90:151-326) in
 // shared memory, two tiles double-buffered.  Warp roles:
 //
-//   optics warps (T_OPT): per pair, setcoef (FP64) into shared memory, the
-//     McICA subcolumn masks (one walk per subcolumn), the solar source; then
-//     per tile the cells (g-point, layer) -- gas optics, clouds, aerosol,
+//   optics warps (T_OPT): per pair, the pair's prepared block (below) into
+//     shared memory; then per tile the cells (g-point, layer) -- gas optics, clouds, aerosol,
 //     delta scaling, the two-stream layer solution -- layer rows taken from
 //     a shared counter, the 32 subcolumns of a row in one warp (32
 //     consecutive g-points: coalesced table reads).
@@ -28,6 +27,15 @@
 //     fraction of the FP32 rate, so its cells are processed 32 at a time);
 //     then finishes the pair (below) and writes its outputs.
 //
+// A separate kernel, k_tiled_prep, prepares each pair beforehand at full
+// occupancy: setcoef in FP32 with the FP64 form's table indices, the McICA subcolumn masks
+// (one walk per subcolumn), the solar source and albedos, the cloud and
+// aerosol inputs in FP32 -- about 16 KB per pair in HBM (60 layers, no
+// aerosol).  In the solve kernel that work would stall the optics warps;
+// read back it costs a few vector loads per pair.  setcoef in FP64 (as the
+// scratch-based kernel does it) would cost more than a tenth of the solve
+// at GB300's FP64 rate.
+//
 // A subcolumn with such a cell is left out of its tile's sums; its R/T
 // column is copied aside (global, per CTA) and swept again with the FP64
 // cells by the FP64 warp, its contribution added before the pair's outputs
@@ -43,16 +51,21 @@
 #ifndef RRSW_TILED_OPT
 #define RRSW_TILED_OPT 13
 #endif
+#ifndef RRSW_TILED_F64
+#define RRSW_TILED_F64 1
+#endif
 
 namespace rrsw {
 
 constexpr int TW = 32;                                   // subcolumns per tile
 constexpr int TILES = COLS_PER_CTA * NGPT / TW;          // 7 tiles per pair
 constexpr int T_OPT = RRSW_TILED_OPT;                    // optics warps
-constexpr int T_REDO = T_OPT;                            // FP64 warp index
-constexpr int T_ADDC = T_OPT + 1;                        // adding warp, clear sky
-constexpr int T_ADDT = T_OPT + 2;                        // adding warp, total sky
-constexpr int T_THREADS = (T_OPT + 3) * 32;
+constexpr int T_F64 = RRSW_TILED_F64;                    // FP64 warps (pairs taken in turn)
+static_assert(T_F64 == 1 || T_F64 == 2, "one FP64 warp, or one per pair parity");
+constexpr int T_REDO = T_OPT;                            // first FP64 warp
+constexpr int T_ADDC = T_OPT + T_F64;                    // adding warp, clear sky
+constexpr int T_ADDT = T_OPT + T_F64 + 1;                // adding warp, total sky
+constexpr int T_THREADS = (T_OPT + T_F64 + 2) * 32;
 constexpr int T_QCAP = 128;                              // FP64 cells per pair
 constexpr int T_RCAP = 64;                               // subcolumns with such cells per pair
 constexpr int T_NF = 10;                                 // tile fields per cell
@@ -61,14 +74,16 @@ enum { TF_REFC, TF_REFDC, TF_ADIRC, TF_ADIFC, TF_DBTC, TF_REF, TF_REFD, TF_ADIR,
 enum { TB_FULL0, TB_FULL1, TB_EMPTY0, TB_EMPTY1, TB_PAIR0, TB_PAIR1, TB_SWEPT0, TB_SWEPT1, TB_FIN0, TB_FIN1,
        TB_N };
 // control words in shared memory
-enum { TC_ROW0, TC_ROW1, TC_QN0, TC_QN1, TC_RN0, TC_RN1, TC_ABORT, TC_LT0, TC_LT1, TC_ACT0, TC_ACT1,
-       TC_OVF0, TC_OVF1, TC_N };
+// (TC_ACT0 + 2 * parity + column: the adding warps read a pair's flags
+// while the optics warps load the next pair's)
+enum { TC_ROW0, TC_ROW1, TC_QN0, TC_QN1, TC_RN0, TC_RN1, TC_ABORT, TC_LT0, TC_LT1, TC_ACT0, TC_ACT1, TC_ACT2,
+       TC_ACT3, TC_OVF0, TC_OVF1, TC_N };
 
 // Shared-memory carve-up of the tiled kernel; the host sizes the launch with
 // the same function.
 struct TSmem {
-    size_t bar, ctl, tm, tile, rup, coef, pk, hrf, mu, cld, mask, kc, ka, omcf, seed, sub, risky, queue, recof,
-        flux, scr, scr2, total;
+    size_t bar, ctl, tm, tile, rup, coef, pk, hrf, mu, cld, mask, sub, risky, queue, recof, flux, scr, scr2,
+        total;
 };
 
 __host__ __device__ inline TSmem tiled_smem(int L, int nq, bool fused, bool cloud_stage) {
@@ -83,15 +98,9 @@ __host__ __device__ inline TSmem tiled_smem(int L, int nq, bool fused, bool clou
     m.pk = o;    o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(int));
     m.hrf = o;   o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(float));
     m.mu = o;    o = align16(o + (size_t)COLS_PER_CTA * sizeof(float));
-    m.cld = m.mask = m.kc = m.ka = m.omcf = m.seed = o;
+    m.cld = m.mask = o;
     if (cloud_stage) { m.cld = o; o = align16(o + (size_t)COLS_PER_CTA * 4 * L * sizeof(float)); }
-    if (fused) {
-        m.mask = o; o = align16(o + (size_t)COLS_PER_CTA * NGPT * 2 * sizeof(uint32_t));
-        m.kc = o;   o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(long long));
-        m.ka = o;   o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(long long));
-        m.omcf = o; o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(double));
-        m.seed = o; o = align16(o + (size_t)COLS_PER_CTA * 4 * sizeof(uint32_t));
-    }
+    if (fused) { m.mask = o; o = align16(o + (size_t)COLS_PER_CTA * NGPT * 2 * sizeof(uint32_t)); }
     m.sub = o;   o = align16(o + (size_t)2 * 3 * COLS_PER_CTA * NGPT * sizeof(float));   // [par][zinc,albp,albd][224]
     m.risky = o; o = align16(o + (size_t)2 * TILES * sizeof(uint32_t));
     m.queue = o; o = align16(o + (size_t)2 * T_QCAP * sizeof(int));
@@ -100,16 +109,15 @@ __host__ __device__ inline TSmem tiled_smem(int L, int nq, bool fused, bool clou
     // adding warps: surface-level sums and lane keys of a tile
     m.scr = o;   o = align16(o + (size_t)16 * TW * sizeof(float));
     // FP64 warp: reduction scratch of the set-aside subcolumns (rows 6-7: 64-bit keys)
-    m.scr2 = o;  o = align16(o + (size_t)16 * TW * sizeof(float));
+    m.scr2 = o;  o = align16(o + (size_t)T_F64 * 16 * TW * sizeof(float));
     m.total = o;
     return m;
 }
 
-// Per-CTA global area of the tiled kernel (bytes): KISS jump columns, the
-// aerosol staged in FP32, and per pair parity the FP64 layer coefficients,
-// the layer thicknesses, the FP64 cells and the set-aside subcolumns.
+// Per-CTA global area of the tiled kernel (bytes): the FP64 warp's albedo
+// scratch and, per pair parity, the FP64 cells and the set-aside subcolumns.
 struct TGlob {
-    size_t xs, rrup, aer, par, coef64, pk, lt, pdp, corr, rec, rec_stride, par_stride, total;
+    size_t rrup, par, corr, rec, rec_stride, par_stride, total;
 };
 
 __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -117,15 +125,9 @@ __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size
 __host__ __device__ inline TGlob tiled_glob(int L) {
     TGlob g;
     size_t o = 0;
-    g.xs = o;   o = align256(o + (size_t)NGPT * 32 * sizeof(uint32_t));
-    g.rrup = o; o = align256(o + (size_t)4 * L * TW * sizeof(float));   // FP64 warp: record sweeps' albedos
-    g.aer = o;  o = align256(o + (size_t)COLS_PER_CTA * 3 * NBND * L * sizeof(float));
+    g.rrup = o; o = align256(o + (size_t)T_F64 * 4 * L * TW * sizeof(float));   // FP64 warps: record sweeps' albedos
     g.par = o;
     size_t p = 0;
-    g.coef64 = p; p = align256(p + (size_t)COLS_PER_CTA * NFR * L * sizeof(double));
-    g.pk = p;     p = align256(p + (size_t)COLS_PER_CTA * L * sizeof(int));
-    g.lt = p;     p = align256(p + (size_t)COLS_PER_CTA * sizeof(int));
-    g.pdp = p;    p = align256(p + (size_t)COLS_PER_CTA * L * sizeof(double));
     g.corr = p;   p = align256(p + (size_t)T_QCAP * T_NF * sizeof(float));
     // record: s, column slot, zinc, albp, albd, pad[3], then T_NF x L fields
     g.rec_stride = align256((8 + (size_t)T_NF * L) * sizeof(float));
@@ -134,6 +136,53 @@ __host__ __device__ inline TGlob tiled_glob(int L) {
     o += 2 * p;
     g.total = o;
     return g;
+}
+
+// A pair's prepared block in global memory (bytes), written by
+// k_tiled_prep and read by k_solve_tiled: setcoef's FP32 coefficients and
+// packed indices, heatfac / dp, dp in FP64, the cloud inputs and the
+// aerosol (FP32), per subcolumn zinc, direct and diffuse albedo, the McICA
+// mask bits, and per column laytrop, the active flag and mu0.
+struct TPrep {
+    size_t coef, pk, hrf, pdp, cld, aer, sub, mask, misc, total;
+};
+enum { TP_LT0, TP_LT1, TP_ACT0, TP_ACT1, TP_MU0, TP_MU1, TP_N };
+
+__host__ __device__ inline TPrep tiled_prep_layout(int L, bool fused, bool cloud_stage, bool aerosol) {
+    TPrep b;
+    size_t o = 0;
+    b.coef = o; o = align16(o + (size_t)COLS_PER_CTA * NFR * L * sizeof(float));
+    b.pk = o;   o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(int));
+    b.hrf = o;  o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(float));
+    b.pdp = o;  o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(double));
+    b.cld = b.aer = b.mask = o;
+    if (cloud_stage) { b.cld = o; o = align16(o + (size_t)COLS_PER_CTA * 4 * L * sizeof(float)); }
+    if (aerosol) { b.aer = o; o = align16(o + (size_t)COLS_PER_CTA * 3 * NBND * L * sizeof(float)); }
+    b.sub = o;  o = align16(o + (size_t)3 * COLS_PER_CTA * NGPT * sizeof(float));
+    if (fused) { b.mask = o; o = align16(o + (size_t)COLS_PER_CTA * NGPT * 2 * sizeof(uint32_t)); }
+    b.misc = o; o = align16(o + (size_t)TP_N * sizeof(int));
+    b.total = align256(o);
+    return b;
+}
+
+// Shared memory of k_tiled_prep (bytes).
+struct TPrepSmem {
+    size_t xs, tm, coef, pk, kc, ka, omcf, seed, misc, total;
+};
+__host__ __device__ inline TPrepSmem tiled_prep_smem(int L) {
+    TPrepSmem m;
+    size_t o = 0;
+    m.xs = o;   o = align16(o + (size_t)NGPT * 32 * sizeof(uint32_t));
+    m.tm = o;   o = align16(o + (size_t)NBND * 2 * sizeof(TmSmem));
+    m.coef = o; o = align16(o + (size_t)COLS_PER_CTA * NFR * L * sizeof(float));
+    m.pk = o;   o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(int));
+    m.kc = o;   o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(long long));
+    m.ka = o;   o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(long long));
+    m.omcf = o; o = align16(o + (size_t)COLS_PER_CTA * L * sizeof(double));
+    m.seed = o; o = align16(o + (size_t)COLS_PER_CTA * 4 * sizeof(uint32_t));
+    m.misc = o; o = align16(o + (size_t)TP_N * sizeof(int));
+    m.total = o;
+    return m;
 }
 
 // ------------------------------------------------------------- mbarriers
@@ -192,17 +241,13 @@ struct TileView {
     float* mu;        // [2]
     float* cld;       // [2][4][L]
     uint32_t* mask;   // [224][2]
-    long long* kc;    // [2][L]
-    long long* ka;    // [2][L]
-    double* omcf;     // [2][L]
-    uint32_t* seed;   // [2][4]
     float* sub;       // [2][3][224]
     uint32_t* risky;  // [2][TILES]
     int* queue;       // [2][T_QCAP]
     short* recof;     // [2][224]
     float* flux;      // [2][2][NQ][L+1]
     float* scr;       // [16][TW] adding warps
-    float* scr2;      // [16][TW] FP64 warp
+    float* scr2;      // [T_F64][16][TW] FP64 warps
 };
 
 __device__ inline TileView tile_view(unsigned char* raw, const TSmem& M) {
@@ -218,10 +263,6 @@ __device__ inline TileView tile_view(unsigned char* raw, const TSmem& M) {
     v.mu = (float*)(raw + M.mu);
     v.cld = (float*)(raw + M.cld);
     v.mask = (uint32_t*)(raw + M.mask);
-    v.kc = (long long*)(raw + M.kc);
-    v.ka = (long long*)(raw + M.ka);
-    v.omcf = (double*)(raw + M.omcf);
-    v.seed = (uint32_t*)(raw + M.seed);
     v.sub = (float*)(raw + M.sub);
     v.risky = (uint32_t*)(raw + M.risky);
     v.queue = (int*)(raw + M.queue);
@@ -294,11 +335,15 @@ __device__ inline void up1(const float* f, float& rup, float& rupd) {
 struct TCtx {
     TileView V;
     TGlob G;
-    unsigned char* glob;  // this CTA's global area
+    TPrep B;
+    unsigned char* glob;        // this CTA's global area
+    const unsigned char* prep;  // the prepared blocks of all pairs
     int L, nmapped, qcap, nlocal;
     bool fused, nomc, cstage;
     volatile int* abort;
 };
+
+__device__ inline const unsigned char* tblk(const TCtx& X, int pair) { return X.prep + (size_t)pair * X.B.total; }
 
 __device__ inline unsigned char* tpar(const TCtx& X, int par) {
     return X.glob + X.G.par + (size_t)par * X.G.par_stride;
@@ -308,136 +353,196 @@ __device__ inline float* trec(const TCtx& X, int par, int r) {
 }
 __device__ inline int tpair(int lp) { return blockIdx.x + lp * gridDim.x; }
 
-// ---- optics warps: per-pair preparation.  setcoef (FP64, explicit
-// roundings) into shared memory and its FP64 copy for the FP64 warp, McICA
+// ---- k_tiled_prep: one CTA (2 columns x 112 g-points) per pair at a time,
+// persistent.  setcoef (FP32, the FP64 form's indices), McICA
 // thresholds, cloud and aerosol inputs; then per column laytrop; then per
-// subcolumn the solar source, the albedos and the McICA mask bits.
+// subcolumn the solar source, the albedos and the McICA mask bits
+// (rrtmg_sw_setcoef.f90:158-301, mcica_subcol_gen_sw.f90:472-600,
+// rrtmg_sw_spcvmc.f90:349-356).
 template <bool MT>
-__device__ void tiled_prep(const SolveParams& P, const TCtx& X, int lp, const KissJump& J,
-                           const double* __restrict__ tab64, const float* __restrict__ tab) {
-    const TileView& V = X.V;
-    const int L = X.L, par = lp & 1, pair = tpair(lp), otid = threadIdx.x;
+__global__ void __launch_bounds__(CTA_THREADS, 4)
+k_tiled_prep(const SolveParams P, const float* __restrict__ tab, const double* __restrict__ tab64) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int L = P.nlay, tid = threadIdx.x;
     const size_t n = (size_t)P.ncol;
-    unsigned char* pb = tpar(X, par);
-    double* coef64 = (double*)(pb + X.G.coef64);
-    int* pkg = (int*)(pb + X.G.pk);
-    int* ltg = (int*)(pb + X.G.lt);
-    double* pdpg = (double*)(pb + X.G.pdp);
-    float* aer = (float*)(X.glob + X.G.aer);
-    for (int it = otid; it < COLS_PER_CTA * L; it += T_OPT * 32) {
-        const int c2 = it / L, lay = it % L + 1, i = lay - 1;
-        const int pcol = pair_col(P, pair, c2, X.nmapped);
-        prep_layer<float>(P, pcol, lay, V.coef + c2 * NFR * L, V.pk + c2 * L, pdpg + c2 * L, L, tab64,
-                          coef64 + c2 * NFR * L);
-        pkg[c2 * L + i] = V.pk[c2 * L + i];
-        V.hrf[c2 * L + i] = (float)(cT.heatfac / pdpg[c2 * L + i]);
-        const bool real = pcol < P.ncol;
-        const size_t kl = (size_t)pcol + n * (size_t)i;
-        if (X.fused) {
-            double cf = real ? P.cldfrac[kl] : 0.0;
-            if (cf < 1.0e-20) cf = 0.0;
-            const double omcf = DS(1.0, cf);
-            V.omcf[c2 * L + i] = omcf;
-            if constexpr (MT) {
-                V.kc[c2 * L + i] = mt_threshold(omcf);
-                V.ka[c2 * L + i] = (P.icld >= 4 && real) ? mt_threshold(P.alpha[kl]) : 0ll;
-            } else {
-                V.kc[c2 * L + i] = kiss_threshold(omcf);
-                V.ka[c2 * L + i] = (P.icld >= 4 && real) ? kiss_threshold(P.alpha[kl]) : 0ll;
-            }
-            if (lay == 1) {
-                uint32_t* sd = V.seed + c2 * 4;
-                if (real && !MT) {
-                    const double p1 = DM(P.play[pcol], 1.e2), p2 = DM(P.play[pcol + n], 1.e2);
-                    if (p1 < p2) set_error(P.err, E_KISSSEED);
-                    sd[0] = kiss_seed(p1);
-                    sd[1] = kiss_seed(p2);
-                    sd[2] = kiss_seed(DM(P.play[pcol + 2 * n], 1.e2));
-                    sd[3] = kiss_seed(DM(P.play[pcol + 3 * n], 1.e2));
+    const bool fused = P.fused && P.icld >= 1, nomc = P.nomcica && P.icld >= 1, cstage = fused || nomc;
+    const TPrep B = tiled_prep_layout(L, fused, cstage, P.iaer != 0);
+    const TPrepSmem M = tiled_prep_smem(L);
+    uint32_t* xs = (uint32_t*)(sm + M.xs);
+    TmSmem* tm = (TmSmem*)(sm + M.tm);
+    float* scoef = (float*)(sm + M.coef);
+    int* spk = (int*)(sm + M.pk);
+    long long* skc = (long long*)(sm + M.kc);
+    long long* ska = (long long*)(sm + M.ka);
+    double* somcf = (double*)(sm + M.omcf);
+    uint32_t* sseed = (uint32_t*)(sm + M.seed);
+    int* smisc = (int*)(sm + M.misc);
+    for (int i = tid; i < NBND * 2; i += CTA_THREADS) {
+        TmSmem d;
+        d.r = cT.tm[i / 2][i % 2];
+        d.selfref = cT.b[i / 2].selfref;
+        d.forref = cT.b[i / 2].forref;
+        d.ng = cT.b[i / 2].ng;
+        d.pad = 0;
+        tm[i] = d;
+    }
+    // KISS: the xorshift part of each subcolumn's stream jump (depends on g)
+    if (fused && !MT && tid < NGPT) xorshift_power(kiss_offset(P.icld, tid, L, P.permuteseed), xs + tid * 32);
+    const int s = tid, c2s = s / NGPT, g = s % NGPT;
+    const int ib = cT.ngb[g], igb = cT.gib[g];
+    KissJump J{1u, 0u, 1u, 1u};
+    if (fused && !MT) J = kiss_jump_consts(kiss_offset(P.icld, g, L, P.permuteseed));
+    __syncthreads();
+    for (int pair = blockIdx.x; pair < P.npairs; pair += gridDim.x) {
+        unsigned char* blk = (unsigned char*)P.tprep + (size_t)pair * B.total;
+        double* pdp = (double*)(blk + B.pdp);
+        float* hrf = (float*)(blk + B.hrf);
+        for (int it = tid; it < COLS_PER_CTA * L; it += CTA_THREADS) {
+            const int c2 = it / L, lay = it % L + 1, i = lay - 1;
+            const int pcol = COLS_PER_CTA * pair + c2;
+            prep_layer_f32(P, pcol, lay, scoef + c2 * NFR * L, spk + c2 * L, pdp + c2 * L, L, tab, tab64);
+            hrf[c2 * L + i] = (float)(cT.heatfac / pdp[c2 * L + i]);
+            const bool real = pcol < P.ncol;
+            const size_t kl = (size_t)pcol + n * (size_t)i;
+            if (fused) {
+                double cf = real ? P.cldfrac[kl] : 0.0;
+                if (cf < 1.0e-20) cf = 0.0;
+                const double omcf = DS(1.0, cf);
+                somcf[c2 * L + i] = omcf;
+                if constexpr (MT) {
+                    skc[c2 * L + i] = mt_threshold(omcf);
+                    ska[c2 * L + i] = (P.icld >= 4 && real) ? mt_threshold(P.alpha[kl]) : 0ll;
                 } else {
-                    sd[0] = sd[1] = sd[2] = sd[3] = 1u;
+                    skc[c2 * L + i] = kiss_threshold(omcf);
+                    ska[c2 * L + i] = (P.icld >= 4 && real) ? kiss_threshold(P.alpha[kl]) : 0ll;
                 }
-            }
-        }
-        if (X.nomc) {
-            // spcvrt_sw takes clear or overcast layers only (rrtmg_sw_rad.nomcica.f90:617-621)
-            const double cf = real ? P.cldfrac[kl] : 0.0;
-            if (cf > 1.e-6 && cf < 1.0 - 1.e-6) set_error(P.err, E_PARTIAL);
-        }
-        if (X.cstage) {
-            float* cd = V.cld + c2 * 4 * L;
-            cd[0 * L + i] = real ? (float)P.ciwp[kl] : 0.0f;
-            cd[1 * L + i] = real ? (float)P.clwp[kl] : 0.0f;
-            cd[2 * L + i] = real ? (float)P.rei[kl] : 0.0f;
-            cd[3 * L + i] = real ? (float)P.rel[kl] : 0.0f;
-        }
-        if (P.iaer != 0) {
-            for (int b = 0; b < NBND; ++b) {
-                double ta = 0.0, oa = 1.0, ga = 0.0;
-                if (real) aerosol(P, pcol, lay, b, tab64, ta, oa, ga);
-                float* ad = aer + c2 * 3 * NBND * L;
-                ad[(0 * NBND + b) * L + i] = (float)ta;
-                ad[(1 * NBND + b) * L + i] = (float)DS(1.0, oa);  // co-albedo, formed in FP64
-                ad[(2 * NBND + b) * L + i] = (float)ga;
-            }
-        }
-    }
-    opt_sync();
-    if (otid < COLS_PER_CTA) {
-        const int c2 = otid;
-        int lt = 0;
-        for (int i = 0; i < L; ++i) lt += (V.pk[c2 * L + i] >> 30) & 1;
-        const int pcol = pair_col(P, pair, c2, X.nmapped);
-        int act = pcol < P.ncol;
-        if (act && (lt < 1 || lt >= L)) {
-            set_error(P.err, E_LAYTROP);
-            act = 0;
-        }
-        V.ctl[TC_LT0 + c2] = lt;
-        V.ctl[TC_ACT0 + c2] = act;
-        ltg[c2] = lt;
-        double cz = act ? P.coszen[pcol] : 1.0;
-        if (cz < 1.e-10) cz = 1.e-10;
-        V.mu[c2] = (float)cz;
-    }
-    opt_sync();
-    if (otid < COLS_PER_CTA * NGPT) {
-        const int s = otid, c2 = s / NGPT, g = s % NGPT;
-        const int ib = cT.ngb[g], igb = cT.gib[g];
-        const int pcol = pair_col(P, pair, c2, X.nmapped);
-        const bool act = V.ctl[TC_ACT0 + c2] != 0;
-        float zinc = 0.0f, albp = 0.0f, albd = 0.0f;
-        if (act) {
-            const bool nir = ib <= 8 || ib == 13;
-            albp = (float)(nir ? P.aldir[pcol] : P.asdir[pcol]);
-            albd = (float)(nir ? P.aldif[pcol] : P.asdif[pcol]);
-            const Coef<float> C{V.coef + c2 * NFR * L, V.pk + c2 * L, L, V.ctl[TC_LT0 + c2]};
-            // zincflx = adjflux * ssi * prmu0 (spcvmc:349-356)
-            const float src = solar_source_generic(ib, igb, C, P, tab, V.tm);
-            zinc = float(P.adjflux[ib]) * src * V.mu[c2];
-        }
-        float* sub = V.sub + par * 3 * COLS_PER_CTA * NGPT;
-        sub[s] = zinc;
-        sub[COLS_PER_CTA * NGPT + s] = albp;
-        sub[2 * COLS_PER_CTA * NGPT + s] = albd;
-        if (X.fused) {
-            uint32_t w0 = 0u, w1 = 0u;
-            if (act) {
-                McicaMask<MT> mc;
-                Kiss k0{1u, 1u, 1u, 1u};
-                if constexpr (!MT) k0 = kiss_start(V.seed + c2 * 4, J, (const uint32_t*)(X.glob + X.G.xs) + g * 32);
-                mc.start(k0, P.icld, MT ? P.mt + mt_offset(P.icld, g, pcol, P.ncol, L) : nullptr);
-                for (int lay = 1; lay <= L; ++lay) {
-                    const int i = lay - 1;
-                    if (mc.step(lay, V.kc[c2 * L + i], V.ka[c2 * L + i], V.omcf[c2 * L + i])) {
-                        if (i < 32) w0 |= 1u << i;
-                        else w1 |= 1u << (i - 32);
+                if (lay == 1) {
+                    uint32_t* sd = sseed + c2 * 4;
+                    if (real && !MT) {
+                        const double p1 = DM(P.play[pcol], 1.e2), p2 = DM(P.play[pcol + n], 1.e2);
+                        if (p1 < p2) set_error(P.err, E_KISSSEED);
+                        sd[0] = kiss_seed(p1);
+                        sd[1] = kiss_seed(p2);
+                        sd[2] = kiss_seed(DM(P.play[pcol + 2 * n], 1.e2));
+                        sd[3] = kiss_seed(DM(P.play[pcol + 3 * n], 1.e2));
+                    } else {
+                        sd[0] = sd[1] = sd[2] = sd[3] = 1u;
                     }
                 }
             }
-            V.mask[s * 2] = w0;
-            V.mask[s * 2 + 1] = w1;
+            if (nomc) {
+                // spcvrt_sw takes clear or overcast layers only (rrtmg_sw_rad.nomcica.f90:617-621)
+                const double cf = real ? P.cldfrac[kl] : 0.0;
+                if (cf > 1.e-6 && cf < 1.0 - 1.e-6) set_error(P.err, E_PARTIAL);
+            }
+            if (cstage) {
+                float* cd = (float*)(blk + B.cld) + c2 * 4 * L;
+                cd[0 * L + i] = real ? (float)P.ciwp[kl] : 0.0f;
+                cd[1 * L + i] = real ? (float)P.clwp[kl] : 0.0f;
+                cd[2 * L + i] = real ? (float)P.rei[kl] : 0.0f;
+                cd[3 * L + i] = real ? (float)P.rel[kl] : 0.0f;
+            }
+            if (P.iaer != 0) {
+                float* ad = (float*)(blk + B.aer) + c2 * 3 * NBND * L;
+                for (int b = 0; b < NBND; ++b) {
+                    double ta = 0.0, oa = 1.0, ga = 0.0;
+                    if (real) aerosol(P, pcol, lay, b, tab64, ta, oa, ga);
+                    ad[(0 * NBND + b) * L + i] = (float)ta;
+                    ad[(1 * NBND + b) * L + i] = (float)DS(1.0, oa);  // co-albedo, formed in FP64
+                    ad[(2 * NBND + b) * L + i] = (float)ga;
+                }
+            }
         }
+        __syncthreads();
+        if (tid < COLS_PER_CTA) {
+            const int c2 = tid;
+            int lt = 0;
+            for (int i = 0; i < L; ++i) lt += (spk[c2 * L + i] >> 30) & 1;
+            const int pcol = COLS_PER_CTA * pair + c2;
+            int act = pcol < P.ncol;
+            if (act && (lt < 1 || lt >= L)) {
+                set_error(P.err, E_LAYTROP);
+                act = 0;
+            }
+            double cz = act ? P.coszen[pcol] : 1.0;
+            if (cz < 1.e-10) cz = 1.e-10;
+            smisc[TP_LT0 + c2] = lt;
+            smisc[TP_ACT0 + c2] = act;
+            smisc[TP_MU0 + c2] = __float_as_int((float)cz);
+        }
+        __syncthreads();
+        {
+            const int c2 = c2s;
+            const int pcol = COLS_PER_CTA * pair + c2;
+            const bool act = smisc[TP_ACT0 + c2] != 0;
+            float zinc = 0.0f, albp = 0.0f, albd = 0.0f;
+            if (act) {
+                const bool nir = ib <= 8 || ib == 13;
+                albp = (float)(nir ? P.aldir[pcol] : P.asdir[pcol]);
+                albd = (float)(nir ? P.aldif[pcol] : P.asdif[pcol]);
+                const Coef<float> C{scoef + c2 * NFR * L, spk + c2 * L, L, smisc[TP_LT0 + c2]};
+                // zincflx = adjflux * ssi * prmu0 (spcvmc:349-356)
+                const float src = solar_source_generic(ib, igb, C, P, tab, tm);
+                zinc = float(P.adjflux[ib]) * src * __int_as_float(smisc[TP_MU0 + c2]);
+            }
+            float* sub = (float*)(blk + B.sub);
+            sub[s] = zinc;
+            sub[COLS_PER_CTA * NGPT + s] = albp;
+            sub[2 * COLS_PER_CTA * NGPT + s] = albd;
+            if (fused) {
+                uint32_t w0 = 0u, w1 = 0u;
+                if (act) {
+                    McicaMask<MT> mc;
+                    Kiss k0{1u, 1u, 1u, 1u};
+                    if constexpr (!MT) k0 = kiss_start(sseed + c2 * 4, J, xs + g * 32);
+                    mc.start(k0, P.icld, MT ? P.mt + mt_offset(P.icld, g, pcol, P.ncol, L) : nullptr);
+                    for (int lay = 1; lay <= L; ++lay) {
+                        const int i = lay - 1;
+                        if (mc.step(lay, skc[c2 * L + i], ska[c2 * L + i], somcf[c2 * L + i])) {
+                            if (i < 32) w0 |= 1u << i;
+                            else w1 |= 1u << (i - 32);
+                        }
+                    }
+                }
+                uint32_t* mk = (uint32_t*)(blk + B.mask);
+                mk[s * 2] = w0;
+                mk[s * 2 + 1] = w1;
+            }
+        }
+        // the coefficients, indices and column words to the block
+        float* cfo = (float*)(blk + B.coef);
+        for (int i = tid; i < COLS_PER_CTA * NFR * L; i += CTA_THREADS) cfo[i] = scoef[i];
+        int* pko = (int*)(blk + B.pk);
+        for (int i = tid; i < COLS_PER_CTA * L; i += CTA_THREADS) pko[i] = spk[i];
+        if (tid < TP_N) ((int*)(blk + B.misc))[tid] = smisc[tid];
+        __syncthreads();
+    }
+}
+
+// 16-byte copy of n bytes (n a multiple of 16) by the optics warps
+__device__ inline void opt_copy(void* dst, const void* src, size_t n) {
+    const float4* a = (const float4*)src;
+    float4* d = (float4*)dst;
+    for (size_t i = threadIdx.x; i < n / 16; i += T_OPT * 32) d[i] = a[i];
+}
+
+// ---- optics warps: pair lp's prepared block into shared memory
+__device__ void tiled_load(const SolveParams& P, const TCtx& X, int lp) {
+    const TileView& V = X.V;
+    const int L = X.L, par = lp & 1;
+    const unsigned char* blk = tblk(X, tpair(lp));
+    opt_copy(V.coef, blk + X.B.coef, align16((size_t)COLS_PER_CTA * NFR * L * sizeof(float)));
+    opt_copy(V.pk, blk + X.B.pk, align16((size_t)COLS_PER_CTA * L * sizeof(int)));
+    opt_copy(V.hrf, blk + X.B.hrf, align16((size_t)COLS_PER_CTA * L * sizeof(float)));
+    if (X.cstage) opt_copy(V.cld, blk + X.B.cld, align16((size_t)COLS_PER_CTA * 4 * L * sizeof(float)));
+    if (X.fused) opt_copy(V.mask, blk + X.B.mask, (size_t)COLS_PER_CTA * NGPT * 2 * sizeof(uint32_t));
+    opt_copy(V.sub + par * 3 * COLS_PER_CTA * NGPT, blk + X.B.sub, (size_t)3 * COLS_PER_CTA * NGPT * sizeof(float));
+    const int* misc = (const int*)(blk + X.B.misc);
+    if (threadIdx.x < COLS_PER_CTA) {
+        const int c2 = threadIdx.x;
+        V.ctl[TC_LT0 + c2] = misc[TP_LT0 + c2];
+        V.ctl[TC_ACT0 + 2 * par + c2] = misc[TP_ACT0 + c2];
+        V.mu[c2] = __int_as_float(misc[TP_MU0 + c2]);
     }
     opt_sync();
 }
@@ -451,11 +556,11 @@ __device__ void tiled_optics(const SolveParams& P, const TCtx& X, int lp, int t,
     const int s = TW * t + lane, c2 = s / NGPT, g = s % NGPT;
     const int ib = cT.ngb[g], igb = cT.gib[g];
     const int pcol = pair_col(P, pair, c2, X.nmapped);
-    const bool act = V.ctl[TC_ACT0 + c2] != 0;
+    const bool act = V.ctl[TC_ACT0 + 2 * par + c2] != 0;
     const Coef<float> C{V.coef + c2 * NFR * L, V.pk + c2 * L, L, V.ctl[TC_LT0 + c2]};
     const float zinc = V.sub[par * 3 * COLS_PER_CTA * NGPT + s];
     const float mu = V.mu[c2];
-    const float* aer = (const float*)(X.glob + X.G.aer) + c2 * 3 * NBND * L;
+    const float* aer = (const float*)(tblk(X, pair) + X.B.aer) + c2 * 3 * NBND * L;
     const float* cld = X.cstage ? V.cld + c2 * 4 * L : nullptr;
     while (true) {
         int r = 0;
@@ -483,7 +588,7 @@ __device__ void tiled_optics(const SolveParams& P, const TCtx& X, int lp, int t,
             if (X.fused) cloudy = (V.mask[s * 2 + (r >> 5)] >> (r & 31)) & 1u;
             cloud_in<float>(P, pcol, g, lay, ib, X.fused, cloudy, cld, ci, tab);
             const float hrs = zinc * V.hrf[c2 * L + r];
-            const CellOpt<float> co = cell_optics<float>(ci, 1, mu, tab, tab64, hrs);
+            const CellOpt<float> co = cell_optics<float>(ci, 1, mu, tab, tab64, hrs, zinc);
             f[TF_REFC] = co.rc.ref; f[TF_REFDC] = co.rc.refd; f[TF_ADIRC] = co.rc.adir; f[TF_ADIFC] = co.rc.adif;
             f[TF_DBTC] = co.zdbtc;
             f[TF_REF] = co.rt.ref; f[TF_REFD] = co.rt.refd; f[TF_ADIR] = co.rt.adir; f[TF_ADIF] = co.rt.adif;
@@ -506,20 +611,20 @@ __device__ void tiled_redo(const SolveParams& P, const TCtx& X, int lp, const do
     const TileView& V = X.V;
     const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
     unsigned char* pb = tpar(X, par);
-    const double* coef64 = (const double*)(pb + X.G.coef64);
-    const int* pkg = (const int*)(pb + X.G.pk);
-    const int* ltg = (const int*)(pb + X.G.lt);
     float* corr = (float*)(pb + X.G.corr);
+    const int* misc = (const int*)(tblk(X, pair) + X.B.misc);
     const int qn = min(V.ctl[TC_QN0 + par], X.qcap);
+    (void)L;
     for (int k = lane; k < qn; k += 32) {
         const int e = V.queue[par * T_QCAP + k];
         const int s = e >> 12, lay = (e >> 1) & 127, c2 = s / NGPT, g = s % NGPT;
         const int pcol = pair_col(P, pair, c2, X.nmapped);
-        const Coef<double> C64{coef64 + c2 * NFR * L, pkg + c2 * L, L, ltg[c2]};
+        Coef64At b;
+        const Coef<double> C64 = coef64_at(P, pcol, lay, misc[TP_LT0 + c2], tab64, b);
         double cz = P.coszen[pcol];
         if (cz < 1.e-10) cz = 1.e-10;
         const CellOpt<float> co =
-            cell_optics_fp64(P, C64, pcol, g, lay, cT.ngb[g], cT.gib[g], X.fused, (e & 1) != 0, cz, tab64);
+            cell_optics_fp64(P, C64, pcol, g, lay, cT.ngb[g], cT.gib[g], X.fused, (e & 1) != 0, cz, tab64, 1);
         float* o = corr + k * T_NF;
         o[TF_REFC] = co.rc.ref; o[TF_REFDC] = co.rc.refd; o[TF_ADIRC] = co.rc.adir; o[TF_ADIFC] = co.rc.adif;
         o[TF_DBTC] = co.zdbtc;
@@ -551,7 +656,7 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
     const int ib = cT.ngb[g];
     const float* sub = V.sub + par * 3 * COLS_PER_CTA * NGPT;
     const float zinc = sub[s], albp = sub[COLS_PER_CTA * NGPT + s], albd = sub[2 * COLS_PER_CTA * NGPT + s];
-    const bool act = V.ctl[TC_ACT0 + c2] != 0;
+    const bool act = V.ctl[TC_ACT0 + 2 * par + c2] != 0;
     const bool risky = (V.risky[par * TILES + t] >> lane) & 1u;
     const bool use = act && !risky;
     // subcolumns with FP64 cells: each warp copies its sky's fields aside
@@ -700,7 +805,9 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
             }
         }
     }
-    __syncwarp();
+    // both warps are done reading this tile's surface rows and keys (scr),
+    // which the next tile's sweeps overwrite
+    add_sync();
 }
 
 // ---- FP64 warp: sweeps of the set-aside subcolumns r0 .. r0+31 of pair lp
@@ -822,8 +929,9 @@ __device__ void tiled_finish(const SolveParams& P, const TCtx& X, int lp) {
             }
         }
         __syncwarp();
-        float* R = (float*)(X.glob + X.G.rrup);
-        for (int r0 = 0; r0 < rn; r0 += TW) tiled_records<NQ>(P, X, lp, r0, rn, R, V.scr2);
+        const int w = (threadIdx.x >> 5) - T_REDO;  // this FP64 warp
+        float* R = (float*)(X.glob + X.G.rrup) + (size_t)w * 4 * L * TW;
+        for (int r0 = 0; r0 < rn; r0 += TW) tiled_records<NQ>(P, X, lp, r0, rn, R, V.scr2 + w * 16 * TW);
     }
     if (lane == 0 && P.stats) {
         if (ovf) atomicAdd(P.stats + 2, 1ull);
@@ -838,7 +946,7 @@ __device__ void tiled_finish(const SolveParams& P, const TCtx& X, int lp) {
         if (k < P.tovfcap) P.tovf[k] = pair;
     }
     // outputs (level 0 = surface)
-    const double* pdpg = (const double*)(tpar(X, par) + X.G.pdp);
+    const double* pdpg = (const double*)(tblk(X, pair) + X.B.pdp);
     constexpr int QX = 8;
     for (int it = lane; it < COLS_PER_CTA * (L + 1); it += 32) {
         const int c2 = it / (L + 1), l = it % (L + 1);
@@ -901,7 +1009,6 @@ __device__ void tiled_zero_bands(const SolveParams& P, const TCtx& X, int lp) {
     __syncwarp();
 }
 
-template <bool MT>
 __global__ void __launch_bounds__(T_THREADS, 1)
 k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* __restrict__ tab64) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -914,7 +1021,9 @@ k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* 
     const TSmem M = tiled_smem(L, NQ, X.fused, X.cstage);
     X.V = tile_view(smem_raw, M);
     X.G = tiled_glob(L);
+    X.B = tiled_prep_layout(L, X.fused, X.cstage, P.iaer != 0);
     X.glob = (unsigned char*)P.scratch + (size_t)blockIdx.x * P.slot_elems * sizeof(float);
+    X.prep = (const unsigned char*)P.tprep;
     X.L = L;
     X.nmapped = P.colmap ? *P.mapcount : 0;
     X.qcap = (P.tile_qcap > 0 && P.tile_qcap < T_QCAP) ? P.tile_qcap : T_QCAP;
@@ -947,19 +1056,13 @@ k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* 
         mbar_init(&X.V.bar[TB_FIN0], 1);
         mbar_init(&X.V.bar[TB_FIN1], 1);
     }
-    // KISS: the xorshift part of each subcolumn's stream jump (depends on g)
-    if (X.fused && !MT && tid < NGPT)
-        xorshift_power(kiss_offset(P.icld, tid, L, P.permuteseed), (uint32_t*)(X.glob + X.G.xs) + tid * 32);
     __syncthreads();
     if (warp < T_OPT) {
-        KissJump J{1u, 0u, 1u, 1u};
-        if (X.fused && !MT && tid < COLS_PER_CTA * NGPT)
-            J = kiss_jump_consts(kiss_offset(P.icld, tid % NGPT, L, P.permuteseed));
         for (int lp = 0; lp < X.nlocal; ++lp) {
             // pair lp - 2 is finished: its parity's per-pair state is free
             if (lp >= 2) mbar_wait(&X.V.bar[TB_FIN0 + (lp & 1)], ((lp - 2) >> 1) & 1, X.abort, P.err);
             opt_sync();  // the previous pair's cells are all written
-            tiled_prep<MT>(P, X, lp, J, tab64, tab);
+            tiled_load(P, X, lp);
             for (int t = 0; t < TILES; ++t) {
                 const int T = TILES * lp + t, b = T & 1;
                 if (T >= 2) mbar_wait(&X.V.bar[TB_EMPTY0 + b], ((T - 2) >> 1) & 1, X.abort, P.err);
@@ -972,8 +1075,8 @@ k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* 
                 }
             }
         }
-    } else if (warp == T_REDO) {
-        for (int lp = 0; lp < X.nlocal; ++lp) {
+    } else if (warp < T_REDO + T_F64) {
+        for (int lp = warp - T_REDO; lp < X.nlocal; lp += T_F64) {
             const int par = lp & 1;
             mbar_wait(&X.V.bar[TB_PAIR0 + par], (lp >> 1) & 1, X.abort, P.err);
             tiled_redo(P, X, lp, tab64);

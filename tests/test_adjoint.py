@@ -145,9 +145,15 @@ def config4_subset(ncol=256):
 @pytest.mark.parametrize("weights", [(1.0, 0.0, 0.0), (0.0, 1.0, 0.0)])
 def test_config4_subset_tangent_linear_matches_central_differences(gpu, weights):
     # 256 columns x 60 layers: FD with relative step 1e-6 within 1e-6 of the
-    # largest |dJ|.  The heating-rate sum is left to the transpose check below:
-    # with this set's 0.01 hPa top its FD quotient is dominated by the FP64
-    # rounding of J (see the module docstring).
+    # largest |dJ|.  The model is piecewise smooth: setcoef's table indices
+    # (jt, jt1, indself, indfor) jump where a layer temperature crosses a
+    # grid line, so a column where some layer's step crosses one has a kink
+    # inside [-2h, 2h] and no central difference to compare with; those
+    # columns are found by their central quotients at steps h and 2h
+    # disagreeing (smooth columns agree to O(h^2), far below the threshold)
+    # and are left out (about one per 256 columns).  The heating-rate sum is left to the
+    # transpose check below: with this set's 0.01 hPa top its FD quotient is
+    # dominated by the FP64 rounding of J (see the module docstring).
     kw, cl = config4_subset()
     d = direction(kw, cl, 17)
     tl = gpu.rrtmg_sw_tl(kw, d, cl, weights)
@@ -158,9 +164,12 @@ def test_config4_subset_tangent_linear_matches_central_differences(gpu, weights)
         return gpu.rrtmg_sw_tl(k2, {}, c2, weights)["J"]
 
     fd = (J(h) - J(-h)) / (2.0 * h)
+    fd2 = (J(2.0 * h) - J(-2.0 * h)) / (4.0 * h)
     scale = max(np.max(np.abs(fd)), 1e-300)
-    err = np.max(np.abs(tl["dJ"] - fd)) / scale
-    assert err <= 1e-6, err
+    kink = np.abs(fd - fd2) > 5e-7 * scale
+    assert kink.sum() <= 0.02 * kw["ncol"], int(kink.sum())
+    err = np.max(np.abs(tl["dJ"] - fd)[~kink]) / scale
+    assert err <= 1e-6, (err, int(kink.sum()))
 
 
 def test_config4_subset_adjoint_is_transpose_of_tangent_linear(gpu):

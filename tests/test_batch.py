@@ -4,8 +4,11 @@ CUDA graph (rrtmg_sw_batch_plan_c / rrtmg_sw_batch_run_c).
 
 Every instance is compared with the single-instance device entry point
 (rrtmg_sw_mcica_dev_c) on the same inputs.  The batch kernel runs the same
-per-column-pair code, so sunlit columns must agree bit for bit (tolerance 0);
-night columns are zero in the batch and within 1e-6 of zero in the single
+per-column-pair code.  The FP64 form is compiled without FMA contraction, so
+its sunlit columns must agree bit for bit (tolerance 0); the FP32 form lets
+the compiler contract each kernel's inlined copy of that code its own way, so
+its sunlit columns must agree to 1e-6 relative (a few FP32 roundings).
+Night columns are zero in the batch and within 1e-6 of zero in the single
 call (the reference clamps mu0 to 1e-10).
 """
 import ctypes as C
@@ -107,7 +110,11 @@ def test_batch_matches_single_instance_calls(torch, form):
         for x, r in zip(insts, ref):
             got = x.outputs()
             for k in OUTS:
-                np.testing.assert_array_equal(got[k][x.sun], r[k][x.sun], err_msg="run %d %s" % (run, k))
+                if form == "fp64":
+                    np.testing.assert_array_equal(got[k][x.sun], r[k][x.sun], err_msg="run %d %s" % (run, k))
+                else:
+                    np.testing.assert_allclose(got[k][x.sun], r[k][x.sun], rtol=1e-6, atol=1e-9,
+                                               err_msg="run %d %s" % (run, k))
                 assert np.all(got[k][~x.sun] == 0.0), (run, k)
                 assert np.all(np.abs(r[k][~x.sun]) <= 1e-6), (run, k)
     plan.close()

@@ -81,6 +81,8 @@ def call(torch, kw, clouds, where, nomcica=False):
         s = torch.cuda.current_stream().cuda_stream
         rc = (L.rrtmg_sw_nomcica_dev_c if nomcica else L.rrtmg_sw_mcica_dev_c)(C.byref(a), C.byref(cl), C.c_void_p(s))
         launches = L.rrtmg_sw_last_launch_count_c()
+    # the tiled FP32 kernel comes with its preparation kernel: two launches per solve
+    launches = (launches, 2 if gi.last_kernel() == gi.KERNEL_FP32_TILED else 1)
     torch.cuda.synchronize()
     assert rc == 0
     res = {k: outs[k].cpu().numpy().reshape(shp, order="F") for k, shp in shapes.items()}
@@ -99,7 +101,7 @@ def test_chunked_host_call_equals_one_device_call(torch, form):
         d, nd = call(torch, kw, clouds, "device")
     finally:
         gi.set_form(gi.FORM_FP64)
-    assert nh == 3 and nd == 1  # one solve per chunk / one for the whole call
+    assert nh[0] == 3 * nh[1] and nd[0] == nd[1]  # one solve per chunk / one for the whole call
     for k in d:
         np.testing.assert_array_equal(h[k], d[k], err_msg=k)
 
@@ -117,6 +119,6 @@ def test_chunked_nomcica_equals_one_device_call(torch):
     clouds["fsfc"] = clouds["asmc"] ** 2
     h, nh = call(torch, kw, clouds, "pinned", nomcica=True)
     d, _ = call(torch, kw, clouds, "device", nomcica=True)
-    assert nh == 3
+    assert nh[0] == 3 * nh[1]
     for k in d:
         np.testing.assert_array_equal(h[k], d[k], err_msg=k)

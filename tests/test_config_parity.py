@@ -6,6 +6,9 @@ sizes, element by element, with the discrete choices checked directly.
   floor (floors 1e-9 W m-2 and 1e-8 K/day, for values near zero), and the
   setcoef_sw indices jp, jt, jt1, indself, indfor and laytrop identical for
   every column and layer (rrtmg_sw_setcoef.f90:158-200).
+* setcoef_sw's indices at their boundaries (pressures on the jp grid and at
+  the laytrop threshold, temperatures on the indself / indfor grids, moved by
+  up to 3e-7 relative): identical to the oracle's in both arithmetic forms.
 * McICA clouds (icld=2, inflgsw=2 iceflgsw=3 liqflgsw=1) with aerosol
   (iaer=10), 16384 columns x 60 layers, FP64 form: the seven subcolumn arrays
   of mcica_subcol_sw identical to the oracle's for all 16384 columns, and the
@@ -95,6 +98,32 @@ def test_clear_sky_1024x60_fp64_elementwise_and_indices():
     for k in ("jp", "jt", "jt1", "indself", "indfor", "laytrop"):
         np.testing.assert_array_equal(g[k], o[k], err_msg=k)
     assert g["jp"].min() >= 1 and g["jp"].max() <= 58 and g["laytrop"].min() >= 1
+
+
+@pytest.mark.parametrize("form", ["fp64", "fp32"])
+def test_setcoef_indices_at_their_boundaries(form):
+    # pressures on the jp grid (36 - 5 (ln p + 0.04) integer) and at the
+    # laytrop threshold ln p = 4.56, temperatures on the indself / indfor
+    # grids, each moved by 0, +-1e-7 or +-3e-7 relative: both forms return the
+    # FP64 indices (the FP32 form re-evaluates near-integer values in FP64)
+    ncol, nlay = 2048, 60
+    c = make_columns(ncol, nlay, 20261277)
+    rng = np.random.default_rng(20261278)
+    dl = np.array([-3e-7, -1e-7, 0.0, 1e-7, 3e-7])
+    grid = np.concatenate([np.exp((36.0 - np.arange(1, 59)) / 5.0 - 0.04), [np.exp(4.56)]])
+    p = np.sort(rng.choice(grid, (ncol, nlay)), axis=1)[:, ::-1] * (1.0 + rng.choice(dl, (ncol, nlay)))
+    tgrid = np.concatenate([188.0 + 7.2 * np.arange(8, 17), 332.0 - 36.0 * np.arange(1, 3)])
+    t = rng.choice(tgrid, (ncol, nlay)) * (1.0 + rng.choice(dl, (ncol, nlay)))
+    kw = gcm_inputs(c, icld=0, iaer=0)
+    kw["play"], kw["tlay"] = p, t
+    gpu.set_form(gpu.FORM_FP32 if form == "fp32" else gpu.FORM_FP64)
+    try:
+        g = gpu.setcoef_indices(**kw)
+    finally:
+        gpu.set_form(gpu.FORM_FP64)
+    o = pyoracle.gcm_setcoef_indices(kw)
+    for k in ("jp", "jt", "jt1", "indself", "indfor", "laytrop"):
+        np.testing.assert_array_equal(g[k], o[k], err_msg=k)
 
 
 def test_mcica_aerosol_16384x60_fp64_masks_and_fluxes():

@@ -106,7 +106,7 @@ def test_tiled_against_oracle(icld, iaer):
     set_env(tiled=True)
     c, clouds, alpha = case(300, 60, 20261220 + icld + iaer, icld, iaer)
     g = run_fp32(c, clouds, icld, iaer, tiled=True)
-    assert gpu.lib().rrtmg_sw_last_launch_count_c() == 1
+    assert gpu.lib().rrtmg_sw_last_launch_count_c() == 2  # preparation + solve
     check_bounds(g, oracle(c, icld, iaer, alpha))
 
 
@@ -148,7 +148,7 @@ def test_tiled_overflow_fallback():
     c, clouds, alpha = case(400, 60, 20261232, 5)
     set_env(tiled=True, qcap=1)
     g = run_fp32(c, clouds, 5, 0, tiled=True)
-    assert gpu.lib().rrtmg_sw_last_launch_count_c() == 2
+    assert gpu.lib().rrtmg_sw_last_launch_count_c() == 3  # + the scratch kernel on the handed-back pairs
     st = gpu.last_fp32_stats()
     assert st["pairs_handed_back"] > 0 and st["redone_cells"] > 0, st
     check_bounds(g, oracle(c, 5, 0, alpha))
@@ -156,10 +156,11 @@ def test_tiled_overflow_fallback():
 
 
 def test_tiled_shared_memory_limit():
-    # 64 layers: the clear-sky kernel fits in shared memory, the McICA one
-    # (subcolumn masks and cloud staging) does not and runs the scratch kernel
+    # 64 layers: the clear-sky kernel fits in shared memory; with McICA
+    # (subcolumn masks and cloud staging) and the extra outputs (16 level sums
+    # instead of 8) it does not, and the scratch kernel runs
     set_env(tiled=True)
     c, clouds, alpha = case(41, 64, 7064, 2)
-    check_bounds(run_fp32(c, clouds, 2, 0, tiled=False), oracle(c, 2, 0, alpha))
+    check_bounds(run_fp32(c, clouds, 2, 0, extra=True, tiled=False), oracle(c, 2, 0, alpha))
     c, clouds, alpha = case(41, 64, 7065, 0)
     check_bounds(run_fp32(c, None, 0, 0, tiled=True), oracle(c, 0, 0, None))
