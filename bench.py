@@ -92,7 +92,10 @@ def algorithmic_flops_per_column(nlay, cloudy_cells_per_col):
 # (dram__bytes_read.sum + dram__bytes_write.sum) in captures at 32768 columns x
 # 60 layers, McICA icld=5; the traffic is per column pair, so a launch's
 # traffic scales with its columns.
-PROFILED_DRAM_BYTES_PER_COLUMN = {"fp32 scratch": 28.38e9 / 32768}
+PROFILED_DRAM_BYTES_PER_COLUMN = {"fp32 scratch": 28.38e9 / 32768,
+                                  "fp32 tiled": (316.876544e6 + 90.473472e6) / 32768}
+# the tiled kernel's preparation kernel (k_tiled_prep), same capture
+PROFILED_PREP_DRAM_BYTES_PER_COLUMN = (222.591744e6 + 209.990656e6) / 32768
 
 
 def algorithmic_bytes_per_column(nlay):
@@ -637,6 +640,12 @@ def main():
     line["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                         "frac": (achieved / peak32) if peak32 else None,
                         "traffic": traffic_col * ncol if (traffic_col and NLAY == 60) else None,
+                        "traffic_source": "ncu dram__bytes_read+write of the solve kernel at 32768 columns, "
+                                          "scaled by columns" + ("; its preparation kernel adds %.0f B per column"
+                                                                 % PROFILED_PREP_DRAM_BYTES_PER_COLUMN
+                                                                 if kernel == "fp32 tiled" else ""),
+                        "time_source": "CUDA events over whole steps (the tiled form's step is its preparation "
+                                       "kernel, ~6 %, and its solve kernel)",
                         "peak_source": "cuBLAS FP32 (non-TF32) 8192^3 GEMM measured in this run",
                         "flops_per_column": fl, "cloudy_cells_per_column": cloudy}
     line["roofline_hbm"] = {"bound": "hbm", "achieved": bytes_col * ncol / (ms32 / 1e3) / 1e9, "peak": hbm,

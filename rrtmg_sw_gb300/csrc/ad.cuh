@@ -363,19 +363,52 @@ __host__ __device__ inline AdSmem ad_smem_layout(int L) {
 }
 
 // Optics of one cell with derivatives (pass 1 and the recomputing reverse
-// pass): Dual<5> over (tlay, h2ovmr, o3vmr, clwp, ciwp) for a cloudy cell;
-// a clear cell does not depend on the water paths, so it runs in Dual<3>
-// and its outputs are widened with zero water-path derivatives.
-template <int N>
-__device__ inline void ad_cell_n(const SolveParams& P, const Dual<3>* coef3, const int* pk, int L, int laytrop,
-                                 int col, int lay, int ib, int igb, bool cloudy, const double* cld, double cossza,
-                                 const double* __restrict__ tab64, Dual<5> out[5]) {
-    typedef Dual<N> D;
-    D cf[NFR];
-    for (int f = 0; f < NFR; ++f) {
-        if constexpr (N == 5) cf[f] = widen(coef3[f * L + lay - 1]);
-        else cf[f] = coef3[f * L + lay - 1];
+// pass).  Gas optics and aerosol depend on (tlay, h2ovmr, o3vmr) only, so
+// they run in Dual<3> for every cell; a cloudy cell widens them to Dual<5>
+// over (tlay, h2ovmr, o3vmr, clwp, ciwp) for cldprmc and the two-stream
+// solution, a clear cell finishes in Dual<3> and is widened with zero
+// water-path derivatives.  Each variant is compiled once (not inlined at
+// its call sites): the kernel's instruction footprint, not its arithmetic,
+// was what its warps waited on most.
+__device__ inline Dual<5> widen5(const Dual<3>& a) { return widen(a); }
+
+__device__ __noinline__ void ad_cell_clear(const CellIn<Dual<3>>& ci, double cossza, Dual<5> out[5]) {
+    Dual<3> o[5];
+    cell_total(ci, cossza, o);
+    for (int k = 0; k < 5; ++k) out[k] = widen5(o[k]);
+}
+
+__device__ __noinline__ void ad_cell_cloudy(const SolveParams& P, const CellIn<Dual<3>>& c3, int col, int lay, int ib,
+                                            const double* cld, int L, double cossza,
+                                            const double* __restrict__ tab64, Dual<5> out[5]) {
+    typedef Dual<5> D;
+    CellIn<D> ci;
+    ci.taug = widen5(c3.taug);
+    ci.taur = widen5(c3.taur);
+    ci.rta = widen5(c3.rta); ci.roa = widen5(c3.roa); ci.rga = widen5(c3.rga); ci.rcoa = widen5(c3.rcoa);
+    ci.cloudy = true;
+    ci.cldf = D(1.0);
+    D ciwp(cld[0 * L + lay - 1]), clwp(cld[1 * L + lay - 1]);
+    clwp.d[3] = 1.0;
+    ciwp.d[4] = 1.0;
+    const D rei(cld[2 * L + lay - 1]), rel(cld[3 * L + lay - 1]);
+    D tc(0.0), oc(1.0), gc(0.0), fsfc(0.0), taor(0.0), coc(0.0);
+    if (P.tauc) {
+        const size_t kb = (size_t)ib + 14 * ((size_t)col + (size_t)P.ncol * (size_t)(lay - 1));
+        tc = D(P.tauc[kb]); oc = D(P.ssac[kb]); gc = D(P.asmc[kb]); fsfc = D(P.fsfc[kb]);
     }
+    cldprmc_g<D>(ib, P.inflag, P.iceflag, P.liqflag, D(1.0), ciwp, clwp, rei, rel, fsfc, tc, oc, gc, taor, coc,
+                 tab64, P.err);
+    ci.tc = tc; ci.oc = oc; ci.gc = gc; ci.coc = coc; ci.taor = taor;
+    cell_total(ci, cossza, out);
+}
+
+__device__ __noinline__ void ad_cell(const SolveParams& P, const Dual<3>* coef3, const int* pk, int L, int laytrop,
+                                     int col, int lay, int ib, int igb, bool cloudy, const double* cld,
+                                     double cossza, const double* __restrict__ tab64, Dual<5> out[5]) {
+    typedef Dual<3> D;
+    D cf[NFR];
+    for (int f = 0; f < NFR; ++f) cf[f] = coef3[f * L + lay - 1];
     const Coef<D> CN{cf, pk + lay - 1, 1, lay <= laytrop ? 1 : 0};
     CellIn<D> ci;
     taumol_g<D>(ib, igb, 1, CN, tab64, ci.taug, ci.taur);
@@ -383,36 +416,8 @@ __device__ inline void ad_cell_n(const SolveParams& P, const Dual<3>* coef3, con
     ci.cloudy = false;
     ci.cldf = D(0.0);
     ci.tc = D(0.0); ci.oc = D(1.0); ci.gc = D(0.0); ci.coc = D(0.0); ci.taor = D(0.0);
-    if constexpr (N == 5) {
-        if (cloudy) {
-            ci.cloudy = true;
-            ci.cldf = D(1.0);
-            D ciwp(cld[0 * L + lay - 1]), clwp(cld[1 * L + lay - 1]);
-            clwp.d[3] = 1.0;
-            ciwp.d[4] = 1.0;
-            const D rei(cld[2 * L + lay - 1]), rel(cld[3 * L + lay - 1]);
-            D tc(0.0), oc(1.0), gc(0.0), fsfc(0.0), taor(0.0), coc(0.0);
-            if (P.tauc) {
-                const size_t kb = (size_t)ib + 14 * ((size_t)col + (size_t)P.ncol * (size_t)(lay - 1));
-                tc = D(P.tauc[kb]); oc = D(P.ssac[kb]); gc = D(P.asmc[kb]); fsfc = D(P.fsfc[kb]);
-            }
-            cldprmc_g<D>(ib, P.inflag, P.iceflag, P.liqflag, D(1.0), ciwp, clwp, rei, rel, fsfc, tc, oc, gc, taor,
-                         coc, tab64, P.err);
-            ci.tc = tc; ci.oc = oc; ci.gc = gc; ci.taor = taor;
-        }
-        cell_total(ci, cossza, out);
-    } else {
-        D o[5];
-        cell_total(ci, cossza, o);
-        for (int k = 0; k < 5; ++k) out[k] = widen(o[k]);
-    }
-}
-
-__device__ inline void ad_cell(const SolveParams& P, const Dual<3>* coef3, const int* pk, int L, int laytrop, int col,
-                               int lay, int ib, int igb, bool cloudy, const double* cld, double cossza,
-                               const double* __restrict__ tab64, Dual<5> out[5]) {
-    if (cloudy) ad_cell_n<5>(P, coef3, pk, L, laytrop, col, lay, ib, igb, true, cld, cossza, tab64, out);
-    else ad_cell_n<3>(P, coef3, pk, L, laytrop, col, lay, ib, igb, false, cld, cossza, tab64, out);
+    if (cloudy) ad_cell_cloudy(P, ci, col, lay, ib, cld, L, cossza, tab64, out);
+    else ad_cell_clear(ci, cossza, out);
 }
 
 __global__ void __launch_bounds__(CTA_THREADS, 2)
