@@ -779,7 +779,8 @@ __device__ inline long long kiss_threshold(double x) {
     const long long lo = -2147483648ll, hi = 2147483647ll;
     if (kiss_real((int32_t)lo) >= x) return lo;
     if (kiss_real((int32_t)hi) < x) return hi + 1;
-    long long k = (long long)floor((x - 0.5) / 2.328306e-10);
+    // first guess by a multiplication (the loops below make it exact)
+    long long k = (long long)floor((x - 0.5) * (1.0 / 2.328306e-10));
     k = k < lo ? lo : (k > hi ? hi : k);
     while (k > lo && kiss_real((int32_t)(k - 1)) >= x) --k;
     while (kiss_real((int32_t)k) < x) ++k;

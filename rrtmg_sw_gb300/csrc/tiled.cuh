@@ -401,7 +401,7 @@ k_tiled_prep(const SolveParams P, const float* __restrict__ tab, const double* _
             const int c2 = it / L, lay = it % L + 1, i = lay - 1;
             const int pcol = COLS_PER_CTA * pair + c2;
             prep_layer_f32(P, pcol, lay, scoef + c2 * NFR * L, spk + c2 * L, pdp + c2 * L, L, tab, tab64);
-            hrf[c2 * L + i] = (float)(cT.heatfac / pdp[c2 * L + i]);
+            hrf[c2 * L + i] = (float)cT.heatfac / (float)pdp[c2 * L + i];  // risk thresholds only
             const bool real = pcol < P.ncol;
             const size_t kl = (size_t)pcol + n * (size_t)i;
             if (fused) {
