@@ -259,7 +259,8 @@ def run_adjoint(args):
         sms = torch.cuda.get_device_properties(0).multi_processor_count
     except Exception:
         pass
-    slot = lambda fields: ((NLAY + 1) * fields * 224 + 2 * 15 * NLAY * 4) * 8
+    # per-CTA scratch (doubles) of the adjoint kernel, 3 resident CTAs per SM
+    slot = lambda fields: ((NLAY + 1) * fields * 224 + 2 * 15 * NLAY * 4) * 8 * 3
     line = {"metric": "adjoint cost relative to the FP64 forward it differentiates (host-array calls, end to end)",
             "value": ad_s / fwd, "unit": "x forward", "n_gpus": 1, "higher_is_better": False,
             "config": {"workload": "%d columns x %d layers, McICA icld=2, objective TOA up + sfc net + HR sum"

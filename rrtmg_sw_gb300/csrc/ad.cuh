@@ -420,7 +420,7 @@ __device__ __noinline__ void ad_cell(const SolveParams& P, const Dual<3>* coef3,
     else ad_cell_clear(ci, cossza, out);
 }
 
-__global__ void __launch_bounds__(CTA_THREADS, 2)
+__global__ void __launch_bounds__(CTA_THREADS, 3)
 k_adjoint(const SolveParams P, const AdParams A, const double* __restrict__ tab64) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = P.nlay;

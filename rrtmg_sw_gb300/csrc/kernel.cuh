@@ -510,7 +510,8 @@ __device__ inline CellOpt<R> cell_optics(const CellIn<R>& ci, int idelm, R prmu0
         zomco = zomco / ztauo;
         RT<R> ro;
         if (ci.cldf > R(1.e-12)) {
-            ro = reftra_g<R>(ztauo, zomco, zcoo, zgco, prmu0, tab, tab64, 1);
+            if constexpr (sizeof(R) == 4) ro = reftra_f32_cloudy(ztauo, zomco, zcoo, zgco, prmu0, tab, tab64);
+            else ro = reftra_g<R>(ztauo, zomco, zcoo, zgco, prmu0, tab, tab64, 1);
         } else {
             ro.ref = R(0); ro.tra = R(1); ro.refd = R(0); ro.trad = R(1);
             ro.adir = R(0); ro.adif = R(0); ro.risky = false;

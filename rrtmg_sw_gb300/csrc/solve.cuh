@@ -661,6 +661,10 @@ struct RT {
 template <typename R>
 __device__ inline RT<R> reftra_g(R zto1, R zw, R zco, R zg, R prmuz, const R* __restrict__ tab,
                                  const double* __restrict__ tab64, int force = -1);
+// FP32 form: the same for a cloudy cell's total sky, compiled once (a few
+// percent of the cells take it; inlined it only grows the kernels' code)
+__device__ RT<float> reftra_f32_cloudy(float zto1, float zw, float zco, float zg, float prmuz,
+                                       const float* __restrict__ tab, const double* __restrict__ tab64);
 
 // FP64 form: the reference's expressions verbatim
 namespace {

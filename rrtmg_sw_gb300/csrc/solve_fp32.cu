@@ -52,9 +52,12 @@ __device__ inline float tbl_exp_om(float x, const float* __restrict__ tab, float
 // FP32 optical depth's own error: strongly absorbing clear layers under a
 // sun near 60 degrees (k ~ 2, mu0 ~ 0.5) sit at resonance, and with a
 // narrower window (5e-7) a flipped entry there moved one UV layer's heating
-// rate by 0.01 K/day.
+// rate by 0.01 K/day.  The amplification reaches well beyond |zrpp| = 0.05:
+// a hazy surface layer with |zrpp| = 0.07 (k mu0 = 1.03) whose exp(-k tau)
+// lookup sat 2.4e-6 (in entries) from an edge had its direct absorptance
+// moved by 6 %, the surface flux by 0.1 W/m2; hence RESONANCE_WIDE = 0.15.
 constexpr float RESONANCE_TOL = 2.0e-3f;
-constexpr float RESONANCE_WIDE = 5.0e-2f;
+constexpr float RESONANCE_WIDE = 0.15f;
 constexpr float RESONANCE_EPS = 2.0e-6f;
 constexpr float CLOUD_EDGE_EPS = 2.0e-7f;  // window of the cloudy total-sky lookups
 
@@ -150,6 +153,12 @@ __device__ __forceinline__ RT<float> reftra_g<float>(float zto1, float zw, float
     o.trad = zrk2 * zem1 * zdend;
     o.adif = om1 * (zrk * om1 + 2.0f * zco * (1.0f + zem1)) * zdend;
     return o;
+}
+
+__device__ __noinline__ RT<float> reftra_f32_cloudy(float zto1, float zw, float zco, float zg, float prmuz,
+                                                    const float* __restrict__ tab,
+                                                    const double* __restrict__ tab64) {
+    return reftra_g<float>(zto1, zw, zco, zg, prmuz, tab, tab64, 1);
 }
 
 // setcoef of the FP32 form for every (column, layer): the diagnostic export
