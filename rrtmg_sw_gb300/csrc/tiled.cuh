@@ -21,11 +21,11 @@
 //     memory), down-sweep with the weighted level fluxes written into the
 //     tile slots the warp has just read; then the g-point sums of spcvmc_sw
 //     (:607-655), one lane per level, half of the levels per warp.
-//   FP64 warp (1): redoes in FP64 the cells whose FP32 discrete choices
-//     (transmittance table entry, conservative switch, resonance) are too
-//     close to call, for the whole pair at once (FP64 runs at a small
+//   FP64 warps (2, pairs in turn): redo in FP64 the cells whose FP32 discrete
+//     choices (transmittance table entry, conservative switch, resonance)
+//     are too close to call, for the whole pair at once (FP64 runs at a small
 //     fraction of the FP32 rate, so its cells are processed 32 at a time);
-//     then finishes the pair (below) and writes its outputs.
+//     then finish the pair (below) and write its outputs.
 //
 // A separate kernel, k_tiled_prep, prepares each pair beforehand at full
 // occupancy: setcoef in FP32 with the FP64 form's table indices, the McICA subcolumn masks
@@ -36,10 +36,10 @@
 // scratch-based kernel does it) would cost more than a tenth of the solve
 // at GB300's FP64 rate.
 //
-// A subcolumn with such a cell is left out of its tile's sums; its R/T
-// column is copied aside (global, per CTA) and swept again with the FP64
-// cells by the FP64 warp, its contribution added before the pair's outputs
-// are written.  Handoffs use mbarriers (tile full / empty, pair produced,
+// A subcolumn with such a cell is left out of its tile's sums; the optics
+// warps copy its R/T column aside (global, per CTA) once the tile is done,
+// and the FP64 warp sweeps it again with the FP64 cells, its contribution
+// added before the pair's outputs are written.  Handoffs use mbarriers (tile full / empty, pair produced,
 // pair swept, pair finished) whose waits give up after ~2^33 cycles with an
 // error code instead of hanging.  A pair with more such cells than the
 // capacities below is listed for the caller, which solves it again with the
@@ -49,10 +49,10 @@
 #include "kernel.cuh"
 
 #ifndef RRSW_TILED_OPT
-#define RRSW_TILED_OPT 13
+#define RRSW_TILED_OPT 20
 #endif
 #ifndef RRSW_TILED_F64
-#define RRSW_TILED_F64 1
+#define RRSW_TILED_F64 2
 #endif
 
 namespace rrsw {
@@ -76,8 +76,7 @@ enum { TB_FULL0, TB_FULL1, TB_EMPTY0, TB_EMPTY1, TB_PAIR0, TB_PAIR1, TB_SWEPT0, 
 // control words in shared memory
 // (TC_ACT0 + 2 * parity + column: the adding warps read a pair's flags
 // while the optics warps load the next pair's)
-enum { TC_ROW0, TC_ROW1, TC_QN0, TC_QN1, TC_RN0, TC_RN1, TC_ABORT, TC_LT0, TC_LT1, TC_ACT0, TC_ACT1, TC_ACT2,
-       TC_ACT3, TC_OVF0, TC_OVF1, TC_N };
+enum { TC_ROW0, TC_ROW1, TC_QN0, TC_QN1, TC_ABORT, TC_LT0, TC_LT1, TC_ACT0, TC_ACT1, TC_ACT2, TC_ACT3, TC_N };
 
 // Shared-memory carve-up of the tiled kernel; the host sizes the launch with
 // the same function.
@@ -606,6 +605,49 @@ __device__ void tiled_optics(const SolveParams& P, const TCtx& X, int lp, int t,
     }
 }
 
+// Record slots of tile t's set-aside subcolumns start after those of the
+// pair's earlier tiles (their risky masks are final once tile t is).
+__device__ inline int tiled_rec_base(const TileView& V, int par, int t) {
+    int base = 0;
+    for (int tt = 0; tt < t; ++tt) base += __popc(V.risky[par * TILES + tt]);
+    return base;
+}
+
+// ---- optics warps, after tile t's cells (buffer b) are all written: the
+// subcolumns with FP64 cells are copied aside (global, per CTA) for the FP64
+// warp's second sweep -- header (subcolumn, column, zinc, albedos) and all
+// ten fields of every layer, spread over the optics warps' threads
+__device__ void tiled_set_aside(const TCtx& X, int lp, int t, int b) {
+    const TileView& V = X.V;
+    const int L = X.L, par = lp & 1;
+    const uint32_t rm = V.risky[par * TILES + t];
+    if (!rm) return;
+    const int base = tiled_rec_base(V, par, t), nr = __popc(rm);
+    const float* tb = V.tile + (size_t)b * T_NF * L * TW;
+    const float* sub = V.sub + par * 3 * COLS_PER_CTA * NGPT;
+    const int per = T_NF * L;
+    for (int it = threadIdx.x; it < nr * (per + 1); it += T_OPT * 32) {
+        const int j = it / (per + 1), rem = it % (per + 1);
+        const int idx = base + j;
+        if (idx >= T_RCAP) continue;  // the pair overflows; the FP64 warp hands it back
+        uint32_t m = rm;  // its j-th set bit
+        for (int k = 0; k < j; ++k) m &= m - 1u;
+        const int lane = __ffs(m) - 1;
+        float* rp = trec(X, par, idx);
+        if (rem < per) {
+            rp[8 + rem] = tb[(size_t)rem * TW + lane];
+        } else {
+            const int s = TW * t + lane;
+            rp[0] = (float)s;
+            rp[1] = (float)(s / NGPT);
+            rp[2] = sub[s];
+            rp[3] = sub[COLS_PER_CTA * NGPT + s];
+            rp[4] = sub[2 * COLS_PER_CTA * NGPT + s];
+            V.recof[par * COLS_PER_CTA * NGPT + s] = (short)idx;
+        }
+    }
+}
+
 // ---- FP64 warp: the pair's queued cells, 32 at a time
 __device__ void tiled_redo(const SolveParams& P, const TCtx& X, int lp, const double* __restrict__ tab64) {
     const TileView& V = X.V;
@@ -659,32 +701,8 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
     const bool act = V.ctl[TC_ACT0 + 2 * par + c2] != 0;
     const bool risky = (V.risky[par * TILES + t] >> lane) & 1u;
     const bool use = act && !risky;
-    // subcolumns with FP64 cells: each warp copies its sky's fields aside
-    // for the pair's second sweep; they stay out of this tile's sums
-    const unsigned rm = __ballot_sync(0xffffffffu, act && risky);
-    if (rm) {
-        const int base = V.ctl[TC_RN0 + par];
-        const int idx = base + __popc(rm & ((1u << lane) - 1u));
-        if (act && risky && idx < T_RCAP) {
-            float* rp = trec(X, par, idx);
-            for (int k = F0; k < F0 + 5; ++k)
-                for (int i = 0; i < L; ++i) rp[8 + k * L + i] = tfield(tb, L, k, i, lane);
-            if (SKY == 1) {
-                rp[0] = (float)s;
-                rp[1] = (float)c2;
-                rp[2] = zinc;
-                rp[3] = albp;
-                rp[4] = albd;
-                V.recof[par * COLS_PER_CTA * NGPT + s] = (short)idx;
-            }
-        }
-        add_sync();  // both warps have read the record count
-        if (SKY == 1 && lane == 0) {
-            const int nb = base + __popc(rm);
-            V.ctl[TC_RN0 + par] = nb;
-            if (nb > T_RCAP) V.ctl[TC_OVF0 + par] = 1;
-        }
-    }
+    // subcolumns with FP64 cells were copied aside by the optics warps
+    // (tiled_set_aside); they stay out of this tile's sums
     float* R = V.rup + (size_t)2 * SKY * L * TW;  // [2][L][TW]: rup, rupd of this sky
     // up-sweep from the surface (vrtqdr:122-140), the next layer's fields
     // loaded while this one is swept
@@ -827,12 +845,20 @@ __device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r
     const int pcol = pair_col(P, pair, c2, X.nmapped);
     const float* fl = rp + 8;
     float rupc = albp, rupdc = albd, rup = albp, rupd = albd;
+    // the records sit in global memory, one per lane: each layer's ten
+    // fields are loaded while the previous layer is swept
+    float fc[5], ft[5], nc[5], nt[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        fc[k] = fl[(TF_REFC + k) * L];
+        ft[k] = fl[(TF_REF + k) * L];
+    }
     for (int i = 0; i < L; ++i) {
-        float fc[5], ft[5];
+        const int in = i + 1 < L ? i + 1 : i;
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
-            fc[k] = fl[(TF_REFC + k) * L + i];
-            ft[k] = fl[(TF_REF + k) * L + i];
+            nc[k] = fl[(TF_REFC + k) * L + in];
+            nt[k] = fl[(TF_REF + k) * L + in];
         }
         up1(fc, rupc, rupdc);
         up1(ft, rup, rupd);
@@ -840,6 +866,11 @@ __device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r
         R[(1 * L + i) * TW + lane] = rupdc;
         R[(2 * L + i) * TW + lane] = rup;
         R[(3 * L + i) * TW + lane] = rupd;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            fc[k] = nc[k];
+            ft[k] = nt[k];
+        }
     }
     const unsigned m0 = __ballot_sync(0xffffffffu, on && c2 == 0);
     const unsigned m1 = __ballot_sync(0xffffffffu, on && c2 == 1);
@@ -847,19 +878,36 @@ __device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r
     down1_init(sc);
     down1_init(stt);
     float q[16];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        fc[k] = fl[(TF_REFC + k) * L + L - 1];
+        ft[k] = fl[(TF_REF + k) * L + L - 1];
+    }
+    float ra[4], rb[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ra[k] = R[(k * L + L - 1) * TW + lane];
     for (int i = L - 1; i >= -1; --i) {
         float qc[4], qt[4], difc, dift;
         if (i >= 0) {
-            float fc[5], ft[5];
+            const int in = i > 0 ? i - 1 : 0;
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
-                fc[k] = fl[(TF_REFC + k) * L + i];
-                ft[k] = fl[(TF_REF + k) * L + i];
+                nc[k] = fl[(TF_REFC + k) * L + in];
+                nt[k] = fl[(TF_REF + k) * L + in];
             }
-            level1(sc, R[(0 * L + i) * TW + lane], R[(1 * L + i) * TW + lane], zinc, qc, difc);
-            level1(stt, R[(2 * L + i) * TW + lane], R[(3 * L + i) * TW + lane], zinc, qt, dift);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) rb[k] = R[(k * L + in) * TW + lane];
+            level1(sc, ra[0], ra[1], zinc, qc, difc);
+            level1(stt, ra[2], ra[3], zinc, qt, dift);
             down1(sc, fc, difc);
             down1(stt, ft, dift);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                fc[k] = nc[k];
+                ft[k] = nt[k];
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) ra[k] = rb[k];
         } else {
             level1(sc, albp, albd, zinc, qc, difc);
             level1(stt, albp, albd, zinc, qt, dift);
@@ -914,8 +962,8 @@ __device__ void tiled_finish(const SolveParams& P, const TCtx& X, int lp) {
     const TileView& V = X.V;
     const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
     const size_t n = (size_t)P.ncol;
-    const int qn = V.ctl[TC_QN0 + par], rn = V.ctl[TC_RN0 + par];
-    const bool ovf = qn > X.qcap || V.ctl[TC_OVF0 + par] != 0;
+    const int qn = V.ctl[TC_QN0 + par], rn = tiled_rec_base(V, par, TILES);
+    const bool ovf = qn > X.qcap || rn > T_RCAP;
     if (!ovf && rn > 0) {
         const float* corr = (const float*)(tpar(X, par) + X.G.corr);
         for (int k = lane; k < qn; k += 32) {
@@ -988,8 +1036,6 @@ __device__ void tiled_finish(const SolveParams& P, const TCtx& X, int lp) {
     if (lane < TILES) V.risky[par * TILES + lane] = 0u;
     if (lane == 0) {
         V.ctl[TC_QN0 + par] = 0;
-        V.ctl[TC_RN0 + par] = 0;
-        V.ctl[TC_OVF0 + par] = 0;
     }
     __syncwarp();
 }
@@ -1067,6 +1113,8 @@ k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* 
                 const int T = TILES * lp + t, b = T & 1;
                 if (T >= 2) mbar_wait(&X.V.bar[TB_EMPTY0 + b], ((T - 2) >> 1) & 1, X.abort, P.err);
                 tiled_optics(P, X, lp, t, b, tab, tab64);
+                opt_sync();  // the tile's cells and risky bits are all written
+                tiled_set_aside(X, lp, t, b);
                 __syncwarp();
                 __threadfence_block();
                 if (lane == 0) {
