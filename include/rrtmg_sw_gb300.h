@@ -197,9 +197,10 @@ int rrtmg_sw_tl_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, const rrtmg_
  * sunlit columns (coszen > 0) on the device before the solve and skips the
  * others, whose outputs are set to zero (the reference solves them with mu0
  * clamped to 1e-10, i.e. 1e-10 of a daytime flux).  Planning runs an
- * autotuner (instance order as given or deepest first, 1 or 2 resident CTAs
- * per SM when shared memory allows; one timed trial each, on the current
- * data) and captures the compaction and the solve in a CUDA graph; a run
+ * autotuner (CTA tile of 2 or 4 columns x 112 g-points, instance order as
+ * given or deepest first, 1 .. n resident CTAs per SM as shared memory
+ * allows; one timed trial each, on the current data) and captures the
+ * compaction and the solve in a CUDA graph; a run
  * replays the graph on `stream` and returns the device error status.  The
  * arithmetic form is the one current at planning.  No counterpart in the
  * reference (a GCM calls rrtmg_sw per chunk of columns). */
@@ -207,10 +208,17 @@ int rrtmg_sw_batch_plan_c(const rrtmg_sw_args *a, const rrtmg_sw_clouds *c, int3
                           void **plan);
 int rrtmg_sw_batch_run_c(void *plan, void *stream);
 /* The autotuner's choice (grid size, deepest-first order) and its trial
- * times in ms, in the order (given order: 1, 2 CTAs per SM; deepest first:
- * 1, 2); ntrials holds the capacity of trial_ms on entry. */
+ * times in ms, in trial order (tile 2 then 4 columns; per tile the given
+ * order then deepest first; per order 1, 2, .. CTAs per SM; tiles whose
+ * shared memory does not fit are skipped); ntrials holds the capacity of
+ * trial_ms on entry. */
 int rrtmg_sw_batch_info_c(void *plan, int32_t *grid, int32_t *deepest_first, float *trial_ms,
                           int32_t *ntrials);
+/* The chosen CTA tile (cols columns x gpoints g-points, one thread per
+ * (column, g-point)) and each trial's candidate, in the trial order of
+ * rrtmg_sw_batch_info_c, as cols << 16 | deepest_first << 8 | CTAs per SM;
+ * ntrials holds the capacity of trial_cfg on entry. */
+int rrtmg_sw_batch_tile_c(void *plan, int32_t *cols, int32_t *gpoints, int32_t *trial_cfg, int32_t *ntrials);
 int rrtmg_sw_batch_free_c(void *plan);
 
 /* Allocation-free device solve.  No counterpart in the reference: it exists

@@ -64,6 +64,7 @@ struct State {
     // of its fallback)
     bool no_tiled = false;
     int tile_qcap = 0;
+    int batch_tile = 0;  // batch plans: 0 = tile chosen by the autotuner, else 2 or 4 columns only
     // host-array calls run on this non-blocking stream (not the legacy
     // default stream, which would serialise against every stream of the host)
     cudaStream_t host_stream = nullptr;
@@ -1190,14 +1191,17 @@ int solve_ad_host(const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, const rrtmg_
 // captured once in a CUDA graph and replayed.
 struct BatchPlan {
     int n = 0, form = 0, grid = 0, desc = 0, device = 0;
+    int tile = COLS_PER_CTA;  // columns per CTA (x 112 g-points)
     size_t smem = 0;
     DevBuf params, maps, offs, counts, scratch, errw;
     int* h_err = nullptr;  // pinned
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    std::vector<float> tune_ms;  // per candidate: (order, blocks per SM) in trial order
+    std::vector<float> tune_ms;  // per candidate: (tile, order, blocks per SM) in trial order
+    std::vector<int> tune_cfg;   // per candidate: tile << 16 | deepest first << 8 | blocks per SM
 };
 
+// Kernel launch of a plan with tile bp.tile, shared memory bp.smem.
 cudaError_t batch_launch(State& st, BatchPlan& bp, int grid, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(bp.errw.p, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
@@ -1206,9 +1210,10 @@ cudaError_t batch_launch(State& st, BatchPlan& bp, int grid, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     if (bp.form == RRTMG_SW_FORM_FP32)
         return launch_batch_fp32((const SolveParams*)bp.params.p, bp.n, (const int*)bp.counts.p,
-                                 (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, grid, bp.smem, s);
+                                 (const float*)st.d_tab32.p, (const double*)st.d_tab64.p, grid, bp.smem, bp.tile,
+                                 s);
     return launch_batch_fp64((const SolveParams*)bp.params.p, bp.n, (const int*)bp.counts.p,
-                             (const double*)st.d_tab64.p, grid, bp.smem, s);
+                             (const double*)st.d_tab64.p, grid, bp.smem, bp.tile, s);
 }
 
 // Upload the instances' parameters in the given order (sunlit lists and
@@ -1249,7 +1254,12 @@ int batch_plan(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, int 
     bp->device = st.device;
     const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
     std::vector<SolveParams> P(n);
-    size_t slot = 0, smem = 0;
+    // tile candidates: 2 or 4 columns x 112 g-points per CTA; shared memory
+    // and scratch slots sized for the deepest instance
+    constexpr int NTILE = 2;
+    const int tiles[NTILE] = {2, 4};
+    size_t slot[NTILE] = {0, 0}, smem[NTILE] = {0, 0};
+    int per_sm[NTILE] = {0, 0};
     long long cols = 0;
     for (int i = 0; i < n; ++i) {
         int rc = check_args(a + i);
@@ -1257,23 +1267,26 @@ int batch_plan(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, int 
         if (!rc) rc = make_params(st, a + i, (c && a[i].icld >= 1) ? c + i : nullptr, P[i]);
         if (!rc && P[i].irng) rc = RRTMG_SW_EIRNG;
         if (rc) { batch_release(bp); return rc; }
-        const size_t si = slot_elems(P[i].nlay, P[i].idelm, fp32);
-        if (si > slot) slot = si;
-        const size_t mi = fp32 ? solve_smem_fp32(P[i]) : solve_smem_fp64(P[i]);
-        if (mi > smem) smem = mi;
+        for (int k = 0; k < NTILE; ++k) {
+            slot[k] = std::max(slot[k], slot_elems(P[i].nlay, P[i].idelm, fp32, tiles[k]));
+            smem[k] = std::max(smem[k], fp32 ? solve_smem_fp32(P[i], tiles[k]) : solve_smem_fp64(P[i], tiles[k]));
+        }
         cols += P[i].ncol;
     }
-    bp->smem = smem;
-    const int per_sm = fp32 ? batch_blocks_per_sm_fp32(smem) : batch_blocks_per_sm_fp64(smem);
-    if (per_sm < 1) { batch_release(bp); return RRTMG_SW_EARGS; }
-    const int grid_max = st.num_sms * per_sm;
     const size_t esz = fp32 ? sizeof(float) : sizeof(double);
+    size_t scratch_bytes = 0;
+    for (int k = 0; k < NTILE; ++k) {
+        per_sm[k] = fp32 ? batch_blocks_per_sm_fp32(smem[k], tiles[k]) : batch_blocks_per_sm_fp64(smem[k], tiles[k]);
+        if (per_sm[k] > 0) scratch_bytes = std::max(scratch_bytes, (size_t)st.num_sms * per_sm[k] * slot[k] * esz);
+    }
+    const bool tile_ok = st.batch_tile == 0 || st.batch_tile == 2 || (st.batch_tile == 4 && per_sm[1] >= 1);
+    if (per_sm[0] < 1 || !tile_ok) { batch_release(bp); return RRTMG_SW_EARGS; }
     cudaError_t e = cudaSuccess;
     if ((e = bp->params.ensure(sizeof(SolveParams) * n)) != cudaSuccess ||
         (e = bp->maps.ensure(sizeof(int) * (size_t)(cols > 0 ? cols : 1))) != cudaSuccess ||
         (e = bp->offs.ensure(sizeof(long long) * n)) != cudaSuccess ||
         (e = bp->counts.ensure(sizeof(int) * n)) != cudaSuccess ||
-        (e = bp->scratch.ensure((size_t)grid_max * slot * esz)) != cudaSuccess ||
+        (e = bp->scratch.ensure(scratch_bytes)) != cudaSuccess ||
         (e = bp->errw.ensure(sizeof(int))) != cudaSuccess ||
         (e = cudaMallocHost((void**)&bp->h_err, sizeof(int))) != cudaSuccess) {
         batch_release(bp);
@@ -1281,35 +1294,47 @@ int batch_plan(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, int 
     }
     for (int i = 0; i < n; ++i) {
         P[i].scratch = bp->scratch.p;
-        P[i].slot_elems = slot;
         P[i].err = (int*)bp->errw.p;
     }
-    // autotuner: instance order (as given / deepest first) x resident CTAs per SM, one timed trial each
+    // autotuner: tile (columns x g-points per CTA) x instance order (as
+    // given / deepest first) x resident CTAs per SM, one timed run each
     std::vector<int> given(n), desc(n);
     for (int i = 0; i < n; ++i) given[i] = desc[i] = i;
     std::stable_sort(desc.begin(), desc.end(), [&](int x, int y) { return P[x].nlay > P[y].nlay; });
+    auto set_tile = [&](int k) {
+        bp->tile = tiles[k];
+        bp->smem = smem[k];
+        for (int i = 0; i < n; ++i) P[i].slot_elems = slot[k];
+    };
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
-    int best_k = 1, best_desc = 0;
-    for (int od = 0; od < 2 && e == cudaSuccess; ++od) {
-        if ((e = batch_upload(*bp, P, od ? desc : given, s)) != cudaSuccess) break;
-        for (int k = 1; k <= per_sm && e == cudaSuccess; ++k) {
-            const int grid = st.num_sms * k;
-            if ((e = batch_launch(st, *bp, grid, s)) != cudaSuccess) break;  // warm-up
-            cudaEventRecord(e0, s);
-            if ((e = batch_launch(st, *bp, grid, s)) != cudaSuccess) break;
-            cudaEventRecord(e1, s);
-            if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            bp->tune_ms.push_back(ms);
-            if (ms < best) { best = ms; best_k = k; best_desc = od; }
+    int best_k = 1, best_desc = 0, best_t = 0;
+    for (int t = 0; t < NTILE && e == cudaSuccess; ++t) {
+        if (per_sm[t] < 1) continue;  // the tile's shared memory does not fit
+        if (st.batch_tile && st.batch_tile != tiles[t]) continue;
+        set_tile(t);
+        for (int od = 0; od < 2 && e == cudaSuccess; ++od) {
+            if ((e = batch_upload(*bp, P, od ? desc : given, s)) != cudaSuccess) break;
+            for (int k = 1; k <= per_sm[t] && e == cudaSuccess; ++k) {
+                const int grid = st.num_sms * k;
+                if ((e = batch_launch(st, *bp, grid, s)) != cudaSuccess) break;  // warm-up
+                cudaEventRecord(e0, s);
+                if ((e = batch_launch(st, *bp, grid, s)) != cudaSuccess) break;
+                cudaEventRecord(e1, s);
+                if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                bp->tune_ms.push_back(ms);
+                bp->tune_cfg.push_back(tiles[t] << 16 | od << 8 | k);
+                if (ms < best) { best = ms; best_k = k; best_desc = od; best_t = t; }
+            }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    set_tile(best_t);
     if (e == cudaSuccess) e = batch_upload(*bp, P, best_desc ? desc : given, s);
     bp->grid = st.num_sms * best_k;
     bp->desc = best_desc;
@@ -1353,6 +1378,8 @@ int rrtmg_sw_ini_c(double cpdair) {
         st.no_tiled = t && std::strcmp(t, "0") == 0;
         const char* q = std::getenv("RRTMG_SW_TILE_QCAP");
         st.tile_qcap = q ? std::atoi(q) : 0;
+        const char* bt = std::getenv("RRTMG_SW_BATCH_TILE");
+        st.batch_tile = bt ? std::atoi(bt) : 0;
     }
     const int rc = upload(st);
     if (rc) return rc;
@@ -1666,6 +1693,19 @@ int rrtmg_sw_batch_info_c(void* plan, int32_t* grid, int32_t* deepest_first, flo
         const int cap = *ntrials;
         *ntrials = (int)bp->tune_ms.size();
         for (int i = 0; trial_ms && i < cap && i < (int)bp->tune_ms.size(); ++i) trial_ms[i] = bp->tune_ms[i];
+    }
+    return RRTMG_SW_OK;
+}
+
+int rrtmg_sw_batch_tile_c(void* plan, int32_t* cols, int32_t* gpoints, int32_t* trial_cfg, int32_t* ntrials) {
+    BatchPlan* bp = (BatchPlan*)plan;
+    if (!bp) return RRTMG_SW_EARGS;
+    if (cols) *cols = bp->tile;
+    if (gpoints) *gpoints = NGPT;
+    if (ntrials) {
+        const int cap = *ntrials;
+        *ntrials = (int)bp->tune_cfg.size();
+        for (int i = 0; trial_cfg && i < cap && i < (int)bp->tune_cfg.size(); ++i) trial_cfg[i] = bp->tune_cfg[i];
     }
     return RRTMG_SW_OK;
 }

@@ -7,13 +7,20 @@ namespace rrsw {
 
 // levels buffered per reduction round of the g-point sums
 constexpr int KLEV = 4;
-// FP32 form: cells to redo in FP64 queued per column pair (one int each:
-// thread << 20 | column slot << 19 | g-point << 12 | layer << 1 | cloudy);
-// cells past the queue are marked in the scratch and redone by their own
-// thread
+// FP32 form: cells to redo in FP64 queued per column group (one int each:
+// thread << 20 | g-point << 12 | layer << 1 | cloudy); cells past the queue
+// are marked in the scratch and redone by their own thread
 constexpr int REDO_QUEUE = 1024;
+// columns per CTA of the batch kernel's tiles (the single-call kernels take
+// COLS_PER_CTA); sMisc holds their laytrop words, then the queue length
+constexpr int MAX_TILE_COLS = 4;
+constexpr int MISC_QN = MAX_TILE_COLS;
 constexpr int KLEV_F32 = 1;
-__host__ __device__ constexpr int klev_of(size_t rsz) { return rsz == 4 ? KLEV_F32 : KLEV; }
+// (FP64 tiles of 4 columns buffer 2 levels: their shared memory then fits
+// the 137-layer case at one CTA per SM; the sums do not depend on it)
+__host__ __device__ constexpr int klev_of(size_t rsz, int nc = COLS_PER_CTA) {
+    return rsz == 4 ? KLEV_F32 : (nc > 2 ? KLEV / 2 : KLEV);
+}
 constexpr int NQ_MAX = 16;
 // g-point sums per level: fu, fd, cu, cd, fddir, cddir; the FP32 form adds
 // the absorption of the layer below the level (total, clear) for its
@@ -567,24 +574,24 @@ static __device__ __noinline__ CellOpt<float> cell_optics_fp64(const SolveParams
     return o;
 }
 
-// A redone cell into its thread's scratch column sv0 (stride CTA_THREADS
-// per field, NS fields per level; the transmittance slots hold
+// A redone cell into its thread's scratch column sv0 (stride nt, the CTA's
+// threads, per field, NS fields per level; the transmittance slots hold
 // absorptances).
-__device__ inline void store_cell(float* sv0, int NS, int L, int lay, const CellOpt<float>& co, int idelm) {
-    float* sv = sv0 + (size_t)(L - lay) * NS * CTA_THREADS;
-    sv[S_REFC * CTA_THREADS] = co.rc.ref;
-    sv[S_REFDC * CTA_THREADS] = co.rc.refd;
-    sv[S_TRAC * CTA_THREADS] = co.rc.adir;
-    sv[S_TRADC * CTA_THREADS] = co.rc.adif;
-    sv[S_DBTC * CTA_THREADS] = co.zdbtc;
-    sv[S_REF * CTA_THREADS] = co.rt.ref;
-    sv[S_REFD * CTA_THREADS] = co.rt.refd;
-    sv[S_TRA * CTA_THREADS] = co.rt.adir;
-    sv[S_TRAD * CTA_THREADS] = co.rt.adif;
-    sv[S_DBT * CTA_THREADS] = co.zdbt;
+__device__ inline void store_cell(float* sv0, int nt, int NS, int L, int lay, const CellOpt<float>& co, int idelm) {
+    float* sv = sv0 + (size_t)(L - lay) * NS * nt;
+    sv[S_REFC * nt] = co.rc.ref;
+    sv[S_REFDC * nt] = co.rc.refd;
+    sv[S_TRAC * nt] = co.rc.adir;
+    sv[S_TRADC * nt] = co.rc.adif;
+    sv[S_DBTC * nt] = co.zdbtc;
+    sv[S_REF * nt] = co.rt.ref;
+    sv[S_REFD * nt] = co.rt.refd;
+    sv[S_TRA * nt] = co.rt.adir;
+    sv[S_TRAD * nt] = co.rt.adif;
+    sv[S_DBT * nt] = co.zdbt;
     if (idelm == 0) {
-        sv[S_DBTCN * CTA_THREADS] = co.dbtcn;
-        sv[S_DBTN * CTA_THREADS] = co.dbtn;
+        sv[S_DBTCN * nt] = co.dbtcn;
+        sv[S_DBTN * nt] = co.dbtn;
     }
 }
 
@@ -592,15 +599,15 @@ __device__ inline void store_cell(float* sv0, int NS, int L, int lay, const Cell
 // scratch column by more than 1e-6 relative in any field (an FP32 choice
 // that went the other way moves a field by ~5e-5 or more; FP32 rounding of
 // the rest stays far below).
-__device__ inline bool cell_changed(const float* sv0, int NS, int L, int lay, const CellOpt<float>& co) {
-    const float* sv = sv0 + (size_t)(L - lay) * NS * CTA_THREADS;
+__device__ inline bool cell_changed(const float* sv0, int nt, int NS, int L, int lay, const CellOpt<float>& co) {
+    const float* sv = sv0 + (size_t)(L - lay) * NS * nt;
     const float nv[10] = {co.rc.ref, co.rc.refd, co.rc.adir, co.rc.adif, co.zdbtc,
                           co.rt.ref, co.rt.refd, co.rt.adir, co.rt.adif, co.zdbt};
     const int fld[10] = {S_REFC, S_REFDC, S_TRAC, S_TRADC, S_DBTC, S_REF, S_REFD, S_TRA, S_TRAD, S_DBT};
     bool ch = false;
 #pragma unroll
     for (int i = 0; i < 10; ++i) {
-        const float o = sv[fld[i] * CTA_THREADS];
+        const float o = sv[fld[i] * nt];
         if (!(fabsf(nv[i] - o) <= 1.0e-6f * fabsf(nv[i]))) ch = true;
     }
     return ch;
@@ -625,12 +632,12 @@ __device__ inline Coef<double> coef64_at(const SolveParams& P, int col, int lay,
 // g-point) again from layer `from` to the top, over cells already redone in
 // FP64 by the CTA's queue, redoing in FP64 any cell still marked in the
 // scratch (one the queue could not hold).
-static __device__ __noinline__ void redo_cells_fp64(const SolveParams& P, int laytrop, float* sv0, int NS,
+static __device__ __noinline__ void redo_cells_fp64(const SolveParams& P, int laytrop, float* sv0, int nt, int NS,
                                                     int col, int g, int ib, int igb, bool fused, double cossza,
                                                     const double* __restrict__ tab64, float albp, float albd,
                                                     int from) {
     const int L = P.nlay;
-    auto at = [&](int lay, int fld) -> float& { return sv0[((size_t)(L - lay) * NS + fld) * CTA_THREADS]; };
+    auto at = [&](int lay, int fld) -> float& { return sv0[((size_t)(L - lay) * NS + fld) * nt]; };
     float rupc_b = albp, rupdc_b = albd, rup_b = albp, rupd_b = albd;
     if (from > 1) {
         rupc_b = at(from - 1, S_RUPC);
@@ -649,7 +656,7 @@ static __device__ __noinline__ void redo_cells_fp64(const SolveParams& P, int la
             const Coef<double> C64 = coef64_at(P, col, lay, laytrop, tab64, b);
             const CellOpt<float> co =
                 cell_optics_fp64(P, C64, col, g, lay, ib, igb, fused, mark < -1.5f, cossza, tab64, 1);
-            store_cell(sv0, NS, L, lay, co, P.idelm);
+            store_cell(sv0, nt, NS, L, lay, co, P.idelm);
         }
         {
             const float ref = at(lay, S_REFC), refd = at(lay, S_REFDC), dbt = at(lay, S_DBTC);
@@ -680,15 +687,17 @@ __device__ inline void warp_sum4(R& v) {
     v += __shfl_xor_sync(0xffffffffu, v, 2);
 }
 
-// Shared-memory carve-up of one CTA (two columns); the host sizes the
-// launch with the same function.
+// Shared-memory carve-up of one CTA of nc columns (x 112 g-points); the
+// host sizes the launch with the same function.
 struct Smem {
     size_t tm, rq, pdp, coef, hrf, pk, misc, kc, ka, omcf, cld, seed, aer, xs, red, flux, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-__host__ __device__ inline Smem smem_layout(int L, int nq, bool fused, bool aer_stage, size_t rsz) {
+__host__ __device__ inline Smem smem_layout(int L, int nq, bool fused, bool aer_stage, size_t rsz,
+                                            int nc = COLS_PER_CTA) {
+    const int nt = nc * NGPT;
     Smem m;
     size_t o = 0;
     m.tm = o;
@@ -697,30 +706,30 @@ __host__ __device__ inline Smem smem_layout(int L, int nq, bool fused, bool aer_
     if (rsz == sizeof(float)) o = align16(o + NBND * 2 * sizeof(TmSmem));
     // FP32 form: queue of the cells to redo in FP64
     m.rq = o;
-    if (rsz == sizeof(float)) o = align16(o + (REDO_QUEUE + CTA_THREADS) * sizeof(int));
-    m.pdp = o;  o = align16(o + COLS_PER_CTA * L * sizeof(double));
-    m.coef = o; o = align16(o + COLS_PER_CTA * NFR * L * rsz);
+    if (rsz == sizeof(float)) o = align16(o + (REDO_QUEUE + nt) * sizeof(int));
+    m.pdp = o;  o = align16(o + nc * L * sizeof(double));
+    m.coef = o; o = align16(o + nc * NFR * L * rsz);
     m.hrf = o;
     if (rsz == sizeof(float)) {
         // FP32 form: heatfac / dp per layer
-        m.hrf = o; o = align16(o + COLS_PER_CTA * L * sizeof(float));
+        m.hrf = o; o = align16(o + nc * L * sizeof(float));
     }
-    m.pk = o;   o = align16(o + COLS_PER_CTA * L * sizeof(int));
-    m.misc = o; o = align16(o + 8 * sizeof(int));
+    m.pk = o;   o = align16(o + nc * L * sizeof(int));
+    m.misc = o; o = align16(o + 8 * sizeof(int));  // laytrop per column [0, nc), redo queue length [MISC_QN]
     m.kc = m.ka = m.omcf = m.cld = m.seed = m.xs = m.aer = o;
     if (fused) {
-        m.kc = o;   o = align16(o + COLS_PER_CTA * L * sizeof(long long));
-        m.ka = o;   o = align16(o + COLS_PER_CTA * L * sizeof(long long));
-        m.omcf = o; o = align16(o + COLS_PER_CTA * L * sizeof(double));
-        m.cld = o;  o = align16(o + COLS_PER_CTA * 4 * L * rsz);
-        m.seed = o; o = align16(o + COLS_PER_CTA * 4 * sizeof(uint32_t));
+        m.kc = o;   o = align16(o + nc * L * sizeof(long long));
+        m.ka = o;   o = align16(o + nc * L * sizeof(long long));
+        m.omcf = o; o = align16(o + nc * L * sizeof(double));
+        m.cld = o;  o = align16(o + nc * 4 * L * rsz);
+        m.seed = o; o = align16(o + nc * 4 * sizeof(uint32_t));
         m.xs = o;   o = align16(o + NGPT * 32 * sizeof(uint32_t));
     }
     if (aer_stage) {
-        m.aer = o;  o = align16(o + COLS_PER_CTA * 3 * NBND * L * rsz);
+        m.aer = o;  o = align16(o + nc * 3 * NBND * L * rsz);
     }
-    m.red = o;  o = align16(o + klev_of(rsz) * nq * CTA_THREADS * rsz);
-    m.flux = o; o = align16(o + COLS_PER_CTA * nq * (L + 1) * rsz);
+    m.red = o;  o = align16(o + klev_of(rsz, nc) * nq * nt * rsz);
+    m.flux = o; o = align16(o + nc * nq * (L + 1) * rsz);
     m.total = o;
     return m;
 }
@@ -735,30 +744,31 @@ __host__ __device__ inline bool stage_aerosol(int iaer) {
     return sizeof(R) == 4 && iaer != 0;
 }
 
-// Shared-memory views of one CTA for the parameters P (two columns).
+// Shared-memory views of one CTA of nc columns for the parameters P.
 template <typename R>
 struct CtaView {
     const TmSmem* sTm;  // [14][2] FP32 form: taumol descriptors
-    int* sRq;           // [REDO_QUEUE] FP32 form: cells to redo in FP64, then [224] replay start per thread
-    double* sPdp;       // [2][L]
-    R* sCoef;           // [2][NFR][L]
-    float* sHrf;        // [2][L] FP32 form: heatfac / dp
-    int* sPk;           // [2][L]
-    int* sMisc;         // laytrop [2]
-    long long* sKc;     // [2][L] McICA threshold of 1 - cldf
-    long long* sKa;     // [2][L] McICA threshold of alpha
-    double* sOmcf;      // [2][L] 1 - cldf (icld 2)
-    R* sCld;            // [2][4][L] ciwp, clwp, rei, rel
-    uint32_t* sSeed;    // [2][4]
+    int* sRq;           // [REDO_QUEUE] FP32 form: cells to redo in FP64, then [nc*112] replay start per thread
+    double* sPdp;       // [nc][L]
+    R* sCoef;           // [nc][NFR][L]
+    float* sHrf;        // [nc][L] FP32 form: heatfac / dp
+    int* sPk;           // [nc][L]
+    int* sMisc;         // laytrop [nc], redo queue length [MISC_QN]
+    long long* sKc;     // [nc][L] McICA threshold of 1 - cldf
+    long long* sKa;     // [nc][L] McICA threshold of alpha
+    double* sOmcf;      // [nc][L] 1 - cldf (icld 2)
+    R* sCld;            // [nc][4][L] ciwp, clwp, rei, rel
+    uint32_t* sSeed;    // [nc][4]
     uint32_t* sXs;      // [112][32] columns of M^n
-    R* sAer;            // [2][3][14][L] tau, ssa, asym
-    R* sRed;            // [KLEV][NQ][224]
-    R* sFlux;           // [2][NQ][L+1]
+    R* sAer;            // [nc][3][14][L] tau, ssa, asym
+    R* sRed;            // [KLEV][NQ][nc*112]
+    R* sFlux;           // [nc][NQ][L+1]
 };
 
 template <typename R>
-__device__ inline CtaView<R> cta_view(unsigned char* smem_raw, const SolveParams& P) {
-    const Smem M = smem_layout(P.nlay, num_q<R>(P.extra != 0), stages_clouds(P), stage_aerosol<R>(P.iaer), sizeof(R));
+__device__ inline CtaView<R> cta_view(unsigned char* smem_raw, const SolveParams& P, int nc = COLS_PER_CTA) {
+    const Smem M =
+        smem_layout(P.nlay, num_q<R>(P.extra != 0), stages_clouds(P), stage_aerosol<R>(P.iaer), sizeof(R), nc);
     CtaView<R> v;
     v.sTm = (const TmSmem*)(smem_raw + M.tm);
     v.sRq = (int*)(smem_raw + M.rq);
@@ -812,31 +822,33 @@ __device__ inline KissJump kiss_setup(const SolveParams& P, uint32_t* sXs, int g
 
 // Column slot and g-point of solve-CTA thread t.  The FP64 forms (taumol_g
 // runs a different FP64 code path per band) use warps of whole bands from
-// both columns (cT.thr_cg: 2200 -> 1750 ms at 262 144 x 60); the FP32 form
-// (one descriptor-driven taumol path, but cloudy layers that differ by
-// column) is faster with 32 consecutive g-points of one column per warp.
+// two columns (cT.thr_cg over each 224 threads, columns 2k and 2k+1:
+// 2200 -> 1750 ms at 262 144 x 60); the FP32 form (one descriptor-driven
+// taumol path, but cloudy layers that differ by column) is faster with 32
+// consecutive g-points of one column per warp.
 template <typename R>
 __device__ inline int thread_col(int t) {
     if constexpr (sizeof(R) == 4) return t / NGPT;
-    else return cT.thr_cg[t] >> 7;
+    else return 2 * (t / (2 * NGPT)) + (cT.thr_cg[t % (2 * NGPT)] >> 7);
 }
 template <typename R>
 __device__ inline int thread_g(int t) {
     if constexpr (sizeof(R) == 4) return t % NGPT;
-    else return cT.thr_cg[t] & 127;
+    else return cT.thr_cg[t % (2 * NGPT)] & 127;
 }
 
-// Column of slot c2 of column pair `pair`: consecutive columns, or through
-// the sunlit-column list of a batch (P.colmap, nmapped entries); ncol marks
-// an empty slot.
-__device__ inline int pair_col(const SolveParams& P, int pair, int c2, int nmapped) {
-    const int k = COLS_PER_CTA * pair + c2;
+// Column of slot c2 of column group `pair` (nc columns): consecutive
+// columns, or through the sunlit-column list of a batch (P.colmap, nmapped
+// entries); ncol marks an empty slot.
+__device__ inline int pair_col(const SolveParams& P, int pair, int c2, int nmapped, int nc = COLS_PER_CTA) {
+    const int k = nc * pair + c2;
     if (!P.colmap) return k;
     return k < nmapped ? P.colmap[k] : P.ncol;
 }
 
-// One column pair: prep, pass 1, pass 2 and outputs.
-template <typename R, bool MT = false>
+// One group of NC columns (a column pair in the single-call kernels): prep,
+// pass 1, pass 2 and outputs, NC x 112 threads.
+template <typename R, bool MT = false, int NC = COLS_PER_CTA>
 __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const CtaView<R>& V, const KissJump& J,
                                            R* scr, const R* __restrict__ tab, const double* __restrict__ tab64) {
     const int L = P.nlay;
@@ -859,6 +871,8 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
     R* sAer = V.sAer;
     R* sRed = V.sRed;
     R* sFlux = V.sFlux;
+    constexpr int NT = NC * NGPT;
+    static_assert(NC % 2 == 0 && NC <= MAX_TILE_COLS, "column pairs (the FP64 thread map), up to MAX_TILE_COLS");
     const int tid = threadIdx.x;
     const int cc = thread_col<R>(tid), g = thread_g<R>(tid);
     const int ib = cT.ngb[g], igb = cT.gib[g];
@@ -870,9 +884,9 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
     __syncthreads();
     // ---------------- prep: one (column, layer) per item; FP64 in the FP64
     // form, FP32 with the FP64 form's indices in the FP32 form
-    for (int it = tid; it < COLS_PER_CTA * L; it += CTA_THREADS) {
+    for (int it = tid; it < NC * L; it += NT) {
         const int c2 = it / L, lay = it % L + 1;
-        const int pcol = pair_col(P, pair, c2, nmapped);
+        const int pcol = pair_col(P, pair, c2, nmapped, NC);
         constexpr bool f32 = sizeof(R) == 4;
         if constexpr (f32)
             prep_layer_f32(P, pcol, lay, sCoef + c2 * NFR * L, sPk + c2 * L, sPdp + c2 * L, L, tab, tab64);
@@ -938,10 +952,10 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         int lt = 0;
         for (int i = 0; i < L; ++i) lt += (sPk[cc * L + i] >> 30) & 1;
         sMisc[cc] = lt;
-        if (cc == 0) sMisc[2] = 0;  // FP32 form: redo queue length
+        if (cc == 0) sMisc[MISC_QN] = 0;  // FP32 form: redo queue length
     }
     __syncthreads();
-    const int col = pair_col(P, pair, cc, nmapped);
+    const int col = pair_col(P, pair, cc, nmapped, NC);
     const Coef<R> C{sCoef + cc * NFR * L, sPk + cc * L, L, sMisc[cc]};
     bool active = col < P.ncol;
     if (active && (C.laytrop < 1 || C.laytrop >= L)) {
@@ -977,7 +991,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
     int redo_from = L + 1;  // FP32 form: lowest layer to redo in FP64
     for (int lay = 1; lay <= L; ++lay) {
         const int jk = L + 1 - lay;
-        R* sv = scr + (size_t)(jk - 1) * NS * CTA_THREADS + tid;
+        R* sv = scr + (size_t)(jk - 1) * NS * NT + tid;
         if (!active) continue;
         R taug, taur;
         if constexpr (sizeof(R) == 4) {
@@ -1013,9 +1027,9 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         int redo = 0;
         if constexpr (sizeof(R) == 4) {
             if (co.risky) {
-                const int qi = atomicAdd(sMisc + 2, 1);
+                const int qi = atomicAdd(sMisc + MISC_QN, 1);
                 if (qi < REDO_QUEUE) {
-                    V.sRq[qi] = (tid << 20) | (cc << 19) | (g << 12) | (lay << 1) | (ci.cloudy ? 1 : 0);
+                    V.sRq[qi] = (tid << 20) | (g << 12) | (lay << 1) | (ci.cloudy ? 1 : 0);
                 } else {
                     redo = ci.cloudy ? 2 : 1;
                     if (lay < redo_from) redo_from = lay;
@@ -1026,8 +1040,8 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         const RT<R>& rt = co.rt;
         const R zdbtc = co.zdbtc, zdbt = co.zdbt;
         if (P.idelm == 0) {
-            sv[S_DBTCN * CTA_THREADS] = co.dbtcn;
-            sv[S_DBTN * CTA_THREADS] = co.dbtn;
+            sv[S_DBTCN * NT] = co.dbtcn;
+            sv[S_DBTN * NT] = co.dbtn;
         }
         // upward adding recurrence (vrtqdr:122-140)
         {
@@ -1047,20 +1061,20 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         // the FP32 form keeps the absorptances in the transmittance slots
         // and rebuilds ptra = 1 - pref - adir, ptrad = 1 - prefd - adif
         constexpr bool keep_abs = sizeof(R) == 4;
-        sv[S_REFC * CTA_THREADS] = rc.ref;
-        sv[S_REFDC * CTA_THREADS] = rc.refd;
-        sv[S_TRAC * CTA_THREADS] = keep_abs ? rc.adir : rc.tra;
-        sv[S_TRADC * CTA_THREADS] = keep_abs ? rc.adif : rc.trad;
-        sv[S_DBTC * CTA_THREADS] = redo ? -(R)redo : zdbtc;
-        sv[S_RUPC * CTA_THREADS] = rupc_b;
-        sv[S_RUPDC * CTA_THREADS] = rupdc_b;
-        sv[S_REF * CTA_THREADS] = rt.ref;
-        sv[S_REFD * CTA_THREADS] = rt.refd;
-        sv[S_TRA * CTA_THREADS] = keep_abs ? rt.adir : rt.tra;
-        sv[S_TRAD * CTA_THREADS] = keep_abs ? rt.adif : rt.trad;
-        sv[S_DBT * CTA_THREADS] = zdbt;
-        sv[S_RUP * CTA_THREADS] = rup_b;
-        sv[S_RUPD * CTA_THREADS] = rupd_b;
+        sv[S_REFC * NT] = rc.ref;
+        sv[S_REFDC * NT] = rc.refd;
+        sv[S_TRAC * NT] = keep_abs ? rc.adir : rc.tra;
+        sv[S_TRADC * NT] = keep_abs ? rc.adif : rc.trad;
+        sv[S_DBTC * NT] = redo ? -(R)redo : zdbtc;
+        sv[S_RUPC * NT] = rupc_b;
+        sv[S_RUPDC * NT] = rupdc_b;
+        sv[S_REF * NT] = rt.ref;
+        sv[S_REFD * NT] = rt.refd;
+        sv[S_TRA * NT] = keep_abs ? rt.adir : rt.tra;
+        sv[S_TRAD * NT] = keep_abs ? rt.adif : rt.trad;
+        sv[S_DBT * NT] = zdbt;
+        sv[S_RUP * NT] = rup_b;
+        sv[S_RUPD * NT] = rupd_b;
     }
 
     if constexpr (sizeof(R) == 4) {
@@ -1071,30 +1085,30 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         int* sRf = V.sRq + REDO_QUEUE;
         sRf[tid] = L + 1;
         __syncthreads();
-        const int nq = min(sMisc[2], REDO_QUEUE);
+        const int nq = min(sMisc[MISC_QN], REDO_QUEUE);
         if (tid == 0 && P.stats) {
-            atomicAdd(P.stats, (unsigned long long)sMisc[2]);
-            if (sMisc[2] > REDO_QUEUE) atomicAdd(P.stats + 1, (unsigned long long)(sMisc[2] - REDO_QUEUE));
+            atomicAdd(P.stats, (unsigned long long)sMisc[MISC_QN]);
+            if (sMisc[MISC_QN] > REDO_QUEUE) atomicAdd(P.stats + 1, (unsigned long long)(sMisc[MISC_QN] - REDO_QUEUE));
         }
-        for (int i = tid; i < nq; i += CTA_THREADS) {
+        for (int i = tid; i < nq; i += NT) {
             const int e = V.sRq[i];
-            const int t = e >> 20, c2 = (e >> 19) & 1, gg = (e >> 12) & 127, lay = (e >> 1) & 2047;
-            const int pcol = pair_col(P, pair, c2, nmapped);
+            const int t = e >> 20, c2 = thread_col<float>(t), gg = (e >> 12) & 127, lay = (e >> 1) & 2047;
+            const int pcol = pair_col(P, pair, c2, nmapped, NC);
             Coef64At b;
             const Coef<double> Cq = coef64_at(P, pcol, lay, sMisc[c2], tab64, b);
             double cz = P.coszen[pcol];
             if (cz < 1.e-10) cz = 1.e-10;
             const CellOpt<float> co = cell_optics_fp64(P, Cq, pcol, gg, lay, cT.ngb[gg], cT.gib[gg], fused, e & 1, cz,
                                                        tab64, 1);
-            if (cell_changed(scr + t, NS, L, lay, co)) {
-                store_cell(scr + t, NS, L, lay, co, P.idelm);
+            if (cell_changed(scr + t, NT, NS, L, lay, co)) {
+                store_cell(scr + t, NT, NS, L, lay, co, P.idelm);
                 atomicMin(sRf + t, lay);
             }
         }
         __syncthreads();
         const int from = min(redo_from, sRf[tid]);
         if (active && from <= L)
-            redo_cells_fp64(P, C.laytrop, scr + tid, NS, col, g, ib, igb, fused, cossza, tab64, albp, albd, from);
+            redo_cells_fp64(P, C.laytrop, scr + tid, NT, NS, col, g, ib, igb, fused, cossza, tab64, albp, albd, from);
     }
 
     // ---------------- pass 2: top -> bottom, level fluxes and g sums
@@ -1112,14 +1126,14 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
         R ref = R(0), refd = R(0), tra = R(0), trad = R(0), dbt = R(0), rup, rupd, dbtcn = R(0), dbtn = R(0);
         R adirc = R(0), adifc = R(0), adirt = R(0), adift = R(0);
         if (jk <= L) {
-            const R* sv = scr + (size_t)(jk - 1) * NS * CTA_THREADS + tid;
-            refc = sv[S_REFC * CTA_THREADS]; refdc = sv[S_REFDC * CTA_THREADS];
-            trac = sv[S_TRAC * CTA_THREADS]; tradc = sv[S_TRADC * CTA_THREADS];
-            dbtc = sv[S_DBTC * CTA_THREADS];
-            rupc = sv[S_RUPC * CTA_THREADS]; rupdc = sv[S_RUPDC * CTA_THREADS];
-            ref = sv[S_REF * CTA_THREADS]; refd = sv[S_REFD * CTA_THREADS];
-            tra = sv[S_TRA * CTA_THREADS]; trad = sv[S_TRAD * CTA_THREADS];
-            dbt = sv[S_DBT * CTA_THREADS];
+            const R* sv = scr + (size_t)(jk - 1) * NS * NT + tid;
+            refc = sv[S_REFC * NT]; refdc = sv[S_REFDC * NT];
+            trac = sv[S_TRAC * NT]; tradc = sv[S_TRADC * NT];
+            dbtc = sv[S_DBTC * NT];
+            rupc = sv[S_RUPC * NT]; rupdc = sv[S_RUPDC * NT];
+            ref = sv[S_REF * NT]; refd = sv[S_REFD * NT];
+            tra = sv[S_TRA * NT]; trad = sv[S_TRAD * NT];
+            dbt = sv[S_DBT * NT];
             if constexpr (sizeof(R) == 4) {
                 adirc = trac; adifc = tradc; adirt = tra; adift = trad;
                 trac = R(1) - refc - adirc;
@@ -1127,15 +1141,15 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
                 tra = R(1) - ref - adirt;
                 trad = R(1) - refd - adift;
             }
-            rup = sv[S_RUP * CTA_THREADS]; rupd = sv[S_RUPD * CTA_THREADS];
-            if (P.idelm == 0) { dbtcn = sv[S_DBTCN * CTA_THREADS]; dbtn = sv[S_DBTN * CTA_THREADS]; }
+            rup = sv[S_RUP * NT]; rupd = sv[S_RUPD * NT];
+            if (P.idelm == 0) { dbtcn = sv[S_DBTCN * NT]; dbtn = sv[S_DBTN * NT]; }
             if constexpr (sizeof(R) == 4) {
                 // the next level's fields into L1 while this level computes and
                 // reduces (the level barriers keep its loads from moving up)
                 if (jk < L) {
-                    const R* nx = sv + (size_t)NS * CTA_THREADS;
+                    const R* nx = sv + (size_t)NS * NT;
 #pragma unroll
-                    for (int f = 0; f < S_DBTCN; ++f) asm volatile("prefetch.global.L1 [%0];" ::"l"(nx + f * CTA_THREADS));
+                    for (int f = 0; f < S_DBTCN; ++f) asm volatile("prefetch.global.L1 [%0];" ::"l"(nx + f * NT));
                 }
             }
         } else {
@@ -1190,16 +1204,16 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
                 tdbtn = dbtn * tdbtn;
             }
         }
-        constexpr int KL = klev_of(sizeof(R));
+        constexpr int KL = klev_of(sizeof(R), NC);
         const int slot = (jk - 1) % KL;
 #pragma unroll
         for (int i = 0; i < NQ_MAX; ++i)
-            if (i < NQ) sRed[(slot * NQ + i) * CTA_THREADS + cc * NGPT + g] = q[i];
+            if (i < NQ) sRed[(slot * NQ + i) * NT + cc * NGPT + g] = q[i];
         if (slot == KL - 1 || jk == L + 1) {
             __syncthreads();
             const int nlev = slot + 1;
-            const int items = COLS_PER_CTA * NQ * nlev;
-            for (int base = 0; base < items * 4; base += CTA_THREADS) {
+            const int items = NC * NQ * nlev;
+            for (int base = 0; base < items * 4; base += NT) {
                 const int t = base + tid;
                 const int item = t >> 2, part = t & 3;
                 R v = R(0);
@@ -1208,7 +1222,7 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
                     c2 = item / (NQ * nlev);
                     qi = (item / nlev) % NQ;
                     s = item % nlev;
-                    const R* src = sRed + (s * NQ + qi) * CTA_THREADS + c2 * NGPT + part * 28;
+                    const R* src = sRed + (s * NQ + qi) * NT + c2 * NGPT + part * 28;
                     for (int j = 0; j < 28; ++j) v += src[j];
                 }
                 warp_sum4(v);
@@ -1219,15 +1233,15 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
             }
             if (P.bands) {
                 // per-band sums of fu, fd, fddir, cu, cd (spcvmc:619-630 per band)
-                const int bitems = COLS_PER_CTA * NBND * 5 * nlev;
-                for (int t = tid; t < bitems; t += CTA_THREADS) {
+                const int bitems = NC * NBND * 5 * nlev;
+                for (int t = tid; t < bitems; t += NT) {
                     const int s = t % nlev, qs = (t / nlev) % 5, b = (t / (nlev * 5)) % NBND;
                     const int c2 = t / (nlev * 5 * NBND);
                     const int qi = qs == 0 ? 0 : qs == 1 ? 1 : qs == 2 ? 4 : qs == 3 ? 2 : 3;
-                    const R* src = sRed + (s * NQ + qi) * CTA_THREADS + c2 * NGPT + cT.b[b].g0;
+                    const R* src = sRed + (s * NQ + qi) * NT + c2 * NGPT + cT.b[b].g0;
                     R v = R(0);
                     for (int j = 0; j < cT.b[b].ng; ++j) v += src[j];
-                    const int ocol = pair_col(P, pair, c2, nmapped);
+                    const int ocol = pair_col(P, pair, c2, nmapped, NC);
                     const int l = L + 1 - (jk - slot + s);  // level index, 0 = surface
                     if (ocol < P.ncol && P.bout[qs])
                         P.bout[qs][(size_t)ocol + n * ((size_t)l + (size_t)(L + 1) * b)] = (double)v;
@@ -1238,9 +1252,9 @@ __device__ __forceinline__ void solve_pair(const SolveParams& P, int pair, const
     }
 
     // ---------------- outputs (level 0 = surface)
-    for (int it = tid; it < COLS_PER_CTA * (L + 1); it += CTA_THREADS) {
+    for (int it = tid; it < NC * (L + 1); it += NT) {
         const int c2 = it / (L + 1), l = it % (L + 1);
-        const int ocol = pair_col(P, pair, c2, nmapped);
+        const int ocol = pair_col(P, pair, c2, nmapped, NC);
         if (ocol >= P.ncol) continue;
         const R* F = sFlux + c2 * NQ * (L + 1);
         const size_t o = (size_t)ocol + n * (size_t)l;
@@ -1302,21 +1316,24 @@ k_solve(const SolveParams P, const R* __restrict__ tab, const double* __restrict
 // ------------------------------------------------------------------ batch
 // Many independent instances (ncol and nlay differ) in one persistent
 // launch.  Each instance's sunlit columns were listed by k_compact; the work
-// items are the column pairs of those lists, instance after instance, and a
-// CTA takes every gridDim.x-th item.  The parameters of the instance at hand
-// are copied to shared memory when the CTA moves to a new instance.
+// items are the NC-column groups of those lists, instance after instance,
+// and a CTA (NC x 112 threads) takes every gridDim.x-th item.  The
+// parameters of the instance at hand are copied to shared memory when the
+// CTA moves to a new instance.  NC (2 or 4) is the tile the batch planner
+// picks by timing.
 
-template <typename R>
-__global__ void __launch_bounds__(CTA_THREADS, 2)
+template <typename R, int NC>
+__global__ void __launch_bounds__(NC * NGPT, 4 / NC)
 k_solve_batch(const SolveParams* __restrict__ Pb, int ninst, const int* __restrict__ counts,
               const R* __restrict__ tab, const double* __restrict__ tab64) {
+    constexpr int NT = NC * NGPT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_pref[MAX_BATCH + 1];
     __shared__ __align__(16) SolveParams sP;
     fill_tm<R>(smem_raw);
     if (threadIdx.x == 0) {
         s_pref[0] = 0;
-        for (int i = 0; i < ninst; ++i) s_pref[i + 1] = s_pref[i] + (counts[i] + COLS_PER_CTA - 1) / COLS_PER_CTA;
+        for (int i = 0; i < ninst; ++i) s_pref[i + 1] = s_pref[i] + (counts[i] + NC - 1) / NC;
     }
     __syncthreads();
     const int total = s_pref[ninst];
@@ -1335,15 +1352,15 @@ k_solve_batch(const SolveParams* __restrict__ Pb, int ninst, const int* __restri
             {
                 const int* src = (const int*)(Pb + lo);
                 int* dst = (int*)&sP;
-                for (int w = threadIdx.x; w < (int)(sizeof(SolveParams) / sizeof(int)); w += CTA_THREADS) dst[w] = src[w];
+                for (int w = threadIdx.x; w < (int)(sizeof(SolveParams) / sizeof(int)); w += NT) dst[w] = src[w];
             }
             __syncthreads();
-            V = cta_view<R>(smem_raw, sP);
+            V = cta_view<R>(smem_raw, sP, NC);
             J = kiss_setup(sP, V.sXs, thread_g<R>(threadIdx.x));
             cur = lo;
         }
         R* scr = (R*)sP.scratch + (size_t)blockIdx.x * sP.slot_elems;
-        solve_pair<R>(sP, item - s_pref[lo], V, J, scr, tab, tab64);
+        solve_pair<R, false, NC>(sP, item - s_pref[lo], V, J, scr, tab, tab64);
     }
 }
 

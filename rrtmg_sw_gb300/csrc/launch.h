@@ -37,22 +37,23 @@ cudaError_t launch_solve_fp32(const SolveParams& P, const float* tab, const doub
 // launch_compact); smem is the largest instance's dynamic shared memory
 cudaError_t launch_compact(const SolveParams* dPb, int n, int* map_all, const long long* map_off, int* counts,
                            cudaStream_t s);
-size_t solve_smem_fp64(const SolveParams& P);
-size_t solve_smem_fp32(const SolveParams& P);
-int batch_blocks_per_sm_fp64(size_t smem);
-int batch_blocks_per_sm_fp32(size_t smem);
+// batch kernel with tiles of nc columns (2 or 4) x 112 g-points per CTA
+size_t solve_smem_fp64(const SolveParams& P, int nc);
+size_t solve_smem_fp32(const SolveParams& P, int nc);
+int batch_blocks_per_sm_fp64(size_t smem, int nc);
+int batch_blocks_per_sm_fp32(size_t smem, int nc);
 cudaError_t launch_batch_fp64(const SolveParams* dPb, int n, const int* counts, const double* tab, int grid,
-                              size_t smem, cudaStream_t s);
+                              size_t smem, int nc, cudaStream_t s);
 cudaError_t launch_batch_fp32(const SolveParams* dPb, int n, const int* counts, const float* tab,
-                              const double* tab64, int grid, size_t smem, cudaStream_t s);
+                              const double* tab64, int grid, size_t smem, int nc, cudaStream_t s);
 // tangent-linear / adjoint (solve_ad.cu)
 cudaError_t upload_tables_ad(const DevTables& t);
 size_t adjoint_slot_elems(int nlay, int store);
 int adjoint_grid(const SolveParams& P, int num_sms);
 cudaError_t launch_adjoint(const SolveParams& P, const AdParams& A, const double* tab64, int num_sms, int* grid_out,
                            cudaStream_t s);
-// scratch elements (of the form's type) per CTA slot
-size_t slot_elems(int nlay, int idelm, bool fp32);
+// scratch elements (of the form's type) per CTA slot of nc columns
+size_t slot_elems(int nlay, int idelm, bool fp32, int nc = COLS_PER_CTA);
 
 // setcoef_sw indices of every (column, layer) through the solve's prep_layer:
 // cf (ncol x NFR x nlay), pk and pdp (ncol x nlay), column-major by column

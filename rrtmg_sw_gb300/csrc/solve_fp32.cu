@@ -239,21 +239,23 @@ cudaError_t launch_solve_fp32(const SolveParams& P, const float* tab, const doub
     return cudaGetLastError();
 }
 
-size_t solve_smem_fp32(const SolveParams& P) {
+size_t solve_smem_fp32(const SolveParams& P, int nc) {
     return smem_layout(P.nlay, num_q<float>(P.extra != 0), stages_clouds(P), stage_aerosol<float>(P.iaer),
-                       sizeof(float)).total;
+                       sizeof(float), nc).total;
 }
 
-int batch_blocks_per_sm_fp32(size_t smem) {
-    cudaFuncSetAttribute(k_solve_batch<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+int batch_blocks_per_sm_fp32(size_t smem, int nc) {
+    const auto kern = nc == 4 ? k_solve_batch<float, 4> : k_solve_batch<float, 2>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_batch<float>, CTA_THREADS, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nc * NGPT, smem);
     return per_sm;
 }
 
 cudaError_t launch_batch_fp32(const SolveParams* dPb, int n, const int* counts, const float* tab,
-                              const double* tab64, int grid, size_t smem, cudaStream_t s) {
-    k_solve_batch<float><<<grid, CTA_THREADS, smem, s>>>(dPb, n, counts, tab, tab64);
+                              const double* tab64, int grid, size_t smem, int nc, cudaStream_t s) {
+    if (nc == 4) k_solve_batch<float, 4><<<grid, 4 * NGPT, smem, s>>>(dPb, n, counts, tab, tab64);
+    else k_solve_batch<float, 2><<<grid, 2 * NGPT, smem, s>>>(dPb, n, counts, tab, tab64);
     return cudaGetLastError();
 }
 

@@ -9,9 +9,9 @@ namespace rrsw {
 
 cudaError_t upload_tables_fp64(const DevTables& t) { return cudaMemcpyToSymbol(cT, &t, sizeof(DevTables)); }
 
-size_t slot_elems(int nlay, int idelm, bool fp32) {
+size_t slot_elems(int nlay, int idelm, bool fp32, int nc) {
     (void)fp32;  // the same level fields in both forms (elements of the form's type)
-    return (size_t)nlay * (size_t)(idelm == 0 ? NS_MAX : S_DBTCN) * CTA_THREADS;
+    return (size_t)nlay * (size_t)(idelm == 0 ? NS_MAX : S_DBTCN) * (size_t)(nc * NGPT);
 }
 
 LaunchInfo plan_fp64(const SolveParams& P, int num_sms) {
@@ -41,21 +41,23 @@ cudaError_t launch_compact(const SolveParams* dPb, int n, int* map_all, const lo
     return cudaGetLastError();
 }
 
-size_t solve_smem_fp64(const SolveParams& P) {
+size_t solve_smem_fp64(const SolveParams& P, int nc) {
     return smem_layout(P.nlay, num_q<double>(P.extra != 0), stages_clouds(P), stage_aerosol<double>(P.iaer),
-                       sizeof(double)).total;
+                       sizeof(double), nc).total;
 }
 
-int batch_blocks_per_sm_fp64(size_t smem) {
-    cudaFuncSetAttribute(k_solve_batch<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+int batch_blocks_per_sm_fp64(size_t smem, int nc) {
+    const auto kern = nc == 4 ? k_solve_batch<double, 4> : k_solve_batch<double, 2>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_batch<double>, CTA_THREADS, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nc * NGPT, smem);
     return per_sm;
 }
 
 cudaError_t launch_batch_fp64(const SolveParams* dPb, int n, const int* counts, const double* tab, int grid,
-                              size_t smem, cudaStream_t s) {
-    k_solve_batch<double><<<grid, CTA_THREADS, smem, s>>>(dPb, n, counts, tab, tab);
+                              size_t smem, int nc, cudaStream_t s) {
+    if (nc == 4) k_solve_batch<double, 4><<<grid, 4 * NGPT, smem, s>>>(dPb, n, counts, tab, tab);
+    else k_solve_batch<double, 2><<<grid, 2 * NGPT, smem, s>>>(dPb, n, counts, tab, tab);
     return cudaGetLastError();
 }
 

@@ -104,6 +104,8 @@ def lib():
         L.rrtmg_sw_batch_run_c.argtypes = [C.c_void_p, C.c_void_p]
         L.rrtmg_sw_batch_info_c.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                             C.POINTER(C.c_float), C.POINTER(C.c_int32)]
+        L.rrtmg_sw_batch_tile_c.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                            C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.rrtmg_sw_batch_free_c.argtypes = [C.c_void_p]
         L.rrtmg_sw_nomcica_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_void_p]
         L.rrtmg_sw_static_dev_c.argtypes = [C.POINTER(RrtmgSwArgs), C.POINTER(RrtmgSwClouds), C.c_void_p]
@@ -387,10 +389,19 @@ class BatchPlan:
         _check(lib().rrtmg_sw_batch_run_c(self.handle, C.c_void_p(stream)))
 
     def info(self):
-        grid, desc, nt = C.c_int32(), C.c_int32(), C.c_int32(16)
-        ms = (C.c_float * 16)()
+        """The autotuner's choice and trials: grid, deepest_first, tile
+        (columns, g-points per CTA), trial_ms and trials (tile columns,
+        deepest first, CTAs per SM) in the same order."""
+        cap = 64
+        grid, desc, nt = C.c_int32(), C.c_int32(), C.c_int32(cap)
+        ms = (C.c_float * cap)()
         _check(lib().rrtmg_sw_batch_info_c(self.handle, C.byref(grid), C.byref(desc), ms, C.byref(nt)))
-        return {"grid": grid.value, "deepest_first": bool(desc.value), "trial_ms": list(ms[:min(nt.value, 16)])}
+        cols, gpts, nc = C.c_int32(), C.c_int32(), C.c_int32(cap)
+        cfg = (C.c_int32 * cap)()
+        _check(lib().rrtmg_sw_batch_tile_c(self.handle, C.byref(cols), C.byref(gpts), cfg, C.byref(nc)))
+        trials = [(v >> 16, bool((v >> 8) & 255), v & 255) for v in cfg[:min(nc.value, cap)]]
+        return {"grid": grid.value, "deepest_first": bool(desc.value), "tile": (cols.value, gpts.value),
+                "trial_ms": list(ms[:min(nt.value, cap)]), "trials": trials}
 
     def close(self):
         if self.handle:

@@ -4,7 +4,9 @@ CUDA graph (rrtmg_sw_batch_plan_c / rrtmg_sw_batch_run_c).
 
 Every instance is compared with the single-instance device entry point
 (rrtmg_sw_mcica_dev_c) on the same inputs.  The batch kernel runs the same
-per-column-pair code.  The FP64 form is compiled without FMA contraction, so
+per-column code, over tiles of 2 or 4 columns per CTA (the autotuner's
+choice; the per-column arithmetic and the order of the g-point sums do not
+depend on the tile).  Each tile is also checked on its own.  The FP64 form is compiled without FMA contraction, so
 its sunlit columns must agree bit for bit (tolerance 0); the FP32 form lets
 the compiler contract each kernel's inlined copy of that code its own way, so
 its sunlit columns must agree to 1e-6 relative (a few FP32 roundings).
@@ -102,6 +104,11 @@ def test_batch_matches_single_instance_calls(torch, form):
     info = plan.info()
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     assert info["grid"] % sms == 0 and len(info["trial_ms"]) >= 2
+    # the autotuner timed both tiles (2 and 4 columns x 112 g-points per CTA:
+    # both fit the 137-layer instance's shared memory) and kept a timed one
+    assert len(info["trials"]) == len(info["trial_ms"])
+    assert {t[0] for t in info["trials"]} == {2, 4}, info["trials"]
+    assert info["tile"][1] == 112 and (info["tile"][0], info["deepest_first"], info["grid"] // sms) in info["trials"]
     for run in range(2):  # graph replays
         for x in insts:
             x.fill_nan()
@@ -117,6 +124,35 @@ def test_batch_matches_single_instance_calls(torch, form):
                                                err_msg="run %d %s" % (run, k))
                 assert np.all(got[k][~x.sun] == 0.0), (run, k)
                 assert np.all(np.abs(r[k][~x.sun]) <= 1e-6), (run, k)
+    plan.close()
+
+
+@pytest.mark.parametrize("tile", [2, 4])
+def test_batch_each_tile_matches_single_calls(torch, tile):
+    # RRTMG_SW_BATCH_TILE (read at rrtmg_sw_ini_c) keeps one tile: both give
+    # the single calls' FP64 values bit for bit
+    gi.set_form(gi.FORM_FP64)
+    insts = [Instance(torch, nc, nl, 960 + i) for i, (nc, nl) in enumerate(SHAPES)]
+    ref = [single(torch, x) for x in insts]
+    os.environ["RRTMG_SW_BATCH_TILE"] = str(tile)
+    try:
+        gi.rrtmg_sw_ini(1.004e3)
+        s = torch.cuda.current_stream().cuda_stream
+        plan = gi.BatchPlan([x.args for x in insts], [x.clouds for x in insts], stream=s)
+    finally:
+        os.environ.pop("RRTMG_SW_BATCH_TILE", None)
+        gi.rrtmg_sw_ini(1.004e3)
+    info = plan.info()
+    assert info["tile"] == (tile, 112) and {t[0] for t in info["trials"]} == {tile}, info
+    for x in insts:
+        x.fill_nan()
+    plan.run(s)
+    torch.cuda.synchronize()
+    for x, r in zip(insts, ref):
+        got = x.outputs()
+        for k in OUTS:
+            np.testing.assert_array_equal(got[k][x.sun], r[k][x.sun], err_msg="tile %d %s" % (tile, k))
+            assert np.all(got[k][~x.sun] == 0.0), k
     plan.close()
 
 
