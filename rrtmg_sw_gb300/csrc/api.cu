@@ -605,6 +605,7 @@ int enqueue_solve(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, c
         P.tovf = P.tovfcount + 1;
         P.tovfcap = P.npairs;
         P.tile_qcap = st.tile_qcap;
+        P.tile_slots = li.tile_slots;
         CK(cudaMemsetAsync(P.tovfcount, 0, sizeof(int), s));
         launches += 1;  // the preparation kernel
     }
@@ -1068,6 +1069,7 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
         P.tovf = tail + 1;
         P.tovfcap = std::min(P.npairs, kStaticOvfCap);
         P.tile_qcap = st.tile_qcap;
+        P.tile_slots = li.tile_slots;
         CK(cudaMemsetAsync(P.tovfcount, 0, sizeof(int), s));
     }
     CK(cudaMemsetAsync(P.err, 0, sizeof(int), s));

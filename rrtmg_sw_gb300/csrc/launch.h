@@ -18,6 +18,7 @@ struct LaunchInfo {
     // bytes of one pair's prepared block (P.tprep holds npairs of them)
     int prep_grid = 0;
     size_t prep_smem = 0, prep_bytes = 0;
+    int tile_slots = 2;  // pair slots of the tiled kernel (SolveParams::tile_slots)
 };
 
 // FP64 form

@@ -56,6 +56,7 @@ struct SolveParams {
     int* tovfcount;
     int tovfcap;
     int tile_qcap;
+    int tile_slots;  // tiled FP32 kernel: pair slots (2 or 3) its shared memory was sized for
     // FP32 form's counters (nullptr: not kept): [0] cells redone in FP64,
     // [1] of those past the scratch kernel's queue (redone by their own
     // thread), [2] column pairs the tiled kernel handed back, [3] subcolumns

@@ -195,7 +195,8 @@ LaunchInfo plan_fp32(const SolveParams& P, int num_sms, bool allow_tiled) {
         // one CTA per SM, persistent over the column pairs
         const bool fused = P.fused && P.icld >= 1, nomc = P.nomcica && P.icld >= 1;
         li.tiled = true;
-        li.smem = tiled_smem(P.nlay, P.extra ? 16 : 8, fused, fused || nomc).total;
+        li.tile_slots = tiled_slots(P, (size_t)smem_optin);
+        li.smem = tiled_smem(P.nlay, P.extra ? 16 : 8, fused, fused || nomc, li.tile_slots).total;
         cudaFuncSetAttribute(k_solve_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)li.smem);
         li.grid = num_sms < P.npairs ? num_sms : P.npairs;
         if (li.grid < 1) li.grid = 1;

@@ -71,12 +71,20 @@ constexpr int T_RCAP = 64;                               // subcolumns with such
 constexpr int T_NF = 10;                                 // tile fields per cell
 constexpr int T_MAXL = 64;                               // layers (two mask words per subcolumn)
 enum { TF_REFC, TF_REFDC, TF_ADIRC, TF_ADIFC, TF_DBTC, TF_REF, TF_REFD, TF_ADIR, TF_ADIF, TF_DBT };
-enum { TB_FULL0, TB_FULL1, TB_EMPTY0, TB_EMPTY1, TB_PAIR0, TB_PAIR1, TB_SWEPT0, TB_SWEPT1, TB_FIN0, TB_FIN1,
-       TB_N };
-// control words in shared memory
-// (TC_ACT0 + 2 * parity + column: the adding warps read a pair's flags
-// while the optics warps load the next pair's)
-enum { TC_ROW0, TC_ROW1, TC_QN0, TC_QN1, TC_ABORT, TC_LT0, TC_LT1, TC_ACT0, TC_ACT1, TC_ACT2, TC_ACT3, TC_N };
+// Pair slots: the per-pair state (solar source and albedos, active flags,
+// FP64 queue, set-aside marks, level sums) of pair lp sits in slot
+// lp % nslot, nslot = 3 when shared memory allows (else 2), so the optics
+// and adding warps can start pair lp while pairs lp - 1 and lp - 2 are still
+// swept or finished.
+constexpr int T_SLOTS = 3;
+// mbarriers: tile buffers (FULL, EMPTY per buffer), then per pair slot the
+// pair produced (PAIR), swept (SWEPT) and finished (FIN)
+enum { TB_FULL0, TB_FULL1, TB_EMPTY0, TB_EMPTY1, TB_PAIR0, TB_SWEPT0 = TB_PAIR0 + T_SLOTS,
+       TB_FIN0 = TB_SWEPT0 + T_SLOTS, TB_N = TB_FIN0 + T_SLOTS };
+// control words in shared memory: row counters per tile buffer; per slot the
+// FP64 queue length and (TC_ACT0 + 2 * slot + column) the active flags
+enum { TC_ROW0, TC_ROW1, TC_ABORT, TC_LT0, TC_LT1, TC_QN0, TC_ACT0 = TC_QN0 + T_SLOTS,
+       TC_N = TC_ACT0 + 2 * T_SLOTS };
 
 // Shared-memory carve-up of the tiled kernel; the host sizes the launch with
 // the same function.
@@ -85,7 +93,7 @@ struct TSmem {
         total;
 };
 
-__host__ __device__ inline TSmem tiled_smem(int L, int nq, bool fused, bool cloud_stage) {
+__host__ __device__ inline TSmem tiled_smem(int L, int nq, bool fused, bool cloud_stage, int nslot) {
     TSmem m;
     size_t o = 0;
     m.bar = o;   o = align16(o + TB_N * sizeof(unsigned long long));
@@ -100,11 +108,12 @@ __host__ __device__ inline TSmem tiled_smem(int L, int nq, bool fused, bool clou
     m.cld = m.mask = o;
     if (cloud_stage) { m.cld = o; o = align16(o + (size_t)COLS_PER_CTA * 4 * L * sizeof(float)); }
     if (fused) { m.mask = o; o = align16(o + (size_t)COLS_PER_CTA * NGPT * 2 * sizeof(uint32_t)); }
-    m.sub = o;   o = align16(o + (size_t)2 * 3 * COLS_PER_CTA * NGPT * sizeof(float));   // [par][zinc,albp,albd][224]
-    m.risky = o; o = align16(o + (size_t)2 * TILES * sizeof(uint32_t));
-    m.queue = o; o = align16(o + (size_t)2 * T_QCAP * sizeof(int));
-    m.recof = o; o = align16(o + (size_t)2 * COLS_PER_CTA * NGPT * sizeof(short));
-    m.flux = o;  o = align16(o + (size_t)2 * COLS_PER_CTA * nq * (L + 1) * sizeof(float));
+    // per pair slot
+    m.sub = o;   o = align16(o + (size_t)nslot * 3 * COLS_PER_CTA * NGPT * sizeof(float));   // [slot][zinc,albp,albd][224]
+    m.risky = o; o = align16(o + (size_t)nslot * TILES * sizeof(uint32_t));
+    m.queue = o; o = align16(o + (size_t)nslot * T_QCAP * sizeof(int));
+    m.recof = o; o = align16(o + (size_t)nslot * COLS_PER_CTA * NGPT * sizeof(short));
+    m.flux = o;  o = align16(o + (size_t)nslot * COLS_PER_CTA * nq * (L + 1) * sizeof(float));
     // adding warps: surface-level sums and lane keys of a tile
     m.scr = o;   o = align16(o + (size_t)16 * TW * sizeof(float));
     // FP64 warp: reduction scratch of the set-aside subcolumns (rows 6-7: 64-bit keys)
@@ -113,8 +122,8 @@ __host__ __device__ inline TSmem tiled_smem(int L, int nq, bool fused, bool clou
     return m;
 }
 
-// Per-CTA global area of the tiled kernel (bytes): the FP64 warp's albedo
-// scratch and, per pair parity, the FP64 cells and the set-aside subcolumns.
+// Per-CTA global area of the tiled kernel (bytes): the FP64 warps' albedo
+// scratch and, per pair slot, the FP64 cells and the set-aside subcolumns.
 struct TGlob {
     size_t rrup, par, corr, rec, rec_stride, par_stride, total;
 };
@@ -132,7 +141,7 @@ __host__ __device__ inline TGlob tiled_glob(int L) {
     g.rec_stride = align256((8 + (size_t)T_NF * L) * sizeof(float));
     g.rec = p;    p = align256(p + (size_t)T_RCAP * g.rec_stride);
     g.par_stride = p;
-    o += 2 * p;
+    o += T_SLOTS * p;
     g.total = o;
     return g;
 }
@@ -240,11 +249,11 @@ struct TileView {
     float* mu;        // [2]
     float* cld;       // [2][4][L]
     uint32_t* mask;   // [224][2]
-    float* sub;       // [2][3][224]
-    uint32_t* risky;  // [2][TILES]
-    int* queue;       // [2][T_QCAP]
-    short* recof;     // [2][224]
-    float* flux;      // [2][2][NQ][L+1]
+    float* sub;       // [slot][3][224]
+    uint32_t* risky;  // [slot][TILES]
+    int* queue;       // [slot][T_QCAP]
+    short* recof;     // [slot][224]
+    float* flux;      // [slot][2][NQ][L+1]
     float* scr;       // [16][TW] adding warps
     float* scr2;      // [T_F64][16][TW] FP64 warps
 };
@@ -337,20 +346,23 @@ struct TCtx {
     TPrep B;
     unsigned char* glob;        // this CTA's global area
     const unsigned char* prep;  // the prepared blocks of all pairs
-    int L, nmapped, qcap, nlocal;
+    int L, nmapped, qcap, nlocal, nslot;
     bool fused, nomc, cstage;
     volatile int* abort;
 };
 
 __device__ inline const unsigned char* tblk(const TCtx& X, int pair) { return X.prep + (size_t)pair * X.B.total; }
 
-__device__ inline unsigned char* tpar(const TCtx& X, int par) {
-    return X.glob + X.G.par + (size_t)par * X.G.par_stride;
+__device__ inline unsigned char* tpar(const TCtx& X, int slot) {
+    return X.glob + X.G.par + (size_t)slot * X.G.par_stride;
 }
-__device__ inline float* trec(const TCtx& X, int par, int r) {
-    return (float*)(tpar(X, par) + X.G.rec + (size_t)r * X.G.rec_stride);
+__device__ inline float* trec(const TCtx& X, int slot, int r) {
+    return (float*)(tpar(X, slot) + X.G.rec + (size_t)r * X.G.rec_stride);
 }
 __device__ inline int tpair(int lp) { return blockIdx.x + lp * gridDim.x; }
+// pair lp's slot, and the phase parity of the slot's barriers for it
+__device__ inline int tslot(const TCtx& X, int lp) { return lp % X.nslot; }
+__device__ inline unsigned tphase(const TCtx& X, int lp) { return (unsigned)(lp / X.nslot) & 1u; }
 
 // ---- k_tiled_prep: one CTA (2 columns x 112 g-points) per pair at a time,
 // persistent.  setcoef (FP32, the FP64 form's indices), McICA
@@ -528,19 +540,19 @@ __device__ inline void opt_copy(void* dst, const void* src, size_t n) {
 // ---- optics warps: pair lp's prepared block into shared memory
 __device__ void tiled_load(const SolveParams& P, const TCtx& X, int lp) {
     const TileView& V = X.V;
-    const int L = X.L, par = lp & 1;
+    const int L = X.L, slot = tslot(X, lp);
     const unsigned char* blk = tblk(X, tpair(lp));
     opt_copy(V.coef, blk + X.B.coef, align16((size_t)COLS_PER_CTA * NFR * L * sizeof(float)));
     opt_copy(V.pk, blk + X.B.pk, align16((size_t)COLS_PER_CTA * L * sizeof(int)));
     opt_copy(V.hrf, blk + X.B.hrf, align16((size_t)COLS_PER_CTA * L * sizeof(float)));
     if (X.cstage) opt_copy(V.cld, blk + X.B.cld, align16((size_t)COLS_PER_CTA * 4 * L * sizeof(float)));
     if (X.fused) opt_copy(V.mask, blk + X.B.mask, (size_t)COLS_PER_CTA * NGPT * 2 * sizeof(uint32_t));
-    opt_copy(V.sub + par * 3 * COLS_PER_CTA * NGPT, blk + X.B.sub, (size_t)3 * COLS_PER_CTA * NGPT * sizeof(float));
+    opt_copy(V.sub + slot * 3 * COLS_PER_CTA * NGPT, blk + X.B.sub, (size_t)3 * COLS_PER_CTA * NGPT * sizeof(float));
     const int* misc = (const int*)(blk + X.B.misc);
     if (threadIdx.x < COLS_PER_CTA) {
         const int c2 = threadIdx.x;
         V.ctl[TC_LT0 + c2] = misc[TP_LT0 + c2];
-        V.ctl[TC_ACT0 + 2 * par + c2] = misc[TP_ACT0 + c2];
+        V.ctl[TC_ACT0 + 2 * slot + c2] = misc[TP_ACT0 + c2];
         V.mu[c2] = __int_as_float(misc[TP_MU0 + c2]);
     }
     opt_sync();
@@ -550,14 +562,14 @@ __device__ void tiled_load(const SolveParams& P, const TCtx& X, int lp) {
 __device__ void tiled_optics(const SolveParams& P, const TCtx& X, int lp, int t, int b,
                              const float* __restrict__ tab, const double* __restrict__ tab64) {
     const TileView& V = X.V;
-    const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
+    const int L = X.L, slot = tslot(X, lp), pair = tpair(lp), lane = threadIdx.x & 31;
     float* tb = V.tile + (size_t)b * T_NF * L * TW;
     const int s = TW * t + lane, c2 = s / NGPT, g = s % NGPT;
     const int ib = cT.ngb[g], igb = cT.gib[g];
     const int pcol = pair_col(P, pair, c2, X.nmapped);
-    const bool act = V.ctl[TC_ACT0 + 2 * par + c2] != 0;
+    const bool act = V.ctl[TC_ACT0 + 2 * slot + c2] != 0;
     const Coef<float> C{V.coef + c2 * NFR * L, V.pk + c2 * L, L, V.ctl[TC_LT0 + c2]};
-    const float zinc = V.sub[par * 3 * COLS_PER_CTA * NGPT + s];
+    const float zinc = V.sub[slot * 3 * COLS_PER_CTA * NGPT + s];
     const float mu = V.mu[c2];
     const float* aer = (const float*)(tblk(X, pair) + X.B.aer) + c2 * 3 * NBND * L;
     const float* cld = X.cstage ? V.cld + c2 * 4 * L : nullptr;
@@ -595,9 +607,9 @@ __device__ void tiled_optics(const SolveParams& P, const TCtx& X, int lp, int t,
             if (co.risky) {
                 // an FP32 choice too close to call: the FP64 warp redoes the
                 // cell, and the subcolumn is swept apart from its tile
-                const int q = atomicAdd(&V.ctl[TC_QN0 + par], 1);
-                if (q < X.qcap) V.queue[par * T_QCAP + q] = (s << 12) | (lay << 1) | (ci.cloudy ? 1 : 0);
-                atomicOr(&V.risky[par * TILES + t], 1u << lane);
+                const int q = atomicAdd(&V.ctl[TC_QN0 + slot], 1);
+                if (q < X.qcap) V.queue[slot * T_QCAP + q] = (s << 12) | (lay << 1) | (ci.cloudy ? 1 : 0);
+                atomicOr(&V.risky[slot * TILES + t], 1u << lane);
             }
         }
 #pragma unroll
@@ -607,9 +619,9 @@ __device__ void tiled_optics(const SolveParams& P, const TCtx& X, int lp, int t,
 
 // Record slots of tile t's set-aside subcolumns start after those of the
 // pair's earlier tiles (their risky masks are final once tile t is).
-__device__ inline int tiled_rec_base(const TileView& V, int par, int t) {
+__device__ inline int tiled_rec_base(const TileView& V, int slot, int t) {
     int base = 0;
-    for (int tt = 0; tt < t; ++tt) base += __popc(V.risky[par * TILES + tt]);
+    for (int tt = 0; tt < t; ++tt) base += __popc(V.risky[slot * TILES + tt]);
     return base;
 }
 
@@ -619,12 +631,12 @@ __device__ inline int tiled_rec_base(const TileView& V, int par, int t) {
 // ten fields of every layer, spread over the optics warps' threads
 __device__ void tiled_set_aside(const TCtx& X, int lp, int t, int b) {
     const TileView& V = X.V;
-    const int L = X.L, par = lp & 1;
-    const uint32_t rm = V.risky[par * TILES + t];
+    const int L = X.L, slot = tslot(X, lp);
+    const uint32_t rm = V.risky[slot * TILES + t];
     if (!rm) return;
-    const int base = tiled_rec_base(V, par, t), nr = __popc(rm);
+    const int base = tiled_rec_base(V, slot, t), nr = __popc(rm);
     const float* tb = V.tile + (size_t)b * T_NF * L * TW;
-    const float* sub = V.sub + par * 3 * COLS_PER_CTA * NGPT;
+    const float* sub = V.sub + slot * 3 * COLS_PER_CTA * NGPT;
     const int per = T_NF * L;
     for (int it = threadIdx.x; it < nr * (per + 1); it += T_OPT * 32) {
         const int j = it / (per + 1), rem = it % (per + 1);
@@ -633,7 +645,7 @@ __device__ void tiled_set_aside(const TCtx& X, int lp, int t, int b) {
         uint32_t m = rm;  // its j-th set bit
         for (int k = 0; k < j; ++k) m &= m - 1u;
         const int lane = __ffs(m) - 1;
-        float* rp = trec(X, par, idx);
+        float* rp = trec(X, slot, idx);
         if (rem < per) {
             rp[8 + rem] = tb[(size_t)rem * TW + lane];
         } else {
@@ -643,7 +655,7 @@ __device__ void tiled_set_aside(const TCtx& X, int lp, int t, int b) {
             rp[2] = sub[s];
             rp[3] = sub[COLS_PER_CTA * NGPT + s];
             rp[4] = sub[2 * COLS_PER_CTA * NGPT + s];
-            V.recof[par * COLS_PER_CTA * NGPT + s] = (short)idx;
+            V.recof[slot * COLS_PER_CTA * NGPT + s] = (short)idx;
         }
     }
 }
@@ -651,14 +663,14 @@ __device__ void tiled_set_aside(const TCtx& X, int lp, int t, int b) {
 // ---- FP64 warp: the pair's queued cells, 32 at a time
 __device__ void tiled_redo(const SolveParams& P, const TCtx& X, int lp, const double* __restrict__ tab64) {
     const TileView& V = X.V;
-    const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
-    unsigned char* pb = tpar(X, par);
+    const int L = X.L, slot = tslot(X, lp), pair = tpair(lp), lane = threadIdx.x & 31;
+    unsigned char* pb = tpar(X, slot);
     float* corr = (float*)(pb + X.G.corr);
     const int* misc = (const int*)(tblk(X, pair) + X.B.misc);
-    const int qn = min(V.ctl[TC_QN0 + par], X.qcap);
+    const int qn = min(V.ctl[TC_QN0 + slot], X.qcap);
     (void)L;
     for (int k = lane; k < qn; k += 32) {
-        const int e = V.queue[par * T_QCAP + k];
+        const int e = V.queue[slot * T_QCAP + k];
         const int s = e >> 12, lay = (e >> 1) & 127, c2 = s / NGPT, g = s % NGPT;
         const int pcol = pair_col(P, pair, c2, X.nmapped);
         Coef64At b;
@@ -690,16 +702,16 @@ __device__ __forceinline__ int q_srow(int k) { return (q_total(k) ? 4 : 0) + q_c
 template <int SKY, int NQ>
 __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, int b) {
     const TileView& V = X.V;
-    const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
+    const int L = X.L, ps = tslot(X, lp), pair = tpair(lp), lane = threadIdx.x & 31;
     const size_t n = (size_t)P.ncol, L1 = (size_t)L + 1;
     constexpr int F0 = SKY_BASE[SKY];
     float* tb = V.tile + (size_t)b * T_NF * L * TW;
     const int s = TW * t + lane, c2 = s / NGPT, g = s % NGPT;
     const int ib = cT.ngb[g];
-    const float* sub = V.sub + par * 3 * COLS_PER_CTA * NGPT;
+    const float* sub = V.sub + ps * 3 * COLS_PER_CTA * NGPT;
     const float zinc = sub[s], albp = sub[COLS_PER_CTA * NGPT + s], albd = sub[2 * COLS_PER_CTA * NGPT + s];
-    const bool act = V.ctl[TC_ACT0 + 2 * par + c2] != 0;
-    const bool risky = (V.risky[par * TILES + t] >> lane) & 1u;
+    const bool act = V.ctl[TC_ACT0 + 2 * ps + c2] != 0;
+    const bool risky = (V.risky[ps * TILES + t] >> lane) & 1u;
     const bool use = act && !risky;
     // subcolumns with FP64 cells were copied aside by the optics warps
     // (tiled_set_aside); they stay out of this tile's sums
@@ -783,7 +795,7 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
                 e[o] += x[1]; e[o + 1] += x[3]; e[o + 2] += x[4]; e[o + 3] += x[5];
             }
         }
-        float* Fl0 = V.flux + ((size_t)(par * COLS_PER_CTA + c0) * NQ) * L1;
+        float* Fl0 = V.flux + ((size_t)(ps * COLS_PER_CTA + c0) * NQ) * L1;
 #pragma unroll
         for (int k = 0; k < 8; ++k) Fl0[k * L1 + v] += a0[k];
         if constexpr (NQ > 8) {
@@ -834,11 +846,11 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
 template <int NQ>
 __device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r0, int rn, float* R, float* scr) {
     const TileView& V = X.V;
-    const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
+    const int L = X.L, slot = tslot(X, lp), pair = tpair(lp), lane = threadIdx.x & 31;
     const size_t n = (size_t)P.ncol, L1 = (size_t)L + 1;
     const int r = r0 + lane;
     const bool on = r < rn;
-    const float* rp = trec(X, par, on ? r : r0);
+    const float* rp = trec(X, slot, on ? r : r0);
     const int s = (int)rp[0], c2 = (int)rp[1], g = s % NGPT, ib = cT.ngb[g];
     const bool uv = ib >= 9 && ib <= 12;
     const float zinc = on ? rp[2] : 0.0f, albp = rp[3], albd = rp[4];
@@ -934,7 +946,7 @@ __device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r
                     m &= m - 1;
                     v += scr[k * TW + j];
                 }
-                V.flux[((size_t)(par * COLS_PER_CTA + c) * NQ + k) * L1 + l] += v;
+                V.flux[((size_t)(slot * COLS_PER_CTA + c) * NQ + k) * L1 + l] += v;
             }
         }
         __syncwarp();
@@ -960,18 +972,18 @@ __device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r
 template <int NQ>
 __device__ void tiled_finish(const SolveParams& P, const TCtx& X, int lp) {
     const TileView& V = X.V;
-    const int L = X.L, par = lp & 1, pair = tpair(lp), lane = threadIdx.x & 31;
+    const int L = X.L, slot = tslot(X, lp), pair = tpair(lp), lane = threadIdx.x & 31;
     const size_t n = (size_t)P.ncol;
-    const int qn = V.ctl[TC_QN0 + par], rn = tiled_rec_base(V, par, TILES);
+    const int qn = V.ctl[TC_QN0 + slot], rn = tiled_rec_base(V, slot, TILES);
     const bool ovf = qn > X.qcap || rn > T_RCAP;
     if (!ovf && rn > 0) {
-        const float* corr = (const float*)(tpar(X, par) + X.G.corr);
+        const float* corr = (const float*)(tpar(X, slot) + X.G.corr);
         for (int k = lane; k < qn; k += 32) {
-            const int e = V.queue[par * T_QCAP + k];
+            const int e = V.queue[slot * T_QCAP + k];
             const int s = e >> 12, lay = (e >> 1) & 127;
-            const int r = V.recof[par * COLS_PER_CTA * NGPT + s];
+            const int r = V.recof[slot * COLS_PER_CTA * NGPT + s];
             if (r >= 0 && r < T_RCAP) {
-                float* rp = trec(X, par, r) + 8;
+                float* rp = trec(X, slot, r) + 8;
 #pragma unroll
                 for (int f = 0; f < T_NF; ++f) rp[f * L + lay - 1] = corr[k * T_NF + f];
             }
@@ -1000,7 +1012,7 @@ __device__ void tiled_finish(const SolveParams& P, const TCtx& X, int lp) {
         const int c2 = it / (L + 1), l = it % (L + 1);
         const int ocol = pair_col(P, pair, c2, X.nmapped);
         if (ocol >= P.ncol) continue;
-        const float* F = V.flux + (size_t)(par * COLS_PER_CTA + c2) * NQ * (L + 1);
+        const float* F = V.flux + (size_t)(slot * COLS_PER_CTA + c2) * NQ * (L + 1);
         const size_t o = (size_t)ocol + n * (size_t)l;
         const double fu = (double)F[0 * (L + 1) + l], fd = (double)F[1 * (L + 1) + l];
         P.swuflx[o] = fu;
@@ -1029,13 +1041,13 @@ __device__ void tiled_finish(const SolveParams& P, const TCtx& X, int lp) {
         }
     }
     __syncwarp();
-    // this parity's per-pair state, ready for pair lp + 2
-    float* F = V.flux + (size_t)par * COLS_PER_CTA * NQ * (L + 1);
+    // this slot's per-pair state, ready for pair lp + nslot
+    float* F = V.flux + (size_t)slot * COLS_PER_CTA * NQ * (L + 1);
     for (int k = lane; k < COLS_PER_CTA * NQ * (L + 1); k += 32) F[k] = 0.0f;
-    for (int k = lane; k < COLS_PER_CTA * NGPT; k += 32) V.recof[par * COLS_PER_CTA * NGPT + k] = -1;
-    if (lane < TILES) V.risky[par * TILES + lane] = 0u;
+    for (int k = lane; k < COLS_PER_CTA * NGPT; k += 32) V.recof[slot * COLS_PER_CTA * NGPT + k] = -1;
+    if (lane < TILES) V.risky[slot * TILES + lane] = 0u;
     if (lane == 0) {
-        V.ctl[TC_QN0 + par] = 0;
+        V.ctl[TC_QN0 + slot] = 0;
     }
     __syncwarp();
 }
@@ -1064,7 +1076,8 @@ k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* 
     X.fused = P.fused && P.icld >= 1;
     X.nomc = P.nomcica && P.icld >= 1;
     X.cstage = X.fused || X.nomc;
-    const TSmem M = tiled_smem(L, NQ, X.fused, X.cstage);
+    X.nslot = P.tile_slots == T_SLOTS ? T_SLOTS : 2;
+    const TSmem M = tiled_smem(L, NQ, X.fused, X.cstage, X.nslot);
     X.V = tile_view(smem_raw, M);
     X.G = tiled_glob(L);
     X.B = tiled_prep_layout(L, X.fused, X.cstage, P.iaer != 0);
@@ -1087,26 +1100,35 @@ k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* 
         tm[i] = d;
     }
     for (int i = tid; i < TC_N; i += T_THREADS) X.V.ctl[i] = 0;
-    for (int i = tid; i < 2 * TILES; i += T_THREADS) X.V.risky[i] = 0u;
-    for (int i = tid; i < 2 * COLS_PER_CTA * NGPT; i += T_THREADS) X.V.recof[i] = -1;
-    for (int i = tid; i < 2 * COLS_PER_CTA * NQ * (L + 1); i += T_THREADS) X.V.flux[i] = 0.0f;
+    for (int i = tid; i < X.nslot * TILES; i += T_THREADS) X.V.risky[i] = 0u;
+    for (int i = tid; i < X.nslot * COLS_PER_CTA * NGPT; i += T_THREADS) X.V.recof[i] = -1;
+    for (int i = tid; i < X.nslot * COLS_PER_CTA * NQ * (L + 1); i += T_THREADS) X.V.flux[i] = 0.0f;
     if (tid == 0) {
         mbar_init(&X.V.bar[TB_FULL0], T_OPT);
         mbar_init(&X.V.bar[TB_FULL1], T_OPT);
         mbar_init(&X.V.bar[TB_EMPTY0], 2);
         mbar_init(&X.V.bar[TB_EMPTY1], 2);
-        mbar_init(&X.V.bar[TB_PAIR0], T_OPT);
-        mbar_init(&X.V.bar[TB_PAIR1], T_OPT);
-        mbar_init(&X.V.bar[TB_SWEPT0], 2);
-        mbar_init(&X.V.bar[TB_SWEPT1], 2);
-        mbar_init(&X.V.bar[TB_FIN0], 1);
-        mbar_init(&X.V.bar[TB_FIN1], 1);
+        for (int k = 0; k < T_SLOTS; ++k) {
+            mbar_init(&X.V.bar[TB_PAIR0 + k], T_OPT);
+            mbar_init(&X.V.bar[TB_SWEPT0 + k], 2);
+            mbar_init(&X.V.bar[TB_FIN0 + k], 1);
+        }
     }
     __syncthreads();
+    // Handoffs per pair lp (slot lp % nslot; a slot's barriers complete one
+    // phase per pair, so the parity of pair lp's phase is (lp / nslot) & 1):
+    // the optics warps arrive PAIR when its cells are all made, the adding
+    // warps SWEPT when its tiles are all swept, the FP64 warp FIN when its
+    // outputs are written.  No barrier can run two phases ahead of a waiter:
+    // the optics and adding warps start pair lp + nslot only after FIN of
+    // pair lp.
     if (warp < T_OPT) {
         for (int lp = 0; lp < X.nlocal; ++lp) {
-            // pair lp - 2 is finished: its parity's per-pair state is free
-            if (lp >= 2) mbar_wait(&X.V.bar[TB_FIN0 + (lp & 1)], ((lp - 2) >> 1) & 1, X.abort, P.err);
+            // pair lp - nslot is finished: the slot's per-pair state is free
+            if (lp >= X.nslot) {
+                const int q = lp - X.nslot;
+                mbar_wait(&X.V.bar[TB_FIN0 + tslot(X, q)], tphase(X, q), X.abort, P.err);
+            }
             opt_sync();  // the previous pair's cells are all written
             tiled_load(P, X, lp);
             for (int t = 0; t < TILES; ++t) {
@@ -1119,28 +1141,32 @@ k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* 
                 __threadfence_block();
                 if (lane == 0) {
                     mbar_arrive(&X.V.bar[TB_FULL0 + b]);
-                    if (t == TILES - 1) mbar_arrive(&X.V.bar[TB_PAIR0 + (lp & 1)]);
+                    if (t == TILES - 1) mbar_arrive(&X.V.bar[TB_PAIR0 + tslot(X, lp)]);
                 }
             }
         }
     } else if (warp < T_REDO + T_F64) {
         for (int lp = warp - T_REDO; lp < X.nlocal; lp += T_F64) {
-            const int par = lp & 1;
-            mbar_wait(&X.V.bar[TB_PAIR0 + par], (lp >> 1) & 1, X.abort, P.err);
+            const int slot = tslot(X, lp);
+            const unsigned ph = tphase(X, lp);
+            mbar_wait(&X.V.bar[TB_PAIR0 + slot], ph, X.abort, P.err);
             tiled_redo(P, X, lp, tab64);
             __syncwarp();
-            mbar_wait(&X.V.bar[TB_SWEPT0 + par], (lp >> 1) & 1, X.abort, P.err);
+            mbar_wait(&X.V.bar[TB_SWEPT0 + slot], ph, X.abort, P.err);
             if (NQ > 8) tiled_finish<16>(P, X, lp);
             else tiled_finish<8>(P, X, lp);
             __threadfence_block();
-            if (lane == 0) mbar_arrive(&X.V.bar[TB_FIN0 + par]);
+            if (lane == 0) mbar_arrive(&X.V.bar[TB_FIN0 + slot]);
         }
     } else {
         const int sky = warp == T_ADDT ? 1 : 0;
         for (int lp = 0; lp < X.nlocal; ++lp) {
-            const int par = lp & 1;
-            // pair lp - 2 is finished: its level sums and set-aside state are free
-            if (lp >= 2) mbar_wait(&X.V.bar[TB_FIN0 + par], ((lp - 2) >> 1) & 1, X.abort, P.err);
+            const int slot = tslot(X, lp);
+            // pair lp - nslot is finished: the slot's level sums are free
+            if (lp >= X.nslot) {
+                const int q = lp - X.nslot;
+                mbar_wait(&X.V.bar[TB_FIN0 + tslot(X, q)], tphase(X, q), X.abort, P.err);
+            }
             if (P.bands && sky == 1) tiled_zero_bands(P, X, lp);
             for (int t = 0; t < TILES; ++t) {
                 const int T = TILES * lp + t, b = T & 1;
@@ -1157,7 +1183,7 @@ k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* 
                     if (sky == 1) X.V.ctl[TC_ROW0 + b] = 0;
                     __threadfence_block();
                     mbar_arrive(&X.V.bar[TB_EMPTY0 + b]);
-                    if (t == TILES - 1) mbar_arrive(&X.V.bar[TB_SWEPT0 + par]);
+                    if (t == TILES - 1) mbar_arrive(&X.V.bar[TB_SWEPT0 + slot]);
                 }
                 __syncwarp();
             }
@@ -1171,7 +1197,14 @@ k_solve_tiled(const SolveParams P, const float* __restrict__ tab, const double* 
 __host__ inline bool tiled_supports(const SolveParams& P, size_t smem_max) {
     if (P.idelm != 1 || P.nlay > T_MAXL || P.colmap) return false;
     const bool fused = P.fused && P.icld >= 1, nomc = P.nomcica && P.icld >= 1;
-    return tiled_smem(P.nlay, P.extra ? 16 : 8, fused, fused || nomc).total <= smem_max;
+    return tiled_smem(P.nlay, P.extra ? 16 : 8, fused, fused || nomc, 2).total <= smem_max;
+}
+
+// Pair slots of a call the tiled kernel takes: 3 when their shared memory
+// fits, else 2.
+__host__ inline int tiled_slots(const SolveParams& P, size_t smem_max) {
+    const bool fused = P.fused && P.icld >= 1, nomc = P.nomcica && P.icld >= 1;
+    return tiled_smem(P.nlay, P.extra ? 16 : 8, fused, fused || nomc, T_SLOTS).total <= smem_max ? T_SLOTS : 2;
 }
 
 }  // namespace rrsw
