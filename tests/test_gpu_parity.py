@@ -1,10 +1,11 @@
 """GPU library vs the FP64 oracle on the same seeded inputs.
 
-Tolerances (stated per test): the plain FP64 form must match the oracle to
-1e-9 relative on fluxes and heating rates (largest absolute difference
-divided by the largest magnitude of the field); McICA masks and subcolumn
-arrays must be bit-exact; the FP32 form must stay within 0.05 W m-2 on
-fluxes and 0.01 K/day on heating rates.
+Tolerances (stated per test): the plain FP64 form must match the oracle
+element by element, |d| <= 1e-9 |ref| + floor, with floors of 1e-9 W m-2 on
+fluxes and 1e-8 K/day on heating rates for values near zero (night
+columns, the top layers); McICA masks and subcolumn arrays must be
+bit-exact; the FP32 form must stay within 0.05 W m-2 on fluxes and
+0.01 K/day on heating rates.
 """
 import numpy as np
 import pytest
@@ -49,14 +50,14 @@ def gpu_call(kw, extra=False, idelm=1, clouds=None):
     return res if extra else {k: res[k] for k in FLUX + HR}
 
 
-def rel_err(a, b):
-    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
-
-
-def assert_parity(g, o, tol=1e-9, keys=FLUX + HR):
+def assert_parity(g, o, tol=1e-9, keys=FLUX + HR, flux_floor=1e-9, hr_floor=1e-8):
+    """Every element: |g - o| <= tol |o| + floor (the heating-rate floor for
+    swhr / swhrc, the flux floor for every flux output)."""
     for k in keys:
-        e = rel_err(g[k], o[k])
-        assert e <= tol, (k, e)
+        d = np.abs(g[k] - o[k])
+        lim = tol * np.abs(o[k]) + (hr_floor if k in HR else flux_floor)
+        bad = d > lim
+        assert not bad.any(), (k, int(bad.sum()), float(np.max(d - lim)))
 
 
 def mcica_oracle(c, icld, seed, irng=0, alpha=None):

@@ -11,7 +11,7 @@ all bit-exact:
        sequential stream; at 2^28 words, two segment sizes against each other
        and host windows at segment starts; the fused solve with irng = 1
        against the oracle's mcica_subcol_sw + rrtmg_sw (FP64 form, 1e-9
-       relative; FP32 form 0.05 W m-2 / 0.01 K/day), its subcolumns through
+       relative element by element; FP32 form 0.05 W m-2 / 0.01 K/day), its subcolumns through
        the device mcica_subcol_sw (bit for bit) and the unfused solve of those
        (1e-12 relative).
 """
@@ -138,8 +138,10 @@ def test_fused_mt_matches_oracle(torch, icld):
     gi.set_form(gi.FORM_FP64)
     g = gi.rrtmg_sw(**gcm_inputs(c, icld=icld, iaer=0), clouds=clouds, extra=True)
     for k in OUTS:
-        e = np.max(np.abs(g[k] - o[k])) / np.max(np.abs(o[k]))
-        assert e <= 1e-9, (k, e)
+        # every element within 1e-9 relative, floors 1e-9 W m-2 / 1e-8 K/day near zero
+        d = np.abs(g[k] - o[k])
+        bad = d > 1e-9 * np.abs(o[k]) + (1e-8 if k in ("swhr", "swhrc") else 1e-9)
+        assert not bad.any(), (k, int(bad.sum()), float(np.max(d)))
     # the same subcolumns through the device McICA + the unfused solve
     z = np.zeros((14, ncol, nlay))
     md = gi.mcica_subcol_sw(1, ncol, nlay, icld, seed, 1, c["play"], c["cldfrac"], c["ciwp"], c["clwp"], c["rei"],

@@ -3,7 +3,7 @@
 CPU: the oracle's non-McICA driver against its McICA driver with every
 subcolumn set to the layer's cloud (the two reference drivers then solve the
 same problem), and its partial-cloud stop.  GPU: the library against the
-oracle, FP64 form to 1e-9 relative, FP32 form within 0.05 W m-2 and
+oracle, FP64 form to 1e-9 relative element by element, FP32 form within 0.05 W m-2 and
 0.01 K/day.
 """
 import numpy as np
@@ -113,8 +113,10 @@ def test_gpu_nomcica_fp64_parity(gpu_lib, inflag, aerosol):
     _, kw, nm = overcast_case(67, 60, 33 + inflag, inflag=inflag, aerosol=aerosol)
     g, o = gpu_nomcica(kw, nm, gpu_lib.FORM_FP64), oracle_nomcica(kw, nm)
     for k in FLUX + HR:
-        e = float(np.max(np.abs(g[k] - o[k])) / max(np.max(np.abs(o[k])), 1e-300))
-        assert e <= 1e-9, (k, e)
+        # every element within 1e-9 relative, floors 1e-9 W m-2 / 1e-8 K/day near zero
+        d = np.abs(g[k] - o[k])
+        bad = d > 1e-9 * np.abs(o[k]) + (1e-8 if k in HR else 1e-9)
+        assert not bad.any(), (k, int(bad.sum()), float(np.max(d)))
 
 
 @pytest.mark.gpu
