@@ -39,9 +39,9 @@
 // A subcolumn with such a cell is left out of its tile's sums; the optics
 // warps copy its R/T column aside (global, per CTA) once the tile is done,
 // and the FP64 warp sweeps it again with the FP64 cells, its contribution
-// added before the pair's outputs are written.  Handoffs use mbarriers (tile full / empty, pair produced,
-// pair swept, pair finished) whose waits give up after ~2^33 cycles with an
-// error code instead of hanging.  A pair with more such cells than the
+// added before the pair's outputs are written.  Handoffs use mbarriers
+// (tile full / empty; per pair slot: pair produced, swept, finished) whose
+// waits give up after ~2^33 cycles with an error code instead of hanging.  A pair with more such cells than the
 // capacities below is listed for the caller, which solves it again with the
 // scratch-based kernel (k_solve<float>).
 #pragma once
