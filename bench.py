@@ -217,26 +217,24 @@ def run_batch(args):
     print(json.dumps(line))
 
 
-def run_adjoint(args):
+def adjoint_workload(args, gi, k=3, recompute=True):
     """Adjoint cost: 65536 columns x 60 layers, McICA clouds (icld=2, masks
     frozen), objective TOA up + surface net + heating-rate sum; forward,
     tangent-linear and adjoint (stored / recomputed local Jacobians) through
-    the host-array C ABI, each timed end to end."""
-    from rrtmg_sw_gb300 import build, interface as gi
+    the host-array C ABI, each timed end to end (best of k after one
+    untimed call)."""
     from rrtmg_sw_gb300.synthetic import gcm_inputs, make_columns
-    build.build()
-    gi.rrtmg_sw_ini(1.004e3)
     gi.set_form(gi.FORM_FP64)
     ncol = args.ncol if args.ncol != NCOL else 65536
     c = make_columns(ncol, NLAY, 20261203 + 4, clouds=True)
     kw = gcm_inputs(c, icld=2, iaer=0)
-    for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl", "taucmcl", "ssacmcl", "asmcmcl", "fsfcmcl"):
-        kw[k] = None  # fused McICA: the subcolumn arrays are not passed
+    for key in MC_NAMES:
+        kw[key] = None  # fused McICA: the subcolumn arrays are not passed
     cl = dict(permuteseed=112, irng=0, cldfrac=c["cldfrac"], ciwp=c["ciwp"], clwp=c["clwp"], rei=c["rei"],
               rel=c["rel"])
     w = (1.0, 1.0, 1.0)
 
-    def best(f, k=3):
+    def best(f):
         f()
         ts = []
         for _ in range(k):
@@ -249,10 +247,25 @@ def run_adjoint(args):
     gi.set_form(gi.FORM_FP32)
     fwd32 = best(lambda: gi.rrtmg_sw(**kw, clouds=cl))
     gi.set_form(gi.FORM_FP64)
-    d = {k: np.ones_like(kw["tlay"]) for k in gi.AD_LAYER}
+    d = {key: np.ones_like(kw["tlay"]) for key in gi.AD_LAYER}
     tl = best(lambda: gi.rrtmg_sw_tl(kw, d, cl, w))
     ad_s = best(lambda: gi.rrtmg_sw_ad(kw, cl, w, store=True))
-    ad_r = best(lambda: gi.rrtmg_sw_ad(kw, cl, w, store=False))
+    res = {"workload": "%d columns x %d layers, McICA icld=2, objective TOA up + sfc net + HR sum, host-array calls "
+                       "end to end, best of %d" % (ncol, NLAY, k),
+           "forward_fp64_ms": fwd, "forward_fp32_ms": fwd32, "tangent_linear_ms": tl, "adjoint_store_ms": ad_s,
+           "adjoint_store_vs_fp64_forward": ad_s / fwd, "adjoint_store_vs_fp32_forward": ad_s / fwd32}
+    if recompute:
+        ad_r = best(lambda: gi.rrtmg_sw_ad(kw, cl, w, store=False))
+        res.update(adjoint_recompute_ms=ad_r, adjoint_recompute_vs_fp64_forward=ad_r / fwd)
+    return res
+
+
+def run_adjoint(args):
+    """The adjoint configuration alone (see adjoint_workload), one JSON line."""
+    from rrtmg_sw_gb300 import build, interface as gi
+    build.build()
+    gi.rrtmg_sw_ini(1.004e3)
+    r = adjoint_workload(args, gi)
     sms = 152
     try:
         import torch
@@ -262,13 +275,10 @@ def run_adjoint(args):
     # per-CTA scratch (doubles) of the adjoint kernel, 3 resident CTAs per SM
     slot = lambda fields: ((NLAY + 1) * fields * 224 + 2 * 15 * NLAY * 4) * 8 * 3
     line = {"metric": "adjoint cost relative to the FP64 forward it differentiates (host-array calls, end to end)",
-            "value": ad_s / fwd, "unit": "x forward", "n_gpus": 1, "higher_is_better": False,
-            "config": {"workload": "%d columns x %d layers, McICA icld=2, objective TOA up + sfc net + HR sum"
-                                   % (ncol, NLAY)},
-            "forward_fp64_ms": fwd, "forward_fp32_ms": fwd32, "tangent_linear_ms": tl, "adjoint_store_ms": ad_s,
-            "adjoint_recompute_ms": ad_r, "adjoint_store_vs_fp64_forward": ad_s / fwd,
-            "adjoint_store_vs_fp32_forward": ad_s / fwd32, "adjoint_recompute_vs_fp64_forward": ad_r / fwd,
+            "value": r["adjoint_store_vs_fp64_forward"], "unit": "x forward", "n_gpus": 1,
+            "higher_is_better": False, "config": {"workload": r["workload"]},
             "scratch_bytes_store": slot(45) * sms, "scratch_bytes_recompute": slot(20) * sms}
+    line.update({k: v for k, v in r.items() if k != "workload"})
     print(json.dumps(line))
 
 
@@ -625,6 +635,9 @@ def main():
         extra["mcica_aer_16384x60"] = small_workload(gi, torch, dev, sid, "16384x60 McICA icld=2 + iaer=10", 16384,
                                                      2, 10, 20261203 + 1)
         extra["batch"] = batch_workload(args, gi, torch, dev, per_instance=False)
+        torch.cuda.empty_cache()
+        # the adjoint's cost against the forward it differentiates (one timed call each)
+        extra["adjoint"] = adjoint_workload(args, gi, k=1, recompute=False)
 
     line = {
         "metric": METRIC, "value": value, "unit": "columns/s", "n_gpus": world, "steps": args.steps,

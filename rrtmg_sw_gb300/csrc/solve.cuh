@@ -367,11 +367,15 @@ __device__ inline void taumol_generic(int ib, int ig, int lay, const Coef<float>
     const float colh2o = c.f(F_H2O, lay);
     float tg = 0.0f, fs = 0.0f;
     int js = 1;
-    if (d.kind == 1) {
+    // A warp's 32 g-points span several bands, so the band kinds share one
+    // path (branches would run one after the other): one species (kind 2)
+    // is two species with fs = 0 and its column times fac; kind 0 has no
+    // major absorber.
+    if (d.kind != 0) {
+        const bool two = d.kind == 1;
         const float ca = c.f(F_H2O + d.sa, lay);
-        const float speccomb = ca + d.strrat * c.f(F_H2O + d.sb, lay);
-        const float specparm = fminf(ca / speccomb, cT.oneminus_f);
-        const float specmult = d.mult * specparm;
+        const float speccomb = two ? ca + d.strrat * c.f(F_H2O + d.sb, lay) : ca * d.fac;
+        const float specmult = two ? d.mult * fminf(ca / speccomb, cT.oneminus_f) : 0.0f;
         const int ij = (int)specmult;
         js = 1 + ij;
         fs = specmult - (float)ij;
@@ -380,17 +384,17 @@ __device__ inline void taumol_generic(int ib, int ig, int lay, const Coef<float>
         const int i0 = ((jp * 5 + (jt - 1)) * nsp + js - 1) * ng + ig - 1;
         const int i1 = (((jp + 1) * 5 + (jt1 - 1)) * nsp + js - 1) * ng + ig - 1;
         const float gs = 1.0f - fs;
-        const float k0 = gs * f00 * ldt(tab, d.ktab + i0) + fs * f00 * ldt(tab, d.ktab + i0 + ng) +
-                         gs * f10 * ldt(tab, d.ktab + i0 + nsp * ng) + fs * f10 * ldt(tab, d.ktab + i0 + (nsp + 1) * ng);
-        const float k1 = gs * f01 * ldt(tab, d.ktab + i1) + fs * f01 * ldt(tab, d.ktab + i1 + ng) +
-                         gs * f11 * ldt(tab, d.ktab + i1 + nsp * ng) + fs * f11 * ldt(tab, d.ktab + i1 + (nsp + 1) * ng);
+        // the fs terms exist for two species only (one species: fs = 0, and
+        // i + (nsp + 1) ng would pass the table's end)
+        const float a1 = two ? ldt(tab, d.ktab + i0 + ng) : 0.0f;
+        const float a3 = two ? ldt(tab, d.ktab + i0 + (nsp + 1) * ng) : 0.0f;
+        const float b1 = two ? ldt(tab, d.ktab + i1 + ng) : 0.0f;
+        const float b3 = two ? ldt(tab, d.ktab + i1 + (nsp + 1) * ng) : 0.0f;
+        const float k0 = gs * f00 * ldt(tab, d.ktab + i0) + fs * f00 * a1 + gs * f10 * ldt(tab, d.ktab + i0 + nsp * ng) +
+                         fs * f10 * a3;
+        const float k1 = gs * f01 * ldt(tab, d.ktab + i1) + fs * f01 * b1 + gs * f11 * ldt(tab, d.ktab + i1 + nsp * ng) +
+                         fs * f11 * b3;
         tg = speccomb * (k0 + k1);
-    } else if (d.kind == 2) {
-        const int i0 = (jp * 5 + (jt - 1)) * ng + ig - 1;
-        const int i1 = ((jp + 1) * 5 + (jt1 - 1)) * ng + ig - 1;
-        const float kk = c.f(F_FAC00, lay) * ldt(tab, d.ktab + i0) + c.f(F_FAC10, lay) * ldt(tab, d.ktab + i0 + ng) +
-                         c.f(F_FAC01, lay) * ldt(tab, d.ktab + i1) + c.f(F_FAC11, lay) * ldt(tab, d.ktab + i1 + ng);
-        tg = c.f(F_H2O + d.sa, lay) * d.fac * kk;
     }
     if (d.cont >= 1) {
         const int indf = c.indfor(lay);

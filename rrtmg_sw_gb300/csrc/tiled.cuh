@@ -713,6 +713,7 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
     const bool act = V.ctl[TC_ACT0 + 2 * ps + c2] != 0;
     const bool risky = (V.risky[ps * TILES + t] >> lane) & 1u;
     const bool use = act && !risky;
+    const float zinc_use = use ? zinc : 0.0f;  // the lanes left out of the sums get zero level fluxes
     // subcolumns with FP64 cells were copied aside by the optics warps
     // (tiled_set_aside); they stay out of this tile's sums
     float* R = V.rup + (size_t)2 * SKY * L * TW;  // [2][L][TW]: rup, rupd of this sky
@@ -747,18 +748,18 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
         for (int k = 0; k < 5; ++k) fn[k] = tfield(tb, L, F0 + k, in, lane);
         rn[0] = R[in * TW + lane];
         rn[1] = R[(L + in) * TW + lane];
-        level1(st, rr[0], rr[1], zinc, q, dif);
+        level1(st, rr[0], rr[1], zinc_use, q, dif);
         down1(st, f, dif);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) tfield(tb, L, F0 + k, i, lane) = use ? q[k] : 0.0f;
+        for (int k = 0; k < 4; ++k) tfield(tb, L, F0 + k, i, lane) = q[k];
 #pragma unroll
         for (int k = 0; k < 5; ++k) f[k] = fn[k];
         rr[0] = rn[0];
         rr[1] = rn[1];
     }
-    level1(st, albp, albd, zinc, q, dif);  // surface
+    level1(st, albp, albd, zinc_use, q, dif);  // surface
 #pragma unroll
-    for (int k = 0; k < 4; ++k) V.scr[(4 * SKY + k) * TW + lane] = use ? q[k] : 0.0f;
+    for (int k = 0; k < 4; ++k) V.scr[(4 * SKY + k) * TW + lane] = q[k];
     int* key = (int*)(V.scr + 8 * TW);
     if (SKY == 1) key[lane] = c2 * 16 + ib;
     const bool uv = ib >= 9 && ib <= 12;  // bands 25-28 (spcvmc:629)
