@@ -411,11 +411,13 @@ __device__ inline void taumol_generic(int ib, int ig, int lay, const Coef<float>
     if (d.minor == 9) tg += 4.35e-4f * c.f(F_O2, lay) / 700.0f;
     else if (d.minor >= 0) tg += c.f(F_H2O + d.minor, lay) * ldt(tab, d.mtab + ig - 1);
     const float colmol = c.f(F_MOL, lay);
-    if (d.rtype == 0) taur = colmol * ldt(tab, d.rtab);
-    else if (d.rtype == 1) taur = colmol * ldt(tab, d.rtab + ig - 1);
-    else {
-        const float ra = ldt(tab, d.rtab + (js - 1) * ng + ig - 1), rb = ldt(tab, d.rtab + js * ng + ig - 1);
-        taur = colmol * (ra + fs * (rb - ra));
+    {
+        // Rayleigh: one value (rtype 0), one per g-point (1), or interpolated
+        // in the species ratio (2); one path, the second read only for rtype 2
+        const int ir = d.rtab + (d.rtype == 2 ? (js - 1) * ng : 0) + (d.rtype >= 1 ? ig - 1 : 0);
+        const float ra = ldt(tab, ir);
+        const float rb = d.rtype == 2 ? ldt(tab, ir + ng) : ra;
+        taur = colmol * (d.rtype == 2 ? ra + fs * (rb - ra) : ra);
     }
     taug = tg;
     js_out = js;
