@@ -61,7 +61,9 @@ constexpr int TW = 32;                                   // subcolumns per tile
 constexpr int TILES = COLS_PER_CTA * NGPT / TW;          // 7 tiles per pair
 constexpr int T_OPT = RRSW_TILED_OPT;                    // optics warps
 constexpr int T_F64 = RRSW_TILED_F64;                    // FP64 warps (pairs taken in turn)
-static_assert(T_F64 == 1 || T_F64 == 2, "one FP64 warp, or one per pair parity");
+// (a third FP64 warp could wait on a slot's barrier two phases early when
+// there are only two pair slots)
+static_assert(T_F64 == 1 || T_F64 == 2, "one or two FP64 warps");
 constexpr int T_REDO = T_OPT;                            // first FP64 warp
 constexpr int T_ADDC = T_OPT + T_F64;                    // adding warp, clear sky
 constexpr int T_ADDT = T_OPT + T_F64 + 1;                // adding warp, total sky
