@@ -327,6 +327,10 @@ int rrtmg_sw_last_launch_count_c(void);
 #define RRTMG_SW_KERNEL_FP32 1
 #define RRTMG_SW_KERNEL_FP32_TILED 2
 int rrtmg_sw_last_kernel_c(void);
+/* Pair slots of the most recent solve's tiled kernel: 3 when their shared
+ * memory fits (60 layers without the extra outputs, for instance), else 2;
+ * 0 when the most recent solve did not run the tiled kernel. */
+int rrtmg_sw_last_tile_slots_c(void);
 /* Counters of the FP32 form over the most recent solve through
  * rrtmg_sw_c / rrtmg_sw_mcica_c / their _dev_ forms (zeros for the FP64
  * form): stats[0] cells whose FP32 optics were too close to a discrete

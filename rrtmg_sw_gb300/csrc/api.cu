@@ -71,6 +71,7 @@ struct State {
     int form = RRTMG_SW_FORM_FP64;
     int last_launches = 0;
     int last_kernel = -1;  // RRTMG_SW_KERNEL_* of the most recent solve's main launch
+    int last_tile_slots = 0;  // pair slots of the most recent tiled launch (0: not tiled)
     int last_ad_store = -1;  // checkpointing choice of the last adjoint / tangent-linear call
     std::string last_cuda;
 };
@@ -592,6 +593,7 @@ int enqueue_solve(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, c
     const bool fp32 = st.form == RRTMG_SW_FORM_FP32;
     LaunchInfo li = fp32 ? plan_fp32(P, st.num_sms, allow_tiled && !st.no_tiled) : plan_fp64(P, st.num_sms);
     st.last_kernel = !fp32 ? RRTMG_SW_KERNEL_FP64 : li.tiled ? RRTMG_SW_KERNEL_FP32_TILED : RRTMG_SW_KERNEL_FP32;
+    st.last_tile_slots = fp32 && li.tiled ? li.tile_slots : 0;
     if (!fp32) li.slot_bytes = slot_elems(P.nlay, P.idelm, false) * sizeof(double);
     P.slot_elems = li.slot_bytes / (fp32 ? sizeof(float) : sizeof(double));
     // tiled: per-CTA areas, then the pairs' prepared blocks, then the overflow list
@@ -1051,6 +1053,7 @@ int solve_static(State& st, const rrtmg_sw_args* a, const rrtmg_sw_clouds* c, cu
     const size_t off_prep = (((size_t)li.grid * li.slot_bytes) + 255) & ~(size_t)255;
     if (li.tiled && off_prep + (size_t)P.npairs * li.prep_bytes > avail) li = plan_fp32(P, st.num_sms, false);
     st.last_kernel = !fp32 ? RRTMG_SW_KERNEL_FP64 : li.tiled ? RRTMG_SW_KERNEL_FP32_TILED : RRTMG_SW_KERNEL_FP32;
+    st.last_tile_slots = fp32 && li.tiled ? li.tile_slots : 0;
     if (!fp32) li.slot_bytes = slot_elems(P.nlay, P.idelm, false) * sizeof(double);
     const size_t slots = avail / li.slot_bytes;
     // one slot per SM, or per column pair when the call has fewer pairs
@@ -1615,6 +1618,7 @@ int rrtmg_sw_get_form_c(void) {
 
 int rrtmg_sw_last_launch_count_c(void) { return S().last_launches; }
 int rrtmg_sw_last_kernel_c(void) { return S().last_kernel; }
+int rrtmg_sw_last_tile_slots_c(void) { return S().last_tile_slots; }
 int rrtmg_sw_last_fp32_stats_c(int64_t* stats) {
     if (!stats) return RRTMG_SW_EARGS;
     for (int i = 0; i < 4; ++i) stats[i] = S().last_stats[i];

@@ -427,6 +427,11 @@ def last_kernel():
     return lib().rrtmg_sw_last_kernel_c()
 
 
+def last_tile_slots():
+    """Pair slots of the most recent solve's tiled kernel (3 or 2; 0: not tiled)."""
+    return lib().rrtmg_sw_last_tile_slots_c()
+
+
 def last_fp32_stats():
     """FP32 form's counters of the most recent solve: cells redone in FP64,
     of those past the scratch kernel's queue, column pairs the tiled kernel

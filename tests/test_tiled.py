@@ -107,6 +107,7 @@ def test_tiled_against_oracle(icld, iaer):
     c, clouds, alpha = case(300, 60, 20261220 + icld + iaer, icld, iaer)
     g = run_fp32(c, clouds, icld, iaer, tiled=True)
     assert gpu.lib().rrtmg_sw_last_launch_count_c() == 2  # preparation + solve
+    assert gpu.last_tile_slots() == 3  # 60 layers, 8 level sums: three pair slots fit
     check_bounds(g, oracle(c, icld, iaer, alpha))
 
 
@@ -130,11 +131,14 @@ def test_tiled_matches_scratch_kernel_with_outputs():
         assert np.max(np.abs(got[k] - ref[k])) <= 1e-4, (k, float(np.max(np.abs(got[k] - ref[k]))))
 
 
-def test_tiled_is_deterministic():
+@pytest.mark.parametrize("extra,slots", [(False, 3), (True, 2)])
+def test_tiled_is_deterministic(extra, slots):
+    # three pair slots, and two when the extra outputs' 16 level sums leave no room for a third
     set_env(tiled=True)
     c, clouds, alpha = case(500, 60, 20261231, 5)
-    a = run_fp32(c, clouds, 5, 0, extra=True, tiled=True)
-    b = run_fp32(c, clouds, 5, 0, extra=True, tiled=True)
+    a = run_fp32(c, clouds, 5, 0, extra=extra, tiled=True)
+    assert gpu.last_tile_slots() == slots
+    b = run_fp32(c, clouds, 5, 0, extra=extra, tiled=True)
     st = gpu.last_fp32_stats()
     # cloudy columns have FP64 cells; none handed back at full capacity
     assert st["redone_cells"] > 0 and st["subcolumns_swept_twice"] > 0 and st["pairs_handed_back"] == 0, st
