@@ -416,8 +416,9 @@ def per_level(got, ref):
 
 
 def small_workload(gi, torch, dev, sid, name, ncol, icld, iaer, seed):
-    """A BASELINE-named configuration at its own size: CPU oracle, GPU FP64
-    and FP32 forms (device-resident, CUDA events), both against the oracle."""
+    """One of the benchmark configurations at its own size (1024 x 60 clear,
+    16384 x 60 McICA + aerosol): CPU oracle, GPU FP64 and FP32 forms
+    (device-resident, CUDA events), both against the oracle."""
     from rrtmg_sw_gb300.synthetic import make_columns
     c = make_columns(ncol, NLAY, seed, clouds=icld > 0, aerosol=iaer == 10)
     dc = DevCase(gi, torch, dev, c, icld, iaer)
