@@ -283,14 +283,23 @@ __device__ inline TileView tile_view(unsigned char* raw, const TSmem& M) {
     return v;
 }
 
-// tile field f of layer index i (0 = surface layer), lane l
-__device__ inline float& tfield(float* tb, int L, int f, int i, int l) { return tb[((size_t)f * L + i) * TW + l]; }
+// Tile buffer layout (T_NF * L * TW floats): per sky (0 clear, 1 total) the
+// fields ref, refd, adir, adif of each (layer index i, lane) as one float4
+// -- one 16-byte access for the adding warps, whose sweeps are bound by
+// instruction issue -- then per sky the direct transmittances.
+__device__ inline float4* tquad(float* tb, int L, int sky, int i) { return (float4*)tb + ((size_t)sky * L + i) * TW; }
+__device__ inline float* tdbt(float* tb, int L, int sky, int i) {
+    return tb + (size_t)8 * L * TW + ((size_t)sky * L + i) * TW;
+}
+// tile field f (TF_*) of layer index i (0 = surface layer), lane l
+__device__ inline float& tfield(float* tb, int L, int f, int i, int l) {
+    const int sky = f >= 5 ? 1 : 0, c = f - 5 * sky;
+    return c < 4 ? ((float*)tquad(tb, L, sky, i))[4 * l + c] : tdbt(tb, L, sky, i)[l];
+}
 
 // ---------------------------------------------------------- adding method
 // One sky's layer fields in a tile: reflectance, diffuse reflectance,
-// absorptance (direct, diffuse incidence), direct transmittance; the clear
-// sky's at TF_REFC, the total sky's at TF_REF.
-constexpr int SKY_BASE[2] = {TF_REFC, TF_REF};
+// absorptance (direct, diffuse incidence), direct transmittance.
 
 // State of one sky's down-sweep of one subcolumn, plus the absorption of the
 // layer above the current level for the heating rate.
@@ -614,8 +623,10 @@ __device__ void tiled_optics(const SolveParams& P, const TCtx& X, int lp, int t,
                 atomicOr(&V.risky[slot * TILES + t], 1u << lane);
             }
         }
-#pragma unroll
-        for (int k = 0; k < T_NF; ++k) tfield(tb, L, k, r, lane) = f[k];
+        tquad(tb, L, 0, r)[lane] = make_float4(f[TF_REFC], f[TF_REFDC], f[TF_ADIRC], f[TF_ADIFC]);
+        tdbt(tb, L, 0, r)[lane] = f[TF_DBTC];
+        tquad(tb, L, 1, r)[lane] = make_float4(f[TF_REF], f[TF_REFD], f[TF_ADIR], f[TF_ADIF]);
+        tdbt(tb, L, 1, r)[lane] = f[TF_DBT];
     }
 }
 
@@ -649,7 +660,7 @@ __device__ void tiled_set_aside(const TCtx& X, int lp, int t, int b) {
         const int lane = __ffs(m) - 1;
         float* rp = trec(X, slot, idx);
         if (rem < per) {
-            rp[8 + rem] = tb[(size_t)rem * TW + lane];
+            rp[8 + rem] = tfield((float*)tb, L, rem / L, rem % L, lane);  // record order: field, layer
         } else {
             const int s = TW * t + lane;
             rp[0] = (float)s;
@@ -689,15 +700,14 @@ __device__ void tiled_redo(const SolveParams& P, const TCtx& X, int lp, const do
     }
 }
 
-// Where a tile keeps the 8 weighted fluxes of a level after the sweeps:
-// level v >= 1 in the slots of layer v-1 that the sweeps have read (clear
-// sky in fields 0-3, total sky in fields 5-8), the surface level in rows of
-// scr.  Order of q: fu, fd, cu, cd, direct total, direct clear, absorption
-// total, absorption clear.
-__device__ __forceinline__ int q_total(int k) { return k < 4 ? ((k >> 1) & 1) == 0 : (k & 1) == 0; }
-__device__ __forceinline__ int q_comp(int k) { return k < 4 ? (k & 1) : (k < 6 ? 2 : 3); }
-__device__ __forceinline__ int q_slot(int k) { return (q_total(k) ? TF_REF : TF_REFC) + q_comp(k); }
-__device__ __forceinline__ int q_srow(int k) { return (q_total(k) ? 4 : 0) + q_comp(k); }
+// Where a tile keeps the weighted fluxes of a level after the sweeps: level
+// v >= 1 in each sky's float4 of layer v-1 that the sweeps have read (up,
+// down, direct, absorption of the layer above), the surface level in scr as
+// float4 [sky][lane].  Order of the 8 sums: fu, fd, cu, cd, direct total,
+// direct clear, absorption total, absorption clear.
+__device__ __forceinline__ void q_order(const float4& c, const float4& t, float* x) {
+    x[0] = t.x; x[1] = t.y; x[2] = c.x; x[3] = c.y; x[4] = t.z; x[5] = c.z; x[6] = t.w; x[7] = c.w;
+}
 
 // ---- adding warps: the vertical sweeps of tile t (buffer b) of pair lp,
 // sky SKY (0 clear, 1 total); then the g-point sums of half the levels
@@ -706,7 +716,6 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
     const TileView& V = X.V;
     const int L = X.L, ps = tslot(X, lp), pair = tpair(lp), lane = threadIdx.x & 31;
     const size_t n = (size_t)P.ncol, L1 = (size_t)L + 1;
-    constexpr int F0 = SKY_BASE[SKY];
     float* tb = V.tile + (size_t)b * T_NF * L * TW;
     const int s = TW * t + lane, c2 = s / NGPT, g = s % NGPT;
     const int ib = cT.ngb[g];
@@ -723,12 +732,15 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
     // loaded while this one is swept
     float ru = albp, rud = albd;
     float f[5], fn[5];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) f[k] = tfield(tb, L, F0 + k, 0, lane);
+    auto load5 = [&](int i, float* g5) {
+        const float4 a = tquad(tb, L, SKY, i)[lane];
+        g5[0] = a.x; g5[1] = a.y; g5[2] = a.z; g5[3] = a.w;
+        g5[4] = tdbt(tb, L, SKY, i)[lane];
+    };
+    load5(0, f);
     for (int i = 0; i < L; ++i) {
         const int in = i + 1 < L ? i + 1 : i;
-#pragma unroll
-        for (int k = 0; k < 5; ++k) fn[k] = tfield(tb, L, F0 + k, in, lane);
+        load5(in, fn);
         up1(f, ru, rud);
         R[i * TW + lane] = ru;
         R[(L + i) * TW + lane] = rud;
@@ -740,28 +752,24 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
     Down1 st;
     down1_init(st);
     float q[4], rr[2], rn[2], dif;
-#pragma unroll
-    for (int k = 0; k < 5; ++k) f[k] = tfield(tb, L, F0 + k, L - 1, lane);
+    load5(L - 1, f);
     rr[0] = R[(L - 1) * TW + lane];
     rr[1] = R[(2 * L - 1) * TW + lane];
     for (int i = L - 1; i >= 0; --i) {
         const int in = i > 0 ? i - 1 : 0;
-#pragma unroll
-        for (int k = 0; k < 5; ++k) fn[k] = tfield(tb, L, F0 + k, in, lane);
+        load5(in, fn);
         rn[0] = R[in * TW + lane];
         rn[1] = R[(L + in) * TW + lane];
         level1(st, rr[0], rr[1], zinc_use, q, dif);
         down1(st, f, dif);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) tfield(tb, L, F0 + k, i, lane) = q[k];
+        tquad(tb, L, SKY, i)[lane] = make_float4(q[0], q[1], q[2], q[3]);
 #pragma unroll
         for (int k = 0; k < 5; ++k) f[k] = fn[k];
         rr[0] = rn[0];
         rr[1] = rn[1];
     }
     level1(st, albp, albd, zinc_use, q, dif);  // surface
-#pragma unroll
-    for (int k = 0; k < 4; ++k) V.scr[(4 * SKY + k) * TW + lane] = q[k];
+    ((float4*)V.scr)[SKY * TW + lane] = make_float4(q[0], q[1], q[2], q[3]);
     int* key = (int*)(V.scr + 8 * TW);
     if (SKY == 1) key[lane] = c2 * 16 + ib;
     const bool uv = ib >= 9 && ib <= 12;  // bands 25-28 (spcvmc:629)
@@ -773,21 +781,18 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
     const int c0 = (TW * t) / NGPT;
     const int cb = ((TW * t + TW - 1) / NGPT == c0) ? TW : NGPT * (c0 + 1) - TW * t;  // first lane of column 1
     for (int v = lane + 32 * SKY; v <= L; v += 64) {
-        const float* src = v ? tb + (size_t)(v - 1) * TW : V.scr;
-        const int stride = v ? L * TW : TW;
-        int slot[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) slot[k] = (v ? q_slot(k) : q_srow(k)) * stride;
+        const float4* sc = v ? tquad(tb, L, 0, v - 1) : (const float4*)V.scr;      // clear sky
+        const float4* stt = v ? tquad(tb, L, 1, v - 1) : (const float4*)V.scr + TW;  // total sky
         float a0[8], a1[8], e0[8], e1[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) a0[k] = a1[k] = e0[k] = e1[k] = 0.0f;
         for (int m = 0; m < TW; ++m) {
-            const int j = (m + lane) & 31;  // rotated: the lanes read 32 different banks
+            const int j = (m + lane) & 31;  // rotated: a quarter warp's lanes read 8 different 16-byte groups
             const bool lo = j < cb;
             float x[8];
+            q_order(sc[j], stt[j], x);
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                x[k] = src[slot[k] + j];
                 if (lo) a0[k] += x[k];
                 else a1[k] += x[k];
             }
@@ -818,15 +823,16 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
             // per-band fluxes (the band loop of spcvmc:619-630): lanes of one
             // (column, band) in order, added to the FP64 outputs (zeroed at
             // the pair's first tile)
-            const int qb[5] = {0, 1, 4, 2, 3};  // fu, fd, fddir, cu, cd
             int j = 0;
             while (j < TW) {
                 const int kj = key[j];
                 float a[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
                 int e = j;
-                for (; e < TW && key[e] == kj; ++e)
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) a[k] += src[slot[qb[k]] + e];
+                for (; e < TW && key[e] == kj; ++e) {
+                    float x[8];
+                    q_order(sc[e], stt[e], x);
+                    a[0] += x[0]; a[1] += x[1]; a[2] += x[4]; a[3] += x[2]; a[4] += x[3];  // fu, fd, fddir, cu, cd
+                }
                 const int pc = pair_col(P, pair, kj >> 4, X.nmapped);
                 if (pc < P.ncol) {
                     const size_t idx = (size_t)pc + n * ((size_t)v + L1 * (size_t)(kj & 15));
