@@ -738,6 +738,7 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
         g5[4] = tdbt(tb, L, SKY, i)[lane];
     };
     load5(0, f);
+#pragma unroll 2  // (by 4 the code outgrows the instruction cache)
     for (int i = 0; i < L; ++i) {
         const int in = i + 1 < L ? i + 1 : i;
         load5(in, fn);
@@ -755,6 +756,7 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
     load5(L - 1, f);
     rr[0] = R[(L - 1) * TW + lane];
     rr[1] = R[(2 * L - 1) * TW + lane];
+#pragma unroll 2
     for (int i = L - 1; i >= 0; --i) {
         const int in = i > 0 ? i - 1 : 0;
         load5(in, fn);
@@ -786,6 +788,8 @@ __device__ void tiled_sweep(const SolveParams& P, const TCtx& X, int lp, int t, 
         float a0[8], a1[8], e0[8], e1[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) a0[k] = a1[k] = e0[k] = e1[k] = 0.0f;
+        // (not unrolled: the kernel's largest stall is instruction fetch)
+#pragma unroll 1
         for (int m = 0; m < TW; ++m) {
             const int j = (m + lane) & 31;  // rotated: a quarter warp's lanes read 8 different 16-byte groups
             const bool lo = j < cb;
