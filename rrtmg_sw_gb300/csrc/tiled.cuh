@@ -878,6 +878,7 @@ __device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r
         fc[k] = fl[(TF_REFC + k) * L];
         ft[k] = fl[(TF_REF + k) * L];
     }
+#pragma unroll 1  // (FP64 warps' loops kept small: they share instruction caches with optics warps)
     for (int i = 0; i < L; ++i) {
         const int in = i + 1 < L ? i + 1 : i;
 #pragma unroll
@@ -911,6 +912,7 @@ __device__ void tiled_records(const SolveParams& P, const TCtx& X, int lp, int r
     float ra[4], rb[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) ra[k] = R[(k * L + L - 1) * TW + lane];
+#pragma unroll 1
     for (int i = L - 1; i >= -1; --i) {
         float qc[4], qt[4], difc, dift;
         if (i >= 0) {
@@ -1021,6 +1023,7 @@ __device__ void tiled_finish(const SolveParams& P, const TCtx& X, int lp) {
     // outputs (level 0 = surface)
     const double* pdpg = (const double*)(tblk(X, pair) + X.B.pdp);
     constexpr int QX = 8;
+#pragma unroll 1
     for (int it = lane; it < COLS_PER_CTA * (L + 1); it += 32) {
         const int c2 = it / (L + 1), l = it % (L + 1);
         const int ocol = pair_col(P, pair, c2, X.nmapped);
