@@ -93,9 +93,9 @@ def algorithmic_flops_per_column(nlay, cloudy_cells_per_col):
 # 60 layers, McICA icld=5; the traffic is per column pair, so a launch's
 # traffic scales with its columns.
 PROFILED_DRAM_BYTES_PER_COLUMN = {"fp32 scratch": 28.38e9 / 32768,
-                                  "fp32 tiled": (330.914304e6 + 113.873408e6) / 32768}
+                                  "fp32 tiled": (331.934208e6 + 114.524672e6) / 32768}
 # the tiled kernel's preparation kernel (k_tiled_prep), same capture
-PROFILED_PREP_DRAM_BYTES_PER_COLUMN = (222.440704e6 + 209.590016e6) / 32768
+PROFILED_PREP_DRAM_BYTES_PER_COLUMN = (222.937088e6 + 209.511936e6) / 32768
 
 
 def algorithmic_bytes_per_column(nlay):
